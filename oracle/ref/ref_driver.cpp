@@ -1,0 +1,185 @@
+/*
+ * Project-written driver that compiles the reference's OWN CPU solver headers
+ * (solverPoissonMPI_CPU/include, read where they lie; nothing is copied) into
+ * oracle/_ref/libppsref.so for the test oracle.  It replaces the reference's
+ * src/main.cpp (CPU/src/main.cpp:19-134) at one rank: build a BlockGrid, a
+ * CommunicatorMPI, the problem plugin and the operator, construct the solver
+ * type that include/inputParam.hpp:24-38 composes, and call operator()(x, b, A).
+ *
+ * Template arguments are compile-time in the reference, so a table of
+ * instantiations covers the Chebyshev degrees and iteration caps the tests use.
+ * The only change around the reference classes is in RefSolver below: the
+ * residual-history array is re-allocated one entry longer, because the reference
+ * writes history[maxIteration] when it stops at the cap (BiCGSTAB.hpp:275-281,
+ * iterativeSolverBase.hpp:43), one past its allocation.
+ */
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <iostream>
+#include <sstream>
+
+#include "ref_setup.hpp"
+
+#include "blockGrid.hpp"
+#include "communicationMPI.hpp"
+#include "matrixFreeOperatorA.hpp"
+#include "solvers.hpp"
+
+namespace {
+
+using NoneP = NoneSolver<3, T_data, 10000, 150>;
+template <int DEG>
+using ChebP = ChebyshevIteration<3, T_data, 10000, DEG, false, false, NoneP>;
+
+template <class Base, int MAXIT>
+struct RefSolver : Base {
+    RefSolver(const BlockGrid<3, T_data>& g, const ExactSolutionAndBCs<3, T_data>& e, CommunicatorMPI<3, T_data>& c)
+        : Base(g, e, c)
+    {
+        delete[] this->errorFromIterationHistory_;
+        this->errorFromIterationHistory_ = new T_data[MAXIT + 1];
+        for (int i = 0; i <= MAXIT; i++) this->errorFromIterationHistory_[i] = -1.0;
+    }
+    const T_data* history() const { return this->errorFromIterationHistory_; }
+};
+
+struct RefArgs {
+    int np[3];
+    double ds[3], origin[3];
+    int bcs[6];
+    double tol, eps, rescale_min, rescale_max;
+    int problem;
+};
+
+struct RefOut {
+    int iterations;
+    double err_iter, err_true, seconds_loop, seconds_call;
+};
+
+template <class S, int MAXIT>
+int run(const RefArgs* a, double* x, double* b, double* hist, RefOut* out)
+{
+    tollScalingFactor = a->tol;    /* with tolerance == 1: toll_ = 1.0 * tol */
+    epsilon = a->eps;
+    rescaleEigMin = a->rescale_min;
+    rescaleEigMax = a->rescale_max;
+    ppsOracleProblem = a->problem;
+
+    const std::array<int, 3> nranks = {1, 1, 1};
+    const std::array<int, 3> npg = {a->np[0], a->np[1], a->np[2]};
+    const std::array<T_data, 3> ds = {a->ds[0], a->ds[1], a->ds[2]};
+    const std::array<T_data, 3> origin = {a->origin[0], a->origin[1], a->origin[2]};
+    const std::array<int, 3> guards = {1, 1, 1};
+    const std::array<int, 6> bcs = {a->bcs[0], a->bcs[1], a->bcs[2], a->bcs[3], a->bcs[4], a->bcs[5]};
+    const std::array<T_data, 6> bcsValue = {0, 0, 0, 0, 0, 0};
+
+    std::ostringstream sink;
+    std::streambuf* saved = std::cout.rdbuf(sink.rdbuf());   /* the reference prints progress */
+    {
+        BlockGrid<3, T_data> grid(nranks, 0, npg, ds, origin, guards, bcs, bcsValue);
+        CommunicatorMPI<3, T_data> comm(grid);
+        ExactSolutionAndBCs<3, T_data> exact;
+        MatrixFreeOperatorA<3, T_data> opA(grid);
+        auto* solver = new RefSolver<S, MAXIT>(grid, exact, comm);
+        const auto t0 = std::chrono::high_resolution_clock::now();
+        (*solver)(x, b, opA);
+        const auto t1 = std::chrono::high_resolution_clock::now();
+        out->iterations = solver->getNumIterationFinal();
+        out->err_iter = solver->getErrorFromIteration();
+        out->err_true = solver->getErrorComputeOperator();
+        out->seconds_loop = out->iterations > 0 ? solver->getDurationSolver().count() : 0.0;
+        out->seconds_call = std::chrono::duration<double>(t1 - t0).count();
+        if (hist)
+            for (int i = 0; i <= out->iterations && i <= MAXIT; i++) hist[i] = solver->history()[i];
+        delete solver;
+    }
+    std::cout.rdbuf(saved);
+    return 0;
+}
+
+typedef int (*run_fn)(const RefArgs*, double*, double*, double*, RefOut*);
+
+struct Entry {
+    int krylov, precond, degree, maxit;
+    run_fn fn;
+};
+
+template <int MAXIT, class P>
+using BiCG = BiCGSTAB<3, T_data, 1, MAXIT, true, true, P>;
+template <int MAXIT, class P>
+using CG = BaseCG<3, T_data, 1, MAXIT, true, true, P>;
+
+#define BICG_CHEB(DEG, MAXIT) {0, 1, DEG, MAXIT, &run<BiCG<MAXIT, ChebP<DEG>>, MAXIT>}
+#define BICG_NONE(MAXIT) {0, 0, 0, MAXIT, &run<BiCG<MAXIT, NoneP>, MAXIT>}
+#define CG_CHEB(DEG, MAXIT) {1, 1, DEG, MAXIT, &run<CG<MAXIT, ChebP<DEG>>, MAXIT>}
+#define CG_NONE(MAXIT) {1, 0, 0, MAXIT, &run<CG<MAXIT, NoneP>, MAXIT>}
+
+const Entry kTable[] = {
+    BICG_CHEB(1, 1700), BICG_CHEB(2, 1700), BICG_CHEB(3, 1700), BICG_CHEB(4, 1700),
+    BICG_CHEB(5, 1700), BICG_CHEB(11, 1700), BICG_CHEB(24, 1700),
+    BICG_CHEB(11, 3), BICG_CHEB(24, 3), BICG_CHEB(11, 20000), BICG_CHEB(24, 1000),
+    BICG_NONE(1700), BICG_NONE(20000),
+    CG_CHEB(2, 1700), CG_CHEB(11, 1700), CG_CHEB(11, 20000), CG_NONE(1700), CG_NONE(20000),
+};
+
+}  // namespace
+
+extern "C" {
+
+/* Solve in place with the reference's classes.  Returns 0, or -2 when the
+ * (krylov, precond, degree, maxit) combination was not instantiated. */
+int ref_solve(int krylov, int precond, int degree, int maxit, const int* np, const double* ds,
+              const double* origin, const int* bcs, double tol, double eps, double rescale_min,
+              double rescale_max, int problem, double* x, double* b, double* hist, int* iterations,
+              double* errs /* err_iter, err_true, seconds_loop, seconds_call */)
+{
+    RefArgs a;
+    for (int d = 0; d < 3; d++) { a.np[d] = np[d]; a.ds[d] = ds[d]; a.origin[d] = origin[d]; }
+    for (int f = 0; f < 6; f++) a.bcs[f] = bcs[f];
+    a.tol = tol; a.eps = eps; a.rescale_min = rescale_min; a.rescale_max = rescale_max; a.problem = problem;
+    for (const Entry& e : kTable) {
+        if (e.krylov == krylov && e.precond == precond && e.maxit == maxit && (precond == 0 || e.degree == degree)) {
+            RefOut o;
+            int rc = e.fn(&a, x, b, hist, &o);
+            *iterations = o.iterations;
+            errs[0] = o.err_iter; errs[1] = o.err_true; errs[2] = o.seconds_loop; errs[3] = o.seconds_call;
+            return rc;
+        }
+    }
+    return -2;
+}
+
+/* The instantiated (krylov, precond, degree, maxit) combinations, 4 ints each. */
+int ref_table(int* out, int cap)
+{
+    const int n = (int)(sizeof(kTable) / sizeof(kTable[0]));
+    for (int i = 0; i < n && i < cap; i++) {
+        out[4 * i] = kTable[i].krylov; out[4 * i + 1] = kTable[i].precond;
+        out[4 * i + 2] = kTable[i].degree; out[4 * i + 3] = kTable[i].maxit;
+    }
+    return n;
+}
+
+/* setProblem through the reference's own IterativeSolverBase
+ * (iterativeSolverBase.hpp:51-55), for checking the built-in problem set-up. */
+int ref_set_problem(const int* np, const double* ds, const double* origin, const int* bcs, int problem,
+                    double* x, double* b)
+{
+    ppsOracleProblem = problem;
+    const std::array<int, 3> nranks = {1, 1, 1};
+    const std::array<int, 3> npg = {np[0], np[1], np[2]};
+    const std::array<T_data, 3> d = {ds[0], ds[1], ds[2]};
+    const std::array<T_data, 3> o = {origin[0], origin[1], origin[2]};
+    const std::array<int, 3> guards = {1, 1, 1};
+    const std::array<int, 6> bc = {bcs[0], bcs[1], bcs[2], bcs[3], bcs[4], bcs[5]};
+    const std::array<T_data, 6> bcsValue = {0, 0, 0, 0, 0, 0};
+    BlockGrid<3, T_data> grid(nranks, 0, npg, d, o, guards, bc, bcsValue);
+    CommunicatorMPI<3, T_data> comm(grid);
+    ExactSolutionAndBCs<3, T_data> exact;
+    NoneP s(grid, exact, comm);
+    s.setProblem(x, b);
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+/*
+ * Project-written configuration header for compiling the reference CPU solver
+ * into the test oracle (oracle/_ref).  It plays the role of the reference's
+ * include/solverSetup.hpp (the reference's documented configuration mechanism is
+ * to edit that file and recompile): it defines that header's include guard so the
+ * reference's own copy is skipped, and provides the same names.
+ *
+ * Values that the reference fixes as constexpr but only uses as ordinary values
+ * (tolerance scale, Chebyshev epsilon and eigenvalue rescaling) are runtime
+ * variables here so one build serves every test configuration; ref_driver.cpp
+ * sets them before constructing a solver.  Names used in `if constexpr` stay
+ * constexpr with the reference's values (solverSetup.hpp:75, 79).
+ */
+#ifndef PPS_ORACLE_REF_SETUP_HPP
+#define PPS_ORACLE_REF_SETUP_HPP
+#define SOLVERSETUP_HPP 1   /* skip the reference's solverSetup.hpp body */
+
+#include <mpi.h>
+#include <cmath>
+
+using T_data = double;
+
+template <typename T>
+inline MPI_Datatype getMPIType();
+template <>
+inline MPI_Datatype getMPIType<float>() { return MPI_FLOAT; }
+template <>
+inline MPI_Datatype getMPIType<double>() { return MPI_DOUBLE; }
+
+constexpr T_data PI = 3.141592653589793;
+inline T_data tollScalingFactor = 1e-10;
+constexpr int orderNeumanBcs = 2;
+constexpr bool trackErrorFromIterationHistory = true;
+inline T_data epsilon = 1e-4;
+inline T_data rescaleEigMin = 500;
+inline T_data rescaleEigMax = 1 - 1e-4;
+
+/* Which built-in manufactured problem ExactSolutionAndBCs evaluates:
+ * 0 = the reference default (solverSetup.hpp:98-160), 1 = the sine product. */
+inline int ppsOracleProblem = 0;
+
+template <int DIM, typename T>
+class ExactSolutionAndBCs {
+public:
+    inline T setFieldB(const T x, const T y, const T z) const
+    {
+        if (ppsOracleProblem == 0) return -sin(x) - cos(y) - 3 * sin(z) + 2 * y * z + 2;
+        return -3 * PI * PI * sin(PI * x) * sin(PI * y) * sin(PI * z);
+    }
+    inline T trueSolutionFxyz(const T x, const T y, const T z) const
+    {
+        if (ppsOracleProblem == 0) return sin(x) + cos(y) + 3 * sin(z) + x * x * y * z + x * x + 10;
+        return sin(PI * x) * sin(PI * y) * sin(PI * z);
+    }
+    inline T trueSolutionDdir(const T x, const T y, const T z, const int dir) const
+    {
+        if (ppsOracleProblem == 0) {
+            if (dir == 0) return cos(x) + 2 * x * y * z + 2 * x;
+            if (dir == 1) return -sin(y) + x * x * z;
+            if (dir == 2) return 3 * cos(z) + x * x * y;
+            return -100;
+        }
+        if (dir == 0) return PI * cos(PI * x) * sin(PI * y) * sin(PI * z);
+        if (dir == 1) return PI * sin(PI * x) * cos(PI * y) * sin(PI * z);
+        if (dir == 2) return PI * sin(PI * x) * sin(PI * y) * cos(PI * z);
+        return -100;
+    }
+};
+
+#endif
