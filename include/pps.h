@@ -1,0 +1,175 @@
+/*
+ * pps.h -- C ABI of libpps, the GB300-native (sm_103a) Poisson solve loop.
+ *
+ * libpps is a drop-in for the solve path of lucak17/ParallelPoissonSolver
+ * (solverPoissonMPI_CPU / solverPoissonMPI_alpaka): a right-preconditioned
+ * BiCGSTAB (or CG) with a Chebyshev-polynomial preconditioner on the 7-point
+ * Laplacian, Dirichlet/Neumann boundary handling and Krylov reductions, on one
+ * GPU as a single domain.  The reference has no C ABI: its boundary is the
+ * solver-class protocol composed in include/inputParam.hpp:24-38.  Each entry
+ * point below names the reference member it replaces.  include/pps_solver.hpp
+ * wraps this ABI back into that class protocol.
+ *
+ * Conventions
+ *   - Fields are caller-owned arrays of (n0+2)(n1+2)(n2+2) doubles, x fastest,
+ *     where n_d = npglobal_d counts the boundary nodes and one guard layer pads
+ *     each side (iterativeSolverBase.hpp:34-35; CPU/src/main.cpp:86-89).
+ *   - The equation is A u = b with A the positive-sign 7-point Laplacian
+ *     (matrixFreeOperatorA.hpp:22-39): for -lap u = f pass b = -f.
+ *   - Every call returns a pps_status; nothing calls exit() (the reference exits
+ *     on a bad configuration, CPU/src/main.cpp:51-55).
+ *   - One solver handle owns one CUDA stream and its device buffers; a handle is
+ *     not thread-safe, distinct handles are independent.
+ */
+#ifndef PPS_H
+#define PPS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPS_ABI_VERSION 1
+
+typedef enum {
+    PPS_OK = 0,
+    PPS_NOT_CONVERGED = 1,      /* stopped at maxit; the reference stops silently       */
+    PPS_BREAKDOWN = 2,          /* a Krylov denominator became zero or non-finite        */
+    PPS_NAN_DETECTED = 3,       /* the residual norm became NaN/Inf                      */
+    PPS_TIMEOUT = 4,            /* a bounded device-side wait gave up                    */
+    PPS_ERR_INVALID_ARG = -1,
+    PPS_ERR_CUDA = -2,
+    PPS_ERR_OUT_OF_MEMORY = -3,
+    PPS_ERR_ZERO_RHS = -4,      /* ||b_adj|| == 0: the normalisation divides by zero     */
+    PPS_ERR_UNSUPPORTED = -5,
+    PPS_ERR_NO_DEVICE = -6
+} pps_status;
+
+/* BlockGrid at one rank (blockGrid.hpp:15-36): npglobal, ds, origin, bcsType. */
+typedef struct {
+    int npglobal[3];            /* grid points per axis, boundary nodes included (>= 3)  */
+    double ds[3];               /* spacing                                                */
+    double origin[3];           /* coordinate of the first data node                     */
+    int bcs[6];                 /* x- x+ y- y+ z- z+ : 0 Dirichlet, 1 Neumann            */
+} pps_grid;
+
+typedef enum { PPS_KRYLOV_BICGSTAB = 0, PPS_KRYLOV_CG = 1 } pps_krylov;
+typedef enum { PPS_PREC_NONE = 0, PPS_PREC_CHEBYSHEV = 1 } pps_precond;
+
+typedef enum {
+    /* FP64 with the reference's expression order and serial reductions: results are
+     * bit-identical to the reference CPU solver at one rank. Slow; for validation. */
+    PPS_FORM_PARITY_FP64 = 0,
+    /* Plain FP64: fused kernels, deterministic tree reductions, scalars on device. */
+    PPS_FORM_FP64 = 1,
+    /* FP32 stencil, smoother and Krylov vectors with FP64-accurate inner products,
+     * wrapped in FP64 iterative refinement on the FP64 true residual. */
+    PPS_FORM_MIXED = 2
+} pps_form;
+
+/* Compile-time parameters of the reference, made runtime (solverSetup.hpp:22-40,
+ * inputParam.hpp:24-38; alpaka preset ALP/include/solverSetup.hpp:52-72). */
+typedef struct {
+    int krylov;                 /* pps_krylov (T_Solver)                                   */
+    int precond;                /* pps_precond (T_Preconditioner)                          */
+    int cheb_degree;            /* chebyshevMax                                             */
+    double cheb_eps;            /* epsilon                                                  */
+    double rescale_min;         /* rescaleEigMin                                            */
+    double rescale_max;         /* rescaleEigMax                                            */
+    double tol;                 /* tolerance * tollScalingFactor (on ||r||/||b_adj||)       */
+    int maxit;                  /* maxIteration of the Krylov loop                          */
+    int form;                   /* pps_form                                                 */
+    double inner_tol;           /* MIXED: relative residual reduction per refinement        */
+    int inner_maxit;            /* MIXED: iteration cap of one inner solve                  */
+    int max_refinements;        /* MIXED: cap on outer refinement steps                     */
+    int check_every;            /* iterations between host polls of the device stop flag;
+                                   0 = automatic.  Results do not depend on it.             */
+    int use_graph;              /* replay the iteration as a CUDA graph (fast forms)        */
+    int device;                 /* CUDA device ordinal                                      */
+} pps_config;
+
+typedef enum { PPS_PRESET_CPU = 0, PPS_PRESET_ALPAKA = 1 } pps_preset;
+
+typedef struct {
+    int iterations;             /* getNumIterationFinal (MIXED: inner iterations, summed)   */
+    int refinements;            /* MIXED: outer refinement steps taken                      */
+    int precond_applications;
+    double err_iter;            /* getErrorFromIteration: recursive ||r||/||b_adj||         */
+    double err_true;            /* getErrorComputeOperator: true FP64 ||b-Ax||/||b_adj||   */
+    double norm_b;              /* ||b_adj|| over the unknowns                              */
+    double seconds_solve;       /* device time from set-up to the final residual           */
+    double seconds_total;       /* host wall time of the call                               */
+    double seconds_h2d;         /* host->device copies inside the call                      */
+    double seconds_d2h;
+    double hbm_bytes;           /* algorithmic bytes of every kernel the solve launched     */
+    int kernel_launches;        /* launches of libpps kernels inside the call               */
+    double sweep_seconds;       /* device time of the Chebyshev sweeps (event-timed)        */
+    int sweep_launches;         /* sweeps launched                                          */
+    double sweep_bytes;         /* algorithmic bytes of those sweeps                        */
+} pps_stats;
+
+typedef struct pps_solver pps_solver;
+
+/* Problem plugin, the ExactSolutionAndBCs class (solverSetup.hpp:94-161). */
+typedef struct {
+    double (*field_b)(double x, double y, double z, void* ctx);              /* setFieldB        */
+    double (*solution)(double x, double y, double z, void* ctx);             /* trueSolutionFxyz */
+    double (*solution_ddir)(double x, double y, double z, int dir, void* ctx); /* trueSolutionDdir */
+    void* ctx;
+} pps_problem;
+
+typedef enum { PPS_PROBLEM_REFERENCE_DEFAULT = 0, PPS_PROBLEM_SINE = 1 } pps_builtin_problem;
+
+/* Defaults of the reference presets: CPU (n=11, eps=1e-4, rescale 500, tol 1e-8,
+ * maxit 1700) or alpaka (n=24, eps=0, rescale 100, tol 1e-10, maxit 1000). */
+pps_status pps_config_default(pps_config* cfg, int preset);
+
+/* Solver constructor (BiCGSTAB.hpp:18-39 with the ChebyshevIteration member,
+ * chebyshevIteration.hpp:19-34): validates, computes the eigenvalue bounds
+ * (blockGrid.hpp:301-340) and allocates every device buffer. */
+pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** out);
+pps_status pps_destroy(pps_solver* s);
+
+/* setProblem (iterativeSolverBase.hpp:51-55): Dirichlet nodes of x from
+ * plugin->solution, b from plugin->field_b at every data node, and the Neumann
+ * face data from plugin->solution_ddir (kept in the solver for the solves). */
+pps_status pps_set_problem(pps_solver* s, const pps_problem* plugin, double* x, double* b);
+pps_status pps_set_problem_builtin(pps_solver* s, int builtin_problem, double* x, double* b);
+/* Neumann data of face f (2*dir+side) at its data nodes, lower remaining axis fastest. */
+pps_status pps_set_neumann(pps_solver* s, int face, const double* values);
+
+/* operator()(x, b, A) (BiCGSTAB.hpp:55-322, BiCGstabAlpaka.hpp:68-475): solves in
+ * place on host arrays; x is in/out (Dirichlet nodes hold the boundary values),
+ * b is input (PARITY form: scaled and unscaled in place exactly like the reference).
+ * Returns PPS_OK, PPS_NOT_CONVERGED, PPS_BREAKDOWN or an error. */
+pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats);
+/* The same with device pointers (fields already resident in HBM). */
+pps_status pps_solve_device(pps_solver* s, double* x_dev, double* b_dev, pps_stats* stats);
+
+/* Getters (iterativeSolverBase.hpp:410-425; iterativeSolverBaseAlpaka.hpp:599-640). */
+pps_status pps_get_stats(const pps_solver* s, pps_stats* stats);
+/* Residual history: entry 0 is the initial true residual, entry i the recursive
+ * residual after iteration i (errorFromIterationHistory_).  *count <= cap. */
+pps_status pps_get_history(const pps_solver* s, double* out, int cap, int* count);
+/* residualHistory.txt writer (iterativeSolverBaseAlpaka.hpp:620-638). */
+pps_status pps_write_residual_history(const pps_solver* s, const char* path);
+
+/* Building blocks, on host arrays of the field layout.
+ * out = A u at the unknowns (MatrixFreeOperatorA::operator(), FP64). */
+pps_status pps_apply_operator(pps_solver* s, const double* u, double* out);
+/* X = M^{-1} B: one preconditioner application (ChebyshevIteration::operator()
+ * in preconditioner mode, chebyshevIteration.hpp:48-140), in the solver's form. */
+pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
+
+/* Number of CUDA devices visible to the library (0 without a GPU). */
+int pps_device_count(void);
+const char* pps_status_string(pps_status st);
+/* Message of the last error on this thread ("" if none). */
+const char* pps_last_error(void);
+int pps_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -174,7 +174,8 @@ def ref_lib():
         dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
         L.ref_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, ip, dp, dp, ip, C.c_double, C.c_double,
-                                C.c_double, C.c_double, C.c_int, dp, dp, C.c_void_p, C.POINTER(C.c_int), dp]
+                                C.c_double, C.c_double, C.c_int, dp, dp, C.c_void_p, C.POINTER(C.c_int), dp,
+                                C.c_void_p]
         L.ref_solve.restype = C.c_int
         L.ref_set_problem.argtypes = [ip, dp, dp, ip, C.c_int, dp, dp]
         L.ref_table.argtypes = [ip, C.c_int]
@@ -225,17 +226,21 @@ def solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, neumann=None) -
                   hist[: st.iterations + 1].copy())
 
 
-def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: int = 0) -> Result:
-    """The reference's own classes, in place on x and b.  `problem` selects the
-    built-in function the reference plugin evaluates for Neumann data."""
+def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: int = 0, neumann=None) -> Result:
+    """The reference's own classes, in place on x and b.  The reference plugin
+    evaluates Neumann data from built-in problem `problem`, or looks it up in the
+    face arrays `neumann` when they are given."""
     L = ref_lib()
     hist = np.full(cfg.maxit + 1, -1.0)
     it = C.c_int(0)
     errs = np.zeros(4)
+    ptrs, keep = _neumann_ptrs(grid, neumann)
+    if neumann is not None:
+        problem = 2
     rc = L.ref_solve(cfg.krylov, cfg.precond, cfg.cheb_degree, cfg.maxit, np.array(grid.np, np.int32),
                      np.array(grid.ds, np.float64), np.array(grid.origin, np.float64), np.array(grid.bcs, np.int32),
                      cfg.tol, cfg.cheb_eps, cfg.rescale_min, cfg.rescale_max, problem, x, b, hist.ctypes.data,
-                     C.byref(it), errs)
+                     C.byref(it), errs, ptrs)
     if rc == -2:
         raise KeyError("combination not instantiated in oracle/_ref")
     n = it.value

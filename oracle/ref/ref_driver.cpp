@@ -65,6 +65,11 @@ int run(const RefArgs* a, double* x, double* b, double* hist, RefOut* out)
     rescaleEigMin = a->rescale_min;
     rescaleEigMax = a->rescale_max;
     ppsOracleProblem = a->problem;
+    for (int q = 0; q < 3; q++) {
+        ppsOracleNp[q] = a->np[q];
+        ppsOracleDs[q] = a->ds[q];
+        ppsOracleOrigin[q] = a->origin[q];
+    }
 
     const std::array<int, 3> nranks = {1, 1, 1};
     const std::array<int, 3> npg = {a->np[0], a->np[1], a->np[2]};
@@ -127,13 +132,15 @@ const Entry kTable[] = {
 
 extern "C" {
 
-/* Solve in place with the reference's classes.  Returns 0, or -2 when the
- * (krylov, precond, degree, maxit) combination was not instantiated. */
+/* Solve in place with the reference's classes.  `problem` selects what the
+ * plugin evaluates for Neumann data (2: the tabulated `faces`).  Returns 0, or -2
+ * when the (krylov, precond, degree, maxit) combination was not instantiated. */
 int ref_solve(int krylov, int precond, int degree, int maxit, const int* np, const double* ds,
               const double* origin, const int* bcs, double tol, double eps, double rescale_min,
               double rescale_max, int problem, double* x, double* b, double* hist, int* iterations,
-              double* errs /* err_iter, err_true, seconds_loop, seconds_call */)
+              double* errs /* err_iter, err_true, seconds_loop, seconds_call */, const double* const* faces)
 {
+    for (int f = 0; f < 6; f++) ppsOracleFaces[f] = faces ? faces[f] : nullptr;
     RefArgs a;
     for (int d = 0; d < 3; d++) { a.np[d] = np[d]; a.ds[d] = ds[d]; a.origin[d] = origin[d]; }
     for (int f = 0; f < 6; f++) a.bcs[f] = bcs[f];

@@ -35,9 +35,30 @@ inline T_data epsilon = 1e-4;
 inline T_data rescaleEigMin = 500;
 inline T_data rescaleEigMax = 1 - 1e-4;
 
-/* Which built-in manufactured problem ExactSolutionAndBCs evaluates:
- * 0 = the reference default (solverSetup.hpp:98-160), 1 = the sine product. */
+/* Which problem ExactSolutionAndBCs evaluates: 0 = the reference default
+ * (solverSetup.hpp:98-160), 1 = the sine product, 2 = tabulated Neumann data
+ * (trueSolutionDdir looks the value up in ppsOracleFaces by the node's indices). */
 inline int ppsOracleProblem = 0;
+inline const double* ppsOracleFaces[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+inline int ppsOracleNp[3] = {0, 0, 0};
+inline double ppsOracleDs[3] = {1, 1, 1};
+inline double ppsOracleOrigin[3] = {0, 0, 0};
+
+/* Data-node index (1..n) of a coordinate x = origin + (i-1)*ds. */
+inline int ppsOracleIndex(double x, int d)
+{
+    return 1 + (int)std::lround((x - ppsOracleOrigin[d]) / ppsOracleDs[d]);
+}
+
+inline double ppsOracleTabulated(double x, double y, double z, int dir)
+{
+    const int idx[3] = {ppsOracleIndex(x, 0), ppsOracleIndex(y, 1), ppsOracleIndex(z, 2)};
+    const int side = idx[dir] == 1 ? 0 : 1;
+    const double* f = ppsOracleFaces[2 * dir + side];
+    if (!f) return 0.0;
+    const int a0 = dir == 0 ? 1 : 0, a1 = dir == 2 ? 1 : 2;
+    return f[(idx[a0] - 1) + (long)ppsOracleNp[a0] * (idx[a1] - 1)];
+}
 
 template <int DIM, typename T>
 class ExactSolutionAndBCs {
@@ -54,6 +75,7 @@ public:
     }
     inline T trueSolutionDdir(const T x, const T y, const T z, const int dir) const
     {
+        if (ppsOracleProblem == 2) return ppsOracleTabulated(x, y, z, dir);
         if (ppsOracleProblem == 0) {
             if (dir == 0) return cos(x) + 2 * x * y * z + 2 * x;
             if (dir == 1) return -sin(y) + x * x * z;

@@ -1,0 +1,354 @@
+"""parallelpoissonsolver_gb300 -- GB300-native Poisson solve loop (host-side mirror).
+
+The compute path is ``libpps.so`` (hand-written sm_103a CUDA behind the C ABI in
+``include/pps.h``).  This module binds that ABI with ctypes and mirrors the
+reference's solver-class protocol (solverPoissonMPI_CPU/include/inputParam.hpp:24-38):
+
+    grid   = BlockGrid(npglobal=(66, 66, 66), ds=(1/65,)*3)
+    solver = BiCGSTAB(grid, ChebyshevIteration(degree=11), tolerance=1e-10, max_iteration=1700)
+    x, b   = grid.new_field(), grid.new_field()
+    solver.set_problem(x, b)          # setProblem  (iterativeSolverBase.hpp:51-55)
+    solver(x, b)                      # operator()  (BiCGSTAB.hpp:55-322)
+    solver.get_num_iteration_final()  # getters     (iterativeSolverBase.hpp:410-425)
+
+There is no CPU fallback: if libpps.so is missing or no GPU is visible, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpps.so")
+
+OK, NOT_CONVERGED, BREAKDOWN, NAN_DETECTED, TIMEOUT = 0, 1, 2, 3, 4
+ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_ZERO_RHS, ERR_UNSUPPORTED, ERR_NO_DEVICE = -1, -2, -3, -4, -5, -6
+KRYLOV_BICGSTAB, KRYLOV_CG = 0, 1
+PREC_NONE, PREC_CHEBYSHEV = 0, 1
+FORM_PARITY_FP64, FORM_FP64, FORM_MIXED = 0, 1, 2
+FORMS = {"parity": FORM_PARITY_FP64, "fp64": FORM_FP64, "mixed": FORM_MIXED}
+PRESET_CPU, PRESET_ALPAKA = 0, 1
+PROBLEM_REFERENCE_DEFAULT, PROBLEM_SINE = 0, 1
+
+# Every symbol include/pps.h declares.
+EXPORTED = [
+    "pps_config_default", "pps_create", "pps_destroy", "pps_set_problem", "pps_set_problem_builtin",
+    "pps_set_neumann", "pps_solve", "pps_solve_device", "pps_get_stats", "pps_get_history",
+    "pps_write_residual_history", "pps_apply_operator", "pps_apply_preconditioner", "pps_device_count",
+    "pps_status_string", "pps_last_error", "pps_abi_version",
+]
+
+
+class PpsGrid(C.Structure):
+    _fields_ = [("npglobal", C.c_int * 3), ("ds", C.c_double * 3), ("origin", C.c_double * 3),
+                ("bcs", C.c_int * 6)]
+
+
+class PpsConfig(C.Structure):
+    _fields_ = [("krylov", C.c_int), ("precond", C.c_int), ("cheb_degree", C.c_int), ("cheb_eps", C.c_double),
+                ("rescale_min", C.c_double), ("rescale_max", C.c_double), ("tol", C.c_double),
+                ("maxit", C.c_int), ("form", C.c_int), ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
+                ("max_refinements", C.c_int), ("check_every", C.c_int), ("use_graph", C.c_int),
+                ("device", C.c_int)]
+
+
+class PpsStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("refinements", C.c_int), ("precond_applications", C.c_int),
+                ("err_iter", C.c_double), ("err_true", C.c_double), ("norm_b", C.c_double),
+                ("seconds_solve", C.c_double), ("seconds_total", C.c_double), ("seconds_h2d", C.c_double),
+                ("seconds_d2h", C.c_double), ("hbm_bytes", C.c_double), ("kernel_launches", C.c_int),
+                ("sweep_seconds", C.c_double), ("sweep_launches", C.c_int), ("sweep_bytes", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PpsError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        msg = f"{where}: {status_string(status)}"
+        detail = last_error()
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load libpps.so (raises if it is missing: there is no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build as _b
+            _b.build()
+        else:
+            raise FileNotFoundError(f"{LIB_PATH} is not built; run parallelpoissonsolver_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.pps_config_default.argtypes = [C.POINTER(PpsConfig), C.c_int]
+    L.pps_create.argtypes = [C.POINTER(PpsGrid), C.POINTER(PpsConfig), C.POINTER(vp)]
+    L.pps_destroy.argtypes = [vp]
+    L.pps_set_problem_builtin.argtypes = [vp, C.c_int, vp, vp]
+    L.pps_set_neumann.argtypes = [vp, C.c_int, vp]
+    L.pps_solve.argtypes = [vp, vp, vp, C.POINTER(PpsStats)]
+    L.pps_solve_device.argtypes = [vp, vp, vp, C.POINTER(PpsStats)]
+    L.pps_get_stats.argtypes = [vp, C.POINTER(PpsStats)]
+    L.pps_get_history.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
+    L.pps_write_residual_history.argtypes = [vp, C.c_char_p]
+    L.pps_apply_operator.argtypes = [vp, vp, vp]
+    L.pps_apply_preconditioner.argtypes = [vp, vp, vp]
+    L.pps_status_string.restype = C.c_char_p
+    L.pps_status_string.argtypes = [C.c_int]
+    L.pps_last_error.restype = C.c_char_p
+    for name in EXPORTED:
+        fn = getattr(L, name)
+        if name not in ("pps_status_string", "pps_last_error"):
+            fn.restype = C.c_int
+    _lib = L
+    return L
+
+
+def status_string(st: int) -> str:
+    try:
+        return load().pps_status_string(st).decode()
+    except Exception:
+        return f"status {st}"
+
+
+def last_error() -> str:
+    try:
+        return load().pps_last_error().decode()
+    except Exception:
+        return ""
+
+
+def device_count() -> int:
+    return int(load().pps_device_count())
+
+
+@dataclass
+class BlockGrid:
+    """Single-rank BlockGrid (blockGrid.hpp:15-36): npglobal counts boundary nodes."""
+    npglobal: Sequence[int]
+    ds: Sequence[float]
+    origin: Sequence[float] = (0.0, 0.0, 0.0)
+    bcs: Sequence[int] = (0, 0, 0, 0, 0, 0)
+
+    @classmethod
+    def cube(cls, m: int, bcs=(0, 0, 0, 0, 0, 0)):
+        """Unit cube with m unknowns per axis (npglobal = m+2, ds = 1/(m+1))."""
+        h = 1.0 / (m + 1)
+        return cls(npglobal=(m + 2,) * 3, ds=(h,) * 3, bcs=tuple(bcs))
+
+    @property
+    def shape(self):
+        n = self.npglobal
+        return (n[2] + 2, n[1] + 2, n[0] + 2)
+
+    def new_field(self) -> np.ndarray:
+        return np.zeros(self.shape, np.float64)
+
+    def unknowns(self):
+        sl = []
+        for d in (2, 1, 0):
+            lo = 1 + (1 if self.bcs[2 * d] == 0 else 0)
+            hi = self.npglobal[d] + 1 - (1 if self.bcs[2 * d + 1] == 0 else 0)
+            sl.append(slice(lo, hi))
+        return tuple(sl)
+
+    def n_unknowns(self) -> int:
+        return int(np.prod([s.stop - s.start for s in self.unknowns()]))
+
+    def c(self) -> PpsGrid:
+        g = PpsGrid()
+        g.npglobal[:] = [int(v) for v in self.npglobal]
+        g.ds[:] = [float(v) for v in self.ds]
+        g.origin[:] = [float(v) for v in self.origin]
+        g.bcs[:] = [int(v) for v in self.bcs]
+        return g
+
+
+@dataclass
+class ChebyshevIteration:
+    """Chebyshev-polynomial preconditioner (chebyshevIteration.hpp:15-156)."""
+    degree: int = 11
+    epsilon: float = 1e-4
+    rescale_eig_min: float = 500.0
+    rescale_eig_max: float = 1.0 - 1e-4
+
+    @classmethod
+    def alpaka_preset(cls):
+        return cls(degree=24, epsilon=0.0, rescale_eig_min=100.0)
+
+
+@dataclass
+class NoneSolver:
+    """Identity preconditioner (noneSolver.hpp:15-27)."""
+
+
+def _ptr(a: np.ndarray) -> int:
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("fields must be C-contiguous float64 arrays")
+    return a.ctypes.data
+
+
+class Solver:
+    """One libpps solver handle (the reference's solver object)."""
+
+    krylov = KRYLOV_BICGSTAB
+
+    def __init__(self, grid: BlockGrid, preconditioner=None, tolerance: float = 1e-8, max_iteration: int = 1700,
+                 form: str | int = "fp64", inner_tol: float = 1e-4, inner_maxit: int = 100000,
+                 max_refinements: int = 12, check_every: int = 0, use_graph: bool = True, device: int = 0):
+        self.grid = grid
+        L = load()
+        cfg = PpsConfig()
+        L.pps_config_default(C.byref(cfg), PRESET_CPU)
+        if preconditioner is None:
+            preconditioner = ChebyshevIteration()
+        cfg.krylov = self.krylov
+        if isinstance(preconditioner, NoneSolver):
+            cfg.precond = PREC_NONE
+        else:
+            cfg.precond = PREC_CHEBYSHEV
+            cfg.cheb_degree = preconditioner.degree
+            cfg.cheb_eps = preconditioner.epsilon
+            cfg.rescale_min = preconditioner.rescale_eig_min
+            cfg.rescale_max = preconditioner.rescale_eig_max
+        cfg.tol = float(tolerance)
+        cfg.maxit = int(max_iteration)
+        cfg.form = FORMS[form] if isinstance(form, str) else int(form)
+        cfg.inner_tol = float(inner_tol)
+        cfg.inner_maxit = int(inner_maxit)
+        cfg.max_refinements = int(max_refinements)
+        cfg.check_every = int(check_every)
+        cfg.use_graph = 1 if use_graph else 0
+        cfg.device = int(device)
+        self.config = cfg
+        h = C.c_void_p()
+        st = L.pps_create(C.byref(grid.c()), C.byref(cfg), C.byref(h))
+        if st != OK:
+            raise PpsError(st, "pps_create")
+        self._h = h
+        self._stats = PpsStats()
+        self.last_status = OK
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pps_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # setProblem (iterativeSolverBase.hpp:51-55)
+    def set_problem(self, x: np.ndarray, b: np.ndarray, problem: int = PROBLEM_REFERENCE_DEFAULT):
+        st = load().pps_set_problem_builtin(self._h, problem, _ptr(x), _ptr(b))
+        if st != OK:
+            raise PpsError(st, "pps_set_problem_builtin")
+
+    def set_neumann(self, face: int, values: np.ndarray):
+        v = np.ascontiguousarray(values, np.float64)
+        st = load().pps_set_neumann(self._h, face, v.ctypes.data)
+        if st != OK:
+            raise PpsError(st, "pps_set_neumann")
+
+    # operator()(x, b, A) (BiCGSTAB.hpp:55-322)
+    def __call__(self, x: np.ndarray, b: np.ndarray, raise_on_error: bool = True) -> int:
+        assert x.shape == self.grid.shape and b.shape == self.grid.shape
+        st = load().pps_solve(self._h, _ptr(x), _ptr(b), C.byref(self._stats))
+        self.last_status = st
+        if st < 0 and raise_on_error:
+            raise PpsError(st, "pps_solve")
+        return st
+
+    solve = __call__
+
+    def solve_device(self, x_ptr: int, b_ptr: int, raise_on_error: bool = True) -> int:
+        st = load().pps_solve_device(self._h, C.c_void_p(x_ptr), C.c_void_p(b_ptr), C.byref(self._stats))
+        self.last_status = st
+        if st < 0 and raise_on_error:
+            raise PpsError(st, "pps_solve_device")
+        return st
+
+    # getters (iterativeSolverBase.hpp:410-425)
+    def stats(self) -> dict:
+        return self._stats.as_dict()
+
+    def get_num_iteration_final(self) -> int:
+        return self._stats.iterations
+
+    def get_error_from_iteration(self) -> float:
+        return self._stats.err_iter
+
+    def get_error_compute_operator(self) -> float:
+        return self._stats.err_true
+
+    def get_duration_solver(self) -> float:
+        return self._stats.seconds_solve
+
+    def history(self) -> np.ndarray:
+        n = C.c_int(0)
+        load().pps_get_history(self._h, None, 0, C.byref(n))
+        out = np.zeros(max(n.value, 1))
+        load().pps_get_history(self._h, out.ctypes.data, n.value, C.byref(n))
+        return out[: n.value]
+
+    def write_residual_history(self, path: str):
+        st = load().pps_write_residual_history(self._h, path.encode())
+        if st != OK:
+            raise PpsError(st, "pps_write_residual_history")
+
+    def apply_operator(self, u: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.zeros_like(u) if out is None else out
+        st = load().pps_apply_operator(self._h, _ptr(np.ascontiguousarray(u)), _ptr(out))
+        if st != OK:
+            raise PpsError(st, "pps_apply_operator")
+        return out
+
+    def apply_preconditioner(self, B: np.ndarray, X: Optional[np.ndarray] = None) -> np.ndarray:
+        X = np.zeros_like(B) if X is None else X
+        st = load().pps_apply_preconditioner(self._h, _ptr(np.ascontiguousarray(B)), _ptr(X))
+        if st != OK:
+            raise PpsError(st, "pps_apply_preconditioner")
+        return X
+
+
+class BiCGSTAB(Solver):
+    """Right-preconditioned BiCGSTAB main loop (BiCGSTAB.hpp:14-335)."""
+    krylov = KRYLOV_BICGSTAB
+
+
+class BaseCG(Solver):
+    """Preconditioned CG main loop (baseCG.hpp:14-269)."""
+    krylov = KRYLOV_CG
+
+
+def check_solution(grid: BlockGrid, x: np.ndarray, exact: np.ndarray):
+    """checkSolutionLocalGlobal (iterativeSolverBase.hpp:283-408) at one rank:
+    (block average |x-u|, point max |x-u|) over the data nodes."""
+    d = tuple(slice(1, n + 1) for n in (grid.npglobal[2], grid.npglobal[1], grid.npglobal[0]))
+    err = np.abs(x[d] - exact[d])
+    return float(err.sum() / err.size), float(err.max())

@@ -1,0 +1,163 @@
+// Internal declarations shared by the kernel and solver translation units of libpps.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pps {
+
+// Geometry of one single-rank grid in the guard-padded field layout
+// (iterativeSolverBase.hpp:34-35): index = i + sj*j + sk*k with
+// 0 <= i < n0+2 etc.; data nodes are 1..n, unknowns lo..hi-1 (blockGrid.hpp:184-222).
+struct Geo {
+    int n[3];
+    int lo[3], hi[3];
+    long long sj, sk, ntot;
+    double ds[3];
+    int bcs[6];
+};
+
+// Launch shape of the z-marching kernels: tiles of (32 x ty) columns in (i, j),
+// each thread walks kchunk planes along k.
+struct Shape {
+    int ty;
+    int ntx, nty, nchunks, kchunk;
+    unsigned nblocks() const { return (unsigned)ntx * (unsigned)nty * (unsigned)nchunks; }
+};
+
+// Device-resident Krylov scalars: the recurrences run on the device so an
+// iteration needs no host round trip (the alpaka reference copies scalars to the
+// host three times per iteration, BiCGstabAlpaka.hpp:254-255,343-344,395-396).
+struct DevState {
+    double rho0;      // rho_k (BiCGSTAB.hpp:127,259) or r.z (CG)
+    double alpha, omega, beta;
+    double err;       // recursive residual norm (unscaled system)
+    double err0;      // initial true residual norm of this (inner) solve
+    double tol_abs;   // stop when err < tol_abs
+    double hist_scale;// history entries are err * hist_scale (1/||b_adj||)
+    double normb;     // ||b_adj||
+    double sums[4];   // raw reduction results of the last reduction kernel
+    int iter;         // iterations completed
+    int maxit;
+    int done;         // 1: converged / stopped; every iteration kernel then returns at once
+    int status;       // pps_status of the stop
+    int rho0_from_r;  // 1: rho0 = <r0,r0> at start (inner solves); 0: rho0 = normb^2
+    int tol_relative; // 1: refinement inner solve: stop at tol_abs, else reduce by max(tol_rel, 0.3*tol_abs/err0)
+    double tol_rel;
+    int hist_cap;
+    int pad_;
+};
+
+enum FinKind : int {
+    FIN_NONE = 0,
+    FIN_NORMB = 1,      // normb = sqrt(sum0)
+    FIN_RES0 = 2,       // initial residual: err0, hist[0], rho0, early stop
+    FIN_ALPHA = 3,      // BiCGSTAB alpha = rho0 / sum0
+    FIN_OMEGA = 4,      // BiCGSTAB omega = sum0 / sum1
+    FIN_CONV = 5,       // BiCGSTAB err, beta, rho0 update, iteration count, stop test
+    FIN_CG_ALPHA = 6,   // CG alpha = rz / pAp
+    FIN_CG_CONV = 7,    // CG beta = rz_new / rz, err, stop test
+    FIN_STORE = 8       // only store sums[] (used by tests and true residuals)
+};
+
+struct RedCtx {
+    double* partials;   // nblocks * 4 doubles
+    unsigned* counter;  // zero between launches; the last block resets it
+    DevState* st;
+    double* hist;
+    int kind;
+};
+
+// Chebyshev coefficients of one sweep in pre-folded form (the alpaka kernels fold
+// the same way, kernelsAlpakaChebyshev.hpp:147-152,234-241):
+//   out = cc*u + cx*(u[i-1]+u[i+1]) + cy*(...) + cz*(...) + cb*B + cw*Z
+struct Coef {
+    double cc, cx, cy, cz, cb, cw, scale;
+};
+
+// Neumann face data on the device: values of du/d(dir) per face (NULL if none).
+struct Faces {
+    const double* g[6];
+};
+
+// ---- launch wrappers (pps_kernels.cu) ----
+Shape make_shape(const Geo& g, int ty, int target_blocks);
+
+// Parity (bit-exact FP64) kernels.
+void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s);
+void par_residual(const Geo& g, const double* x, const double* b, double* r, cudaStream_t s);
+void par_adjust_b(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s);
+void par_cheb_s01(const Geo& g, const double* B, double* Y, double* Z, double theta, double t2rd, cudaStream_t s);
+void par_cheb_sweep(const Geo& g, const double* Y, const double* B, const double* Z, double* W, double rc,
+                    double two_sigma, double two_over_delta, double ro, cudaStream_t s);
+void par_neg(const Geo& g, const double* W, double* X, cudaStream_t s);
+void par_axpy(const Geo& g, double* r, const double* v, double a, cudaStream_t s);
+void par_update_x_all(const Geo& g, double* x, const double* Mp, const double* z, double a, double w, cudaStream_t s);
+void par_update_x(const Geo& g, double* x, const double* p, double a, cudaStream_t s);
+void par_update_p(const Geo& g, double* p, const double* r, const double* AMp, double beta, double omega, cudaStream_t s);
+void par_update_p_cg(const Geo& g, double* p, const double* z, double beta, cudaStream_t s);
+void par_scale_all(const Geo& g, double* x, double* b, double v, int divide, cudaStream_t s);
+void seq_dot2(const Geo& g, const double* a1, const double* b1, const double* a2, const double* b2, double* out,
+              cudaStream_t s);
+
+// Neumann ghost fill (iterativeSolverBase.hpp:62-169): field_mode adds the flux term.
+template <typename T>
+void neumann_fill(const Geo& g, T* field, Faces f, int field_mode, double normb, cudaStream_t s);
+
+// Fast kernels, T = float or double storage.
+template <typename T>
+void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, T* Z, const Coef& cy, double inv_theta,
+                   int mode, const int* done, cudaStream_t s);
+template <typename T>
+void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& c,
+                     const int* done, cudaStream_t s);
+template <typename T>
+void fast_scale_copy(const Geo& g, const Shape& sh, const T* B, T* X, double a, const int* done, cudaStream_t s);
+template <typename T>
+void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T* Au, const Coef& a,
+                      RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T* Au, const Coef& a,
+                       RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_axpy_alpha(const Geo& g, const Shape& sh, T* r, const T* v, const DevState* st, cudaStream_t s);
+template <typename T>
+void fast_update_xr(const Geo& g, const Shape& sh, T* x, const T* Mp, const T* z, T* r, const T* Az,
+                    const T* r0, RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_update_p(const Geo& g, const Shape& sh, T* p, const T* r, const T* AMp, const DevState* st,
+                   cudaStream_t s);
+// CG pieces (baseCG.hpp:115-228).
+template <typename T>
+void fast_cg_stencil_dot(const Geo& g, const Shape& sh, const T* p, const T* r, const T* z, T* Ap,
+                         const Coef& a, RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_cg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+                       cudaStream_t s);
+template <typename T>
+void fast_cg_dot_rz(const Geo& g, const Shape& sh, const T* r, const T* z, RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const DevState* st, cudaStream_t s);
+
+// FP64 true residual r = b - A x written as TR (also into r0 and p when given),
+// with sum r^2 in FP64.
+template <typename TR>
+void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
+                   const Coef& a, RedCtx rc, cudaStream_t s);
+// ||b_adj||^2 over the unknowns, b_adj formed on the fly (FP64).
+void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
+                    cudaStream_t s);
+// x += scale * e at the unknowns (FP64 += FP32).
+void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState* st,
+                         cudaStream_t s);
+template <typename T>
+void fill_field(T* p, long long n, T v, cudaStream_t s);
+// Scalar state helpers.
+void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
+                int rho0_from_r, double hist_scale, int hist_cap, cudaStream_t s);
+
+int launches_counter_reset();
+int launches_counter();
+void launches_counter_add(int d);
+
+}  // namespace pps

@@ -1,0 +1,1200 @@
+// CUDA kernels of libpps for sm_103a (GB300).
+//
+// Two families:
+//   * par_*  : the reference's FP64 arithmetic in its exact operand order, every
+//              operation an explicitly rounded intrinsic (no FMA contraction), so
+//              results are bit-identical to the reference CPU solver.  Reductions
+//              are serial sums in the reference's k,j,i loop order (seq_dot2).
+//   * fast_* : z-marching stencil kernels with pre-folded coefficients and FMA,
+//              templated on the storage type (double, or float for the mixed form),
+//              fused with their dot products.  Reductions are deterministic: a fixed
+//              shuffle tree per block, block partials in global memory, and the last
+//              block to finish sums the partials in block order and advances the
+//              Krylov scalars on the device (no host round trip).
+#include "pps_internal.h"
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace pps {
+
+static int g_launches = 0;
+int launches_counter_reset() { int v = g_launches; g_launches = 0; return v; }
+int launches_counter() { return g_launches; }
+void launches_counter_add(int d) { g_launches += d; }
+#define PPS_COUNT_LAUNCH() (++g_launches)
+
+// ---------------------------------------------------------------------------
+// Parity kernels (FP64, exact reference expression order)
+// ---------------------------------------------------------------------------
+
+struct Lin {
+    int ux, uy, uz;
+    long long n;
+};
+
+__host__ __device__ inline Lin unknown_box(const Geo& g)
+{
+    Lin L;
+    L.ux = g.hi[0] - g.lo[0];
+    L.uy = g.hi[1] - g.lo[1];
+    L.uz = g.hi[2] - g.lo[2];
+    L.n = (long long)L.ux * L.uy * L.uz;
+    return L;
+}
+
+__device__ __forceinline__ long long lin_to_index(const Geo& g, const Lin& L, long long t)
+{
+    const int i = g.lo[0] + (int)(t % L.ux);
+    const long long q = t / L.ux;
+    const int j = g.lo[1] + (int)(q % L.uy);
+    const int k = g.lo[2] + (int)(q / L.uy);
+    return i + g.sj * j + g.sk * k;
+}
+
+// (d[c-1] - 2*d[c] + d[c+1])/(h0*h0) + ... (matrixFreeOperatorA.hpp:34-38)
+__device__ __forceinline__ double opA_exact(const double* __restrict__ d, long long c, long long sj, long long sk,
+                                            double h2x, double h2y, double h2z)
+{
+    const double two_c = __dmul_rn(2.0, d[c]);
+    const double tx = __ddiv_rn(__dadd_rn(__dsub_rn(d[c - 1], two_c), d[c + 1]), h2x);
+    const double ty = __ddiv_rn(__dadd_rn(__dsub_rn(d[c - sj], two_c), d[c + sj]), h2y);
+    const double tz = __ddiv_rn(__dadd_rn(__dsub_rn(d[c - sk], two_c), d[c + sk]), h2z);
+    return __dadd_rn(__dadd_rn(tx, ty), tz);
+}
+
+#define PAR_LOOP(g, L)                                                                          \
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < L.n;             \
+         t += (long long)gridDim.x * blockDim.x)
+
+static inline unsigned par_blocks(long long n)
+{
+    long long b = (n + 255) / 256;
+    if (b > 152LL * 64) b = 152LL * 64;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+__global__ void k_par_stencil(Geo g, const double* __restrict__ u, double* __restrict__ out, double h2x,
+                              double h2y, double h2z)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        out[c] = opA_exact(u, c, g.sj, g.sk, h2x, h2y, h2z);
+    }
+}
+
+__global__ void k_par_residual(Geo g, const double* __restrict__ x, const double* __restrict__ b,
+                               double* __restrict__ r, double h2x, double h2y, double h2z)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        r[c] = __dsub_rn(b[c], opA_exact(x, c, g.sj, g.sk, h2x, h2y, h2z));
+    }
+}
+
+// b_adj at the unknowns (adjustFieldBForDirichletNeumanBCs, iterativeSolverBase.hpp:429-534):
+// the same subtractions/additions applied to one point in the reference's face order.
+__device__ __forceinline__ double badj_exact(const Geo& g, const double* __restrict__ b,
+                                             const double* __restrict__ x, const Faces& f, long long c, int i,
+                                             int j, int k)
+{
+    double v = b[c];
+    const int idx[3] = {i, j, k};
+    const long long step[3] = {1, g.sj, g.sk};
+    for (int d = 0; d < 3; d++) {
+        const double h2 = __dmul_rn(g.ds[d], g.ds[d]);
+        // low face
+        if (g.bcs[2 * d] == 0) {
+            if (idx[d] == 2) v = __dsub_rn(v, __ddiv_rn(x[c - step[d]], h2));
+        } else if (idx[d] == 1 && f.g[2 * d]) {
+            long long fi;
+            if (d == 0) fi = (long long)(j - 1) + (long long)g.n[1] * (k - 1);
+            else if (d == 1) fi = (long long)(i - 1) + (long long)g.n[0] * (k - 1);
+            else fi = (long long)(i - 1) + (long long)g.n[0] * (j - 1);
+            v = __dadd_rn(v, __ddiv_rn(__dmul_rn(2.0, f.g[2 * d][fi]), g.ds[d]));
+        }
+        // high face
+        if (g.bcs[2 * d + 1] == 0) {
+            if (idx[d] == g.n[d] - 1) v = __dsub_rn(v, __ddiv_rn(x[c + step[d]], h2));
+        } else if (idx[d] == g.n[d] && f.g[2 * d + 1]) {
+            long long fi;
+            if (d == 0) fi = (long long)(j - 1) + (long long)g.n[1] * (k - 1);
+            else if (d == 1) fi = (long long)(i - 1) + (long long)g.n[0] * (k - 1);
+            else fi = (long long)(i - 1) + (long long)g.n[0] * (j - 1);
+            v = __dsub_rn(v, __ddiv_rn(__dmul_rn(2.0, f.g[2 * d + 1][fi]), g.ds[d]));
+        }
+    }
+    return v;
+}
+
+__global__ void k_par_adjust_b(Geo g, const double* __restrict__ b, const double* __restrict__ x, Faces f,
+                               double* __restrict__ bt)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const int i = g.lo[0] + (int)(t % L.ux);
+        const long long q = t / L.ux;
+        const int j = g.lo[1] + (int)(q % L.uy);
+        const int k = g.lo[2] + (int)(q / L.uy);
+        const long long c = i + g.sj * j + g.sk * k;
+        bt[c] = badj_exact(g, b, x, f, c, i, j, k);
+    }
+}
+
+// Z = B/theta; Y = 2*rho/delta * (2*B + A(B)/theta)   (chebyshevIteration.hpp:79-90)
+__global__ void k_par_cheb_s01(Geo g, const double* __restrict__ B, double* __restrict__ Y, double* __restrict__ Z,
+                               double theta, double t2rd, double h2x, double h2y, double h2z)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        Z[c] = __ddiv_rn(B[c], theta);
+        const double ab = opA_exact(B, c, g.sj, g.sk, h2x, h2y, h2z);
+        Y[c] = __dmul_rn(t2rd, __dadd_rn(__dmul_rn(2.0, B[c]), __ddiv_rn(ab, theta)));
+    }
+}
+
+// W = rho*(2*sigma*Y + 2/delta*(B + A(Y)) - rhoOld*Z)   (chebyshevIteration.hpp:110)
+__global__ void k_par_cheb_sweep(Geo g, const double* __restrict__ Y, const double* __restrict__ B,
+                                 const double* __restrict__ Z, double* __restrict__ W, double rc, double two_sigma,
+                                 double two_over_delta, double ro, double h2x, double h2y, double h2z)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        const double ay = opA_exact(Y, c, g.sj, g.sk, h2x, h2y, h2z);
+        const double t1 = __dmul_rn(two_sigma, Y[c]);
+        const double t2 = __dmul_rn(two_over_delta, __dadd_rn(B[c], ay));
+        W[c] = __dmul_rn(rc, __dsub_rn(__dadd_rn(t1, t2), __dmul_rn(ro, Z[c])));
+    }
+}
+
+__global__ void k_par_neg(Geo g, const double* __restrict__ W, double* __restrict__ X)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        X[c] = __dmul_rn(-1.0, W[c]);
+    }
+}
+
+__global__ void k_par_axpy(Geo g, double* __restrict__ r, const double* __restrict__ v, double a)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        r[c] = __dsub_rn(r[c], __dmul_rn(a, v[c]));
+    }
+}
+
+// x = x + a*Mp + w*z over every point of the field (BiCGSTAB.hpp:227-230)
+__global__ void k_par_update_x_all(long long n, double* __restrict__ x, const double* __restrict__ Mp,
+                                   const double* __restrict__ z, double a, double w)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        x[c] = __dadd_rn(__dadd_rn(x[c], __dmul_rn(a, Mp[c])), __dmul_rn(w, z[c]));
+}
+
+__global__ void k_par_update_x(Geo g, double* __restrict__ x, const double* __restrict__ p, double a)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        x[c] = __dadd_rn(x[c], __dmul_rn(a, p[c]));
+    }
+}
+
+// p = r + beta*(p - omega*AMp)   (BiCGSTAB.hpp:269)
+__global__ void k_par_update_p(Geo g, double* __restrict__ p, const double* __restrict__ r,
+                               const double* __restrict__ AMp, double beta, double omega)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        p[c] = __dadd_rn(r[c], __dmul_rn(beta, __dsub_rn(p[c], __dmul_rn(omega, AMp[c]))));
+    }
+}
+
+// p = z + beta*p   (baseCG.hpp:204)
+__global__ void k_par_update_p_cg(Geo g, double* __restrict__ p, const double* __restrict__ z, double beta)
+{
+    const Lin L = unknown_box(g);
+    PAR_LOOP(g, L)
+    {
+        const long long c = lin_to_index(g, L, t);
+        p[c] = __dadd_rn(z[c], __dmul_rn(beta, p[c]));
+    }
+}
+
+__global__ void k_par_scale_all(long long n, double* __restrict__ x, double* __restrict__ b, double v, int divide)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        if (divide) {
+            x[c] = __ddiv_rn(x[c], v);
+            b[c] = __ddiv_rn(b[c], v);
+        } else {
+            x[c] = __dmul_rn(x[c], v);
+            b[c] = __dmul_rn(b[c], v);
+        }
+    }
+}
+
+// Serial sums s1 = sum a1*b1, s2 = sum a2*b2 over the unknowns in k,j,i order.
+// One block: all threads form products of a chunk into shared memory, then one
+// thread adds them in order, exactly as the reference's loop does.
+constexpr int SEQ_THREADS = 512;
+constexpr int SEQ_CHUNK = 2048;
+
+__global__ void __launch_bounds__(SEQ_THREADS) k_seq_dot2(Geo g, const double* __restrict__ a1,
+                                                          const double* __restrict__ b1, const double* __restrict__ a2,
+                                                          const double* __restrict__ b2, double* __restrict__ out)
+{
+    __shared__ double p1[SEQ_CHUNK];
+    __shared__ double p2[SEQ_CHUNK];
+    const Lin L = unknown_box(g);
+    double s1 = 0.0, s2 = 0.0;
+    const bool two = (a2 != nullptr);
+    for (long long base = 0; base < L.n; base += SEQ_CHUNK) {
+        const int m = (int)((L.n - base) < SEQ_CHUNK ? (L.n - base) : SEQ_CHUNK);
+        for (int q = threadIdx.x; q < m; q += blockDim.x) {
+            const long long c = lin_to_index(g, L, base + q);
+            p1[q] = __dmul_rn(a1[c], b1[c]);
+            if (two) p2[q] = __dmul_rn(a2[c], b2[c]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (two) {
+                for (int q = 0; q < m; q++) {
+                    s1 = __dadd_rn(s1, p1[q]);
+                    s2 = __dadd_rn(s2, p2[q]);
+                }
+            } else {
+                for (int q = 0; q < m; q++) s1 = __dadd_rn(s1, p1[q]);
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = s1;
+        out[1] = s2;
+    }
+}
+
+void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s)
+{
+    k_par_stencil<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, u, out, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
+                                                                 g.ds[2] * g.ds[2]);
+    PPS_COUNT_LAUNCH();
+}
+void par_residual(const Geo& g, const double* x, const double* b, double* r, cudaStream_t s)
+{
+    k_par_residual<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, x, b, r, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
+                                                                  g.ds[2] * g.ds[2]);
+    PPS_COUNT_LAUNCH();
+}
+void par_adjust_b(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s)
+{
+    k_par_adjust_b<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, b, x, f, bt);
+    PPS_COUNT_LAUNCH();
+}
+void par_cheb_s01(const Geo& g, const double* B, double* Y, double* Z, double theta, double t2rd, cudaStream_t s)
+{
+    k_par_cheb_s01<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, B, Y, Z, theta, t2rd, g.ds[0] * g.ds[0],
+                                                                  g.ds[1] * g.ds[1], g.ds[2] * g.ds[2]);
+    PPS_COUNT_LAUNCH();
+}
+void par_cheb_sweep(const Geo& g, const double* Y, const double* B, const double* Z, double* W, double rc,
+                    double two_sigma, double two_over_delta, double ro, cudaStream_t s)
+{
+    k_par_cheb_sweep<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, Y, B, Z, W, rc, two_sigma, two_over_delta, ro,
+                                                                    g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
+                                                                    g.ds[2] * g.ds[2]);
+    PPS_COUNT_LAUNCH();
+}
+void par_neg(const Geo& g, const double* W, double* X, cudaStream_t s)
+{
+    k_par_neg<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, W, X);
+    PPS_COUNT_LAUNCH();
+}
+void par_axpy(const Geo& g, double* r, const double* v, double a, cudaStream_t s)
+{
+    k_par_axpy<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, r, v, a);
+    PPS_COUNT_LAUNCH();
+}
+void par_update_x_all(const Geo& g, double* x, const double* Mp, const double* z, double a, double w, cudaStream_t s)
+{
+    k_par_update_x_all<<<par_blocks(g.ntot), 256, 0, s>>>(g.ntot, x, Mp, z, a, w);
+    PPS_COUNT_LAUNCH();
+}
+void par_update_x(const Geo& g, double* x, const double* p, double a, cudaStream_t s)
+{
+    k_par_update_x<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, x, p, a);
+    PPS_COUNT_LAUNCH();
+}
+void par_update_p(const Geo& g, double* p, const double* r, const double* AMp, double beta, double omega, cudaStream_t s)
+{
+    k_par_update_p<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, p, r, AMp, beta, omega);
+    PPS_COUNT_LAUNCH();
+}
+void par_update_p_cg(const Geo& g, double* p, const double* z, double beta, cudaStream_t s)
+{
+    k_par_update_p_cg<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, p, z, beta);
+    PPS_COUNT_LAUNCH();
+}
+void par_scale_all(const Geo& g, double* x, double* b, double v, int divide, cudaStream_t s)
+{
+    k_par_scale_all<<<par_blocks(g.ntot), 256, 0, s>>>(g.ntot, x, b, v, divide);
+    PPS_COUNT_LAUNCH();
+}
+void seq_dot2(const Geo& g, const double* a1, const double* b1, const double* a2, const double* b2, double* out,
+              cudaStream_t s)
+{
+    k_seq_dot2<<<1, SEQ_THREADS, 0, s>>>(g, a1, b1, a2, b2, out);
+    PPS_COUNT_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// Neumann ghost fill (both families; the arithmetic matches the reference order)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void k_neumann_fill(Geo g, T* __restrict__ field, Faces f, int face, int field_mode, double normb)
+{
+    const int dir = face / 2, side = face % 2;
+    const int a0 = dir == 0 ? 1 : 0;          // first remaining axis
+    const int a1 = dir == 2 ? 1 : 2;          // second remaining axis
+    const int na = g.n[a0], nb = g.n[a1];
+    const long long step = dir == 0 ? 1 : (dir == 1 ? g.sj : g.sk);
+    const long long stride[3] = {1, g.sj, g.sk};
+    const long long total = (long long)na * nb;
+    const double* gf = f.g[face];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const int ia = 1 + (int)(t % na);
+        const int ib = 1 + (int)(t / na);
+        const int inode = side == 0 ? 1 : g.n[dir];
+        const long long c = inode * stride[dir] + ia * stride[a0] + ib * stride[a1];
+        const long long ghost = side == 0 ? c - step : c + step;
+        const long long mirror = side == 0 ? c + step : c - step;
+        if (field_mode) {
+            const double gv = gf ? gf[t] : 0.0;
+            const double term = __ddiv_rn(__dmul_rn(__dmul_rn(2.0, g.ds[dir]), gv), normb);
+            const double m = (double)field[mirror];
+            field[ghost] = (T)(side == 0 ? __dsub_rn(m, term) : __dadd_rn(m, term));
+        } else {
+            field[ghost] = field[mirror];
+        }
+    }
+}
+
+template <typename T>
+void neumann_fill(const Geo& g, T* field, Faces f, int field_mode, double normb, cudaStream_t s)
+{
+    for (int face = 0; face < 6; face++) {
+        if (g.bcs[face] != 1) continue;
+        const int dir = face / 2;
+        const long long total = (long long)g.n[dir == 0 ? 1 : 0] * g.n[dir == 2 ? 1 : 2];
+        unsigned blocks = (unsigned)((total + 255) / 256);
+        if (blocks > 1024) blocks = 1024;
+        k_neumann_fill<T><<<blocks, 256, 0, s>>>(g, field, f, face, field_mode, normb);
+        PPS_COUNT_LAUNCH();
+    }
+}
+template void neumann_fill<double>(const Geo&, double*, Faces, int, double, cudaStream_t);
+template void neumann_fill<float>(const Geo&, float*, Faces, int, double, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Fast kernels
+// ---------------------------------------------------------------------------
+
+Shape make_shape(const Geo& g, int ty, int target_blocks)
+{
+    Shape sh;
+    sh.ty = ty;
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
+    sh.ntx = (ux + 31) / 32;
+    sh.nty = (uy + ty - 1) / ty;
+    const long long tiles = (long long)sh.ntx * sh.nty;
+    long long chunks = (target_blocks + tiles - 1) / tiles;
+    if (chunks < 1) chunks = 1;
+    if (chunks > uz) chunks = uz;
+    sh.kchunk = (int)((uz + chunks - 1) / chunks);
+    sh.nchunks = (uz + sh.kchunk - 1) / sh.kchunk;
+    return sh;
+}
+
+// Fused multiply-add for either storage type.
+__device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+struct Col {
+    int i, j, k0, k1;
+    long long c;
+    bool active;
+};
+
+__device__ __forceinline__ Col column(const Geo& g, const Shape& sh)
+{
+    Col q;
+    const int bx = blockIdx.x % sh.ntx;
+    const int by = blockIdx.x / sh.ntx;
+    q.i = g.lo[0] + bx * 32 + threadIdx.x;
+    q.j = g.lo[1] + by * sh.ty + threadIdx.y;
+    q.k0 = g.lo[2] + blockIdx.y * sh.kchunk;
+    q.k1 = min(q.k0 + sh.kchunk, g.hi[2]);
+    q.active = q.i < g.hi[0] && q.j < g.hi[1];
+    q.c = q.i + g.sj * q.j + g.sk * q.k0;
+    return q;
+}
+
+static inline dim3 grid_of(const Shape& sh) { return dim3((unsigned)(sh.ntx * sh.nty), (unsigned)sh.nchunks, 1); }
+static inline dim3 block_of(const Shape& sh) { return dim3(32, (unsigned)sh.ty, 1); }
+
+// Accumulator of exact products: FP64 FMA for double data; for float data a
+// double-float pair (Dekker/Knuth error-free product and sum in FP32), so the
+// inner products of the mixed form are FP64-accurate without FP64 arithmetic
+// per point (GB300 runs FP64 at 1/64 of the FP32 rate).
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double a, double b) { s = fmx(a, b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float a, float b)
+    {
+        const float p = __fmul_rn(a, b);
+        const float e = __fmaf_rn(a, b, -p);
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(t, e));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ void finalize(const RedCtx& rc, const double* tot)
+{
+    DevState* st = rc.st;
+    for (int q = 0; q < 4; q++) st->sums[q] = tot[q];
+    switch (rc.kind) {
+    case FIN_NORMB:
+        st->normb = sqrt(tot[0]);
+        break;
+    case FIN_RES0: {
+        const double e0 = sqrt(tot[0]);
+        st->err0 = e0;
+        st->err = e0;
+        if (rc.hist && st->hist_cap > 0) rc.hist[0] = e0 * st->hist_scale;
+        st->rho0 = st->rho0_from_r ? tot[0] : st->normb * st->normb;
+        st->iter = 0;
+        if (!(e0 == e0) || isinf(e0)) {
+            st->status = 3;
+            st->done = 1;
+        } else if (e0 < st->tol_abs) {
+            st->status = 0;
+            st->done = 1;
+        } else {
+            st->done = 0;
+            st->status = 0;
+            // inner solve of a refinement step: reduce by tol_rel, or less if enough
+            if (st->tol_relative) st->tol_abs = fmax(st->tol_rel, 0.3 * st->tol_abs / e0) * e0;
+        }
+        break;
+    }
+    case FIN_ALPHA: {
+        const double a = st->rho0 / tot[0];
+        st->alpha = a;
+        if (!isfinite(a)) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
+    case FIN_OMEGA: {
+        const double w = tot[0] / tot[1];
+        st->omega = w;
+        if (!isfinite(w) || w == 0.0) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
+    case FIN_CONV: {
+        const double err = sqrt(tot[1]);
+        const double rho1 = tot[0];
+        st->err = err;
+        st->beta = rho1 / st->rho0 * st->alpha / st->omega;
+        st->rho0 = rho1;
+        st->iter += 1;
+        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
+        if (!isfinite(err)) {
+            st->status = 3;
+            st->done = 1;
+        } else if (err < st->tol_abs) {
+            st->status = 0;
+            st->done = 1;
+        } else if (st->iter >= st->maxit) {
+            st->status = 1;
+            st->done = 1;
+        } else if (!isfinite(st->beta)) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
+    case FIN_CG_ALPHA: {
+        st->rho0 = tot[0];                    // r.z
+        st->alpha = tot[0] / tot[1];          // r.z / p.Ap
+        if (!isfinite(st->alpha)) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
+    case FIN_CG_CONV: {
+        const double err = sqrt(tot[1]);
+        st->err = err;
+        st->beta = tot[0] / st->rho0;         // r_new.z_new / r.z
+        st->iter += 1;
+        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
+        if (!isfinite(err)) {
+            st->status = 3;
+            st->done = 1;
+        } else if (err < st->tol_abs) {
+            st->status = 0;
+            st->done = 1;
+        } else if (st->iter >= st->maxit) {
+            st->status = 1;
+            st->done = 1;
+        }
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+// Block reduction of NS partial sums, then the last block reduces all block
+// partials in block order and runs the finalizer.  Every thread of every block
+// must call this (inactive threads pass zeros).
+template <int NS>
+__device__ __forceinline__ void reduce_finalize(double (&v)[NS], const RedCtx& rc)
+{
+    __shared__ double sm[32][NS];
+    __shared__ int is_last;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nthr = blockDim.x * blockDim.y;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = (nthr + 31) >> 5;
+    const unsigned nblocks = gridDim.x * gridDim.y;
+    const unsigned bid = blockIdx.x + gridDim.x * blockIdx.y;
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+        const double w = warp_sum(v[q]);
+        if (lane == 0) sm[warp][q] = w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; q++) {
+            double s = 0.0;
+            for (int w = 0; w < nwarp; w++) s += sm[w][q];
+            rc.partials[(size_t)bid * 4 + q] = s;
+        }
+        __threadfence();
+        const unsigned ticket = atomicAdd(rc.counter, 1u);
+        is_last = (ticket == nblocks - 1);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double acc[NS];
+#pragma unroll
+    for (int q = 0; q < NS; q++) acc[q] = 0.0;
+    for (unsigned b = tid; b < nblocks; b += nthr) {
+#pragma unroll
+        for (int q = 0; q < NS; q++) acc[q] += __ldcg(&rc.partials[(size_t)b * 4 + q]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+        const double w = warp_sum(acc[q]);
+        if (lane == 0) sm[warp][q] = w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double tot[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < NS; q++) {
+            double s = 0.0;
+            for (int w = 0; w < nwarp; w++) s += sm[w][q];
+            tot[q] = s;
+        }
+        finalize(rc, tot);
+        __threadfence();
+        *rc.counter = 0u;
+    }
+}
+
+#define EARLY_EXIT(done)                                      \
+    if (done != nullptr && *(volatile const int*)(done) != 0) return;
+
+// Y = cc*B + cx*(Bx pair) + cy*(By pair) + cz*(Bz pair); Z = B/theta.
+// mode 0: write Y and Z; mode 1: write X(=Y pointer) = scale*Y only (degree 3).
+template <typename T>
+__global__ void __launch_bounds__(256) k_cheb_s01(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ Y,
+                                                  T* __restrict__ Z, Coef cf, T inv_theta, int mode, const int* done)
+{
+    EARLY_EXIT(done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz, sc = (T)cf.scale;
+    const long long sj = g.sj, sk = g.sk;
+    long long c = q.c;
+    T bm = B[c - sk], bc = B[c];
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        const T bp = B[c + sk];
+        const T sx = B[c - 1] + B[c + 1];
+        const T sy = B[c - sj] + B[c + sj];
+        T y = cc * bc;
+        y = fmx(cx, sx, y);
+        y = fmx(cy, sy, y);
+        y = fmx(cz, bm + bp, y);
+        if (mode == 0) {
+            Y[c] = y;
+            Z[c] = bc * inv_theta;
+        } else {
+            Y[c] = sc * y;
+        }
+        bm = bc;
+        bc = bp;
+        c += sk;
+    }
+}
+
+// W = cc*Y + cx*(Yx pair) + cy*(...) + cz*(...) + cb*B + cw*Z, times scale (-1 for the output X).
+template <typename T>
+__global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __restrict__ Y,
+                                                    const T* __restrict__ B, const T* __restrict__ Z,
+                                                    T* __restrict__ W, Coef cf, const int* done)
+{
+    EARLY_EXIT(done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T cc = (T)(cf.cc * cf.scale), cx = (T)(cf.cx * cf.scale), cy = (T)(cf.cy * cf.scale),
+            cz = (T)(cf.cz * cf.scale), cb = (T)(cf.cb * cf.scale), cw = (T)(cf.cw * cf.scale);
+    const long long sj = g.sj, sk = g.sk;
+    long long c = q.c;
+    T ym = Y[c - sk], yc = Y[c];
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        const T yp = Y[c + sk];
+        const T sx = Y[c - 1] + Y[c + 1];
+        const T sy = Y[c - sj] + Y[c + sj];
+        T w = cc * yc;
+        w = fmx(cx, sx, w);
+        w = fmx(cy, sy, w);
+        w = fmx(cz, ym + yp, w);
+        w = fmx(cb, B[c], w);
+        w = fmx(cw, Z[c], w);
+        W[c] = w;
+        ym = yc;
+        yc = yp;
+        c += sk;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_scale_copy(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ X, T a,
+                                                    const int* done)
+{
+    EARLY_EXIT(done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        X[c] = a * B[c];
+        c += g.sk;
+    }
+}
+
+// Au = A(u); sum r0*Au   (BiCGSTAB.hpp:142-164, BiCGstab1Kernel)
+template <typename T>
+__global__ void __launch_bounds__(256) k_stencil_dot(Geo g, Shape sh, const T* __restrict__ u,
+                                                     const T* __restrict__ r0, T* __restrict__ Au, Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> acc;
+    if (q.active) {
+        const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz;
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        T um = u[c - sk], uc = u[c];
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T up = u[c + sk];
+            const T sx = u[c - 1] + u[c + 1];
+            const T sy = u[c - sj] + u[c + sj];
+            T a = cc * uc;
+            a = fmx(cx, sx, a);
+            a = fmx(cy, sy, a);
+            a = fmx(cz, um + up, a);
+            Au[c] = a;
+            acc.add(r0[c], a);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[1] = {acc.value()};
+    reduce_finalize<1>(v, rc);
+}
+
+// Au = A(u); sum r*Au, sum Au*Au   (BiCGSTAB.hpp:189-225, BiCGstab2Kernel)
+template <typename T>
+__global__ void __launch_bounds__(256) k_stencil_dot2(Geo g, Shape sh, const T* __restrict__ u,
+                                                      const T* __restrict__ r, T* __restrict__ Au, Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1, a2;
+    if (q.active) {
+        const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz;
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        T um = u[c - sk], uc = u[c];
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T up = u[c + sk];
+            const T sx = u[c - 1] + u[c + 1];
+            const T sy = u[c - sj] + u[c + sj];
+            T a = cc * uc;
+            a = fmx(cx, sx, a);
+            a = fmx(cy, sy, a);
+            a = fmx(cz, um + up, a);
+            Au[c] = a;
+            a1.add(r[c], a);
+            a2.add(a, a);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[2] = {a1.value(), a2.value()};
+    reduce_finalize<2>(v, rc);
+}
+
+// r -= alpha*v   (BiCGSTAB.hpp:167-178)
+template <typename T>
+__global__ void __launch_bounds__(256) k_axpy_alpha(Geo g, Shape sh, T* __restrict__ r, const T* __restrict__ v,
+                                                    const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T a = (T)st->alpha;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        r[c] = fmx(-a, v[c], r[c]);
+        c += g.sk;
+    }
+}
+
+// x += alpha*Mp + omega*z; r -= omega*Az; sums r0*r, r*r   (BiCGSTAB.hpp:227-257)
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ Mp,
+                                                   const T* __restrict__ z, T* __restrict__ r,
+                                                   const T* __restrict__ Az, const T* __restrict__ r0, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1, a2;
+    if (q.active) {
+        const T a = (T)rc.st->alpha, w = (T)rc.st->omega;
+        long long c = q.c;
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            x[c] = fmx(w, z[c], fmx(a, Mp[c], x[c]));
+            const T rn = fmx(-w, Az[c], r[c]);
+            r[c] = rn;
+            a1.add(r0[c], rn);
+            a2.add(rn, rn);
+            c += g.sk;
+        }
+    }
+    double v[2] = {a1.value(), a2.value()};
+    reduce_finalize<2>(v, rc);
+}
+
+// p = r + beta*(p - omega*AMp)   (BiCGSTAB.hpp:261-272)
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_p(Geo g, Shape sh, T* __restrict__ p, const T* __restrict__ r,
+                                                  const T* __restrict__ AMp, const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T be = (T)st->beta, w = (T)st->omega;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        p[c] = fmx(be, fmx(-w, AMp[c], p[c]), r[c]);
+        c += g.sk;
+    }
+}
+
+// CG: Ap = A(p); sums r*z, p*Ap   (baseCG.hpp:126-150)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_stencil_dot(Geo g, Shape sh, const T* __restrict__ p,
+                                                        const T* __restrict__ r, const T* __restrict__ z,
+                                                        T* __restrict__ Ap, Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1, a2;
+    if (q.active) {
+        const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz;
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        T um = p[c - sk], uc = p[c];
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T up = p[c + sk];
+            const T sx = p[c - 1] + p[c + 1];
+            const T sy = p[c - sj] + p[c + sj];
+            T a = cc * uc;
+            a = fmx(cx, sx, a);
+            a = fmx(cy, sy, a);
+            a = fmx(cz, um + up, a);
+            Ap[c] = a;
+            a1.add(r[c], z[c]);
+            a2.add(uc, a);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[2] = {a1.value(), a2.value()};
+    reduce_finalize<2>(v, rc);
+}
+
+// CG: x += alpha*p; r -= alpha*Ap   (baseCG.hpp:154-165)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
+                                                      T* __restrict__ r, const T* __restrict__ Ap, const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T a = (T)st->alpha;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        x[c] = fmx(a, p[c], x[c]);
+        r[c] = fmx(-a, Ap[c], r[c]);
+        c += g.sk;
+    }
+}
+
+// CG: sums r*z, r*r   (baseCG.hpp:169-194)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_dot_rz(Geo g, Shape sh, const T* __restrict__ r, const T* __restrict__ z,
+                                                   RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1, a2;
+    if (q.active) {
+        long long c = q.c;
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T rv = r[c];
+            a1.add(rv, z[c]);
+            a2.add(rv, rv);
+            c += g.sk;
+        }
+    }
+    double v[2] = {a1.value(), a2.value()};
+    reduce_finalize<2>(v, rc);
+}
+
+// CG: p = z + beta*p   (baseCG.hpp:197-207)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_update_p(Geo g, Shape sh, T* __restrict__ p, const T* __restrict__ z,
+                                                     const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T be = (T)st->beta;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        p[c] = fmx(be, p[c], z[c]);
+        c += g.sk;
+    }
+}
+
+// r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
+// stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
+template <typename TR>
+__global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double* __restrict__ x,
+                                                  const double* __restrict__ b, TR* __restrict__ r,
+                                                  TR* __restrict__ r0, TR* __restrict__ p, Coef cf, RedCtx rc)
+{
+    const Col q = column(g, sh);
+    double s = 0.0;
+    if (q.active) {
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        double um = x[c - sk], uc = x[c];
+        for (int k = q.k0; k < q.k1; k++) {
+            const double up = x[c + sk];
+            const double sx = x[c - 1] + x[c + 1];
+            const double sy = x[c - sj] + x[c + sj];
+            double a = cf.cc * uc;
+            a = fmx(cf.cx, sx, a);
+            a = fmx(cf.cy, sy, a);
+            a = fmx(cf.cz, um + up, a);
+            const double rv = b[c] - a;
+            const TR rs = (TR)rv;
+            r[c] = rs;
+            if (r0) r0[c] = rs;
+            if (p) p[c] = rs;
+            s = fmx(rv, rv, s);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[1] = {s};
+    reduce_finalize<1>(v, rc);
+}
+
+// sum b_adj^2 over the unknowns (normalizeProblemToFieldBNorm, iterativeSolverBase.hpp:171-234)
+__global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double* __restrict__ b,
+                                                   const double* __restrict__ x, Faces f, RedCtx rc)
+{
+    const Col q = column(g, sh);
+    double s = 0.0;
+    if (q.active) {
+        long long c = q.c;
+        for (int k = q.k0; k < q.k1; k++) {
+            const double v = badj_exact(g, b, x, f, c, q.i, q.j, k);
+            s = fmx(v, v, s);
+            c += g.sk;
+        }
+    }
+    double v[1] = {s};
+    reduce_finalize<1>(v, rc);
+}
+
+__global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double* __restrict__ x,
+                                                        const float* __restrict__ e)
+{
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    long long c = q.c;
+    for (int k = q.k0; k < q.k1; k++) {
+        x[c] += (double)e[c];
+        c += g.sk;
+    }
+}
+
+template <typename T>
+__global__ void k_fill(T* p, long long n, T v)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        p[c] = v;
+}
+
+__global__ void k_state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
+                             int rho0_from_r, double hist_scale, int hist_cap)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->rho0 = 1.0;
+        st->alpha = st->omega = st->beta = 1.0;
+        st->err = -1.0;
+        st->err0 = -1.0;
+        st->tol_abs = tol_abs;
+        st->tol_rel = tol_rel;
+        st->tol_relative = tol_relative;
+        st->rho0_from_r = rho0_from_r;
+        st->hist_scale = hist_scale;
+        st->hist_cap = hist_cap;
+        st->iter = 0;
+        st->maxit = maxit;
+        st->done = 0;
+        st->status = 0;
+        for (int q = 0; q < 4; q++) st->sums[q] = 0.0;
+    }
+}
+
+// ---- wrappers ----
+
+template <typename T>
+void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, T* Z, const Coef& cy, double inv_theta, int mode,
+                   const int* done, cudaStream_t s)
+{
+    k_cheb_s01<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, Z, cy, (T)inv_theta, mode, done);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& c,
+                     const int* done, cudaStream_t s)
+{
+    k_cheb_sweep<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_scale_copy(const Geo& g, const Shape& sh, const T* B, T* X, double a, const int* done, cudaStream_t s)
+{
+    k_scale_copy<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, X, (T)a, done);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T* Au, const Coef& a, RedCtx rc,
+                      cudaStream_t s)
+{
+    k_stencil_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r0, Au, a, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T* Au, const Coef& a, RedCtx rc,
+                       cudaStream_t s)
+{
+    k_stencil_dot2<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r, Au, a, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_axpy_alpha(const Geo& g, const Shape& sh, T* r, const T* v, const DevState* st, cudaStream_t s)
+{
+    k_axpy_alpha<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, v, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_update_xr(const Geo& g, const Shape& sh, T* x, const T* Mp, const T* z, T* r, const T* Az, const T* r0,
+                    RedCtx rc, cudaStream_t s)
+{
+    k_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, Mp, z, r, Az, r0, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_update_p(const Geo& g, const Shape& sh, T* p, const T* r, const T* AMp, const DevState* st, cudaStream_t s)
+{
+    k_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, r, AMp, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_cg_stencil_dot(const Geo& g, const Shape& sh, const T* p, const T* r, const T* z, T* Ap, const Coef& a,
+                         RedCtx rc, cudaStream_t s)
+{
+    k_cg_stencil_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, r, z, Ap, a, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_cg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+                       cudaStream_t s)
+{
+    k_cg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_cg_dot_rz(const Geo& g, const Shape& sh, const T* r, const T* z, RedCtx rc, cudaStream_t s)
+{
+    k_cg_dot_rz<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const DevState* st, cudaStream_t s)
+{
+    k_cg_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, z, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename TR>
+void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
+                   const Coef& a, RedCtx rc, cudaStream_t s)
+{
+    k_residual<TR><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+    PPS_COUNT_LAUNCH();
+}
+void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
+                    cudaStream_t s)
+{
+    k_norm_badj<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
+    PPS_COUNT_LAUNCH();
+}
+void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s)
+{
+    k_add_correction<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, e);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fill_field(T* p, long long n, T v, cudaStream_t s)
+{
+    k_fill<T><<<par_blocks(n), 256, 0, s>>>(p, n, v);
+    PPS_COUNT_LAUNCH();
+}
+void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
+                int rho0_from_r, double hist_scale, int hist_cap, cudaStream_t s)
+{
+    k_state_init<<<1, 32, 0, s>>>(st, hist, maxit, tol_abs, tol_rel, tol_relative, rho0_from_r, hist_scale, hist_cap);
+    PPS_COUNT_LAUNCH();
+}
+
+#define PPS_INST(T)                                                                                              \
+    template void fast_cheb_s01<T>(const Geo&, const Shape&, const T*, T*, T*, const Coef&, double, int,         \
+                                   const int*, cudaStream_t);                                                    \
+    template void fast_cheb_sweep<T>(const Geo&, const Shape&, const T*, const T*, const T*, T*, const Coef&,    \
+                                     const int*, cudaStream_t);                                                  \
+    template void fast_scale_copy<T>(const Geo&, const Shape&, const T*, T*, double, const int*, cudaStream_t); \
+    template void fast_stencil_dot<T>(const Geo&, const Shape&, const T*, const T*, T*, const Coef&, RedCtx,     \
+                                      cudaStream_t);                                                             \
+    template void fast_stencil_dot2<T>(const Geo&, const Shape&, const T*, const T*, T*, const Coef&, RedCtx,    \
+                                       cudaStream_t);                                                            \
+    template void fast_axpy_alpha<T>(const Geo&, const Shape&, T*, const T*, const DevState*, cudaStream_t);     \
+    template void fast_update_xr<T>(const Geo&, const Shape&, T*, const T*, const T*, T*, const T*, const T*,    \
+                                    RedCtx, cudaStream_t);                                                       \
+    template void fast_update_p<T>(const Geo&, const Shape&, T*, const T*, const T*, const DevState*,            \
+                                   cudaStream_t);                                                                \
+    template void fast_cg_stencil_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, T*,             \
+                                         const Coef&, RedCtx, cudaStream_t);                                     \
+    template void fast_cg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, const DevState*,    \
+                                       cudaStream_t);                                                            \
+    template void fast_cg_dot_rz<T>(const Geo&, const Shape&, const T*, const T*, RedCtx, cudaStream_t);         \
+    template void fast_cg_update_p<T>(const Geo&, const Shape&, T*, const T*, const DevState*, cudaStream_t);    \
+    template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
+                                   const Coef&, RedCtx, cudaStream_t);                                           \
+    template void fill_field<T>(T*, long long, T, cudaStream_t);
+
+PPS_INST(double)
+PPS_INST(float)
+
+}  // namespace pps

@@ -1,0 +1,1255 @@
+// Solver objects and the C ABI of libpps (include/pps.h).
+//
+// One pps_solver is the GPU counterpart of one reference solver object
+// (BiCGSTAB<...,ChebyshevIteration<...>> composed in inputParam.hpp:33): it owns
+// its device work fields, the Chebyshev parameters, a CUDA stream and the
+// device-resident Krylov scalars.  Three forms share the same object:
+//   PARITY_FP64  host-driven loop over the par_* kernels, scalars on the host in
+//                the reference's order, serial device sums -> bit-identical.
+//   FP64         device-driven loop over the fast kernels (scalars on device,
+//                optional CUDA-graph replay, host polls a stop flag).
+//   MIXED        FP64 iterative refinement: FP64 true residual on the device,
+//                inner BiCGSTAB/CG with FP32 fields and FP64-accurate dots.
+#include "../../include/pps.h"
+#include "pps_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace pps;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& m) { g_last_error = m; }
+
+struct CudaFail {
+    cudaError_t err;
+};
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+            throw CudaFail{e_};                                                               \
+        }                                                                                     \
+    } while (0)
+
+const double kPi = 3.141592653589793;
+
+// Built-in manufactured problems (the reference default of solverSetup.hpp:98-160,
+// and the sine product used for the 64^3 eigenvector case).
+double builtin_f(double x, double y, double z, void* ctx)
+{
+    const int p = *(const int*)ctx;
+    if (p == 0) return -sin(x) - cos(y) - 3 * sin(z) + 2 * y * z + 2;
+    return -3 * kPi * kPi * sin(kPi * x) * sin(kPi * y) * sin(kPi * z);
+}
+double builtin_u(double x, double y, double z, void* ctx)
+{
+    const int p = *(const int*)ctx;
+    if (p == 0) return sin(x) + cos(y) + 3 * sin(z) + x * x * y * z + x * x + 10;
+    return sin(kPi * x) * sin(kPi * y) * sin(kPi * z);
+}
+double builtin_du(double x, double y, double z, int dir, void* ctx)
+{
+    const int p = *(const int*)ctx;
+    if (p == 0) {
+        if (dir == 0) return cos(x) + 2 * x * y * z + 2 * x;
+        if (dir == 1) return -sin(y) + x * x * z;
+        return 3 * cos(z) + x * x * y;
+    }
+    if (dir == 0) return kPi * cos(kPi * x) * sin(kPi * y) * sin(kPi * z);
+    if (dir == 1) return kPi * sin(kPi * x) * cos(kPi * y) * sin(kPi * z);
+    return kPi * sin(kPi * x) * sin(kPi * y) * cos(kPi * z);
+}
+
+template <typename T>
+struct Fields {
+    T *p = nullptr, *r = nullptr, *r0 = nullptr, *Mp = nullptr, *AMp = nullptr, *z = nullptr, *Az = nullptr;
+    T *Y = nullptr, *Z = nullptr, *W = nullptr, *e = nullptr;
+};
+
+}  // namespace
+
+struct pps_solver {
+    pps_grid grid;
+    pps_config cfg;
+    Geo geo;
+    Shape shape;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    double eig[2] = {0, 0};
+    double theta = 0, delta = 0, sigma = 0;
+    long long n_unknowns = 0;
+
+    double* d_x = nullptr;   // device copies of the caller's fields (host-array path)
+    double* d_b = nullptr;
+    double* d_bt = nullptr;  // parity: adjusted b
+    double* d_dot = nullptr; // parity: serial sums
+    Fields<double> f64;
+    Fields<float> f32;
+    DevState* d_st = nullptr;
+    DevState* h_st = nullptr;  // pinned
+    double* d_hist = nullptr;
+    int hist_cap = 0;
+    double* d_partials = nullptr;
+    unsigned* d_counter = nullptr;
+    double* h_dot = nullptr;   // pinned
+
+    double* d_faces[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool has_neumann = false;
+
+    std::vector<double> history;
+    pps_stats stats;
+    double cheb_rho_curr_first = 0;
+
+    // Parity-form Chebyshev buffers rotate like the reference's member pointers.
+    double *pY = nullptr, *pZ = nullptr, *pW = nullptr;
+
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    const void* g_key_x = nullptr;
+    const void* g_key_b = nullptr;
+    int g_iters = 0;
+    int g_form = -1;
+    double g_bytes = 0;
+    int g_launches = 0;
+    double g_sweep_bytes = 0;
+    int g_sweep_launches = 0;
+
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
+    int sweep_ev_used = 0;
+    double bytes_acc = 0;
+    int launches_acc = 0;
+    double sweep_bytes_acc = 0;
+    int sweep_launch_acc = 0;
+};
+
+namespace {
+
+Faces faces_of(const pps_solver* s)
+{
+    Faces f;
+    for (int i = 0; i < 6; i++) f.g[i] = s->d_faces[i];
+    return f;
+}
+
+RedCtx red(pps_solver* s, int kind)
+{
+    RedCtx rc;
+    rc.partials = s->d_partials;
+    rc.counter = s->d_counter;
+    rc.st = s->d_st;
+    rc.hist = s->d_hist;
+    rc.kind = kind;
+    return rc;
+}
+
+// A(u) = cc*u + c_d*(pairs) with c_d = 1/h_d^2  (matrixFreeOperatorA.hpp:34-38)
+Coef op_coef(const Geo& g)
+{
+    Coef c;
+    const double ix = 1.0 / (g.ds[0] * g.ds[0]), iy = 1.0 / (g.ds[1] * g.ds[1]), iz = 1.0 / (g.ds[2] * g.ds[2]);
+    c.cc = -2.0 * (ix + iy + iz);
+    c.cx = ix;
+    c.cy = iy;
+    c.cz = iz;
+    c.cb = 0;
+    c.cw = 0;
+    c.scale = 1.0;
+    return c;
+}
+
+long long face_count(const pps_solver* s, int f)
+{
+    const int d = f / 2;
+    const int* n = s->grid.npglobal;
+    if (d == 0) return (long long)n[1] * n[2];
+    if (d == 1) return (long long)n[0] * n[2];
+    return (long long)n[0] * n[1];
+}
+
+template <typename T>
+void alloc_fields(Fields<T>& F, long long ntot, bool with_e)
+{
+    T** all[] = {&F.p, &F.r, &F.r0, &F.Mp, &F.AMp, &F.z, &F.Az, &F.Y, &F.Z, &F.W};
+    for (T** q : all) {
+        CK(cudaMalloc((void**)q, sizeof(T) * (size_t)ntot));
+        CK(cudaMemset(*q, 0, sizeof(T) * (size_t)ntot));
+    }
+    if (with_e) {
+        CK(cudaMalloc((void**)&F.e, sizeof(T) * (size_t)ntot));
+        CK(cudaMemset(F.e, 0, sizeof(T) * (size_t)ntot));
+    }
+}
+
+template <typename T>
+void free_fields(Fields<T>& F)
+{
+    T* all[] = {F.p, F.r, F.r0, F.Mp, F.AMp, F.z, F.Az, F.Y, F.Z, F.W, F.e};
+    for (T* q : all)
+        if (q) cudaFree(q);
+    F = Fields<T>();
+}
+
+template <typename T>
+void zero_fields(Fields<T>& F, long long ntot, cudaStream_t st)
+{
+    T* all[] = {F.p, F.r, F.r0, F.Mp, F.AMp, F.z, F.Az};
+    for (T* q : all) CK(cudaMemsetAsync(q, 0, sizeof(T) * (size_t)ntot, st));
+}
+
+void free_all(pps_solver* s)
+{
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    free_fields(s->f64);
+    free_fields(s->f32);
+    void* ptrs[] = {s->d_x, s->d_b, s->d_bt, s->d_dot, s->d_st, s->d_hist, s->d_partials, s->d_counter};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (int i = 0; i < 6; i++)
+        if (s->d_faces[i]) cudaFree(s->d_faces[i]);
+    if (s->h_st) cudaFreeHost(s->h_st);
+    if (s->h_dot) cudaFreeHost(s->h_dot);
+    for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+// ---------------------------------------------------------------------------
+// PARITY form: the reference's loop with the par_* kernels
+// ---------------------------------------------------------------------------
+
+double par_dot(pps_solver* s, const double* a, const double* b)
+{
+    seq_dot2(s->geo, a, b, nullptr, nullptr, s->d_dot, s->stream);
+    CK(cudaMemcpyAsync(s->h_dot, s->d_dot, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return s->h_dot[0];
+}
+
+void par_dot2(pps_solver* s, const double* a1, const double* b1, const double* a2, const double* b2, double* o1,
+              double* o2)
+{
+    seq_dot2(s->geo, a1, b1, a2, b2, s->d_dot, s->stream);
+    CK(cudaMemcpyAsync(s->h_dot, s->d_dot, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *o1 = s->h_dot[0];
+    *o2 = s->h_dot[1];
+}
+
+void par_neumann_helper(pps_solver* s, double* f)
+{
+    if (s->has_neumann) neumann_fill<double>(s->geo, f, faces_of(s), 0, 1.0, s->stream);
+}
+
+// ChebyshevIteration::operator() in preconditioner mode (chebyshevIteration.hpp:48-140)
+void par_precond(pps_solver* s, double* B, double* X)
+{
+    const Geo& g = s->geo;
+    if (s->cfg.precond == PPS_PREC_NONE) {
+        CK(cudaMemcpyAsync(X, B, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, s->stream));
+        return;
+    }
+    const double sigma = s->sigma, delta = s->delta, theta = s->theta;
+    double rhoOld = 1 / sigma;
+    double rhoCurr = 1 / (2 * sigma - rhoOld);
+    par_neumann_helper(s, B);
+    par_cheb_s01(g, B, s->pY, s->pZ, theta, 2 * rhoCurr / delta, s->stream);
+    for (int it = 2; it <= s->cfg.cheb_degree; it++) {
+        rhoOld = rhoCurr;
+        rhoCurr = 1 / (2 * sigma - rhoOld);
+        par_neumann_helper(s, s->pY);
+        par_cheb_sweep(g, s->pY, B, s->pZ, s->pW, rhoCurr, 2 * sigma, 2 / delta, rhoOld, s->stream);
+        std::swap(s->pZ, s->pY);
+        std::swap(s->pW, s->pY);
+    }
+    par_neg(g, s->pW, X, s->stream);
+}
+
+double par_true_residual(pps_solver* s, double* x, double* b, double* r, double normb)
+{
+    if (s->has_neumann) neumann_fill<double>(s->geo, x, faces_of(s), 1, normb, s->stream);
+    par_residual(s->geo, x, b, r, s->stream);
+    return std::sqrt(par_dot(s, r, r));
+}
+
+pps_status solve_parity(pps_solver* s, double* x, double* b)
+{
+    const Geo& g = s->geo;
+    Fields<double>& F = s->f64;
+    cudaStream_t st = s->stream;
+    pps_stats& S = s->stats;
+    const double toll = s->cfg.tol;
+    zero_fields(F, g.ntot, st);
+    s->history.assign(1, -1.0);
+
+    if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+    // normalizeProblemToFieldBNorm (iterativeSolverBase.hpp:171-234)
+    par_adjust_b(g, b, x, faces_of(s), s->d_bt, st);
+    const double normb = std::sqrt(par_dot(s, s->d_bt, s->d_bt));
+    S.norm_b = normb;
+    if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    par_scale_all(g, x, b, normb, 1, st);
+    double errC = par_true_residual(s, x, b, F.r, normb);
+    S.err_true = errC;
+    S.err_iter = -1.0;
+    s->history[0] = errC;
+    S.iterations = 0;
+    if (errC < toll) return PPS_OK;   // the reference returns here, x and b still scaled
+
+    CK(cudaMemcpyAsync(F.p, F.r, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(F.r0, F.r, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+    double rho0 = 1, rho1 = 1, alphak = 1, omegak = 1, betak = 1, s1 = 0, s2 = 0;
+    int iter = 0;
+    const bool cg = s->cfg.krylov == PPS_KRYLOV_CG;
+    if (cg) {
+        // BaseCG::operator() (baseCG.hpp:109-228)
+        double* zk = F.z;
+        double* Apk = F.AMp;
+        par_precond(s, F.r, zk);
+        S.precond_applications++;
+        CK(cudaMemcpyAsync(F.p, zk, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        double pSum1 = 0, pSum2 = 0, pSumRk = 0;
+        while (iter < s->cfg.maxit) {
+            par_stencil(g, F.p, Apk, st);
+            par_dot2(s, F.r, zk, F.p, Apk, &pSum1, &pSum2);
+            alphak = pSum1 / pSum2;
+            par_update_x(g, x, F.p, alphak, st);
+            par_axpy(g, F.r, Apk, alphak, st);
+            par_precond(s, F.r, zk);
+            S.precond_applications++;
+            par_dot2(s, F.r, zk, F.r, F.r, &pSum2, &pSumRk);
+            betak = pSum2 / pSum1;
+            S.err_iter = std::sqrt(pSumRk);
+            par_update_p_cg(g, F.p, zk, betak, st);
+            iter++;
+            s->history.push_back(S.err_iter);
+            if (S.err_iter < toll) break;
+        }
+    } else {
+        // BiCGSTAB::operator() (BiCGSTAB.hpp:131-292)
+        while (iter < s->cfg.maxit) {
+            par_precond(s, F.p, F.Mp);
+            par_neumann_helper(s, F.Mp);
+            par_stencil(g, F.Mp, F.AMp, st);
+            s2 = par_dot(s, F.r0, F.AMp);
+            alphak = rho0 / s2;
+            par_axpy(g, F.r, F.AMp, alphak, st);
+            par_precond(s, F.r, F.z);
+            par_neumann_helper(s, F.z);
+            S.precond_applications += 2;
+            par_stencil(g, F.z, F.Az, st);
+            par_dot2(s, F.r, F.Az, F.Az, F.Az, &s1, &s2);
+            omegak = s1 / s2;
+            par_update_x_all(g, x, F.Mp, F.z, alphak, omegak, st);
+            par_axpy(g, F.r, F.Az, omegak, st);
+            par_dot2(s, F.r0, F.r, F.r, F.r, &s1, &s2);
+            S.err_iter = std::sqrt(s2);
+            rho1 = s1;
+            betak = rho1 / rho0 * alphak / omegak;
+            rho0 = rho1;
+            par_update_p(g, F.p, F.r, F.AMp, betak, omegak, st);
+            iter++;
+            s->history.push_back(S.err_iter);
+            if (S.err_iter < toll) break;
+        }
+        if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, normb, st);
+    }
+    S.iterations = iter;
+    S.err_true = par_true_residual(s, x, b, F.r, normb);
+    par_scale_all(g, x, b, normb, 0, st);
+    return iter >= s->cfg.maxit && !(S.err_iter < toll) ? PPS_NOT_CONVERGED : PPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 and MIXED forms: device-driven loops over the fast kernels
+// ---------------------------------------------------------------------------
+
+template <typename T>
+double bytes_of(long long n, int words)
+{
+    return (double)n * words * sizeof(T);
+}
+
+// Pre-folded Chebyshev coefficients for the fast kernels.
+Coef cheb_s01_coef(const pps_solver* s, double rhoCurr)
+{
+    const Coef a = op_coef(s->geo);
+    const double t = 2 * rhoCurr / s->delta;   // Y = t*(2B + A(B)/theta)
+    Coef c;
+    c.cc = t * (2.0 + a.cc / s->theta);
+    c.cx = t * a.cx / s->theta;
+    c.cy = t * a.cy / s->theta;
+    c.cz = t * a.cz / s->theta;
+    c.cb = 0;
+    c.cw = 0;
+    c.scale = 1.0;
+    return c;
+}
+
+Coef cheb_sweep_coef(const pps_solver* s, double rhoCurr, double rhoOld, double scale)
+{
+    const Coef a = op_coef(s->geo);
+    const double tod = 2.0 / s->delta;   // W = rc*(2 sigma Y + 2/delta (B + A Y) - ro Z)
+    Coef c;
+    c.cc = rhoCurr * (2.0 * s->sigma + tod * a.cc);
+    c.cx = rhoCurr * tod * a.cx;
+    c.cy = rhoCurr * tod * a.cy;
+    c.cz = rhoCurr * tod * a.cz;
+    c.cb = rhoCurr * tod;
+    c.cw = -rhoCurr * rhoOld;
+    c.scale = scale;
+    return c;
+}
+
+struct Launcher {
+    pps_solver* s;
+    bool profile;
+    double bytes = 0;
+    int launches = 0;
+};
+
+// One preconditioner application X = M^{-1} B in storage type T.  The two last
+// sweeps of the reference are dead (its output is s_{n-2}, chebyshevIteration.hpp:
+// 114-125), so sweeps run for i = 2..n-2 and the last one writes X = -s_{n-2}.
+template <typename T>
+void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+{
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    const long long N = s->n_unknowns;
+    const int* done = &s->d_st->done;
+    if (s->cfg.precond == PPS_PREC_NONE) {
+        CK(cudaMemcpyAsync(X, B, sizeof(T) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        L.bytes += bytes_of<T>(g.ntot, 2);
+        return;
+    }
+    if (s->has_neumann) {
+        neumann_fill<T>(g, B, faces_of(s), 0, 1.0, st);
+        L.launches += 2;
+    }
+    const int n = s->cfg.cheb_degree;
+    const double sigma = s->sigma;
+    double rhoOld = 1 / sigma;
+    double rhoCurr = 1 / (2 * sigma - rhoOld);
+    if (n == 1) {
+        fill_field<T>(X, g.ntot, (T)(-0.0), st);
+        L.bytes += bytes_of<T>(g.ntot, 1);
+        L.launches++;
+        return;
+    }
+    if (n == 2) {
+        fast_scale_copy<T>(g, s->shape, B, X, -1.0 / s->theta, done, st);
+        L.bytes += bytes_of<T>(N, 2);
+        L.launches++;
+        return;
+    }
+    Coef c01 = cheb_s01_coef(s, rhoCurr);
+    if (n == 3) {
+        c01.scale = -1.0;
+        fast_cheb_s01<T>(g, s->shape, B, X, nullptr, c01, 1.0 / s->theta, 1, done, st);
+        L.bytes += bytes_of<T>(N, 2);
+        L.launches++;
+        return;
+    }
+    T* Y = F.Y;
+    T* Z = F.Z;
+    T* W = F.W;
+    fast_cheb_s01<T>(g, s->shape, B, Y, Z, c01, 1.0 / s->theta, 0, done, st);
+    L.bytes += bytes_of<T>(N, 3);
+    L.launches++;
+    const bool prof = L.profile && s->sweep_ev_used + 2 <= (int)s->sweep_ev.size();
+    if (prof) CK(cudaEventRecord(s->sweep_ev[s->sweep_ev_used], st));
+    for (int it = 2; it <= n - 2; it++) {
+        rhoOld = rhoCurr;
+        rhoCurr = 1 / (2 * sigma - rhoOld);
+        if (s->has_neumann) {
+            neumann_fill<T>(g, Y, faces_of(s), 0, 1.0, st);
+            L.launches += 2;
+        }
+        const bool last = (it == n - 2);
+        const Coef c = cheb_sweep_coef(s, rhoCurr, rhoOld, last ? -1.0 : 1.0);
+        fast_cheb_sweep<T>(g, s->shape, Y, B, Z, last ? X : W, c, done, st);
+        L.bytes += bytes_of<T>(N, 4);
+        L.launches++;
+        s->sweep_bytes_acc += bytes_of<T>(N, 4);
+        s->sweep_launch_acc++;
+        if (!last) {
+            T* t = Z;   // (Y, Z, W) <- (W, Y, Z)
+            Z = Y;
+            Y = W;
+            W = t;
+        }
+    }
+    if (prof) {
+        CK(cudaEventRecord(s->sweep_ev[s->sweep_ev_used + 1], st));
+        s->sweep_ev_used += 2;
+    }
+}
+
+// One BiCGSTAB iteration (BiCGSTAB.hpp:133-272) on the fast kernels; xacc is the
+// field the corrections accumulate in (x itself for FP64, the FP32 correction for MIXED).
+template <typename T>
+void fast_bicgstab_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
+{
+    const Geo& g = s->geo;
+    const Shape& sh = s->shape;
+    cudaStream_t st = s->stream;
+    const long long N = s->n_unknowns;
+    const Coef a = op_coef(g);
+    fast_precond<T>(s, F, F.p, F.Mp, L);
+    if (s->has_neumann) neumann_fill<T>(g, F.Mp, faces_of(s), 0, 1.0, st);
+    fast_stencil_dot<T>(g, sh, F.Mp, F.r0, F.AMp, a, red(s, FIN_ALPHA), st);
+    fast_axpy_alpha<T>(g, sh, F.r, F.AMp, s->d_st, st);
+    fast_precond<T>(s, F, F.r, F.z, L);
+    if (s->has_neumann) neumann_fill<T>(g, F.z, faces_of(s), 0, 1.0, st);
+    fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red(s, FIN_OMEGA), st);
+    fast_update_xr<T>(g, sh, xacc, F.Mp, F.z, F.r, F.Az, F.r0, red(s, FIN_CONV), st);
+    fast_update_p<T>(g, sh, F.p, F.r, F.AMp, s->d_st, st);
+    L.bytes += bytes_of<T>(N, 3 + 3 + 3 + 8 + 4);
+    L.launches += 5;
+}
+
+// One CG iteration (baseCG.hpp:115-228). The caller applied z = M^{-1} r and p = z.
+template <typename T>
+void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
+{
+    const Geo& g = s->geo;
+    const Shape& sh = s->shape;
+    cudaStream_t st = s->stream;
+    const long long N = s->n_unknowns;
+    const Coef a = op_coef(g);
+    fast_cg_stencil_dot<T>(g, sh, F.p, F.r, F.z, F.AMp, a, red(s, FIN_CG_ALPHA), st);
+    fast_cg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
+    fast_precond<T>(s, F, F.r, F.z, L);
+    fast_cg_dot_rz<T>(g, sh, F.r, F.z, red(s, FIN_CG_CONV), st);
+    fast_cg_update_p<T>(g, sh, F.p, F.z, s->d_st, st);
+    L.bytes += bytes_of<T>(N, 4 + 6 + 2 + 3);
+    L.launches += 4;
+}
+
+template <typename T>
+void fast_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
+{
+    if (s->cfg.krylov == PPS_KRYLOV_CG) fast_cg_iteration<T>(s, F, xacc, L);
+    else fast_bicgstab_iteration<T>(s, F, xacc, L);
+}
+
+void read_state(pps_solver* s)
+{
+    CK(cudaMemcpyAsync(s->h_st, s->d_st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+}
+
+int auto_check_every(const pps_solver* s, int elem_size)
+{
+    if (s->cfg.check_every > 0) return s->cfg.check_every;
+    // Estimated iteration time against a ~0.4 ms polling period.
+    const int n = std::max(s->cfg.cheb_degree, 4);
+    const double bytes = (double)s->n_unknowns * elem_size * (2.0 * (3 + 4 * (n - 3)) + 21);
+    const double t_iter = bytes / 5.0e12 + 25 * 3e-6;
+    int c = (int)(4e-4 / t_iter);
+    return std::max(1, std::min(c, 16));
+}
+
+// Runs Krylov iterations until the device stop flag is set. With use_graph, a
+// chunk of `chunk` iterations is captured once and replayed.
+template <typename T>
+pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launcher& L)
+{
+    const int chunk = auto_check_every(s, (int)sizeof(T));
+    const bool graph = s->cfg.use_graph != 0 && !L.profile;
+    for (;;) {
+        if (graph) {
+            if (!(s->gexec && s->g_key_x == xacc && s->g_form == form && s->g_iters == chunk)) {
+                if (s->gexec) {
+                    cudaGraphExecDestroy(s->gexec);
+                    s->gexec = nullptr;
+                }
+                cudaGraph_t gr;
+                Launcher LG{s, false};
+                const double sb = s->sweep_bytes_acc;
+                const int sl = s->sweep_launch_acc;
+                const int c0 = launches_counter();
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, LG);
+                CK(cudaStreamEndCapture(s->stream, &gr));
+                LG.launches = launches_counter() - c0;
+                launches_counter_add(-LG.launches);
+                CK(cudaGraphInstantiate(&s->gexec, gr, 0));
+                cudaGraphDestroy(gr);
+                s->g_key_x = xacc;
+                s->g_form = form;
+                s->g_iters = chunk;
+                s->g_bytes = LG.bytes;
+                s->g_launches = LG.launches;
+                s->g_sweep_bytes = s->sweep_bytes_acc - sb;
+                s->g_sweep_launches = s->sweep_launch_acc - sl;
+                s->sweep_bytes_acc = sb;
+                s->sweep_launch_acc = sl;
+            }
+            CK(cudaGraphLaunch(s->gexec, s->stream));
+            L.bytes += s->g_bytes;
+            launches_counter_add(s->g_launches);
+            s->sweep_bytes_acc += s->g_sweep_bytes;
+            s->sweep_launch_acc += s->g_sweep_launches;
+        } else {
+            for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, L);
+        }
+        read_state(s);
+        if (s->h_st->done) break;
+    }
+    return (pps_status)s->h_st->status;
+}
+
+void pull_history(pps_solver* s, int n_iter, bool append)
+{
+    const int n = std::min(n_iter + 1, s->hist_cap);
+    std::vector<double> h((size_t)std::max(n, 0));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(h.data(), s->d_hist, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (!append) s->history.clear();
+    const size_t start = append && !s->history.empty() ? 1 : 0;
+    for (size_t i = start; i < h.size(); i++) s->history.push_back(h[i]);
+}
+
+double norm_badj(pps_solver* s, const double* x, const double* b)
+{
+    state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
+    fast_norm_badj(s->geo, s->shape, b, x, faces_of(s), red(s, FIN_NORMB), s->stream);
+    read_state(s);
+    return s->h_st->normb;
+}
+
+// FP64 form: the reference algorithm on the unscaled system. Scaling commutes with
+// every step, so rho0 = ||b_adj||^2 and tol_abs = tol*||b_adj|| reproduce the
+// normalised iteration (rho0 = 1, BiCGSTAB.hpp:127) without two scaling passes.
+pps_status solve_fp64(pps_solver* s, double* x, const double* b)
+{
+    const Geo& g = s->geo;
+    Fields<double>& F = s->f64;
+    cudaStream_t st = s->stream;
+    pps_stats& S = s->stats;
+    Launcher L{s, s->cfg.use_graph == 0};
+    if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+    const double normb = norm_badj(s, x, b);
+    S.norm_b = normb;
+    if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    const Coef a = op_coef(g);
+    state_init(s->d_st, s->d_hist, s->cfg.maxit, s->cfg.tol * normb, 0.0, 0, 0, 1.0 / normb, s->hist_cap, st);
+    fast_residual<double>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st);
+    L.bytes += bytes_of<double>(s->n_unknowns, 5) + bytes_of<double>(s->n_unknowns, 1) * 2;
+    pps_status rc = PPS_OK;
+    read_state(s);
+    if (!s->h_st->done) {
+        if (s->cfg.krylov == PPS_KRYLOV_CG) {
+            fast_precond<double>(s, F, F.r, F.z, L);
+            CK(cudaMemcpyAsync(F.p, F.z, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        }
+        rc = run_iterations<double>(s, F, x, PPS_FORM_FP64, L);
+    } else {
+        rc = (pps_status)s->h_st->status;
+    }
+    S.iterations = s->h_st->iter;
+    S.err_iter = s->h_st->iter > 0 ? s->h_st->err / normb : -1.0;
+    pull_history(s, S.iterations, false);
+    S.precond_applications += S.iterations * (s->cfg.krylov == PPS_KRYLOV_CG ? 1 : 2);
+    // final true residual (computeErrorOperatorA after the loop, BiCGSTAB.hpp:305-308)
+    if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+    fast_residual<double>(g, s->shape, x, b, F.Az, nullptr, nullptr, a, red(s, FIN_STORE), st);
+    read_state(s);
+    S.err_true = std::sqrt(s->h_st->sums[0]) / normb;
+    S.hbm_bytes += L.bytes;
+    return rc;
+}
+
+// MIXED form: FP64 iterative refinement around an FP32 inner solve.
+pps_status solve_mixed(pps_solver* s, double* x, const double* b)
+{
+    const Geo& g = s->geo;
+    Fields<float>& F = s->f32;
+    cudaStream_t st = s->stream;
+    pps_stats& S = s->stats;
+    Launcher L{s, s->cfg.use_graph == 0};
+    if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+    const double normb = norm_badj(s, x, b);
+    S.norm_b = normb;
+    if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    const Coef a = op_coef(g);
+    const double tol_abs = s->cfg.tol * normb;
+    s->history.clear();
+    int total_iter = 0;
+    pps_status rc = PPS_NOT_CONVERGED;
+    double err_outer = 0;
+    for (int ref = 0; ref <= s->cfg.max_refinements; ref++) {
+        const int remaining = s->cfg.maxit - total_iter;
+        // FIN_RES0 stops when the FP64 residual meets tol_abs; otherwise it sets the
+        // inner target max(inner_tol, 0.3*tol_abs/err0)*err0 on the device.
+        state_init(s->d_st, s->d_hist, std::max(1, std::min(s->cfg.inner_maxit, remaining)), tol_abs,
+                   s->cfg.inner_tol, 1, 1, 1.0 / normb, s->hist_cap, st);
+        fast_residual<float>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st);
+        L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 3);
+        read_state(s);
+        err_outer = s->h_st->err0;
+        if (s->history.empty()) s->history.push_back(err_outer / normb);
+        else s->history.back() = err_outer / normb;   // true residual replaces the recursive estimate
+        if (err_outer < tol_abs) {
+            rc = PPS_OK;
+            break;
+        }
+        if (ref == s->cfg.max_refinements || remaining <= 0) break;
+        fill_field<float>(F.e, g.ntot, 0.0f, st);
+        if (s->cfg.krylov == PPS_KRYLOV_CG) {
+            fast_precond<float>(s, F, F.r, F.z, L);
+            CK(cudaMemcpyAsync(F.p, F.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        }
+        pps_status irc = run_iterations<float>(s, F, F.e, PPS_FORM_MIXED, L);
+        const int it = s->h_st->iter;
+        total_iter += it;
+        pull_history(s, it, true);
+        S.precond_applications += it * (s->cfg.krylov == PPS_KRYLOV_CG ? 1 : 2);
+        S.err_iter = s->h_st->err / normb;
+        fast_add_correction(g, s->shape, x, F.e, s->d_st, st);
+        L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 1);
+        if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+        S.refinements++;
+        if (irc == PPS_NAN_DETECTED) {
+            rc = irc;
+            break;
+        }
+    }
+    S.iterations = total_iter;
+    S.err_true = err_outer / normb;
+    S.hbm_bytes += L.bytes;
+    return rc;
+}
+
+pps_status validate(const pps_grid* g, const pps_config* c)
+{
+    if (!g || !c) return PPS_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; d++) {
+        if (g->npglobal[d] < 3) { set_error("npglobal must be >= 3 on every axis"); return PPS_ERR_INVALID_ARG; }
+        if (!(g->ds[d] > 0.0) || !std::isfinite(g->ds[d])) { set_error("ds must be positive"); return PPS_ERR_INVALID_ARG; }
+    }
+    const double G = (double)(g->npglobal[0] + 2) * (g->npglobal[1] + 2) * (g->npglobal[2] + 2);
+    if (G > 4.0e9) { set_error("grid too large for the 32-bit plane indexing"); return PPS_ERR_INVALID_ARG; }
+    for (int f = 0; f < 6; f++)
+        if (g->bcs[f] != 0 && g->bcs[f] != 1) { set_error("bcs must be 0 (Dirichlet) or 1 (Neumann)"); return PPS_ERR_INVALID_ARG; }
+    if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
+    if (c->precond != PPS_PREC_NONE && c->precond != PPS_PREC_CHEBYSHEV) { set_error("unknown precond"); return PPS_ERR_INVALID_ARG; }
+    if (c->precond == PPS_PREC_CHEBYSHEV && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
+    if (c->maxit < 0 || c->maxit > 100000000) { set_error("maxit out of range"); return PPS_ERR_INVALID_ARG; }
+    if (!(c->tol >= 0.0)) { set_error("tol must be >= 0"); return PPS_ERR_INVALID_ARG; }
+    if (c->form < PPS_FORM_PARITY_FP64 || c->form > PPS_FORM_MIXED) { set_error("unknown form"); return PPS_ERR_INVALID_ARG; }
+    if (c->form == PPS_FORM_MIXED && (!(c->inner_tol > 0.0 && c->inner_tol < 1.0) || c->inner_maxit < 1 || c->max_refinements < 1)) {
+        set_error("mixed form needs 0 < inner_tol < 1, inner_maxit >= 1, max_refinements >= 1");
+        return PPS_ERR_INVALID_ARG;
+    }
+    return PPS_OK;
+}
+
+void coords(const pps_solver* s, int i, int j, int k, double* x, double* y, double* z)
+{
+    // iterativeSolverBase.hpp:547-549 at rank location 0
+    const double* o = s->grid.origin;
+    const double* d = s->grid.ds;
+    *x = o[0] + (i - 1) * d[0] + 0 * (s->grid.npglobal[0]) * d[0];
+    *y = o[1] + (j - 1) * d[1] + 0 * (s->grid.npglobal[1]) * d[1];
+    *z = o[2] + (k - 1) * d[2] + 0 * (s->grid.npglobal[2]) * d[2];
+}
+
+template <typename Fn>
+pps_status guarded(Fn&& fn)
+{
+    try {
+        return fn();
+    } catch (const CudaFail&) {
+        return PPS_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return PPS_ERR_OUT_OF_MEMORY;
+    }
+}
+
+pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
+{
+    pps_stats& S = s->stats;
+    const double h2d = S.seconds_h2d, d2h = S.seconds_d2h;
+    std::memset(&S, 0, sizeof(S));
+    S.seconds_h2d = h2d;
+    S.seconds_d2h = d2h;
+    s->sweep_ev_used = 0;
+    s->sweep_bytes_acc = 0;
+    s->sweep_launch_acc = 0;
+    launches_counter_reset();
+    CK(cudaEventRecord(s->ev0, s->stream));
+    pps_status rc;
+    if (s->cfg.form == PPS_FORM_PARITY_FP64) rc = solve_parity(s, x_dev, b_dev);
+    else if (s->cfg.form == PPS_FORM_FP64) rc = solve_fp64(s, x_dev, b_dev);
+    else rc = solve_mixed(s, x_dev, b_dev);
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    S.seconds_solve = ms * 1e-3;
+    S.kernel_launches = launches_counter();
+    // sweep timing from event pairs
+    double sw = 0;
+    for (int q = 0; q + 1 < s->sweep_ev_used; q += 2) {
+        float m = 0;
+        CK(cudaEventElapsedTime(&m, s->sweep_ev[q], s->sweep_ev[q + 1]));
+        sw += m * 1e-3;
+    }
+    S.sweep_seconds = sw;
+    S.sweep_launches = s->sweep_launch_acc;
+    S.sweep_bytes = s->sweep_bytes_acc;
+    return rc;
+}
+
+}  // namespace
+
+// Extra graph bookkeeping fields live outside the struct definition above.
+// (declared here to keep the struct readable)
+
+extern "C" {
+
+pps_status pps_config_default(pps_config* c, int preset)
+{
+    if (!c) return PPS_ERR_INVALID_ARG;
+    std::memset(c, 0, sizeof(*c));
+    c->krylov = PPS_KRYLOV_BICGSTAB;
+    c->precond = PPS_PREC_CHEBYSHEV;
+    if (preset == PPS_PRESET_ALPAKA) {
+        // ALP/include/solverSetup.hpp:52-72
+        c->cheb_degree = 24;
+        c->cheb_eps = 0.0;
+        c->rescale_min = 100.0;
+        c->rescale_max = 1.0 - 1e-4;
+        c->tol = 1.0 * 1e-10;
+        c->maxit = 1000;
+    } else if (preset == PPS_PRESET_CPU) {
+        // CPU/include/solverSetup.hpp:22-40
+        c->cheb_degree = 11;
+        c->cheb_eps = 1e-4;
+        c->rescale_min = 500.0;
+        c->rescale_max = 1.0 - 1e-4;
+        c->tol = (double)100 * 1e-10;
+        c->maxit = 1700;
+    } else {
+        return PPS_ERR_INVALID_ARG;
+    }
+    c->form = PPS_FORM_FP64;
+    c->inner_tol = 1e-4;
+    c->inner_maxit = 100000;
+    c->max_refinements = 12;
+    c->check_every = 0;
+    c->use_graph = 1;
+    c->device = 0;
+    return PPS_OK;
+}
+
+pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** out)
+{
+    if (!out) return PPS_ERR_INVALID_ARG;
+    *out = nullptr;
+    pps_status v = validate(grid, cfg);
+    if (v != PPS_OK) return v;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_error("no CUDA device");
+        return PPS_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        set_error("device ordinal out of range");
+        return PPS_ERR_INVALID_ARG;
+    }
+    pps_solver* s = new (std::nothrow) pps_solver();
+    if (!s) return PPS_ERR_OUT_OF_MEMORY;
+    s->grid = *grid;
+    s->cfg = *cfg;
+    pps_status rc = guarded([&]() -> pps_status {
+        CK(cudaSetDevice(cfg->device));
+        s->device = cfg->device;
+        Geo& g = s->geo;
+        for (int d = 0; d < 3; d++) {
+            g.n[d] = grid->npglobal[d];
+            g.ds[d] = grid->ds[d];
+            g.lo[d] = 1 + (grid->bcs[2 * d] == 0 ? 1 : 0);
+            g.hi[d] = grid->npglobal[d] + 1 - (grid->bcs[2 * d + 1] == 0 ? 1 : 0);
+        }
+        for (int f = 0; f < 6; f++) {
+            g.bcs[f] = grid->bcs[f];
+            if (grid->bcs[f] == 1) s->has_neumann = true;
+        }
+        g.sj = grid->npglobal[0] + 2;
+        g.sk = g.sj * (grid->npglobal[1] + 2);
+        g.ntot = g.sk * (grid->npglobal[2] + 2);
+        s->n_unknowns = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
+        s->shape = make_shape(g, 8, 152 * 8 * 4);
+        // computeEigenvalues, global bounds (blockGrid.hpp:322-339)
+        double eigMin = 0, eigMax = 0;
+        for (int i = 0; i < 3; i++) {
+            int ni = grid->npglobal[i];
+            if (grid->bcs[2 * i] == 0) ni -= 1;
+            if (grid->bcs[2 * i + 1] == 0) ni -= 1;
+            const double dsi = grid->ds[i];
+            eigMin += 4 * sin(1 * kPi / 2 / (ni + 1)) * sin(1 * kPi / 2 / (ni + 1)) / (dsi * dsi);
+            eigMax += 4 * sin(ni * kPi / 2 / (ni + 1)) * sin(ni * kPi / 2 / (ni + 1)) / (dsi * dsi);
+        }
+        s->eig[0] = eigMin;
+        s->eig[1] = eigMax;
+        // ChebyshevIteration constructor (chebyshevIteration.hpp:22-26)
+        s->theta = (eigMin * cfg->rescale_min + eigMax * cfg->rescale_max) * 0.5 * (1.0 + cfg->cheb_eps);
+        s->delta = (eigMin * cfg->rescale_min - eigMax * cfg->rescale_max) * 0.5;
+        s->sigma = s->theta / s->delta;
+
+        CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&s->ev0));
+        CK(cudaEventCreate(&s->ev1));
+        const size_t fb = sizeof(double) * (size_t)g.ntot;
+        CK(cudaMalloc((void**)&s->d_x, fb));
+        CK(cudaMalloc((void**)&s->d_b, fb));
+        if (cfg->form == PPS_FORM_MIXED) {
+            alloc_fields<float>(s->f32, g.ntot, true);
+        } else {
+            alloc_fields<double>(s->f64, g.ntot, false);
+        }
+        if (cfg->form == PPS_FORM_PARITY_FP64) {
+            CK(cudaMalloc((void**)&s->d_bt, fb));
+            CK(cudaMemset(s->d_bt, 0, fb));
+            s->pY = s->f64.Y;
+            s->pZ = s->f64.Z;
+            s->pW = s->f64.W;
+        }
+        CK(cudaMalloc((void**)&s->d_dot, 4 * sizeof(double)));
+        CK(cudaMalloc((void**)&s->d_st, sizeof(DevState)));
+        CK(cudaMemset(s->d_st, 0, sizeof(DevState)));
+        CK(cudaMallocHost((void**)&s->h_st, sizeof(DevState)));
+        CK(cudaMallocHost((void**)&s->h_dot, 4 * sizeof(double)));
+        s->hist_cap = cfg->maxit + 2;
+        CK(cudaMalloc((void**)&s->d_hist, sizeof(double) * (size_t)s->hist_cap));
+        const unsigned nb = std::max(s->shape.nblocks(), 1u);
+        CK(cudaMalloc((void**)&s->d_partials, sizeof(double) * 4 * (size_t)nb));
+        CK(cudaMalloc((void**)&s->d_counter, sizeof(unsigned)));
+        CK(cudaMemset(s->d_counter, 0, sizeof(unsigned)));
+        for (int f = 0; f < 6; f++) {
+            if (grid->bcs[f] != 1) continue;
+            const long long m = face_count(s, f);
+            CK(cudaMalloc((void**)&s->d_faces[f], sizeof(double) * (size_t)m));
+            CK(cudaMemset(s->d_faces[f], 0, sizeof(double) * (size_t)m));
+        }
+        if (cfg->use_graph == 0) {
+            const int pairs = 2 * (cfg->maxit + 2) + 64;
+            s->sweep_ev.resize((size_t)std::min(pairs, 20000) * 2);
+            for (auto& e : s->sweep_ev) CK(cudaEventCreate(&e));
+        }
+        CK(cudaStreamSynchronize(s->stream));
+        std::memset(&s->stats, 0, sizeof(s->stats));
+        return PPS_OK;
+    });
+    if (rc != PPS_OK) {
+        free_all(s);
+        delete s;
+        return rc == PPS_ERR_CUDA ? PPS_ERR_OUT_OF_MEMORY : rc;
+    }
+    *out = s;
+    return PPS_OK;
+}
+
+pps_status pps_destroy(pps_solver* s)
+{
+    if (!s) return PPS_ERR_INVALID_ARG;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return PPS_OK;
+}
+
+pps_status pps_set_problem(pps_solver* s, const pps_problem* p, double* x, double* b)
+{
+    if (!s || !p || !x || !b || !p->field_b || !p->solution) return PPS_ERR_INVALID_ARG;
+    const int* n = s->grid.npglobal;
+    const long long sj = n[0] + 2, sk = sj * (n[1] + 2);
+    // applyDirichletBCsFromFunction (iterativeSolverBase.hpp:557-603)
+    for (int f = 0; f < 6; f++) {
+        if (s->grid.bcs[f] != 0) continue;
+        const int d = f / 2, side = f % 2;
+        int lo[3] = {1, 1, 1}, hi[3] = {n[0] + 1, n[1] + 1, n[2] + 1};
+        if (side == 0) hi[d] = lo[d] + 1;
+        else lo[d] = hi[d] - 1;
+        for (int k = lo[2]; k < hi[2]; k++)
+            for (int j = lo[1]; j < hi[1]; j++)
+                for (int i = lo[0]; i < hi[0]; i++) {
+                    double cx, cy, cz;
+                    coords(s, i, j, k, &cx, &cy, &cz);
+                    x[i + sj * j + sk * k] = p->solution(cx, cy, cz, p->ctx);
+                }
+    }
+    // setFieldValuefromFunction (iterativeSolverBase.hpp:537-555)
+    for (int k = 1; k <= n[2]; k++)
+        for (int j = 1; j <= n[1]; j++)
+            for (int i = 1; i <= n[0]; i++) {
+                double cx, cy, cz;
+                coords(s, i, j, k, &cx, &cy, &cz);
+                b[i + sj * j + sk * k] = p->field_b(cx, cy, cz, p->ctx);
+            }
+    // Neumann face data from trueSolutionDdir
+    if (s->has_neumann) {
+        if (!p->solution_ddir) return PPS_ERR_INVALID_ARG;
+        for (int f = 0; f < 6; f++) {
+            if (s->grid.bcs[f] != 1) continue;
+            const int d = f / 2, side = f % 2;
+            const int a0 = d == 0 ? 1 : 0, a1 = d == 2 ? 1 : 2;
+            std::vector<double> vals((size_t)face_count(s, f));
+            for (int ib = 1; ib <= n[a1]; ib++)
+                for (int ia = 1; ia <= n[a0]; ia++) {
+                    int idx[3];
+                    idx[d] = side == 0 ? 1 : n[d];
+                    idx[a0] = ia;
+                    idx[a1] = ib;
+                    double cx, cy, cz;
+                    coords(s, idx[0], idx[1], idx[2], &cx, &cy, &cz);
+                    vals[(size_t)(ia - 1) + (size_t)n[a0] * (ib - 1)] = p->solution_ddir(cx, cy, cz, d, p->ctx);
+                }
+            pps_status rc = pps_set_neumann(s, f, vals.data());
+            if (rc != PPS_OK) return rc;
+        }
+    }
+    return PPS_OK;
+}
+
+pps_status pps_set_problem_builtin(pps_solver* s, int which, double* x, double* b)
+{
+    if (which != PPS_PROBLEM_REFERENCE_DEFAULT && which != PPS_PROBLEM_SINE) return PPS_ERR_INVALID_ARG;
+    static const int ids[2] = {0, 1};
+    pps_problem p;
+    p.field_b = builtin_f;
+    p.solution = builtin_u;
+    p.solution_ddir = builtin_du;
+    p.ctx = (void*)&ids[which];
+    return pps_set_problem(s, &p, x, b);
+}
+
+pps_status pps_set_neumann(pps_solver* s, int face, const double* values)
+{
+    if (!s || face < 0 || face > 5 || !values) return PPS_ERR_INVALID_ARG;
+    if (s->grid.bcs[face] != 1) {
+        set_error("face is not a Neumann face");
+        return PPS_ERR_INVALID_ARG;
+    }
+    return guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        CK(cudaMemcpy(s->d_faces[face], values, sizeof(double) * (size_t)face_count(s, face), cudaMemcpyHostToDevice));
+        return PPS_OK;
+    });
+}
+
+pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats)
+{
+    if (!s || !x || !b) return PPS_ERR_INVALID_ARG;
+    const auto t0 = std::chrono::steady_clock::now();
+    pps_status rc = guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        const size_t fb = sizeof(double) * (size_t)s->geo.ntot;
+        const auto a = std::chrono::steady_clock::now();
+        CK(cudaMemcpyAsync(s->d_x, x, fb, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->d_b, b, fb, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        s->stats.seconds_h2d = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        s->stats.seconds_d2h = 0;
+        pps_status r = solve_core(s, s->d_x, s->d_b);
+        if (r < 0) return r;
+        const auto c = std::chrono::steady_clock::now();
+        CK(cudaMemcpyAsync(x, s->d_x, fb, cudaMemcpyDeviceToHost, s->stream));
+        if (s->cfg.form == PPS_FORM_PARITY_FP64)
+            CK(cudaMemcpyAsync(b, s->d_b, fb, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        s->stats.seconds_d2h = std::chrono::duration<double>(std::chrono::steady_clock::now() - c).count();
+        return r;
+    });
+    s->stats.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = s->stats;
+    return rc;
+}
+
+pps_status pps_solve_device(pps_solver* s, double* x_dev, double* b_dev, pps_stats* stats)
+{
+    if (!s || !x_dev || !b_dev) return PPS_ERR_INVALID_ARG;
+    const auto t0 = std::chrono::steady_clock::now();
+    pps_status rc = guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        s->stats.seconds_h2d = 0;
+        s->stats.seconds_d2h = 0;
+        return solve_core(s, x_dev, b_dev);
+    });
+    s->stats.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = s->stats;
+    return rc;
+}
+
+pps_status pps_get_stats(const pps_solver* s, pps_stats* stats)
+{
+    if (!s || !stats) return PPS_ERR_INVALID_ARG;
+    *stats = s->stats;
+    return PPS_OK;
+}
+
+pps_status pps_get_history(const pps_solver* s, double* out, int cap, int* count)
+{
+    if (!s || !count || cap < 0 || (cap > 0 && !out)) return PPS_ERR_INVALID_ARG;
+    const int n = (int)std::min<size_t>(s->history.size(), (size_t)cap);
+    for (int i = 0; i < n; i++) out[i] = s->history[(size_t)i];
+    *count = (int)s->history.size();
+    return PPS_OK;
+}
+
+pps_status pps_write_residual_history(const pps_solver* s, const char* path)
+{
+    // Format of iterativeSolverBaseAlpaka.hpp:620-638: solver time, iterations,
+    // preconditioner applications, then one residual per line.
+    if (!s || !path) return PPS_ERR_INVALID_ARG;
+    FILE* f = fopen(path, "w");
+    if (!f) {
+        set_error(std::string("cannot open ") + path);
+        return PPS_ERR_INVALID_ARG;
+    }
+    fprintf(f, "%.17g\n%d\n%d\n", s->stats.seconds_solve, s->stats.iterations, s->stats.precond_applications);
+    for (double v : s->history) fprintf(f, "%.17g\n", v);
+    fclose(f);
+    return PPS_OK;
+}
+
+pps_status pps_apply_operator(pps_solver* s, const double* u, double* out)
+{
+    if (!s || !u || !out) return PPS_ERR_INVALID_ARG;
+    return guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        const size_t fb = sizeof(double) * (size_t)s->geo.ntot;
+        CK(cudaMemcpyAsync(s->d_x, u, fb, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->d_b, out, fb, cudaMemcpyHostToDevice, s->stream));
+        if (s->cfg.form == PPS_FORM_PARITY_FP64) {
+            par_stencil(s->geo, s->d_x, s->d_b, s->stream);
+        } else {
+            state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
+            // A u = b - (b - A u): use the residual kernel with b = 0 and negate via a second pass
+            double* tmp = s->cfg.form == PPS_FORM_MIXED ? nullptr : s->f64.Az;
+            if (tmp) {
+                CK(cudaMemsetAsync(tmp, 0, fb, s->stream));
+                fast_stencil_dot<double>(s->geo, s->shape, s->d_x, tmp, s->d_b, op_coef(s->geo),
+                                         red(s, FIN_STORE), s->stream);
+            } else {
+                float* t32 = s->f32.Az;
+                float* u32 = s->f32.Y;
+                float* o32 = s->f32.W;
+                // FP32 operator on the rounded input
+                std::vector<float> hu((size_t)s->geo.ntot), ho((size_t)s->geo.ntot);
+                for (long long q = 0; q < s->geo.ntot; q++) hu[(size_t)q] = (float)u[q];
+                CK(cudaMemcpyAsync(u32, hu.data(), sizeof(float) * (size_t)s->geo.ntot, cudaMemcpyHostToDevice, s->stream));
+                CK(cudaMemsetAsync(t32, 0, sizeof(float) * (size_t)s->geo.ntot, s->stream));
+                CK(cudaMemsetAsync(o32, 0, sizeof(float) * (size_t)s->geo.ntot, s->stream));
+                fast_stencil_dot<float>(s->geo, s->shape, u32, t32, o32, op_coef(s->geo), red(s, FIN_STORE), s->stream);
+                CK(cudaMemcpyAsync(ho.data(), o32, sizeof(float) * (size_t)s->geo.ntot, cudaMemcpyDeviceToHost, s->stream));
+                CK(cudaStreamSynchronize(s->stream));
+                const long long sj = s->geo.sj, sk = s->geo.sk;
+                for (int k = s->geo.lo[2]; k < s->geo.hi[2]; k++)
+                    for (int j = s->geo.lo[1]; j < s->geo.hi[1]; j++)
+                        for (int i = s->geo.lo[0]; i < s->geo.hi[0]; i++) {
+                            const long long c = i + sj * j + sk * k;
+                            out[c] = (double)ho[(size_t)c];
+                        }
+                return PPS_OK;
+            }
+        }
+        CK(cudaMemcpyAsync(out, s->d_b, fb, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        return PPS_OK;
+    });
+}
+
+pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
+{
+    if (!s || !B || !X) return PPS_ERR_INVALID_ARG;
+    return guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        const Geo& g = s->geo;
+        const size_t fb = sizeof(double) * (size_t)g.ntot;
+        if (s->cfg.form == PPS_FORM_PARITY_FP64) {
+            CK(cudaMemcpyAsync(s->d_b, B, fb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(s->d_x, X, fb, cudaMemcpyHostToDevice, s->stream));
+            par_precond(s, s->d_b, s->d_x);
+            CK(cudaMemcpyAsync(X, s->d_x, fb, cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            return PPS_OK;
+        }
+        state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
+        Launcher L{s, false};
+        if (s->cfg.form == PPS_FORM_FP64) {
+            CK(cudaMemcpyAsync(s->f64.r, B, fb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(s->f64.z, X, fb, cudaMemcpyHostToDevice, s->stream));
+            fast_precond<double>(s, s->f64, s->f64.r, s->f64.z, L);
+            CK(cudaMemcpyAsync(X, s->f64.z, fb, cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            return PPS_OK;
+        }
+        std::vector<float> hb((size_t)g.ntot), hx((size_t)g.ntot);
+        for (long long q = 0; q < g.ntot; q++) {
+            hb[(size_t)q] = (float)B[q];
+            hx[(size_t)q] = (float)X[q];
+        }
+        CK(cudaMemcpyAsync(s->f32.r, hb.data(), sizeof(float) * (size_t)g.ntot, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->f32.z, hx.data(), sizeof(float) * (size_t)g.ntot, cudaMemcpyHostToDevice, s->stream));
+        fast_precond<float>(s, s->f32, s->f32.r, s->f32.z, L);
+        CK(cudaMemcpyAsync(hx.data(), s->f32.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (long long q = 0; q < g.ntot; q++) X[q] = (double)hx[(size_t)q];
+        return PPS_OK;
+    });
+}
+
+int pps_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+const char* pps_status_string(pps_status st)
+{
+    switch (st) {
+    case PPS_OK: return "ok";
+    case PPS_NOT_CONVERGED: return "not converged (iteration cap reached)";
+    case PPS_BREAKDOWN: return "Krylov breakdown";
+    case PPS_NAN_DETECTED: return "NaN/Inf in the residual";
+    case PPS_TIMEOUT: return "device wait timed out";
+    case PPS_ERR_INVALID_ARG: return "invalid argument";
+    case PPS_ERR_CUDA: return "CUDA error";
+    case PPS_ERR_OUT_OF_MEMORY: return "out of memory";
+    case PPS_ERR_ZERO_RHS: return "zero right-hand side";
+    case PPS_ERR_UNSUPPORTED: return "unsupported";
+    case PPS_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* pps_last_error(void) { return g_last_error.c_str(); }
+
+int pps_abi_version(void) { return PPS_ABI_VERSION; }
+
+}  // extern "C"

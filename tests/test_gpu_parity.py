@@ -1,0 +1,255 @@
+"""GPU parity of libpps against the oracle, through the C ABI.
+
+* PARITY form: bit-identical to the oracle (itself bit-identical to the reference)
+  on every golden case, including Neumann faces, CG, no preconditioner, degrees
+  1/2/3/5, the iteration cap, the early return and one-unknown axes;
+* FP64 form: the same iterations (+-1) and a solution within the reference's own
+  reduction-order envelope (rel-L2 <= 1e-9 at a 1e-10 stop; <= 1e-11 when both stop
+  at 1e-13, the bar of the measured envelope 9.0e-14 plus margin);
+* MIXED form: FP64 true residual <= tol, solution within the discretisation-free
+  distance the stopping test allows;
+* building blocks: the operator and one preconditioner application per form.
+"""
+import numpy as np
+import pytest
+
+import parallelpoissonsolver_gb300 as pps
+from cases import BY_NAME, CASES, random_inputs
+from conftest import load_golden, rel_l2, same_bits
+
+pytestmark = pytest.mark.gpu
+
+FULL = [c["name"] for c in CASES if c["store"] == "full"]
+
+
+def grid_of(case):
+    return pps.BlockGrid(npglobal=case["np"], ds=case["ds"], origin=case["origin"], bcs=case["bcs"])
+
+
+def ogrid_of(O, case):
+    return O.Grid(np=case["np"], ds=case["ds"], origin=case["origin"], bcs=case["bcs"])
+
+
+def make_solver(case, form, **over):
+    c = {**case["cfg"], **over}
+    prec = pps.NoneSolver() if c["precond"] == 0 else pps.ChebyshevIteration(
+        c["cheb_degree"], c["cheb_eps"], c["rescale_min"], c["rescale_max"])
+    cls = pps.BaseCG if c["krylov"] == 1 else pps.BiCGSTAB
+    return cls(grid_of(case), prec, tolerance=c["tol"], max_iteration=c["maxit"], form=form)
+
+
+def case_inputs(O, case):
+    kind, arg = case["inputs"]
+    if case["store"] == "full":
+        g = load_golden(case["name"])
+        faces = [g.get(f"face{f}") for f in range(6)]
+        return g["x_in"].copy(), g["b_in"].copy(), faces
+    x, b, faces = O.set_problem(ogrid_of(O, case), arg)
+    return x, b, faces
+
+
+def run_gpu(case, form, x, b, faces, **over):
+    s = make_solver(case, form, **over)
+    for f, a in enumerate(faces):
+        if a is not None:
+            s.set_neumann(f, a)
+    st = s(x, b, raise_on_error=False)
+    return s, st
+
+
+def run_oracle(O, case, x, b, faces, **over):
+    faces_o = faces if any(f is not None for f in faces) else None
+    return O.solve(ogrid_of(O, case), O.Config(**{**case["cfg"], **over}), x, b, faces_o)
+
+
+@pytest.mark.parametrize("name", FULL)
+def test_parity_form_is_bit_identical(gpu, oracle, name):
+    case = BY_NAME[name]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    r = run_oracle(oracle, case, xo, bo, faces)
+    s, st = run_gpu(case, "parity", x, b, faces)
+    assert st >= 0
+    assert s.get_num_iteration_final() == r.iterations
+    assert same_bits(x, xo) and same_bits(b, bo)
+    assert same_bits(s.history(), r.history)
+    assert same_bits(s.get_error_compute_operator(), r.err_true)
+    g = load_golden(name)
+    assert s.get_num_iteration_final() == int(g["iterations"])
+    if not np.isnan(g["err_true"]):
+        assert rel_l2(x, g["x_out"]) < 1e-13
+    s.close()
+
+
+@pytest.mark.parametrize("name", ["config1_sine_m64", "case1b_problem0_m64"])
+def test_parity_form_64cubed(gpu, oracle, name):
+    case = BY_NAME[name]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    r = run_oracle(oracle, case, xo, bo, faces)
+    s, st = run_gpu(case, "parity", x, b, faces)
+    assert st == pps.OK
+    assert s.get_num_iteration_final() == r.iterations == int(load_golden(name)["iterations"])
+    assert same_bits(x, xo)
+
+
+CONVERGING = [n for n in FULL if n not in ("degree1_m8", "cg_neumann_m8", "iteration_cap_m12")]
+
+
+@pytest.mark.parametrize("name", CONVERGING)
+def test_fp64_form_matches_oracle(gpu, oracle, name):
+    case = BY_NAME[name]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    r = run_oracle(oracle, case, xo, bo, faces)
+    s, st = run_gpu(case, "fp64", x, b, faces)
+    assert st == pps.OK
+    assert abs(s.get_num_iteration_final() - r.iterations) <= 1
+    if r.iterations == 0:
+        # the reference leaves x scaled by 1/||b_adj|| on its early return; the FP64
+        # form returns the unscaled x unchanged
+        return
+    tol = case["cfg"]["tol"]
+    # reassociation envelope: 1e-9 at a 1e-10 stop, 1e-11 at 1e-13 (FP64 rounding only)
+    bound = 1e-11 if tol < 1e-12 else 1e-9
+    assert rel_l2(x, xo) <= bound
+    assert s.get_error_compute_operator() < 10 * tol
+
+
+@pytest.mark.parametrize("name", ["dirichlet_random_m10", "neumann_problem0_m10", "neumann_random_ragged",
+                                  "cg_chebyshev_m10", "no_preconditioner_m10", "dirichlet_problem0_aniso"])
+def test_mixed_form_reaches_fp64_tolerance(gpu, oracle, name):
+    case = BY_NAME[name]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    run_oracle(oracle, case, xo, bo, faces, tol=1e-13, maxit=20000)
+    s, st = run_gpu(case, "mixed", x, b, faces)
+    assert st == pps.OK, pps.status_string(st)
+    assert s.get_error_compute_operator() <= case["cfg"]["tol"]
+    assert s.stats()["refinements"] >= 1
+    assert rel_l2(x, xo) < 1e-6
+
+
+def test_fp64_1e13_within_envelope(gpu, oracle):
+    """Both stop at 1e-13: plain FP64 GPU vs the reference <= 1e-11 rel-L2 (measured
+    reference-vs-reference envelope at this stop: 9.0e-14)."""
+    case = BY_NAME["case1b_problem0_m64_tol1e13"]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    r = run_oracle(oracle, case, xo, bo, faces)
+    s, st = run_gpu(case, "fp64", x, b, faces)
+    assert st == pps.OK
+    assert abs(s.get_num_iteration_final() - r.iterations) <= 1
+    assert rel_l2(x, xo) <= 1e-11
+
+
+def test_fp64_config1_and_1b(gpu, oracle):
+    for name in ("config1_sine_m64", "case1b_problem0_m64"):
+        case = BY_NAME[name]
+        x, b, faces = case_inputs(oracle, case)
+        xo, bo = x.copy(), b.copy()
+        r = run_oracle(oracle, case, xo, bo, faces)
+        for form in ("fp64", "mixed"):
+            xg = x.copy()
+            s, st = run_gpu(case, form, xg, b.copy(), faces)
+            assert st == pps.OK
+            assert s.get_error_compute_operator() <= 1e-10
+            if form == "fp64":
+                assert abs(s.get_num_iteration_final() - r.iterations) <= 1
+                assert rel_l2(xg, xo) <= 1e-9
+
+
+def test_fp64_is_deterministic(gpu, oracle):
+    case = BY_NAME["case1b_problem0_m64"]
+    outs = []
+    for _ in range(2):
+        x, b, faces = case_inputs(oracle, case)
+        run_gpu(case, "fp64", x, b, faces)
+        outs.append(x)
+    assert same_bits(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("form", ["parity", "fp64"])
+def test_operator_kernel(gpu, oracle, form):
+    rng = np.random.default_rng(3)
+    case = dict(np=(13, 10, 17), ds=(0.1, 0.07, 0.13), origin=(0.0, 0.0, 0.0), bcs=(0, 1, 1, 0, 0, 0),
+                cfg=BY_NAME["dirichlet_random_m10"]["cfg"])
+    u = rng.standard_normal(grid_of(case).shape)
+    s = make_solver(case, form)
+    got = s.apply_operator(u)
+    want = oracle.apply_A(ogrid_of(oracle, case), u)
+    sl = grid_of(case).unknowns()
+    if form == "parity":
+        assert same_bits(got[sl], want[sl])
+    else:
+        assert np.max(np.abs(got[sl] - want[sl])) <= 1e-12 * np.max(np.abs(want[sl]))
+
+
+@pytest.mark.parametrize("form,degree", [("parity", 11), ("parity", 3), ("fp64", 11), ("fp64", 2), ("fp64", 4),
+                                         ("fp64", 24), ("mixed", 11)])
+def test_preconditioner_kernel(gpu, oracle, form, degree):
+    rng = np.random.default_rng(degree)
+    case = dict(np=(12, 14, 11), ds=(0.1, 0.1, 0.1), origin=(0.0, 0.0, 0.0), bcs=(0, 0, 1, 0, 0, 1),
+                cfg={**BY_NAME["dirichlet_random_m10"]["cfg"], "cheb_degree": degree})
+    g = grid_of(case)
+    B = np.zeros(g.shape)
+    sl = g.unknowns()
+    B[sl] = rng.standard_normal(B[sl].shape)
+    s = make_solver(case, form)
+    got = s.apply_preconditioner(B.copy())
+    want = oracle.cheb_apply(ogrid_of(oracle, case), oracle.Config(**case["cfg"]), B.copy())
+    if form == "parity":
+        assert same_bits(got[sl], want[sl])
+    else:
+        tol = 1e-12 if form == "fp64" else 2e-5
+        assert rel_l2(got[sl], want[sl]) <= tol
+
+
+def test_error_statuses(gpu, oracle):
+    case = BY_NAME["dirichlet_random_m10"]
+    x, b, faces = case_inputs(oracle, case)
+    # zero right-hand side and zero boundary data: ||b_adj|| = 0
+    s, st = run_gpu(case, "fp64", np.zeros_like(x), np.zeros_like(b), faces)
+    assert st == pps.ERR_ZERO_RHS
+    # iteration cap
+    s, st = run_gpu(case, "fp64", x.copy(), b.copy(), faces, maxit=3)
+    assert st == pps.NOT_CONVERGED and s.get_num_iteration_final() == 3
+    # degree 1: the reference's preconditioner returns 0 and its alpha divides by 0
+    s, st = run_gpu(BY_NAME["degree1_m8"], "fp64", *case_inputs(oracle, BY_NAME["degree1_m8"]))
+    assert st == pps.BREAKDOWN
+    # NaN in the input
+    xb = x.copy()
+    bb = b.copy()
+    bb[5, 5, 5] = np.nan
+    s, st = run_gpu(case, "fp64", xb, bb, faces)
+    assert st in (pps.NAN_DETECTED, pps.BREAKDOWN, pps.ERR_ZERO_RHS)
+
+
+def test_solve_device_matches_host_path(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    case = BY_NAME["neumann_random_ragged"]
+    x, b, faces = case_inputs(oracle, case)
+    xh = x.copy()
+    s, st = run_gpu(case, "fp64", xh, b.copy(), faces)
+    xd = torch.from_numpy(x.copy()).cuda()
+    bd = torch.from_numpy(b.copy()).cuda()
+    s2 = make_solver(case, "fp64")
+    for f, a in enumerate(faces):
+        if a is not None:
+            s2.set_neumann(f, a)
+    torch.cuda.synchronize()
+    assert s2.solve_device(xd.data_ptr(), bd.data_ptr()) == pps.OK
+    assert same_bits(xd.cpu().numpy(), xh)
+
+
+def test_residual_history_file(gpu, oracle, tmp_path):
+    case = BY_NAME["dirichlet_random_m10"]
+    x, b, faces = case_inputs(oracle, case)
+    s, st = run_gpu(case, "fp64", x, b, faces)
+    p = tmp_path / "residualHistory.txt"
+    s.write_residual_history(str(p))
+    lines = p.read_text().split()
+    assert int(lines[1]) == s.get_num_iteration_final()
+    h = np.array([float(v) for v in lines[3:]])
+    assert len(h) == s.get_num_iteration_final() + 1
+    assert h[-1] < case["cfg"]["tol"]

@@ -1,0 +1,139 @@
+"""The oracle pinned against the reference (CPU only).
+
+* every golden fixture (made by the reference's own solver, tests/golden/make_golden.py)
+  is reproduced by the C restatement: bit for bit on x86-64, where the fixtures were
+  made, and to 1e-13 with equal iteration counts elsewhere (libm may differ);
+* where oracle/_ref is built, fresh random cases match the reference bit for bit;
+* threading the element-wise passes does not change a bit.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from cases import BY_NAME, CASES, random_inputs
+from conftest import load_golden, rel_l2, same_bits
+
+X86 = platform.machine() in ("x86_64", "AMD64")
+
+
+def grid_of(O, case):
+    return O.Grid(np=case["np"], ds=case["ds"], origin=case["origin"], bcs=case["bcs"])
+
+
+def inputs_of(O, case, g):
+    kind, arg = case["inputs"]
+    if case["store"] == "full":
+        x, b = g["x_in"].copy(), g["b_in"].copy()
+        faces = [g.get(f"face{f}") for f in range(6)]
+        if all(f is None for f in faces):
+            faces = None
+        return x, b, faces
+    grid = grid_of(O, case)
+    x, b, faces = O.set_problem(grid, arg)
+    if not any(f is not None for f in faces):
+        faces = None
+    return x, b, faces
+
+
+@pytest.mark.parametrize("name", [c["name"] for c in CASES])
+def test_port_matches_golden(oracle, name):
+    case = BY_NAME[name]
+    g = load_golden(name)
+    grid = grid_of(oracle, case)
+    x, b, faces = inputs_of(oracle, case, g)
+    res = oracle.solve(grid, oracle.Config(**case["cfg"]), x, b, faces)
+    assert res.iterations == int(g["iterations"])
+    if case["store"] == "full":
+        if X86:
+            assert same_bits(x, g["x_out"]) and same_bits(b, g["b_out"])
+            assert same_bits(res.history, g["history"])
+        else:
+            assert np.isnan(g["err_true"]) or rel_l2(x, g["x_out"]) < 1e-13
+    else:
+        sample = x.ravel()[g["sample_index"]]
+        if X86:
+            assert same_bits(sample, g["x_out_sample"])
+            assert same_bits(res.history, g["history"])
+        else:
+            assert rel_l2(sample, g["x_out_sample"]) < 1e-12
+
+
+def test_port_cheb_params_match_golden(oracle):
+    for case in CASES:
+        g = load_golden(case["name"])
+        p = oracle.cheb_params(grid_of(oracle, case), oracle.Config(**case["cfg"]))
+        if X86:
+            assert p == (float(g["theta"]), float(g["delta"]), float(g["sigma"]))
+        else:
+            assert np.allclose(p, (g["theta"], g["delta"], g["sigma"]), rtol=1e-15)
+
+
+def test_set_problem_matches_reference(oracle):
+    if not oracle.ref_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    for bcs in [(0,) * 6, (0, 1, 0, 1, 0, 1)]:
+        for p in (0, 1):
+            grid = oracle.Grid(np=(9, 7, 8), ds=(0.1, 0.2, 0.15), origin=(0.5, -1.0, 0.25), bcs=bcs)
+            x, b, _ = oracle.set_problem(grid, p)
+            xr, br = oracle.ref_set_problem(grid, p)
+            assert same_bits(x, xr) and same_bits(b, br)
+
+
+@pytest.mark.parametrize("seed,bcs,kw", [
+    (101, (0,) * 6, {}),
+    (102, (0, 1, 1, 0, 0, 1), {}),
+    (103, (0,) * 6, dict(krylov=1)),
+    (104, (1, 0, 0, 0, 0, 0), dict(cheb_degree=24, cheb_eps=0.0, rescale_min=100.0, maxit=1000)),
+    (105, (0,) * 6, dict(precond=0)),
+    (106, (0,) * 6, dict(cheb_degree=4)),
+])
+def test_port_matches_reference_random(oracle, seed, bcs, kw):
+    if not oracle.ref_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    rng = np.random.default_rng(seed)
+    n = tuple(int(v) for v in rng.integers(5, 13, 3))
+    case = dict(np=n, ds=tuple(float(v) for v in rng.uniform(0.05, 0.2, 3)), origin=(0.0, 0.0, 0.0), bcs=bcs)
+    grid = grid_of(oracle, case)
+    x0, b0, faces = random_inputs(case, seed)
+    if not any(f is not None for f in faces):
+        faces = None
+    cfg = oracle.Config(**{**dict(tol=1e-10, maxit=1700), **kw})
+    xr, br = x0.copy(), b0.copy()
+    r = oracle.ref_solve(grid, cfg, xr, br, neumann=faces)
+    xp, bp = x0.copy(), b0.copy()
+    p = oracle.solve(grid, cfg, xp, bp, faces)
+    assert r.iterations == p.iterations
+    assert same_bits(xr, xp) and same_bits(br, bp) and same_bits(r.history, p.history)
+
+
+def test_threads_do_not_change_bits(oracle):
+    case = BY_NAME["neumann_random_ragged"]
+    g = load_golden(case["name"])
+    grid = grid_of(oracle, case)
+    outs = []
+    for t in (1, 4):
+        x, b, faces = inputs_of(oracle, case, g)
+        oracle.solve(grid, oracle.Config(**{**case["cfg"], "threads": t}), x, b, faces)
+        outs.append(x)
+    assert same_bits(outs[0], outs[1])
+
+
+def test_operator_against_numpy(oracle):
+    """MatrixFreeOperatorA restated in numpy (matrixFreeOperatorA.hpp:34-38), same operand order."""
+    rng = np.random.default_rng(7)
+    grid = oracle.Grid(np=(7, 6, 5), ds=(0.1, 0.2, 0.3), bcs=(0, 1, 0, 0, 1, 0))
+    u = rng.standard_normal(grid.shape)
+    out = oracle.apply_A(grid, u)
+    s = grid.unknown_slices()
+    z, y, x = s
+
+    def sh(dz, dy, dx):
+        return u[z.start + dz:z.stop + dz, y.start + dy:y.stop + dy, x.start + dx:x.stop + dx]
+
+    c = u[s]
+    h = grid.ds
+    ref = ((sh(0, 0, -1) - 2 * c + sh(0, 0, 1)) / (h[0] * h[0])
+           + (sh(0, -1, 0) - 2 * c + sh(0, 1, 0)) / (h[1] * h[1])
+           + (sh(-1, 0, 0) - 2 * c + sh(1, 0, 0)) / (h[2] * h[2]))
+    assert same_bits(out[s], ref)
