@@ -1,0 +1,372 @@
+"""Benchmark of the Poisson solve loop on GB300 (one JSON line on stdout).
+
+Metric: time to ||r||/||b|| <= 1e-10 at 512^3 (plain FP64 vs mixed precision),
+with HBM GB/s of the dominant kernel.  Workload: 512^3 unknowns, Dirichlet 0, b = -f
+with f a seeded unit-RMS Gaussian random field, P(k) ~ k^-2 (seed 2), solved by
+BiCGSTAB + Chebyshev(11) (the reference CPU preset) from x = 0.
+
+One step = one full solve.  `value` is the device time per solve of the fastest
+form (MIXED) with the fields resident in HBM; `e2e` is the same solve through
+pps_solve() on pinned host buffers, copies included; the plain FP64 form is timed
+beside it.  Every field is 0.5-1.1 GB, far larger than the 129 MB L2, so no L2 flush
+is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--size M] [--impl reference]
+
+--impl reference times the reference's CPU implementation of the path on the host
+cores: the oracle's C restatement (bit-identical to the reference solver), all
+host threads on the element-wise passes, sums serial as in the reference.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed FP32/FP64 vs plain FP64), 1 GB300"
+TOL = 1e-10
+DEGREE = 11
+# Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload: the plain
+# FP64 GPU form runs the reference algorithm (same iteration count +-1, checked on
+# the golden cases) and measured this count; the CPU leg multiplies its timed
+# per-iteration cost by it.
+REFERENCE_ITERATIONS = {512: 166}
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "cheb_sweep_fp32_traffic.txt")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Replica coordination under torchrun: barrier and max over ranks (gloo, host)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        busy = [v for v in sm if mx and v > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_ratio():
+    """dram bytes / algorithmic bytes of one FP32 sweep launch, from the committed ncu summary."""
+    if not os.path.exists(PROFILE_TRAFFIC):
+        return None
+    for line in open(PROFILE_TRAFFIC):
+        if line.startswith("traffic_over_algorithmic:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def make_inputs(m: int):
+    from parallelpoissonsolver_gb300 import workloads
+    b = workloads.random_field(m, seed=2, slope=-2.0)
+    x = np.zeros_like(b)
+    return x, b
+
+
+def run_gpu(args, dist: Dist):
+    import torch
+
+    import parallelpoissonsolver_gb300 as pps
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    m = args.size
+    grid = pps.BlockGrid.cube(m)
+    n_unknowns = m ** 3
+    x_h, b_h = make_inputs(m)
+    b_d = torch.from_numpy(b_h).to(f"cuda:{dev}")
+    x_d = torch.zeros_like(b_d)
+    G = b_h.size
+    prec = pps.ChebyshevIteration(DEGREE)
+
+    mixed = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
+                         device=dev)
+    plain = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="fp64", use_graph=False,
+                         device=dev)
+
+    def solve(s):
+        x_d.zero_()
+        torch.cuda.current_stream().synchronize()   # the solver runs on its own stream
+        st = s.solve_device(x_d.data_ptr(), b_d.data_ptr())
+        if st != pps.OK:
+            raise RuntimeError(f"solve failed: {pps.status_string(st)}")
+        return s.stats()
+
+    for _ in range(args.warmup):
+        solve(mixed)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K mixed solves, fields resident in HBM ----
+    dist.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    stats = []
+    with ClockSampler(dev) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            stats.append(solve(mixed))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    dist.barrier()
+    dev_times = [s["seconds_solve"] for s in stats]
+    t_step = dist.max(sum(dev_times) / len(dev_times))
+    del stream
+    mixed_x = x_d.clone()
+
+    # ---- plain FP64 form, same workload ----
+    plain_stats = []
+    for _ in range(max(1, args.plain_steps)):
+        plain_stats.append(solve(plain))
+    t_plain = sum(s["seconds_solve"] for s in plain_stats) / len(plain_stats)
+    plain_x = x_d.clone()
+    rel_diff = float(torch.linalg.norm(mixed_x - plain_x) / torch.linalg.norm(plain_x))
+
+    # ---- e2e: the C ABI on pinned host buffers, copies inside the timed region ----
+    xp = torch.zeros(b_h.shape, dtype=torch.float64).pin_memory()
+    bp = torch.from_numpy(b_h).pin_memory()
+    xn, bn = xp.numpy(), bp.numpy()
+    e2e = []
+    for k in range(args.steps + 1):
+        xn[...] = 0.0
+        t = time.perf_counter()
+        st = mixed(xn, bn)
+        el = time.perf_counter() - t
+        if st != pps.OK:
+            raise RuntimeError(f"e2e solve failed: {pps.status_string(st)}")
+        if k > 0:
+            e2e.append(el)
+    t_e2e = dist.max(sum(e2e) / len(e2e))
+
+    # ---- roofline of the dominant kernel (the FP32 Chebyshev sweep) ----
+    sweep_s = sum(s["sweep_seconds"] for s in stats)
+    sweep_n = sum(s["sweep_launches"] for s in stats)
+    sweep_b = sum(s["sweep_bytes"] for s in stats)
+    peak, peak_src = measured_peaks()
+    achieved = (sweep_b / sweep_s) / 1e9 if sweep_s > 0 else None
+    ratio = traffic_ratio()
+    per_launch_alg = sweep_b / sweep_n if sweep_n else None
+    p_sweep_s = sum(s["sweep_seconds"] for s in plain_stats)
+    p_sweep_b = sum(s["sweep_bytes"] for s in plain_stats)
+
+    out = {
+        "metric": METRIC,
+        "value": t_step,
+        "unit": "s",
+        "n_gpus": dist.ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 stencil/smoother/Krylov fields + f64 residual/dots/refinement",
+        "data": "synthetic: seeded k^-2 Gaussian random field (numpy PCG64 seed 2), unit RMS",
+        "config": {
+            "workload": f"{m}^3 interior unknowns, h=1/{m + 1}, Dirichlet 0, -lap u = f, f ~ P(k) k^-2 field; "
+                        f"BiCGSTAB + Chebyshev({DEGREE}) preconditioner, stop at ||r||/||b_adj|| <= {TOL:g}",
+            "form": "mixed: FP32 inner BiCGSTAB/Chebyshev with FP64-accurate dots, FP64 iterative refinement",
+            "l2": "no flush: every field (0.5-1.1 GB) exceeds the 129 MB L2",
+            "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU, single domain",
+            "iterations": stats[-1]["iterations"],
+            "refinements": stats[-1]["refinements"],
+            "err_true": stats[-1]["err_true"],
+        },
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8},
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "plain_fp64": {
+            "value": t_plain, "unit": "s", "iterations": plain_stats[-1]["iterations"],
+            "err_true": plain_stats[-1]["err_true"],
+            "sweep_gbs": (p_sweep_b / p_sweep_s) / 1e9 if p_sweep_s > 0 else None,
+        },
+        "speedup_mixed_vs_fp64": t_plain / t_step,
+        "mixed_vs_fp64_rel_l2": rel_diff,
+        "hbm_gbs_solve": stats[-1]["hbm_bytes"] / stats[-1]["seconds_solve"] / 1e9,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "k_cheb_sweep<float> (Chebyshev sweep, 16 B per unknown)",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
+            "traffic": (ratio * per_launch_alg) if (ratio and per_launch_alg) else None,
+            "algorithmic_bytes_per_launch": per_launch_alg,
+            "launches_timed": sweep_n,
+        },
+        "clocks": clocks.summary(),
+        "wall_s_timed_region": wall,
+    }
+    mixed.close()
+    plain.close()
+    return out, plain_stats[-1]["iterations"]
+
+
+def cpu_sample(m: int, iterations_needed: int | None, threads: int):
+    """Bounded sample of the reference CPU solve on this workload: set-up plus a few
+    BiCGSTAB iterations of the oracle port (bit-identical to the reference)."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    g = O.cube(m)
+    x0, b0 = make_inputs(m)
+    # warm the thread pool and page in the fields, then time set-up + 3 iterations
+    O.solve(g, O.Config(tol=TOL, maxit=1, threads=threads), x0.copy(), b0.copy())
+    x, b = x0.copy(), b0.copy()
+    t = time.perf_counter()
+    r = O.solve(g, O.Config(tol=TOL, maxit=3, threads=threads), x, b)
+    total = time.perf_counter() - t
+    t_iter = r.seconds_loop / max(r.iterations, 1)
+    t_setup = max(total - r.seconds_loop, 0.0)
+    n_it = iterations_needed if iterations_needed else 1
+    return {
+        "value": t_setup + n_it * t_iter,
+        "unit": "s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{m}^3, set-up + 3 BiCGSTAB iterations of the oracle port (bit-identical to the "
+                  f"reference CPU solver; {threads} threads on element-wise passes, serial sums); "
+                  f"extrapolated to {n_it} iterations: {t_iter:.3f} s/iteration, {t_setup:.3f} s set-up",
+        "seconds_per_iteration": t_iter,
+        "seconds_setup": t_setup,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    args = ap.parse_args()
+    threads = args.cpu_threads or os.cpu_count() or 1
+
+    dist = Dist()
+    if args.impl == "reference":
+        if dist.rank == 0:
+            n_it = REFERENCE_ITERATIONS.get(args.size)
+            samples = [cpu_sample(args.size, n_it, threads) for _ in range(max(1, args.steps))]
+            v = sum(s["value"] for s in samples) / len(samples)
+            line = {
+                "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (same workload)",
+                "config": {"workload": f"{args.size}^3, Dirichlet 0, k^-2 random field, BiCGSTAB+Chebyshev(11), "
+                                       f"tol {TOL:g}", "iterations_extrapolated": n_it},
+                "cpu_baseline": {k: samples[-1][k] for k in ("kind", "cores", "sample")} | {"value": v,
+                                                                                           "unit": "s"},
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            }
+            print(json.dumps(line), flush=True)
+        dist.close()
+        return
+
+    out, iters_fp64 = run_gpu(args, dist)
+    if dist.rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_sample(args.size, iters_fp64, threads)
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()
