@@ -66,9 +66,9 @@ CASES = [
          store="full"),
     # 64^3 interior, h = 1/65: the sine right-hand side (an exact discrete eigenvector,
     # 1 iteration) and the non-degenerate companion (reference default manufactured solution).
-    dict(name="config1_sine_m64", **cube(64), bcs=(0,) * 6, cfg=cfg(), inputs=("problem", 1), store="summary"),
-    dict(name="case1b_problem0_m64", **cube(64), bcs=(0,) * 6, cfg=cfg(), inputs=("problem", 0), store="summary"),
-    dict(name="case1b_problem0_m64_tol1e13", **cube(64), bcs=(0,) * 6, cfg=cfg(tol=1e-13, maxit=20000),
+    dict(name="sine_eigenvector_m64", **cube(64), bcs=(0,) * 6, cfg=cfg(), inputs=("problem", 1), store="summary"),
+    dict(name="problem0_m64", **cube(64), bcs=(0,) * 6, cfg=cfg(), inputs=("problem", 0), store="summary"),
+    dict(name="problem0_m64_tol1e13", **cube(64), bcs=(0,) * 6, cfg=cfg(tol=1e-13, maxit=20000),
          inputs=("problem", 0), store="summary"),
 ]
 

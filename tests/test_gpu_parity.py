@@ -81,7 +81,7 @@ def test_parity_form_is_bit_identical(gpu, oracle, name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["config1_sine_m64", "case1b_problem0_m64"])
+@pytest.mark.parametrize("name", ["sine_eigenvector_m64", "problem0_m64"])
 def test_parity_form_64cubed(gpu, oracle, name):
     case = BY_NAME[name]
     x, b, faces = case_inputs(oracle, case)
@@ -133,7 +133,7 @@ def test_mixed_form_reaches_fp64_tolerance(gpu, oracle, name):
 def test_fp64_1e13_within_envelope(gpu, oracle):
     """Both stop at 1e-13: plain FP64 GPU vs the reference <= 1e-11 rel-L2 (measured
     reference-vs-reference envelope at this stop: 9.0e-14)."""
-    case = BY_NAME["case1b_problem0_m64_tol1e13"]
+    case = BY_NAME["problem0_m64_tol1e13"]
     x, b, faces = case_inputs(oracle, case)
     xo, bo = x.copy(), b.copy()
     r = run_oracle(oracle, case, xo, bo, faces)
@@ -143,8 +143,8 @@ def test_fp64_1e13_within_envelope(gpu, oracle):
     assert rel_l2(x, xo) <= 1e-11
 
 
-def test_fp64_config1_and_1b(gpu, oracle):
-    for name in ("config1_sine_m64", "case1b_problem0_m64"):
+def test_fp64_sine_and_problem0_64cubed(gpu, oracle):
+    for name in ("sine_eigenvector_m64", "problem0_m64"):
         case = BY_NAME[name]
         x, b, faces = case_inputs(oracle, case)
         xo, bo = x.copy(), b.copy()
@@ -160,7 +160,7 @@ def test_fp64_config1_and_1b(gpu, oracle):
 
 
 def test_fp64_is_deterministic(gpu, oracle):
-    case = BY_NAME["case1b_problem0_m64"]
+    case = BY_NAME["problem0_m64"]
     outs = []
     for _ in range(2):
         x, b, faces = case_inputs(oracle, case)
