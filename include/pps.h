@@ -162,6 +162,29 @@ pps_status pps_apply_operator(pps_solver* s, const double* u, double* out);
  * in preconditioner mode, chebyshevIteration.hpp:48-140), in the solver's form. */
 pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
 
+/* Operator apply that allocates nothing.  No counterpart in the reference: it is for
+ * callers that cannot call cudaMalloc -- code recorded into a CUDA graph (no
+ * allocation while a stream is captured), loops that forbid allocation after
+ * start-up, or plugins whose host framework owns all device memory -- and so
+ * cannot create a pps_solver.
+ *
+ * On device pointers of the field layout: out_dev = A u at the unknowns (the FP64
+ * form's kernel; every other entry of out_dev is left as it was) and
+ * *energy_dev = sum of u*(A u) over the unknowns.  Work is queued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream); the call does not wait.
+ *
+ * Its reduction scratch is a file-scope __device__ array of
+ * 512 + 32*PPS_NOALLOC_MAX_BLOCKS bytes (about 512 KiB) that every GPU which loads
+ * the library holds until the process exits.  Grids whose launch needs more than
+ * PPS_NOALLOC_MAX_BLOCKS thread blocks are rejected with PPS_ERR_INVALID_ARG.
+ * The first call on each device looks up the array's device address with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the one array, so calls that overlap on the GPU (other streams, other
+ * threads) race: serialise them. */
+#define PPS_NOALLOC_MAX_BLOCKS 16384
+pps_status pps_apply_operator_noalloc(const pps_grid* grid, const double* u_dev, double* out_dev,
+                                      double* energy_dev, void* stream);
+
 /* Number of CUDA devices visible to the library (0 without a GPU). */
 int pps_device_count(void);
 const char* pps_status_string(pps_status st);

@@ -40,7 +40,7 @@ EXPORTED = [
     "pps_config_default", "pps_create", "pps_destroy", "pps_set_problem", "pps_set_problem_builtin",
     "pps_set_neumann", "pps_solve", "pps_solve_device", "pps_get_stats", "pps_get_history",
     "pps_write_residual_history", "pps_apply_operator", "pps_apply_preconditioner", "pps_device_count",
-    "pps_status_string", "pps_last_error", "pps_abi_version",
+    "pps_status_string", "pps_last_error", "pps_abi_version", "pps_apply_operator_noalloc",
 ]
 
 
@@ -110,6 +110,7 @@ def load(build_if_missing: bool = False):
     L.pps_write_residual_history.argtypes = [vp, C.c_char_p]
     L.pps_apply_operator.argtypes = [vp, vp, vp]
     L.pps_apply_preconditioner.argtypes = [vp, vp, vp]
+    L.pps_apply_operator_noalloc.argtypes = [C.POINTER(PpsGrid), vp, vp, vp, vp]
     L.pps_status_string.restype = C.c_char_p
     L.pps_status_string.argtypes = [C.c_int]
     L.pps_last_error.restype = C.c_char_p
@@ -344,6 +345,13 @@ class BiCGSTAB(Solver):
 class BaseCG(Solver):
     """Preconditioned CG main loop (baseCG.hpp:14-269)."""
     krylov = KRYLOV_CG
+
+
+def apply_operator_noalloc(grid: BlockGrid, u_ptr: int, out_ptr: int, energy_ptr: int, stream: int = 0) -> int:
+    """pps_apply_operator_noalloc on device pointers: out = A u at the unknowns and
+    energy = sum u*(A u), with no device allocation (see include/pps.h)."""
+    return int(load().pps_apply_operator_noalloc(C.byref(grid.c()), C.c_void_p(u_ptr), C.c_void_p(out_ptr),
+                                                 C.c_void_p(energy_ptr), C.c_void_p(stream or None)))
 
 
 def check_solution(grid: BlockGrid, x: np.ndarray, exact: np.ndarray):

@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Records the message pps_last_error() returns on this thread.
+extern "C" void pps_internal_set_error(const char* msg);
+
 namespace pps {
 
 // Geometry of one single-rank grid in the guard-padded field layout

@@ -1250,6 +1250,8 @@ const char* pps_status_string(pps_status st)
 
 const char* pps_last_error(void) { return g_last_error.c_str(); }
 
+void pps_internal_set_error(const char* msg) { set_error(msg ? msg : ""); }
+
 int pps_abi_version(void) { return PPS_ABI_VERSION; }
 
 }  // extern "C"

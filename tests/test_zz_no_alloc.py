@@ -1,0 +1,54 @@
+"""pps_apply_operator_noalloc: the operator apply for callers that cannot allocate
+device memory (graph-captured code, allocation-free loops, plugins whose host owns
+all device memory).  Called through the C ABI on device buffers the test owns, twice
+in a row, and checked against the existing entry point pps_apply_operator (FP64
+form) with the tolerance of the operator-kernel test (1e-12 of the largest value),
+and its energy sum u.(Au) against the same sum taken on the host.
+
+This file is named to be collected last, so a run that stops at the first failure
+has already run every other test."""
+import numpy as np
+import pytest
+
+import parallelpoissonsolver_gb300 as pps
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_operator_matches_existing_entry_point(gpu):
+    torch = pytest.importorskip("torch")
+    grid = pps.BlockGrid(npglobal=(37, 29, 41), ds=(0.05, 0.07, 0.04), bcs=(0, 1, 1, 0, 0, 0))
+    sl = grid.unknowns()
+    solver = pps.BiCGSTAB(grid, pps.ChebyshevIteration(11), form="fp64")
+    rng = np.random.default_rng(2024)
+    energy = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for call in range(2):
+        u = rng.standard_normal(grid.shape)
+        fill = rng.standard_normal(grid.shape)       # entries outside the unknowns must survive
+        want = solver.apply_operator(u, fill.copy())
+        u_d = torch.from_numpy(u).cuda()
+        out_d = torch.from_numpy(fill.copy()).cuda()
+        torch.cuda.synchronize()
+        st = pps.apply_operator_noalloc(grid, u_d.data_ptr(), out_d.data_ptr(), energy.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream)
+        assert st == pps.OK, pps.last_error()
+        torch.cuda.synchronize()
+        got = out_d.cpu().numpy()
+        scale = np.max(np.abs(want[sl]))
+        assert np.max(np.abs(got[sl] - want[sl])) <= 1e-12 * scale, f"call {call}"
+        mask = np.ones(grid.shape, bool)
+        mask[sl] = False
+        assert np.array_equal(got[mask], fill[mask]), f"call {call}: entries outside the unknowns changed"
+        e_host = float(np.sum(u[sl] * want[sl]))
+        assert abs(energy.item() - e_host) <= 1e-12 * np.sum(np.abs(u[sl] * want[sl])), f"call {call}"
+    solver.close()
+
+
+def test_noalloc_rejects_grids_beyond_the_scratch(gpu):
+    torch = pytest.importorskip("torch")
+    # 4096 x 4096 planes need 128 x 512 tiles = 65536 blocks of partials (> 16384)
+    grid = pps.BlockGrid(npglobal=(4098, 4098, 3), ds=(1e-3, 1e-3, 1e-3))
+    dummy = torch.zeros(1, dtype=torch.float64, device="cuda")
+    st = pps.apply_operator_noalloc(grid, dummy.data_ptr(), dummy.data_ptr(), dummy.data_ptr(), 0)
+    assert st == pps.ERR_INVALID_ARG
+    assert "static scratch" in pps.last_error()
