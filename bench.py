@@ -36,10 +36,10 @@ sys.path.insert(0, ROOT)
 METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed FP32/FP64 vs plain FP64), 1 GB300"
 TOL = 1e-10
 DEGREE = 11
-# Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload: the plain
-# FP64 GPU form runs the reference algorithm (same iteration count +-1, checked on
-# the golden cases) and measured this count; the CPU leg multiplies its timed
-# per-iteration cost by it.
+# Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload, measured by
+# running the oracle's C restatement (bit-identical to the reference solver) to
+# convergence at 512^3 on the GB300 host (16 threads: 172 s, true ||r||/||b|| 9.3e-11).
+# The CPU leg multiplies its timed per-iteration cost by it.
 REFERENCE_ITERATIONS = {512: 166}
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "cheb_sweep_fp32_traffic.txt")
 
@@ -177,9 +177,11 @@ def run_gpu(args, dist: Dist):
     prec = pps.ChebyshevIteration(DEGREE)
 
     mixed = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
-                         device=dev)
+                         inner_tol=args.inner_tol, device=dev)
     plain = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="fp64", use_graph=False,
                          device=dev)
+
+    tuned = {"mixed": mixed.autotune(), "fp64": plain.autotune()}
 
     def solve(s):
         x_d.zero_()
@@ -266,6 +268,7 @@ def run_gpu(args, dist: Dist):
             "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU, single domain",
             "iterations": stats[-1]["iterations"],
             "refinements": stats[-1]["refinements"],
+            "tiles": tuned,
             "err_true": stats[-1]["err_true"],
         },
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8},
@@ -334,6 +337,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--inner-tol", type=float, default=3e-3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -363,7 +367,7 @@ def main():
     out, iters_fp64 = run_gpu(args, dist)
     if dist.rank == 0:
         if not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_sample(args.size, iters_fp64, threads)
+            out["cpu_baseline"] = cpu_sample(args.size, REFERENCE_ITERATIONS.get(args.size) or iters_fp64, threads)
         print(json.dumps(out), flush=True)
     dist.close()
 

@@ -162,6 +162,25 @@ pps_status pps_apply_operator(pps_solver* s, const double* u, double* out);
  * in preconditioner mode, chebyshevIteration.hpp:48-140), in the solver's form. */
 pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
 
+/* Tile shapes of the z-marching kernels (fast forms).  A tile is (32*cx) x ty
+ * columns; each thread walks along z; `waves` sets the grid to about
+ * waves x 152 SMs x resident blocks.  cheb_* apply to the Chebyshev kernels,
+ * other_* to the Krylov update/stencil kernels.  *_us: measured per launch. */
+typedef struct {
+    int cheb_ty, cheb_cx, cheb_waves;
+    int other_ty, other_waves;
+    double cheb_us, other_us;
+} pps_tuning;
+
+/* Autotuner (no reference counterpart; the reference fixes its launch shapes,
+ * ALP/include/alpakaHelper.hpp:122-140): times every candidate shape of the sweep
+ * and of the stencil+dot kernel on this solver's grid and buffers, applies the
+ * fastest and returns it.  Candidates: ty 2/4/8, cx 1/2, waves 1/2/4/8. */
+pps_status pps_autotune(pps_solver* s, pps_tuning* out);
+pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out);
+/* Applies a stored tuning (e.g. from a table persisted by the caller). */
+pps_status pps_set_tuning(pps_solver* s, const pps_tuning* t);
+
 /* Operator apply that allocates nothing.  No counterpart in the reference: it is for
  * callers that cannot call cudaMalloc -- code recorded into a CUDA graph (no
  * allocation while a stream is captured), loops that forbid allocation after

@@ -41,6 +41,7 @@ EXPORTED = [
     "pps_set_neumann", "pps_solve", "pps_solve_device", "pps_get_stats", "pps_get_history",
     "pps_write_residual_history", "pps_apply_operator", "pps_apply_preconditioner", "pps_device_count",
     "pps_status_string", "pps_last_error", "pps_abi_version", "pps_apply_operator_noalloc",
+    "pps_autotune", "pps_get_tuning", "pps_set_tuning",
 ]
 
 
@@ -66,6 +67,21 @@ class PpsStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PpsTuning(C.Structure):
+    _fields_ = [("cheb_ty", C.c_int), ("cheb_cx", C.c_int), ("cheb_waves", C.c_int), ("other_ty", C.c_int),
+                ("other_waves", C.c_int), ("cheb_us", C.c_double), ("other_us", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        for k, _ in cls._fields_:
+            setattr(t, k, d[k])
+        return t
 
 
 class PpsError(RuntimeError):
@@ -111,6 +127,9 @@ def load(build_if_missing: bool = False):
     L.pps_apply_operator.argtypes = [vp, vp, vp]
     L.pps_apply_preconditioner.argtypes = [vp, vp, vp]
     L.pps_apply_operator_noalloc.argtypes = [C.POINTER(PpsGrid), vp, vp, vp, vp]
+    L.pps_autotune.argtypes = [vp, C.POINTER(PpsTuning)]
+    L.pps_get_tuning.argtypes = [vp, C.POINTER(PpsTuning)]
+    L.pps_set_tuning.argtypes = [vp, C.POINTER(PpsTuning)]
     L.pps_status_string.restype = C.c_char_p
     L.pps_status_string.argtypes = [C.c_int]
     L.pps_last_error.restype = C.c_char_p
@@ -212,7 +231,7 @@ class Solver:
     krylov = KRYLOV_BICGSTAB
 
     def __init__(self, grid: BlockGrid, preconditioner=None, tolerance: float = 1e-8, max_iteration: int = 1700,
-                 form: str | int = "fp64", inner_tol: float = 1e-4, inner_maxit: int = 100000,
+                 form: str | int = "fp64", inner_tol: float = 3e-3, inner_maxit: int = 100000,
                  max_refinements: int = 12, check_every: int = 0, use_graph: bool = True, device: int = 0):
         self.grid = grid
         L = load()
@@ -321,6 +340,46 @@ class Solver:
         st = load().pps_write_residual_history(self._h, path.encode())
         if st != OK:
             raise PpsError(st, "pps_write_residual_history")
+
+    def tuning_key(self) -> str:
+        n = self.grid.npglobal
+        return f"{n[0]}x{n[1]}x{n[2]}:form{self.config.form}"
+
+    def autotune(self, cache: Optional[str] = None) -> dict:
+        """Pick the tile shapes of the z-marching kernels for this grid (pps_autotune).
+        With `cache`, a JSON table keyed by grid and form is read first and updated
+        after a new measurement, so a grid is tuned once per machine."""
+        import json
+        key = self.tuning_key()
+        table = {}
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                table = json.load(f)
+            if key in table:
+                self.set_tuning(table[key])
+                return table[key]
+        t = PpsTuning()
+        st = load().pps_autotune(self._h, C.byref(t))
+        if st != OK:
+            raise PpsError(st, "pps_autotune")
+        d = t.as_dict()
+        if cache:
+            table[key] = d
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return d
+
+    def tuning(self) -> dict:
+        t = PpsTuning()
+        load().pps_get_tuning(self._h, C.byref(t))
+        return t.as_dict()
+
+    def set_tuning(self, d: dict):
+        st = load().pps_set_tuning(self._h, C.byref(PpsTuning.from_dict(d)))
+        if st != OK:
+            raise PpsError(st, "pps_set_tuning")
 
     def apply_operator(self, u: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
         out = np.zeros_like(u) if out is None else out

@@ -24,6 +24,7 @@ struct Geo {
 // each thread walks kchunk planes along k.
 struct Shape {
     int ty;
+    int cx;           // columns per thread along x (tile width 32*cx); Chebyshev kernels only
     int ntx, nty, nchunks, kchunk;
     unsigned nblocks() const { return (unsigned)ntx * (unsigned)nty * (unsigned)nchunks; }
 };
@@ -84,7 +85,7 @@ struct Faces {
 };
 
 // ---- launch wrappers (pps_kernels.cu) ----
-Shape make_shape(const Geo& g, int ty, int target_blocks);
+Shape make_shape(const Geo& g, int ty, int target_blocks, int cx = 1);
 
 // Parity (bit-exact FP64) kernels.
 void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s);
@@ -108,9 +109,10 @@ template <typename T>
 void neumann_fill(const Geo& g, T* field, Faces f, int field_mode, double normb, cudaStream_t s);
 
 // Fast kernels, T = float or double storage.
+// Y = s1 (pre-folded coefficients; scale -1 gives X = -s1 directly).
 template <typename T>
-void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, T* Z, const Coef& cy, double inv_theta,
-                   int mode, const int* done, cudaStream_t s);
+void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& cy, const int* done, cudaStream_t s);
+// One sweep; Z == nullptr for the first sweep (s0 folded into the B coefficient).
 template <typename T>
 void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& c,
                      const int* done, cudaStream_t s);

@@ -418,12 +418,13 @@ template void neumann_fill<float>(const Geo&, float*, Faces, int, double, cudaSt
 // Fast kernels
 // ---------------------------------------------------------------------------
 
-Shape make_shape(const Geo& g, int ty, int target_blocks)
+Shape make_shape(const Geo& g, int ty, int target_blocks, int cx)
 {
     Shape sh;
     sh.ty = ty;
+    sh.cx = cx;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
-    sh.ntx = (ux + 31) / 32;
+    sh.ntx = (ux + 32 * cx - 1) / (32 * cx);
     sh.nty = (uy + ty - 1) / ty;
     const long long tiles = (long long)sh.ntx * sh.nty;
     long long chunks = (target_blocks + tiles - 1) / tiles;
@@ -662,69 +663,128 @@ __device__ __forceinline__ void reduce_finalize(double (&v)[NS], const RedCtx& r
 #define EARLY_EXIT(done)                                      \
     if (done != nullptr && *(volatile const int*)(done) != 0) return;
 
-// Y = cc*B + cx*(Bx pair) + cy*(By pair) + cz*(Bz pair); Z = B/theta.
-// mode 0: write Y and Z; mode 1: write X(=Y pointer) = scale*Y only (degree 3).
+// Chebyshev coefficients cast to the storage type on the host (no FP64 work
+// in the FP32 kernels; GB300 issues FP64 at 1/64 of the FP32 rate).
 template <typename T>
+struct CT {
+    T cc, cx, cy, cz, cb, cw;
+};
+
+template <typename T>
+static CT<T> cast_coef(const Coef& c)
+{
+    CT<T> o;
+    o.cc = (T)(c.cc * c.scale);
+    o.cx = (T)(c.cx * c.scale);
+    o.cy = (T)(c.cy * c.scale);
+    o.cz = (T)(c.cz * c.scale);
+    o.cb = (T)(c.cb * c.scale);
+    o.cw = (T)(c.cw * c.scale);
+    return o;
+}
+
+// First column of this thread in a tile of (32*CX) x ty columns; the thread's
+// other columns sit 32, 64, ... further along x.
+__device__ __forceinline__ Col column_cx(const Geo& g, const Shape& sh, int cxw)
+{
+    Col q;
+    const int bx = blockIdx.x % sh.ntx;
+    const int by = blockIdx.x / sh.ntx;
+    q.i = g.lo[0] + bx * 32 * cxw + threadIdx.x;
+    q.j = g.lo[1] + by * sh.ty + threadIdx.y;
+    q.k0 = g.lo[2] + blockIdx.y * sh.kchunk;
+    q.k1 = min(q.k0 + sh.kchunk, g.hi[2]);
+    q.active = q.j < g.hi[1];
+    q.c = q.i + g.sj * q.j + g.sk * q.k0;
+    return q;
+}
+
+// s1 of the preconditioner (chebyshevIteration.hpp:79-90) in pre-folded form:
+//   Y = cc*B + cx*(Bx pair) + cy*(By pair) + cz*(Bz pair)
+// s0 = B/theta is never stored: the first sweep folds it into its B coefficient.
+// With the output scale -1 folded into the coefficients this also writes X = -s1
+// directly (degree 3).
+template <typename T, int CX>
 __global__ void __launch_bounds__(256) k_cheb_s01(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ Y,
-                                                  T* __restrict__ Z, Coef cf, T inv_theta, int mode, const int* done)
+                                                  CT<T> cf, const int* done)
 {
     EARLY_EXIT(done);
-    const Col q = column(g, sh);
+    const Col q = column_cx(g, sh, CX);
     if (!q.active) return;
-    const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz, sc = (T)cf.scale;
     const long long sj = g.sj, sk = g.sk;
-    long long c = q.c;
-    T bm = B[c - sk], bc = B[c];
-#pragma unroll 4
+    bool on[CX];
+    T bm[CX], bc[CX];
+#pragma unroll
+    for (int u = 0; u < CX; u++) {
+        on[u] = q.i + 32 * u < g.hi[0];
+        const long long c = q.c + 32 * u;
+        bm[u] = on[u] ? B[c - sk] : T(0);
+        bc[u] = on[u] ? B[c] : T(0);
+    }
+    long long c0 = q.c;
+#pragma unroll 2
     for (int k = q.k0; k < q.k1; k++) {
-        const T bp = B[c + sk];
-        const T sx = B[c - 1] + B[c + 1];
-        const T sy = B[c - sj] + B[c + sj];
-        T y = cc * bc;
-        y = fmx(cx, sx, y);
-        y = fmx(cy, sy, y);
-        y = fmx(cz, bm + bp, y);
-        if (mode == 0) {
+#pragma unroll
+        for (int u = 0; u < CX; u++) {
+            if (!on[u]) continue;
+            const long long c = c0 + 32 * u;
+            const T bp = B[c + sk];
+            const T sx = B[c - 1] + B[c + 1];
+            const T sy = B[c - sj] + B[c + sj];
+            T y = cf.cc * bc[u];
+            y = fmx(cf.cx, sx, y);
+            y = fmx(cf.cy, sy, y);
+            y = fmx(cf.cz, bm[u] + bp, y);
             Y[c] = y;
-            Z[c] = bc * inv_theta;
-        } else {
-            Y[c] = sc * y;
+            bm[u] = bc[u];
+            bc[u] = bp;
         }
-        bm = bc;
-        bc = bp;
-        c += sk;
+        c0 += sk;
     }
 }
 
-// W = cc*Y + cx*(Yx pair) + cy*(...) + cz*(...) + cb*B + cw*Z, times scale (-1 for the output X).
-template <typename T>
+// One sweep (chebyshevIteration.hpp:110) in pre-folded form:
+//   W = cc*Y + cx*(Yx pair) + cy*(Yy pair) + cz*(Yz pair) + cb*B [+ cw*Z]
+// HAS_Z = false for the first sweep, whose Z = s0 = B/theta is folded into cb.
+template <typename T, int CX, bool HAS_Z>
 __global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __restrict__ Y,
                                                     const T* __restrict__ B, const T* __restrict__ Z,
-                                                    T* __restrict__ W, Coef cf, const int* done)
+                                                    T* __restrict__ W, CT<T> cf, const int* done)
 {
     EARLY_EXIT(done);
-    const Col q = column(g, sh);
+    const Col q = column_cx(g, sh, CX);
     if (!q.active) return;
-    const T cc = (T)(cf.cc * cf.scale), cx = (T)(cf.cx * cf.scale), cy = (T)(cf.cy * cf.scale),
-            cz = (T)(cf.cz * cf.scale), cb = (T)(cf.cb * cf.scale), cw = (T)(cf.cw * cf.scale);
     const long long sj = g.sj, sk = g.sk;
-    long long c = q.c;
-    T ym = Y[c - sk], yc = Y[c];
-#pragma unroll 4
+    bool on[CX];
+    T ym[CX], yc[CX];
+#pragma unroll
+    for (int u = 0; u < CX; u++) {
+        on[u] = q.i + 32 * u < g.hi[0];
+        const long long c = q.c + 32 * u;
+        ym[u] = on[u] ? Y[c - sk] : T(0);
+        yc[u] = on[u] ? Y[c] : T(0);
+    }
+    long long c0 = q.c;
+#pragma unroll 2
     for (int k = q.k0; k < q.k1; k++) {
-        const T yp = Y[c + sk];
-        const T sx = Y[c - 1] + Y[c + 1];
-        const T sy = Y[c - sj] + Y[c + sj];
-        T w = cc * yc;
-        w = fmx(cx, sx, w);
-        w = fmx(cy, sy, w);
-        w = fmx(cz, ym + yp, w);
-        w = fmx(cb, B[c], w);
-        w = fmx(cw, Z[c], w);
-        W[c] = w;
-        ym = yc;
-        yc = yp;
-        c += sk;
+#pragma unroll
+        for (int u = 0; u < CX; u++) {
+            if (!on[u]) continue;
+            const long long c = c0 + 32 * u;
+            const T yp = Y[c + sk];
+            const T sx = Y[c - 1] + Y[c + 1];
+            const T sy = Y[c - sj] + Y[c + sj];
+            T w = cf.cc * yc[u];
+            w = fmx(cf.cx, sx, w);
+            w = fmx(cf.cy, sy, w);
+            w = fmx(cf.cz, ym[u] + yp, w);
+            w = fmx(cf.cb, B[c], w);
+            if (HAS_Z) w = fmx(cf.cw, Z[c], w);
+            W[c] = w;
+            ym[u] = yc[u];
+            yc[u] = yp;
+        }
+        c0 += sk;
     }
 }
 
@@ -1060,17 +1120,25 @@ __global__ void k_state_init(DevState* st, double* hist, int maxit, double tol_a
 // ---- wrappers ----
 
 template <typename T>
-void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, T* Z, const Coef& cy, double inv_theta, int mode,
-                   const int* done, cudaStream_t s)
+void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& cy, const int* done, cudaStream_t s)
 {
-    k_cheb_s01<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, Z, cy, (T)inv_theta, mode, done);
+    const CT<T> c = cast_coef<T>(cy);
+    if (sh.cx == 2) k_cheb_s01<T, 2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
+    else k_cheb_s01<T, 1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
-void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& c,
+void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& cf,
                      const int* done, cudaStream_t s)
 {
-    k_cheb_sweep<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+    const CT<T> c = cast_coef<T>(cf);
+    if (Z) {
+        if (sh.cx == 2) k_cheb_sweep<T, 2, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+        else k_cheb_sweep<T, 1, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+    } else {
+        if (sh.cx == 2) k_cheb_sweep<T, 2, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+        else k_cheb_sweep<T, 1, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+    }
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1170,8 +1238,8 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
 }
 
 #define PPS_INST(T)                                                                                              \
-    template void fast_cheb_s01<T>(const Geo&, const Shape&, const T*, T*, T*, const Coef&, double, int,         \
-                                   const int*, cudaStream_t);                                                    \
+    template void fast_cheb_s01<T>(const Geo&, const Shape&, const T*, T*, const Coef&, const int*,               \
+                                   cudaStream_t);                                                                \
     template void fast_cheb_sweep<T>(const Geo&, const Shape&, const T*, const T*, const T*, T*, const Coef&,    \
                                      const int*, cudaStream_t);                                                  \
     template void fast_scale_copy<T>(const Geo&, const Shape&, const T*, T*, double, const int*, cudaStream_t); \

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -86,7 +87,9 @@ struct pps_solver {
     pps_grid grid;
     pps_config cfg;
     Geo geo;
-    Shape shape;
+    Shape shape;        // z-marching kernels other than the Chebyshev ones
+    Shape shape_cheb;   // Chebyshev s1 and sweep kernels
+    pps_tuning tuning;
     int device = 0;
     cudaStream_t stream = nullptr;
     double eig[2] = {0, 0};
@@ -458,10 +461,11 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
         L.launches++;
         return;
     }
+    const Shape& shc = s->shape_cheb;
     Coef c01 = cheb_s01_coef(s, rhoCurr);
     if (n == 3) {
         c01.scale = -1.0;
-        fast_cheb_s01<T>(g, s->shape, B, X, nullptr, c01, 1.0 / s->theta, 1, done, st);
+        fast_cheb_s01<T>(g, shc, B, X, c01, done, st);
         L.bytes += bytes_of<T>(N, 2);
         L.launches++;
         return;
@@ -469,8 +473,8 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
     T* Y = F.Y;
     T* Z = F.Z;
     T* W = F.W;
-    fast_cheb_s01<T>(g, s->shape, B, Y, Z, c01, 1.0 / s->theta, 0, done, st);
-    L.bytes += bytes_of<T>(N, 3);
+    fast_cheb_s01<T>(g, shc, B, Y, c01, done, st);
+    L.bytes += bytes_of<T>(N, 2);
     L.launches++;
     const bool prof = L.profile && s->sweep_ev_used + 2 <= (int)s->sweep_ev.size();
     if (prof) CK(cudaEventRecord(s->sweep_ev[s->sweep_ev_used], st));
@@ -482,11 +486,18 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
             L.launches += 2;
         }
         const bool last = (it == n - 2);
-        const Coef c = cheb_sweep_coef(s, rhoCurr, rhoOld, last ? -1.0 : 1.0);
-        fast_cheb_sweep<T>(g, s->shape, Y, B, Z, last ? X : W, c, done, st);
-        L.bytes += bytes_of<T>(N, 4);
+        Coef c = cheb_sweep_coef(s, rhoCurr, rhoOld, last ? -1.0 : 1.0);
+        const bool first = (it == 2);
+        if (first) {
+            // Z = s0 = B/theta: fold it into the B coefficient instead of storing s0
+            c.cb += c.cw / s->theta;
+            c.cw = 0.0;
+        }
+        fast_cheb_sweep<T>(g, shc, Y, B, first ? nullptr : Z, last ? X : W, c, done, st);
+        const int words = first ? 3 : 4;
+        L.bytes += bytes_of<T>(N, words);
         L.launches++;
-        s->sweep_bytes_acc += bytes_of<T>(N, 4);
+        s->sweep_bytes_acc += bytes_of<T>(N, words);
         s->sweep_launch_acc++;
         if (!last) {
             T* t = Z;   // (Y, Z, W) <- (W, Y, Z)
@@ -740,6 +751,110 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
     return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: tile shapes of the z-marching kernels, timed on the solver's grid
+// ---------------------------------------------------------------------------
+
+const int kTys[] = {2, 4, 8};
+const int kCxs[] = {1, 2};
+const int kWaves[] = {1, 2, 4, 8};
+
+int resident_blocks(int ty)
+{
+    const int threads = 32 * ty;
+    return std::min(32, 2048 / threads);
+}
+
+Shape tuned_shape(const Geo& g, int ty, int cx, int waves)
+{
+    return make_shape(g, ty, waves * 152 * resident_blocks(ty), cx);
+}
+
+unsigned max_candidate_blocks(const Geo& g)
+{
+    unsigned m = 0;
+    for (int ty : kTys)
+        for (int w : kWaves) m = std::max(m, tuned_shape(g, ty, 1, w).nblocks());
+    return m;
+}
+
+template <typename T>
+double time_launches(pps_solver* s, int reps, const std::function<void()>& launch)
+{
+    launch();   // warm-up
+    CK(cudaEventRecord(s->ev0, s->stream));
+    for (int r = 0; r < reps; r++) launch();
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    return 1e3 * ms / reps;
+}
+
+template <typename T>
+void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
+{
+    const Geo& g = s->geo;
+    const long long N = s->n_unknowns;
+    const int reps = N > (1LL << 24) ? 5 : 20;
+    state_init(s->d_st, s->d_hist, 1, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
+    const Coef c = cheb_sweep_coef(s, 0.5, 0.5, 1.0);
+    double best_us = 1e30;
+    for (int ty : kTys)
+        for (int cx : kCxs)
+            for (int w : kWaves) {
+                const Shape sh = tuned_shape(g, ty, cx, w);
+                const double us = time_launches<T>(s, reps, [&]() {
+                    fast_cheb_sweep<T>(g, sh, F.Y, F.r, F.Z, F.W, c, &s->d_st->done, s->stream);
+                });
+                if (us < best_us) {
+                    best_us = us;
+                    best->cheb_ty = ty;
+                    best->cheb_cx = cx;
+                    best->cheb_waves = w;
+                    best->cheb_us = us;
+                }
+            }
+    const Coef a = op_coef(g);
+    best_us = 1e30;
+    for (int ty : kTys)
+        for (int w : kWaves) {
+            const Shape sh = tuned_shape(g, ty, 1, w);
+            const double us = time_launches<T>(s, reps, [&]() {
+                state_init(s->d_st, s->d_hist, 1, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
+                fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red(s, FIN_STORE), s->stream);
+            });
+            if (us < best_us) {
+                best_us = us;
+                best->other_ty = ty;
+                best->other_waves = w;
+                best->other_us = us;
+            }
+        }
+}
+
+void apply_tuning(pps_solver* s, const pps_tuning& t)
+{
+    s->tuning = t;
+    s->shape_cheb = tuned_shape(s->geo, t.cheb_ty, t.cheb_cx, t.cheb_waves);
+    s->shape = tuned_shape(s->geo, t.other_ty, 1, t.other_waves);
+    if (s->gexec) {   // captured launches carry the old shapes
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+}
+
+bool tuning_valid(const pps_tuning* t)
+{
+    auto in = [](int v, const int* a, int n) {
+        for (int i = 0; i < n; i++)
+            if (a[i] == v) return true;
+        return false;
+    };
+    return in(t->cheb_ty, kTys, 3) && in(t->cheb_cx, kCxs, 2) && in(t->cheb_waves, kWaves, 4) &&
+           in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4);
+}
+
 pps_status validate(const pps_grid* g, const pps_config* c)
 {
     if (!g || !c) return PPS_ERR_INVALID_ARG;
@@ -855,7 +970,7 @@ pps_status pps_config_default(pps_config* c, int preset)
         return PPS_ERR_INVALID_ARG;
     }
     c->form = PPS_FORM_FP64;
-    c->inner_tol = 1e-4;
+    c->inner_tol = 3e-3;
     c->inner_maxit = 100000;
     c->max_refinements = 12;
     c->check_every = 0;
@@ -902,6 +1017,14 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         g.ntot = g.sk * (grid->npglobal[2] + 2);
         s->n_unknowns = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
         s->shape = make_shape(g, 8, 152 * 8 * 4);
+        s->shape_cheb = s->shape;
+        s->tuning.cheb_ty = 8;
+        s->tuning.cheb_cx = 1;
+        s->tuning.cheb_waves = 4;
+        s->tuning.other_ty = 8;
+        s->tuning.other_waves = 4;
+        s->tuning.cheb_us = 0.0;
+        s->tuning.other_us = 0.0;
         // computeEigenvalues, global bounds (blockGrid.hpp:322-339)
         double eigMin = 0, eigMax = 0;
         for (int i = 0; i < 3; i++) {
@@ -944,7 +1067,7 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         CK(cudaMallocHost((void**)&s->h_dot, 4 * sizeof(double)));
         s->hist_cap = cfg->maxit + 2;
         CK(cudaMalloc((void**)&s->d_hist, sizeof(double) * (size_t)s->hist_cap));
-        const unsigned nb = std::max(s->shape.nblocks(), 1u);
+        const unsigned nb = std::max(max_candidate_blocks(g), 1u);
         CK(cudaMalloc((void**)&s->d_partials, sizeof(double) * 4 * (size_t)nb));
         CK(cudaMalloc((void**)&s->d_counter, sizeof(unsigned)));
         CK(cudaMemset(s->d_counter, 0, sizeof(unsigned)));
@@ -1221,6 +1344,43 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         for (long long q = 0; q < g.ntot; q++) X[q] = (double)hx[(size_t)q];
         return PPS_OK;
     });
+}
+
+pps_status pps_autotune(pps_solver* s, pps_tuning* out)
+{
+    if (!s) return PPS_ERR_INVALID_ARG;
+    if (s->cfg.form == PPS_FORM_PARITY_FP64) {
+        set_error("the PARITY form has no tunable tile shapes");
+        return PPS_ERR_UNSUPPORTED;
+    }
+    return guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        pps_tuning t = s->tuning;
+        if (s->cfg.form == PPS_FORM_MIXED) autotune_fields<float>(s, s->f32, &t);
+        else autotune_fields<double>(s, s->f64, &t);
+        CK(cudaStreamSynchronize(s->stream));
+        apply_tuning(s, t);
+        if (out) *out = t;
+        return PPS_OK;
+    });
+}
+
+pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out)
+{
+    if (!s || !out) return PPS_ERR_INVALID_ARG;
+    *out = s->tuning;
+    return PPS_OK;
+}
+
+pps_status pps_set_tuning(pps_solver* s, const pps_tuning* t)
+{
+    if (!s || !t) return PPS_ERR_INVALID_ARG;
+    if (!tuning_valid(t)) {
+        set_error("tuning outside the candidate set (ty 2/4/8, cx 1/2, waves 1/2/4/8)");
+        return PPS_ERR_INVALID_ARG;
+    }
+    apply_tuning(s, *t);
+    return PPS_OK;
 }
 
 int pps_device_count(void)

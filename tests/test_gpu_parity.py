@@ -253,3 +253,29 @@ def test_residual_history_file(gpu, oracle, tmp_path):
     h = np.array([float(v) for v in lines[3:]])
     assert len(h) == s.get_num_iteration_final() + 1
     assert h[-1] < case["cfg"]["tol"]
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_autotune_keeps_results(gpu, oracle, form, tmp_path):
+    case = BY_NAME["neumann_random_ragged"]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    r = run_oracle(oracle, case, xo, bo, faces)
+    s = make_solver(case, form)
+    cache = str(tmp_path / "tuning.json")
+    t = s.autotune(cache=cache)
+    assert t["cheb_ty"] in (2, 4, 8) and t["cheb_cx"] in (1, 2) and t["cheb_us"] > 0
+    assert s.tuning()["cheb_waves"] == t["cheb_waves"]
+    for f, a in enumerate(faces):
+        if a is not None:
+            s.set_neumann(f, a)
+    assert s(x, b) == pps.OK
+    assert s.get_error_compute_operator() <= case["cfg"]["tol"]
+    if form == "fp64":
+        assert abs(s.get_num_iteration_final() - r.iterations) <= 1
+        assert rel_l2(x, xo) <= 1e-9
+    # a second solver reads the table instead of measuring again
+    s2 = make_solver(case, form)
+    assert s2.autotune(cache=cache) == t
+    with pytest.raises(pps.PpsError):
+        s2.set_tuning({**t, "cheb_ty": 3})
