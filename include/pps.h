@@ -181,6 +181,41 @@ pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out);
 /* Applies a stored tuning (e.g. from a table persisted by the caller). */
 pps_status pps_set_tuning(pps_solver* s, const pps_tuning* t);
 
+/* ---- Batches: many independent Dirichlet grids solved together ----
+ * No reference counterpart (the reference solves one grid per run).  Every problem
+ * runs the reference's BiCGSTAB + Chebyshev solve on its own grid, in the MIXED
+ * form; each loop phase is one launch over all problems, the inner iteration is
+ * replayed as a CUDA graph, and per-problem tile shapes come from the autotuner.
+ * Fields live in device pools owned by the batch (pps_batch_set/get copy them,
+ * pps_batch_field_device exposes them). */
+typedef struct pps_batch pps_batch;
+
+typedef struct {
+    double seconds_solve;       /* device time of the whole batched solve                  */
+    int kernel_launches;
+    int graph_replays;
+    double max_err_true;        /* max over problems of the FP64 ||b-Ax||/||b_adj||        */
+    int max_iterations;         /* max over problems of the inner iterations               */
+    int sum_iterations;
+    int max_refinements;
+    int converged;              /* problems that reached tol                               */
+    double unknowns;            /* sum of the problems' unknowns                           */
+} pps_batch_stats;
+
+/* cfg: form PPS_FORM_MIXED, krylov BiCGSTAB, Chebyshev degree >= 4; grids all-Dirichlet. */
+pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* cfg, pps_batch** out);
+pps_status pps_batch_destroy(pps_batch* batch);
+pps_status pps_batch_set(pps_batch* batch, int p, const double* x, const double* b);
+pps_status pps_batch_get(pps_batch* batch, int p, double* x, pps_stats* stats);
+pps_status pps_batch_field_device(pps_batch* batch, int p, double** x_dev, double** b_dev);
+/* Times the batched sweep for every grid shape in the batch over candidate tiles
+ * (columns per thread 1/2, z-chunk 8..128) and keeps the fastest per shape. */
+pps_status pps_batch_autotune(pps_batch* batch);
+pps_status pps_batch_tile(const pps_batch* batch, int p, int* cx, int* kchunk);
+/* Solves every problem to cfg->tol (FP64 true residual).  PPS_NOT_CONVERGED if any
+ * problem stopped short. */
+pps_status pps_batch_solve(pps_batch* batch, pps_batch_stats* stats);
+
 /* Operator apply that allocates nothing.  No counterpart in the reference: it is for
  * callers that cannot call cudaMalloc -- code recorded into a CUDA graph (no
  * allocation while a stream is captured), loops that forbid allocation after

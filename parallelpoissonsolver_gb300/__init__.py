@@ -42,6 +42,8 @@ EXPORTED = [
     "pps_write_residual_history", "pps_apply_operator", "pps_apply_preconditioner", "pps_device_count",
     "pps_status_string", "pps_last_error", "pps_abi_version", "pps_apply_operator_noalloc",
     "pps_autotune", "pps_get_tuning", "pps_set_tuning",
+    "pps_batch_create", "pps_batch_destroy", "pps_batch_set", "pps_batch_get", "pps_batch_field_device",
+    "pps_batch_autotune", "pps_batch_tile", "pps_batch_solve",
 ]
 
 
@@ -82,6 +84,15 @@ class PpsTuning(C.Structure):
         for k, _ in cls._fields_:
             setattr(t, k, d[k])
         return t
+
+
+class PpsBatchStats(C.Structure):
+    _fields_ = [("seconds_solve", C.c_double), ("kernel_launches", C.c_int), ("graph_replays", C.c_int),
+                ("max_err_true", C.c_double), ("max_iterations", C.c_int), ("sum_iterations", C.c_int),
+                ("max_refinements", C.c_int), ("converged", C.c_int), ("unknowns", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class PpsError(RuntimeError):
@@ -130,6 +141,14 @@ def load(build_if_missing: bool = False):
     L.pps_autotune.argtypes = [vp, C.POINTER(PpsTuning)]
     L.pps_get_tuning.argtypes = [vp, C.POINTER(PpsTuning)]
     L.pps_set_tuning.argtypes = [vp, C.POINTER(PpsTuning)]
+    L.pps_batch_create.argtypes = [C.c_int, C.POINTER(PpsGrid), C.POINTER(PpsConfig), C.POINTER(vp)]
+    L.pps_batch_destroy.argtypes = [vp]
+    L.pps_batch_set.argtypes = [vp, C.c_int, vp, vp]
+    L.pps_batch_get.argtypes = [vp, C.c_int, vp, C.POINTER(PpsStats)]
+    L.pps_batch_field_device.argtypes = [vp, C.c_int, C.POINTER(vp), C.POINTER(vp)]
+    L.pps_batch_autotune.argtypes = [vp]
+    L.pps_batch_tile.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.pps_batch_solve.argtypes = [vp, C.POINTER(PpsBatchStats)]
     L.pps_status_string.restype = C.c_char_p
     L.pps_status_string.argtypes = [C.c_int]
     L.pps_last_error.restype = C.c_char_p
@@ -404,6 +423,83 @@ class BiCGSTAB(Solver):
 class BaseCG(Solver):
     """Preconditioned CG main loop (baseCG.hpp:14-269)."""
     krylov = KRYLOV_CG
+
+
+class Batch:
+    """Many independent Dirichlet grids solved together (pps_batch_*): the MIXED form
+    of BiCGSTAB + Chebyshev per problem, one launch per phase over all problems,
+    the inner iteration replayed as a CUDA graph."""
+
+    def __init__(self, grids: Sequence[BlockGrid], preconditioner: Optional[ChebyshevIteration] = None,
+                 tolerance: float = 1e-10, inner_tol: float = 3e-3, inner_maxit: int = 5000,
+                 max_refinements: int = 12, check_every: int = 8, use_graph: bool = True, device: int = 0):
+        L = load()
+        self.grids = list(grids)
+        prec = preconditioner or ChebyshevIteration()
+        cfg = PpsConfig()
+        L.pps_config_default(C.byref(cfg), PRESET_CPU)
+        cfg.cheb_degree, cfg.cheb_eps = prec.degree, prec.epsilon
+        cfg.rescale_min, cfg.rescale_max = prec.rescale_eig_min, prec.rescale_eig_max
+        cfg.form = FORM_MIXED
+        cfg.tol, cfg.inner_tol, cfg.inner_maxit = float(tolerance), float(inner_tol), int(inner_maxit)
+        cfg.max_refinements, cfg.check_every = int(max_refinements), int(check_every)
+        cfg.use_graph, cfg.device = (1 if use_graph else 0), int(device)
+        arr = (PpsGrid * len(self.grids))(*[g.c() for g in self.grids])
+        h = C.c_void_p()
+        st = L.pps_batch_create(len(self.grids), arr, C.byref(cfg), C.byref(h))
+        if st != OK:
+            raise PpsError(st, "pps_batch_create")
+        self._h = h
+        self._stats = PpsBatchStats()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pps_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, p: int, x: np.ndarray, b: np.ndarray):
+        st = load().pps_batch_set(self._h, p, _ptr(x), _ptr(b))
+        if st != OK:
+            raise PpsError(st, "pps_batch_set")
+
+    def get(self, p: int, x: Optional[np.ndarray] = None):
+        x = self.grids[p].new_field() if x is None else x
+        ps = PpsStats()
+        st = load().pps_batch_get(self._h, p, _ptr(x), C.byref(ps))
+        if st != OK:
+            raise PpsError(st, "pps_batch_get")
+        return x, ps.as_dict()
+
+    def field_device(self, p: int):
+        xd, bd = C.c_void_p(), C.c_void_p()
+        load().pps_batch_field_device(self._h, p, C.byref(xd), C.byref(bd))
+        return xd.value, bd.value
+
+    def autotune(self):
+        st = load().pps_batch_autotune(self._h)
+        if st != OK:
+            raise PpsError(st, "pps_batch_autotune")
+        out = []
+        for p in range(len(self.grids)):
+            cx, kc = C.c_int(), C.c_int()
+            load().pps_batch_tile(self._h, p, C.byref(cx), C.byref(kc))
+            out.append((cx.value, kc.value))
+        return out
+
+    def solve(self, raise_on_error: bool = True) -> int:
+        st = load().pps_batch_solve(self._h, C.byref(self._stats))
+        if st < 0 and raise_on_error:
+            raise PpsError(st, "pps_batch_solve")
+        return st
+
+    def stats(self) -> dict:
+        return self._stats.as_dict()
 
 
 def apply_operator_noalloc(grid: BlockGrid, u_ptr: int, out_ptr: int, energy_ptr: int, stream: int = 0) -> int:

@@ -84,6 +84,58 @@ struct Faces {
     const double* g[6];
 };
 
+// ---- batches of independent grids (pps_batch_kernels.cuh, pps_batch.cu) ----
+
+// One problem of a batch: its geometry, the offset of its field in every pooled
+// array, its tile shape and its range of launch blocks.
+struct BProb {
+    Geo g;
+    long long off;
+    unsigned first_block, nblocks;
+    int ntx, nty, nchunks, kchunk, cx;
+};
+
+struct BatchDev {
+    const BProb* prob;
+    const unsigned* blk2prob;   // launch block -> problem
+    int nprob;
+    unsigned total_blocks;
+};
+
+// Per-problem state: the inner Krylov scalars plus the refinement bookkeeping.
+struct BState {
+    DevState s;
+    double tol_rel_outer;   // tolerance on ||r||/||b_adj||
+    double tol_outer;       // tol_rel_outer * ||b_adj||
+    double err_outer;       // last FP64 true residual norm
+    int finished;           // 1: converged (or failed); every kernel skips the problem
+    int refinements;
+    int total_iters;
+    int outer_status;
+};
+
+void b_refine_init(const BatchDev& B, BState* bst, int inner_maxit, double inner_tol, cudaStream_t s);
+void b_refine_end(const BatchDev& B, BState* bst, cudaStream_t s);
+void b_norm_badj(const BatchDev& B, const double* b, const double* x, double* part, unsigned* cnt, BState* bst,
+                 cudaStream_t s);
+void b_residual(const BatchDev& B, const double* x, const double* b, float* r, float* r0, float* p, double* part,
+                unsigned* cnt, BState* bst, cudaStream_t s);
+void b_zero(const BatchDev& B, float* e, const BState* bst, cudaStream_t s);
+void b_add_correction(const BatchDev& B, double* x, const float* e, const BState* bst, cudaStream_t s);
+void b_cheb_s01(const BatchDev& B, const float* Bf, float* Y, const void* coef, int cstride, int ci,
+                const BState* bst, cudaStream_t s);
+void b_cheb_sweep(const BatchDev& B, const float* Y, const float* Bf, const float* Z, float* W, const void* coef,
+                  int cstride, int ci, const BState* bst, cudaStream_t s);
+void b_stencil_dot(const BatchDev& B, const float* u, const float* w, float* Au, int nsums, double* part,
+                   unsigned* cnt, BState* bst, cudaStream_t s);
+void b_axpy_alpha(const BatchDev& B, float* r, const float* v, const BState* bst, cudaStream_t s);
+void b_update_xr(const BatchDev& B, float* x, const float* Mp, const float* z, float* r, const float* Az,
+                 const float* r0, double* part, unsigned* cnt, BState* bst, cudaStream_t s);
+void b_update_p(const BatchDev& B, float* p, const float* r, const float* AMp, const BState* bst, cudaStream_t s);
+// Casts n pre-folded coefficient sets to the device layout of the float kernels.
+void b_cast_coef(const struct Coef* in, void* out, size_t n);
+size_t b_coef_size();
+
 // ---- launch wrappers (pps_kernels.cu) ----
 Shape make_shape(const Geo& g, int ty, int target_blocks, int cx = 1);
 

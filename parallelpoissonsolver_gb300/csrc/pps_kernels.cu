@@ -1237,6 +1237,8 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
     PPS_COUNT_LAUNCH();
 }
 
+#include "pps_batch_kernels.cuh"
+
 #define PPS_INST(T)                                                                                              \
     template void fast_cheb_s01<T>(const Geo&, const Shape&, const T*, T*, const Coef&, const int*,               \
                                    cudaStream_t);                                                                \
