@@ -54,7 +54,10 @@ typedef struct {
     int bcs[6];                 /* x- x+ y- y+ z- z+ : 0 Dirichlet, 1 Neumann            */
 } pps_grid;
 
-typedef enum { PPS_KRYLOV_BICGSTAB = 0, PPS_KRYLOV_CG = 1 } pps_krylov;
+/* BiCGSTAB (BiCGSTAB.hpp), CG (baseCG.hpp), and flexible CG (no reference
+ * counterpart: BaseCG with a Polak-Ribiere beta, for preconditioners that change
+ * between applications, FP64 and MIXED forms only). */
+typedef enum { PPS_KRYLOV_BICGSTAB = 0, PPS_KRYLOV_CG = 1, PPS_KRYLOV_FCG = 2 } pps_krylov;
 typedef enum { PPS_PREC_NONE = 0, PPS_PREC_CHEBYSHEV = 1 } pps_precond;
 
 typedef enum {
@@ -215,6 +218,34 @@ pps_status pps_batch_tile(const pps_batch* batch, int p, int* cx, int* kchunk);
 /* Solves every problem to cfg->tol (FP64 true residual).  PPS_NOT_CONVERGED if any
  * problem stopped short. */
 pps_status pps_batch_solve(pps_batch* batch, pps_batch_stats* stats);
+
+/* ---- Learned preconditioner: a 3-D convolutional U-Net ----
+ * No reference counterpart.  3 levels with c1/c2/c3 channels (16/32/64), 3x3x3
+ * kernels, BF16 weights and activations with FP32 accumulation on the tensor cores,
+ * trained by the project's own forward/backward kernels and Adam.  Arrays are dense
+ * FP32 [nz][ny][nx] device arrays (extents multiples of 4); the parameter vector is,
+ * per layer, W[27][cin][cout] (tap = kz*9 + ky*3 + kx) then b[cout]. */
+typedef struct pps_unet pps_unet;
+pps_status pps_unet_create(int c1, int c2, int c3, unsigned long long seed, int device, pps_unet** out);
+pps_status pps_unet_destroy(pps_unet* net);
+int pps_unet_param_count(const pps_unet* net);
+pps_status pps_unet_get_params(const pps_unet* net, float* out);
+pps_status pps_unet_set_params(pps_unet* net, const float* in);
+/* normalize = 1: the input is scaled to unit RMS and the output scaled back. */
+pps_status pps_unet_forward(pps_unet* net, int nx, int ny, int nz, const float* in_dev, float* out_dev,
+                            int normalize);
+/* MSE loss of the (unnormalised) output against target, and its gradient (host array
+ * of pps_unet_param_count floats). */
+pps_status pps_unet_gradients(pps_unet* net, int nx, int ny, int nz, const float* in_dev, const float* target_dev,
+                              float* grads, double* loss);
+/* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss of one sample. */
+pps_status pps_unet_train_step(pps_unet* net, int nx, int ny, int nz, const float* in_dev, const float* target_dev,
+                               float lr, double* loss);
+/* 2x grid transfers of dense unknown arrays (coarse extents nx, ny, nz; the fine
+ * grid has twice as many unknowns per axis, coarse unknown i on fine unknown 2i+1):
+ * full-weighting restriction and trilinear prolongation (its transpose / 8). */
+pps_status pps_restrict2(int nx, int ny, int nz, const float* fine_dev, float* coarse_dev);
+pps_status pps_prolong2(int nx, int ny, int nz, const float* coarse_dev, float* fine_dev);
 
 /* Operator apply that allocates nothing.  No counterpart in the reference: it is for
  * callers that cannot call cudaMalloc -- code recorded into a CUDA graph (no

@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(HERE, "libpps.so")
 
 OK, NOT_CONVERGED, BREAKDOWN, NAN_DETECTED, TIMEOUT = 0, 1, 2, 3, 4
 ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_ZERO_RHS, ERR_UNSUPPORTED, ERR_NO_DEVICE = -1, -2, -3, -4, -5, -6
-KRYLOV_BICGSTAB, KRYLOV_CG = 0, 1
+KRYLOV_BICGSTAB, KRYLOV_CG, KRYLOV_FCG = 0, 1, 2
 PREC_NONE, PREC_CHEBYSHEV = 0, 1
 FORM_PARITY_FP64, FORM_FP64, FORM_MIXED = 0, 1, 2
 FORMS = {"parity": FORM_PARITY_FP64, "fp64": FORM_FP64, "mixed": FORM_MIXED}
@@ -44,6 +44,8 @@ EXPORTED = [
     "pps_autotune", "pps_get_tuning", "pps_set_tuning",
     "pps_batch_create", "pps_batch_destroy", "pps_batch_set", "pps_batch_get", "pps_batch_field_device",
     "pps_batch_autotune", "pps_batch_tile", "pps_batch_solve",
+    "pps_unet_create", "pps_unet_destroy", "pps_unet_param_count", "pps_unet_get_params", "pps_unet_set_params",
+    "pps_unet_forward", "pps_unet_gradients", "pps_unet_train_step", "pps_restrict2", "pps_prolong2",
 ]
 
 
@@ -149,6 +151,16 @@ def load(build_if_missing: bool = False):
     L.pps_batch_autotune.argtypes = [vp]
     L.pps_batch_tile.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.pps_batch_solve.argtypes = [vp, C.POINTER(PpsBatchStats)]
+    L.pps_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.c_int, C.POINTER(vp)]
+    L.pps_unet_destroy.argtypes = [vp]
+    L.pps_unet_param_count.argtypes = [vp]
+    L.pps_unet_get_params.argtypes = [vp, vp]
+    L.pps_unet_set_params.argtypes = [vp, vp]
+    L.pps_unet_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int]
+    L.pps_unet_gradients.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, C.POINTER(C.c_double)]
+    L.pps_unet_train_step.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_float, C.POINTER(C.c_double)]
+    L.pps_restrict2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
+    L.pps_prolong2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_status_string.restype = C.c_char_p
     L.pps_status_string.argtypes = [C.c_int]
     L.pps_last_error.restype = C.c_char_p
@@ -425,6 +437,12 @@ class BaseCG(Solver):
     krylov = KRYLOV_CG
 
 
+class FlexibleCG(Solver):
+    """Flexible CG: BaseCG's loop with a Polak-Ribiere beta, so the preconditioner may
+    change between applications (no reference counterpart; FP64 and MIXED forms)."""
+    krylov = KRYLOV_FCG
+
+
 class Batch:
     """Many independent Dirichlet grids solved together (pps_batch_*): the MIXED form
     of BiCGSTAB + Chebyshev per problem, one launch per phase over all problems,
@@ -500,6 +518,102 @@ class Batch:
 
     def stats(self) -> dict:
         return self._stats.as_dict()
+
+
+class UNet:
+    """The learned preconditioner's 3-D U-Net (pps_unet_*): 3 levels, c1/c2/c3
+    channels, 3x3x3 kernels, BF16 weights/activations, FP32 accumulation, trained by
+    the library's own forward/backward kernels.  Arrays are device pointers of dense
+    FP32 [nz][ny][nx] fields; extents must be multiples of 4."""
+
+    def __init__(self, channels=(16, 32, 64), seed: int = 0, device: int = 0):
+        h = C.c_void_p()
+        st = load().pps_unet_create(channels[0], channels[1], channels[2], seed, device, C.byref(h))
+        if st != OK:
+            raise PpsError(st, "pps_unet_create")
+        self._h = h
+        self.channels = tuple(channels)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pps_unet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def param_count(self) -> int:
+        return int(load().pps_unet_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.param_count(), np.float32)
+        st = load().pps_unet_get_params(self._h, out.ctypes.data)
+        if st != OK:
+            raise PpsError(st, "pps_unet_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.param_count()
+        st = load().pps_unet_set_params(self._h, p.ctypes.data)
+        if st != OK:
+            raise PpsError(st, "pps_unet_set_params")
+
+    def forward(self, shape, in_ptr: int, out_ptr: int, normalize: bool = True):
+        nz, ny, nx = shape
+        st = load().pps_unet_forward(self._h, nx, ny, nz, C.c_void_p(in_ptr), C.c_void_p(out_ptr), int(normalize))
+        if st != OK:
+            raise PpsError(st, "pps_unet_forward")
+
+    def gradients(self, shape, in_ptr: int, target_ptr: int):
+        nz, ny, nx = shape
+        g = np.zeros(self.param_count(), np.float32)
+        loss = C.c_double(0)
+        st = load().pps_unet_gradients(self._h, nx, ny, nz, C.c_void_p(in_ptr), C.c_void_p(target_ptr),
+                                       g.ctypes.data, C.byref(loss))
+        if st != OK:
+            raise PpsError(st, "pps_unet_gradients")
+        return loss.value, g
+
+    def train_step(self, shape, in_ptr: int, target_ptr: int, lr: float) -> float:
+        nz, ny, nx = shape
+        loss = C.c_double(0)
+        st = load().pps_unet_train_step(self._h, nx, ny, nz, C.c_void_p(in_ptr), C.c_void_p(target_ptr),
+                                        C.c_float(lr), C.byref(loss))
+        if st != OK:
+            raise PpsError(st, "pps_unet_train_step")
+        return loss.value
+
+    def save(self, path: str):
+        np.savez(path, params=self.get_params(), channels=np.array(self.channels))
+
+    @classmethod
+    def load_file(cls, path: str, device: int = 0):
+        d = np.load(path)
+        net = cls(tuple(int(c) for c in d["channels"]), device=device)
+        net.set_params(d["params"])
+        return net
+
+
+def restrict2(coarse_shape, fine_ptr: int, coarse_ptr: int):
+    nz, ny, nx = coarse_shape
+    st = load().pps_restrict2(nx, ny, nz, C.c_void_p(fine_ptr), C.c_void_p(coarse_ptr))
+    if st != OK:
+        raise PpsError(st, "pps_restrict2")
+
+
+def prolong2(coarse_shape, coarse_ptr: int, fine_ptr: int):
+    nz, ny, nx = coarse_shape
+    st = load().pps_prolong2(nx, ny, nz, C.c_void_p(coarse_ptr), C.c_void_p(fine_ptr))
+    if st != OK:
+        raise PpsError(st, "pps_prolong2")
 
 
 def apply_operator_noalloc(grid: BlockGrid, u_ptr: int, out_ptr: int, energy_ptr: int, stream: int = 0) -> int:

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpps.so")
-SOURCES = ["pps_kernels.cu", "pps_solver.cu", "pps_noalloc.cu", "pps_batch.cu"]
+SOURCES = ["pps_kernels.cu", "pps_solver.cu", "pps_noalloc.cu", "pps_batch.cu", "pps_unet_kernels.cu",
+           "pps_unet.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               # host code rounds every product and sum separately (aarch64 g++ would fuse them)

@@ -594,6 +594,28 @@ __device__ void finalize(const RedCtx& rc, const double* tot)
         }
         break;
     }
+    case FIN_FCG_CONV: {
+        // flexible CG, Polak-Ribiere: beta = z_new.(r_new - r_old) / (z_old.r_old)
+        const double err = sqrt(tot[2]);
+        st->err = err;
+        st->beta = (tot[0] - tot[1]) / st->rho0;
+        st->iter += 1;
+        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
+        if (!isfinite(err)) {
+            st->status = 3;
+            st->done = 1;
+        } else if (err < st->tol_abs) {
+            st->status = 0;
+            st->done = 1;
+        } else if (st->iter >= st->maxit) {
+            st->status = 1;
+            st->done = 1;
+        } else if (!isfinite(st->beta)) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
     default:
         break;
     }
@@ -1022,6 +1044,50 @@ __global__ void __launch_bounds__(256) k_cg_update_p(Geo g, Shape sh, T* __restr
     }
 }
 
+// FCG: x += alpha*p; r_old = r; r -= alpha*Ap
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
+                                                       T* __restrict__ r, T* __restrict__ r_old,
+                                                       const T* __restrict__ Ap, const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const T a = (T)st->alpha;
+    long long c = q.c;
+#pragma unroll 4
+    for (int k = q.k0; k < q.k1; k++) {
+        x[c] = fmx(a, p[c], x[c]);
+        const T rv = r[c];
+        r_old[c] = rv;
+        r[c] = fmx(-a, Ap[c], rv);
+        c += g.sk;
+    }
+}
+
+// FCG: sums z.r, z.r_old, r.r after the (possibly nonlinear) preconditioner
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_dot(Geo g, Shape sh, const T* __restrict__ r, const T* __restrict__ z,
+                                                 const T* __restrict__ r_old, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1, a2, a3;
+    if (q.active) {
+        long long c = q.c;
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T rv = r[c], zv = z[c];
+            a1.add(zv, rv);
+            a2.add(zv, r_old[c]);
+            a3.add(rv, rv);
+            c += g.sk;
+        }
+    }
+    double v[3] = {a1.value(), a2.value(), a3.value()};
+    reduce_finalize<3>(v, rc);
+}
+
 // r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
 // stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
 template <typename TR>
@@ -1206,6 +1272,19 @@ void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const Dev
     k_cg_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, z, st);
     PPS_COUNT_LAUNCH();
 }
+template <typename T>
+void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, T* r_old, const T* Ap,
+                        const DevState* st, cudaStream_t s)
+{
+    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, r_old, Ap, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* r_old, RedCtx rc, cudaStream_t s)
+{
+    k_fcg_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, r_old, rc);
+    PPS_COUNT_LAUNCH();
+}
 template <typename TR>
 void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
                    const Coef& a, RedCtx rc, cudaStream_t s)
@@ -1260,6 +1339,9 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
                                        cudaStream_t);                                                            \
     template void fast_cg_dot_rz<T>(const Geo&, const Shape&, const T*, const T*, RedCtx, cudaStream_t);         \
     template void fast_cg_update_p<T>(const Geo&, const Shape&, T*, const T*, const DevState*, cudaStream_t);    \
+    template void fast_fcg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, T*, const T*,                \
+                                        const DevState*, cudaStream_t);                                          \
+    template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
                                    const Coef&, RedCtx, cudaStream_t);                                           \
     template void fill_field<T>(T*, long long, T, cudaStream_t);

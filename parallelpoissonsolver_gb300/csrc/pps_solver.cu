@@ -512,6 +512,13 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
     }
 }
 
+// Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity).
+template <typename T>
+void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+{
+    fast_precond<T>(s, F, B, X, L);
+}
+
 // One BiCGSTAB iteration (BiCGSTAB.hpp:133-272) on the fast kernels; xacc is the
 // field the corrections accumulate in (x itself for FP64, the FP32 correction for MIXED).
 template <typename T>
@@ -553,10 +560,31 @@ void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     L.launches += 4;
 }
 
+// One flexible-CG iteration: CG with beta = z_new.(r_new - r_old) / (z_old.r_old), so
+// the preconditioner may change from one application to the next.  r_old lives in
+// the Az field, which CG does not use.
+template <typename T>
+void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
+{
+    const Geo& g = s->geo;
+    const Shape& sh = s->shape;
+    cudaStream_t st = s->stream;
+    const long long N = s->n_unknowns;
+    const Coef a = op_coef(g);
+    fast_cg_stencil_dot<T>(g, sh, F.p, F.r, F.z, F.AMp, a, red(s, FIN_CG_ALPHA), st);
+    fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.Az, F.AMp, s->d_st, st);
+    precond_any<T>(s, F, F.r, F.z, L);
+    fast_fcg_dot<T>(g, sh, F.r, F.z, F.Az, red(s, FIN_FCG_CONV), st);
+    fast_cg_update_p<T>(g, sh, F.p, F.z, s->d_st, st);
+    L.bytes += bytes_of<T>(N, 4 + 7 + 3 + 3);
+    L.launches += 4;
+}
+
 template <typename T>
 void fast_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
 {
     if (s->cfg.krylov == PPS_KRYLOV_CG) fast_cg_iteration<T>(s, F, xacc, L);
+    else if (s->cfg.krylov == PPS_KRYLOV_FCG) fast_fcg_iteration<T>(s, F, xacc, L);
     else fast_bicgstab_iteration<T>(s, F, xacc, L);
 }
 
@@ -669,8 +697,8 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     pps_status rc = PPS_OK;
     read_state(s);
     if (!s->h_st->done) {
-        if (s->cfg.krylov == PPS_KRYLOV_CG) {
-            fast_precond<double>(s, F, F.r, F.z, L);
+        if (s->cfg.krylov == PPS_KRYLOV_CG || s->cfg.krylov == PPS_KRYLOV_FCG) {
+            precond_any<double>(s, F, F.r, F.z, L);
             CK(cudaMemcpyAsync(F.p, F.z, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
         }
         rc = run_iterations<double>(s, F, x, PPS_FORM_FP64, L);
@@ -680,7 +708,7 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     S.iterations = s->h_st->iter;
     S.err_iter = s->h_st->iter > 0 ? s->h_st->err / normb : -1.0;
     pull_history(s, S.iterations, false);
-    S.precond_applications += S.iterations * (s->cfg.krylov == PPS_KRYLOV_CG ? 1 : 2);
+    S.precond_applications += S.iterations * (s->cfg.krylov == PPS_KRYLOV_BICGSTAB ? 2 : 1);
     // final true residual (computeErrorOperatorA after the loop, BiCGSTAB.hpp:305-308)
     if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
     fast_residual<double>(g, s->shape, x, b, F.Az, nullptr, nullptr, a, red(s, FIN_STORE), st);
@@ -726,15 +754,15 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         }
         if (ref == s->cfg.max_refinements || remaining <= 0) break;
         fill_field<float>(F.e, g.ntot, 0.0f, st);
-        if (s->cfg.krylov == PPS_KRYLOV_CG) {
-            fast_precond<float>(s, F, F.r, F.z, L);
+        if (s->cfg.krylov == PPS_KRYLOV_CG || s->cfg.krylov == PPS_KRYLOV_FCG) {
+            precond_any<float>(s, F, F.r, F.z, L);
             CK(cudaMemcpyAsync(F.p, F.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
         }
         pps_status irc = run_iterations<float>(s, F, F.e, PPS_FORM_MIXED, L);
         const int it = s->h_st->iter;
         total_iter += it;
         pull_history(s, it, true);
-        S.precond_applications += it * (s->cfg.krylov == PPS_KRYLOV_CG ? 1 : 2);
+        S.precond_applications += it * (s->cfg.krylov == PPS_KRYLOV_BICGSTAB ? 2 : 1);
         S.err_iter = s->h_st->err / normb;
         fast_add_correction(g, s->shape, x, F.e, s->d_st, st);
         L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 1);
@@ -866,7 +894,8 @@ pps_status validate(const pps_grid* g, const pps_config* c)
     if (G > 4.0e9) { set_error("grid too large for the 32-bit plane indexing"); return PPS_ERR_INVALID_ARG; }
     for (int f = 0; f < 6; f++)
         if (g->bcs[f] != 0 && g->bcs[f] != 1) { set_error("bcs must be 0 (Dirichlet) or 1 (Neumann)"); return PPS_ERR_INVALID_ARG; }
-    if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
+    if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG && c->krylov != PPS_KRYLOV_FCG) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
+    if (c->krylov == PPS_KRYLOV_FCG && c->form == PPS_FORM_PARITY_FP64) { set_error("flexible CG has no reference counterpart, so no PARITY form"); return PPS_ERR_UNSUPPORTED; }
     if (c->precond != PPS_PREC_NONE && c->precond != PPS_PREC_CHEBYSHEV) { set_error("unknown precond"); return PPS_ERR_INVALID_ARG; }
     if (c->precond == PPS_PREC_CHEBYSHEV && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
     if (c->maxit < 0 || c->maxit > 100000000) { set_error("maxit out of range"); return PPS_ERR_INVALID_ARG; }

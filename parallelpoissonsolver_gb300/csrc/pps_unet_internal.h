@@ -1,0 +1,48 @@
+// Internal declarations of the learned preconditioner (U-Net) kernels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "pps_internal.h"
+
+namespace pps {
+namespace unet {
+
+struct Dims {
+    int D, H, W;   // z, y, x extents of an activation grid
+};
+
+typedef __nv_bfloat16 bf16;
+
+// 3x3x3 zero-padded convolution on tensor cores (Cin, Cout multiples of 16, Cout <= 96).
+void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
+          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s);
+void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* G, int ldg, int cg0, int Cout,
+                float* dW, cudaStream_t s);
+void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* db, cudaStream_t s);
+void relu_bwd(long long nv, bf16* G, int ldg, int cg0, const bf16* Y, int ldy, int cy0, int C, cudaStream_t s);
+void pool2(const Dims& dout, const bf16* in, int ldi, int ci0, bf16* out, int C, cudaStream_t s);
+void pool2_bwd(const Dims& dout, const bf16* gout, bf16* gin, int ldi, int ci0, int C, cudaStream_t s);
+void up2(const Dims& dfine, const bf16* in, int C, bf16* out, int ldo, int co0, cudaStream_t s);
+void up2_bwd(const Dims& dcoarse, const bf16* gout, int ldo, int co0, bf16* gin, int C, cudaStream_t s);
+void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s);
+void mse(long long nv, const float* out, int ldo, const float* t, bf16* G, int ldg, double* loss, cudaStream_t s);
+void adam(long long n, float* p, const float* g, float* m, float* v, bf16* pb, float lr, float b1, float b2, float eps,
+          int step, cudaStream_t s);
+void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s);
+void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s);
+void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s);
+void rms(long long n, const float* a, float* out, cudaStream_t s);
+
+// Solver field (guard-padded, Dirichlet unknowns) <-> dense unknown arrays.
+template <typename T>
+void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s);
+template <typename T>
+void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s);
+// 2x full-weighting restriction and trilinear prolongation of dense unknown arrays.
+void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s);
+void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
+
+}  // namespace unet
+}  // namespace pps

@@ -1,0 +1,587 @@
+// Kernels of the learned preconditioner: a 3-D convolutional U-Net with BF16 weights
+// and activations and FP32 accumulation, plus the grid-transfer kernels that move a
+// solver field to the network's grid and back.  No reference counterpart.
+//
+// Activations are channels-last: act[((z*H + y)*W + x)*ld + c0 + c], BF16, where a
+// tensor may occupy a channel slot [c0, c0+C) of a wider buffer (the U-Net's skip
+// concatenations).  Convolutions are 3x3x3, zero-padded, stride 1, as implicit
+// GEMMs on the tensor cores: M = voxels, N = output channels, K = 27 taps x input
+// channels, 16x16x16 BF16 fragments with FP32 accumulators.
+#include "pps_unet_internal.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <mma.h>
+
+namespace pps {
+namespace unet {
+
+using namespace nvcuda;
+typedef __nv_bfloat16 bf16;
+
+constexpr int TILE_V = 64;   // voxels (along x) per conv block: 4 warps x 16
+
+// ---------------------------------------------------------------------------
+// Convolution, forward: Y[v][co] = act(bias[co] + sum_tap sum_ci X[v+off(tap)][ci] W[tap][ci][co])
+// Cin, Cout multiples of 16, Cout <= 96.  One block: 64 consecutive voxels of one
+// (z, y) row, all output channels.
+// ---------------------------------------------------------------------------
+template <bool RELU, bool OUT_F32>
+__global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
+                                              const bf16* __restrict__ Wt, const float* __restrict__ bias,
+                                              void* __restrict__ Yv, int ldy, int cy0, int Cout)
+{
+    __shared__ __align__(32) bf16 sA[TILE_V * 16];
+    __shared__ __align__(32) bf16 sB[16 * 96];
+    __shared__ __align__(32) float sC[TILE_V * 96];
+    const int ntx = (d.W + TILE_V - 1) / TILE_V;
+    const int xt = blockIdx.x % ntx;
+    const int y = (blockIdx.x / ntx) % d.H;
+    const int z = blockIdx.x / (ntx * d.H);
+    const int x0 = xt * TILE_V;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nfrag = Cout / 16;
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[6];
+#pragma unroll
+    for (int f = 0; f < 6; f++) wmma::fill_fragment(acc[f], 0.0f);
+
+    for (int tap = 0; tap < 27; tap++) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const int zz = z + dz, yy = y + dy;
+        const bool row_ok = zz >= 0 && zz < d.D && yy >= 0 && yy < d.H;
+        for (int c0 = 0; c0 < Cin; c0 += 16) {
+            // A tile: 64 voxels x 16 channels; each thread moves 8 channels (16 B)
+            {
+                const int v = tid >> 1, h = tid & 1;
+                const int xx = x0 + v + dx;
+                uint4 val = make_uint4(0, 0, 0, 0);
+                if (row_ok && xx >= 0 && xx < d.W && x0 + v < d.W) {
+                    const bf16* src = X + ((long long)(zz * d.H + yy) * d.W + xx) * ldx + cx0 + c0 + 8 * h;
+                    val = *reinterpret_cast<const uint4*>(src);
+                }
+                *reinterpret_cast<uint4*>(&sA[v * 16 + 8 * h]) = val;
+            }
+            // B tile: 16 input channels x Cout
+            for (int q = tid; q < 16 * Cout / 8; q += 128) {
+                const int row = q / (Cout / 8), col8 = q % (Cout / 8);
+                const bf16* src = Wt + ((long long)tap * Cin + c0 + row) * Cout + 8 * col8;
+                *reinterpret_cast<uint4*>(&sB[row * 96 + 8 * col8]) = *reinterpret_cast<const uint4*>(src);
+            }
+            __syncthreads();
+            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
+            wmma::load_matrix_sync(a, sA + warp * 16 * 16, 16);
+#pragma unroll
+            for (int f = 0; f < 6; f++) {
+                if (f < nfrag) {
+                    wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> bfr;
+                    wmma::load_matrix_sync(bfr, sB + f * 16, 96);
+                    wmma::mma_sync(acc[f], a, bfr, acc[f]);
+                }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < 6; f++)
+        if (f < nfrag) wmma::store_matrix_sync(sC + warp * 16 * 96 + f * 16, acc[f], 96, wmma::mem_row_major);
+    __syncthreads();
+    for (int q = tid; q < TILE_V * Cout; q += 128) {
+        const int v = q / Cout, co = q % Cout;
+        if (x0 + v >= d.W) continue;
+        float val = sC[v * 96 + co] + (bias ? bias[co] : 0.0f);
+        if (RELU) val = fmaxf(val, 0.0f);
+        const long long o = ((long long)(z * d.H + y) * d.W + x0 + v) * ldy + cy0 + co;
+        if (OUT_F32) reinterpret_cast<float*>(Yv)[o] = val;
+        else reinterpret_cast<bf16*>(Yv)[o] = __float2bfloat16(val);
+    }
+}
+
+void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
+          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
+{
+    const int ntx = (d.W + TILE_V - 1) / TILE_V;
+    const unsigned blocks = (unsigned)(ntx * d.H * d.D);
+    if (out_f32) {
+        if (relu) k_conv<true, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        else k_conv<false, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+    } else {
+        if (relu) k_conv<true, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        else k_conv<false, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient: dW[tap][ci][co] += sum_v X[v+off(tap)][ci] * dY[v][co]
+// One block per (tap, z-plane): a GEMM with K = the plane's voxels, accumulated in
+// fragments and added to the FP32 gradient with atomics.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_conv_wgrad(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
+                                                    const bf16* __restrict__ G, int ldg, int cg0, int Cout,
+                                                    float* __restrict__ dW)
+{
+    __shared__ __align__(32) bf16 sX[TILE_V * 96];    // 64 voxels x Cin   (col-major A: ci x v)
+    __shared__ __align__(32) bf16 sG[TILE_V * 96];    // 64 voxels x Cout  (row-major B: v x co)
+    __shared__ __align__(32) float sC[96 * 96 / 4];   // staging of one warp's fragments
+    const int tap = blockIdx.x % 27;
+    const int z = blockIdx.x / 27;
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int mi = Cin / 16, ni = Cout / 16, nf = mi * ni;   // fragment pairs, split over warps
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[9];
+#pragma unroll
+    for (int f = 0; f < 9; f++) wmma::fill_fragment(acc[f], 0.0f);
+    const int zz = z + dz;
+    const bool plane_ok = zz >= 0 && zz < d.D;
+    if (plane_ok) {
+        const int ntx = (d.W + TILE_V - 1) / TILE_V;
+        for (int y = 0; y < d.H; y++) {
+            const int yy = y + dy;
+            const bool row_ok = yy >= 0 && yy < d.H;
+            if (!row_ok) continue;
+            for (int xt = 0; xt < ntx; xt++) {
+                const int x0 = xt * TILE_V;
+                for (int q = tid; q < TILE_V * Cin / 8; q += 128) {
+                    const int v = q / (Cin / 8), c8 = q % (Cin / 8);
+                    const int xx = x0 + v + dx;
+                    uint4 val = make_uint4(0, 0, 0, 0);
+                    if (x0 + v < d.W && xx >= 0 && xx < d.W)
+                        val = *reinterpret_cast<const uint4*>(X + ((long long)(zz * d.H + yy) * d.W + xx) * ldx + cx0 + 8 * c8);
+                    *reinterpret_cast<uint4*>(&sX[v * 96 + 8 * c8]) = val;
+                }
+                for (int q = tid; q < TILE_V * Cout / 8; q += 128) {
+                    const int v = q / (Cout / 8), c8 = q % (Cout / 8);
+                    uint4 val = make_uint4(0, 0, 0, 0);
+                    if (x0 + v < d.W)
+                        val = *reinterpret_cast<const uint4*>(G + ((long long)(z * d.H + y) * d.W + x0 + v) * ldg + cg0 + 8 * c8);
+                    *reinterpret_cast<uint4*>(&sG[v * 96 + 8 * c8]) = val;
+                }
+                __syncthreads();
+                for (int k = 0; k < TILE_V; k += 16) {
+#pragma unroll
+                    for (int f = 0; f < 9; f++) {
+                        const int pair = warp + 4 * f;
+                        if (pair < nf) {
+                            const int m = pair / ni, n = pair % ni;
+                            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::col_major> a;
+                            wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> b;
+                            wmma::load_matrix_sync(a, sX + k * 96 + m * 16, 96);
+                            wmma::load_matrix_sync(b, sG + k * 96 + n * 16, 96);
+                            wmma::mma_sync(acc[f], a, b, acc[f]);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    }
+    // accumulate into dW[tap][ci][co], one warp at a time through the staging tile
+    for (int w = 0; w < 4; w++) {
+        if (warp == w) {
+#pragma unroll
+            for (int f = 0; f < 9; f++) {
+                const int pair = warp + 4 * f;
+                if (pair < nf) {
+                    const int m = pair / ni, n = pair % ni;
+                    wmma::store_matrix_sync(sC, acc[f], 16, wmma::mem_row_major);
+                    __syncwarp();
+                    for (int q = tid & 31; q < 256; q += 32) {
+                        const int r = q / 16, c = q % 16;
+                        const float v = sC[q];
+                        if (v != 0.0f) atomicAdd(&dW[((long long)tap * Cin + m * 16 + r) * Cout + n * 16 + c], v);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* G, int ldg, int cg0, int Cout,
+                float* dW, cudaStream_t s)
+{
+    k_conv_wgrad<<<(unsigned)(27 * d.D), 128, 0, s>>>(d, X, ldx, cx0, Cin, G, ldg, cg0, Cout, dW);
+}
+
+// db[co] += sum_v G[v][co]
+__global__ void k_bias_grad(long long nv, const bf16* __restrict__ G, int ldg, int cg0, int Cout, float* __restrict__ db)
+{
+    __shared__ float s[96];
+    for (int c = threadIdx.x; c < Cout; c += blockDim.x) s[c] = 0.0f;
+    __syncthreads();
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv * Cout;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long v = q / Cout;
+        const int c = (int)(q % Cout);
+        atomicAdd(&s[c], __bfloat162float(G[v * ldg + cg0 + c]));
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < Cout; c += blockDim.x) atomicAdd(&db[c], s[c]);
+}
+
+void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* db, cudaStream_t s)
+{
+    long long blocks = (nv * Cout + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
+    k_bias_grad<<<(unsigned)blocks, 256, 0, s>>>(nv, G, ldg, cg0, Cout, db);
+}
+
+// G[v][c] *= (Y[v][c] > 0): ReLU backward through the layer's own output.
+__global__ void k_relu_bwd(long long nv, bf16* __restrict__ G, int ldg, int cg0, const bf16* __restrict__ Y, int ldy,
+                           int cy0, int C)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv * C; q += (long long)gridDim.x * blockDim.x) {
+        const long long v = q / C;
+        const int c = (int)(q % C);
+        if (!(__bfloat162float(Y[v * ldy + cy0 + c]) > 0.0f)) G[v * ldg + cg0 + c] = __float2bfloat16(0.0f);
+    }
+}
+
+static unsigned eblocks(long long n)
+{
+    long long b = (n + 255) / 256;
+    if (b > 152LL * 32) b = 152LL * 32;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+void relu_bwd(long long nv, bf16* G, int ldg, int cg0, const bf16* Y, int ldy, int cy0, int C, cudaStream_t s)
+{
+    k_relu_bwd<<<eblocks(nv * C), 256, 0, s>>>(nv, G, ldg, cg0, Y, ldy, cy0, C);
+}
+
+// 2x average pooling: out (D/2,H/2,W/2) dense C channels <- in slot of ldi
+__global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0, bf16* __restrict__ out, int C)
+{
+    const long long n = (long long)dout.D * dout.H * dout.W * C;
+    const int Hi = dout.H * 2, Wi = dout.W * 2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(q % C);
+        const long long v = q / C;
+        const int x = (int)(v % dout.W), y = (int)((v / dout.W) % dout.H), z = (int)(v / ((long long)dout.W * dout.H));
+        float s = 0.0f;
+        for (int o = 0; o < 8; o++) {
+            const int zz = 2 * z + (o >> 2), yy = 2 * y + ((o >> 1) & 1), xx = 2 * x + (o & 1);
+            s += __bfloat162float(in[((long long)(zz * Hi + yy) * Wi + xx) * ldi + ci0 + c]);
+        }
+        out[q] = __float2bfloat16(0.125f * s);
+    }
+}
+
+void pool2(const Dims& dout, const bf16* in, int ldi, int ci0, bf16* out, int C, cudaStream_t s)
+{
+    k_pool2<<<eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s>>>(dout, in, ldi, ci0, out, C);
+}
+
+// pooling backward: gin slot (fine) += g_out/8 at each of the 8 children
+__global__ void k_pool2_bwd(Dims dout, const bf16* __restrict__ gout, bf16* __restrict__ gin, int ldi, int ci0, int C)
+{
+    const int Hi = dout.H * 2, Wi = dout.W * 2;
+    const long long n = (long long)dout.D * 8 * dout.H * dout.W * C;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(q % C);
+        const long long vf = q / C;
+        const int xx = (int)(vf % Wi), yy = (int)((vf / Wi) % Hi), zz = (int)(vf / ((long long)Wi * Hi));
+        const long long vc = ((long long)(zz / 2) * dout.H + yy / 2) * dout.W + xx / 2;
+        bf16* p = gin + vf * ldi + ci0 + c;
+        *p = __float2bfloat16(__bfloat162float(*p) + 0.125f * __bfloat162float(gout[vc * C + c]));
+    }
+}
+
+void pool2_bwd(const Dims& dout, const bf16* gout, bf16* gin, int ldi, int ci0, int C, cudaStream_t s)
+{
+    k_pool2_bwd<<<eblocks((long long)dout.D * 8 * dout.H * dout.W * C), 256, 0, s>>>(dout, gout, gin, ldi, ci0, C);
+}
+
+// nearest 2x upsampling: out slot (fine) <- in dense (coarse)
+__global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __restrict__ out, int ldo, int co0)
+{
+    const long long n = (long long)dfine.D * dfine.H * dfine.W * C;
+    const int Hc = dfine.H / 2, Wc = dfine.W / 2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(q % C);
+        const long long v = q / C;
+        const int x = (int)(v % dfine.W), y = (int)((v / dfine.W) % dfine.H), z = (int)(v / ((long long)dfine.W * dfine.H));
+        out[v * ldo + co0 + c] = in[((long long)(z / 2) * Hc + y / 2) * Wc * C + (long long)(x / 2) * C + c];
+    }
+}
+
+void up2(const Dims& dfine, const bf16* in, int C, bf16* out, int ldo, int co0, cudaStream_t s)
+{
+    k_up2<<<eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s>>>(dfine, in, C, out, ldo, co0);
+}
+
+// upsampling backward: gin (coarse dense) = sum of the 8 children of gout's slot
+__global__ void k_up2_bwd(Dims dcoarse, const bf16* __restrict__ gout, int ldo, int co0, bf16* __restrict__ gin, int C)
+{
+    const long long n = (long long)dcoarse.D * dcoarse.H * dcoarse.W * C;
+    const int Hf = dcoarse.H * 2, Wf = dcoarse.W * 2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(q % C);
+        const long long v = q / C;
+        const int x = (int)(v % dcoarse.W), y = (int)((v / dcoarse.W) % dcoarse.H),
+                  z = (int)(v / ((long long)dcoarse.W * dcoarse.H));
+        float s = 0.0f;
+        for (int o = 0; o < 8; o++) {
+            const int zz = 2 * z + (o >> 2), yy = 2 * y + ((o >> 1) & 1), xx = 2 * x + (o & 1);
+            s += __bfloat162float(gout[((long long)(zz * Hf + yy) * Wf + xx) * ldo + co0 + c]);
+        }
+        gin[q] = __float2bfloat16(s);
+    }
+}
+
+void up2_bwd(const Dims& dcoarse, const bf16* gout, int ldo, int co0, bf16* gin, int C, cudaStream_t s)
+{
+    k_up2_bwd<<<eblocks((long long)dcoarse.D * dcoarse.H * dcoarse.W * C), 256, 0, s>>>(dcoarse, gout, ldo, co0, gin, C);
+}
+
+// Wf[tap'][co][ci] = W[26-tap][ci][co]: the weights of the backward-data convolution.
+__global__ void k_flip(const bf16* __restrict__ W, bf16* __restrict__ Wf, int Cin, int Cout)
+{
+    const int n = 27 * Cin * Cout;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int co = q % Cout, ci = (q / Cout) % Cin, tap = q / (Cout * Cin);
+        Wf[((long long)(26 - tap) * Cout + co) * Cin + ci] = W[q];
+    }
+}
+
+void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s)
+{
+    k_flip<<<(27 * Cin * Cout + 255) / 256, 256, 0, s>>>(W, Wf, Cin, Cout);
+}
+
+// MSE on channel 0 of an FP32 output slab [v][ld]: loss += sum (o - t)^2 / n,
+// gradient G[v][0] = 2 (o - t) / n, other channels 0.
+__global__ void k_mse(long long nv, const float* __restrict__ out, int ldo, const float* __restrict__ t,
+                      bf16* __restrict__ G, int ldg, double* loss)
+{
+    double s = 0.0;
+    const float inv = (float)(1.0 / (double)nv);
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
+        const float e = out[v * ldo] - t[v];
+        s += (double)e * (double)e;
+        G[v * ldg] = __float2bfloat16(2.0f * e * inv);
+        for (int c = 1; c < ldg; c++) G[v * ldg + c] = __float2bfloat16(0.0f);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, s / (double)nv);
+}
+
+void mse(long long nv, const float* out, int ldo, const float* t, bf16* G, int ldg, double* loss, cudaStream_t s)
+{
+    k_mse<<<eblocks(nv), 256, 0, s>>>(nv, out, ldo, t, G, ldg, loss);
+}
+
+// Adam on FP32 master parameters; refreshes the BF16 copy of the weights.
+__global__ void k_adam(long long n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, bf16* __restrict__ pb, float lr, float b1, float b2, float eps, float c1,
+                       float c2)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const float gq = g[q];
+        const float mq = b1 * m[q] + (1.0f - b1) * gq;
+        const float vq = b2 * v[q] + (1.0f - b2) * gq * gq;
+        m[q] = mq;
+        v[q] = vq;
+        const float upd = lr * (mq / c1) / (sqrtf(vq / c2) + eps);
+        const float pn = p[q] - upd;
+        p[q] = pn;
+        if (pb) pb[q] = __float2bfloat16(pn);
+    }
+}
+
+void adam(long long n, float* p, const float* g, float* m, float* v, bf16* pb, float lr, float b1, float b2, float eps,
+          int step, cudaStream_t s)
+{
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    k_adam<<<eblocks(n), 256, 0, s>>>(n, p, g, m, v, pb, lr, b1, b2, eps, c1, c2);
+}
+
+__global__ void k_f32_to_bf16(long long n, const float* __restrict__ a, bf16* __restrict__ b)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        b[q] = __float2bfloat16(a[q]);
+}
+
+void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s) { k_f32_to_bf16<<<eblocks(n), 256, 0, s>>>(n, a, b); }
+
+// Dense FP32 input [v] -> channel 0 of a BF16 activation [v][ld], scaled by 1/(*rms)
+// (rms == nullptr: scale 1); the other channels zero.
+__global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const float* rms, bf16* __restrict__ act, int ld)
+{
+    const float sc = rms ? (*rms > 0.0f ? 1.0f / *rms : 0.0f) : 1.0f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
+        act[v * ld] = __float2bfloat16(in[v] * sc);
+        for (int c = 1; c < ld; c++) act[v * ld + c] = __float2bfloat16(0.0f);
+    }
+}
+
+void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s)
+{
+    k_dense_to_act<<<eblocks(nv), 256, 0, s>>>(nv, in, rms, act, ld);
+}
+
+// channel 0 of an FP32 output slab -> dense FP32, times (*rms) * gain
+__global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int ld, const float* rms, float gain,
+                               float* __restrict__ dense)
+{
+    const float sc = (rms ? *rms : 1.0f) * gain;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x)
+        dense[v] = out[v * ld] * sc;
+}
+
+void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s)
+{
+    k_out_to_dense<<<eblocks(nv), 256, 0, s>>>(nv, out, ld, rms, gain, dense);
+}
+
+// rms of a dense FP32 array into *rms (single block, deterministic)
+__global__ void k_rms(long long n, const float* __restrict__ a, float* rms)
+{
+    __shared__ double sm[32];
+    double s = 0.0;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) s += (double)a[q] * (double)a[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
+        *rms = (float)sqrt(t / (double)(n > 0 ? n : 1));
+    }
+}
+
+void rms(long long n, const float* a, float* out, cudaStream_t s) { k_rms<<<1, 1024, 0, s>>>(n, a, out); }
+
+// ---------------------------------------------------------------------------
+// Grid transfers between a solver field (guard-padded layout, Dirichlet unknowns
+// 2..n-1 per axis) and dense [z][y][x] arrays of its unknowns.
+// ---------------------------------------------------------------------------
+
+// dense = field unknowns (type T -> float)
+template <typename T>
+__global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restrict__ dense)
+{
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
+    const long long n = (long long)ux * uy * uz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % ux), j = (int)((q / ux) % uy), k = (int)(q / ((long long)ux * uy));
+        dense[q] = (float)f[(g.lo[0] + i) + g.sj * (g.lo[1] + j) + g.sk * (g.lo[2] + k)];
+    }
+}
+
+// field unknowns (+)= scale * dense
+template <typename T>
+__global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __restrict__ f, float scale, int add)
+{
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
+    const long long n = (long long)ux * uy * uz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % ux), j = (int)((q / ux) % uy), k = (int)(q / ((long long)ux * uy));
+        const long long c = (g.lo[0] + i) + g.sj * (g.lo[1] + j) + g.sk * (g.lo[2] + k);
+        const T v = (T)(scale * dense[q]);
+        f[c] = add ? f[c] + v : v;
+    }
+}
+
+template <typename T>
+void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
+{
+    const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
+    k_field_to_dense<T><<<eblocks(n), 256, 0, s>>>(g, f, dense);
+}
+
+template <typename T>
+void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s)
+{
+    const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
+    k_dense_to_field<T><<<eblocks(n), 256, 0, s>>>(g, dense, f, scale, add);
+}
+
+template void field_to_dense<float>(const Geo&, const float*, float*, cudaStream_t);
+template void field_to_dense<double>(const Geo&, const double*, float*, cudaStream_t);
+template void dense_to_field<float>(const Geo&, const float*, float*, float, int, cudaStream_t);
+template void dense_to_field<double>(const Geo&, const float*, double*, float, int, cudaStream_t);
+
+// Full-weighting restriction of dense unknown arrays, fine (2m) -> coarse (m) per
+// axis: coarse unknown I sits on fine unknown 2I+1 (0-based), weights 1/4,1/2,1/4
+// per axis; fine values beyond the grid are the Dirichlet zero.
+__global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __restrict__ coarse)
+{
+    const int Wf = dc.W * 2, Hf = dc.H * 2, Df = dc.D * 2;
+    const long long n = (long long)dc.D * dc.H * dc.W;
+    const float w1[3] = {0.25f, 0.5f, 0.25f};
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % dc.W), y = (int)((q / dc.W) % dc.H), z = (int)(q / ((long long)dc.W * dc.H));
+        float s = 0.0f;
+        for (int a = 0; a < 3; a++) {
+            const int zz = 2 * z + a;
+            if (zz >= Df) continue;
+            for (int b = 0; b < 3; b++) {
+                const int yy = 2 * y + b;
+                if (yy >= Hf) continue;
+                for (int c = 0; c < 3; c++) {
+                    const int xx = 2 * x + c;
+                    if (xx >= Wf) continue;
+                    s += w1[a] * w1[b] * w1[c] * fine[((long long)zz * Hf + yy) * Wf + xx];
+                }
+            }
+        }
+        coarse[q] = s;
+    }
+}
+
+void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
+{
+    k_restrict<<<eblocks((long long)dc.D * dc.H * dc.W), 256, 0, s>>>(dc, fine, coarse);
+}
+
+// Trilinear prolongation, coarse (m) -> fine (2m): fine unknown i takes coarse
+// (i-1)/2 exactly when i is odd (0-based), the mean of its two coarse neighbours
+// otherwise (zero beyond the grid); the transpose of k_restrict up to a factor 8.
+__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine)
+{
+    const int Wf = dc.W * 2, Hf = dc.H * 2, Df = dc.D * 2;
+    const long long n = (long long)Df * Hf * Wf;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % Wf), y = (int)((q / Wf) % Hf), z = (int)(q / ((long long)Wf * Hf));
+        int i0[3], i1[3];
+        float w0[3], w1v[3];
+        const int idx[3] = {x, y, z};
+        const int nc[3] = {dc.W, dc.H, dc.D};
+        for (int d = 0; d < 3; d++) {
+            if (idx[d] & 1) {
+                i0[d] = (idx[d] - 1) / 2;
+                i1[d] = i0[d];
+                w0[d] = 1.0f;
+                w1v[d] = 0.0f;
+            } else {
+                i0[d] = idx[d] / 2 - 1;
+                i1[d] = idx[d] / 2;
+                w0[d] = 0.5f;
+                w1v[d] = 0.5f;
+            }
+            (void)nc;
+        }
+        float s = 0.0f;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                for (int c = 0; c < 2; c++) {
+                    const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = c ? i1[0] : i0[0];
+                    const float w = (a ? w1v[2] : w0[2]) * (b ? w1v[1] : w0[1]) * (c ? w1v[0] : w0[0]);
+                    if (w == 0.0f || zz < 0 || yy < 0 || xx < 0 || zz >= dc.D || yy >= dc.H || xx >= dc.W) continue;
+                    s += w * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
+                }
+        fine[q] = s;
+    }
+}
+
+void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
+{
+    k_prolong<<<eblocks((long long)dc.D * 8 * dc.H * dc.W), 256, 0, s>>>(dc, coarse, fine);
+}
+
+}  // namespace unet
+}  // namespace pps

@@ -279,3 +279,28 @@ def test_autotune_keeps_results(gpu, oracle, form, tmp_path):
     assert s2.autotune(cache=cache) == t
     with pytest.raises(pps.PpsError):
         s2.set_tuning({**t, "cheb_ty": 3})
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_flexible_cg_converges(gpu, oracle, form):
+    case = BY_NAME["dirichlet_random_m10"]
+    x, b, faces = case_inputs(oracle, case)
+    xo, bo = x.copy(), b.copy()
+    oracle.solve(ogrid_of(oracle, case), oracle.Config(**{**case["cfg"], "tol": 1e-13, "maxit": 20000}), xo, bo)
+    c = case["cfg"]
+    s = pps.FlexibleCG(grid_of(case), pps.ChebyshevIteration(c["cheb_degree"], c["cheb_eps"], c["rescale_min"]),
+                       tolerance=1e-10, max_iteration=1700, form=form)
+    assert s(x, b) == pps.OK
+    assert s.get_error_compute_operator() <= 1e-10
+    assert rel_l2(x, xo) < 1e-7
+    # with a fixed (linear, symmetric) preconditioner FCG needs about the CG count
+    xc = case_inputs(oracle, case)[0]
+    cg = pps.BaseCG(grid_of(case), pps.ChebyshevIteration(c["cheb_degree"], c["cheb_eps"], c["rescale_min"]),
+                    tolerance=1e-10, max_iteration=1700, form=form)
+    assert cg(xc, case_inputs(oracle, case)[1]) == pps.OK
+    assert abs(s.get_num_iteration_final() - cg.get_num_iteration_final()) <= 3
+
+
+def test_flexible_cg_has_no_parity_form(gpu):
+    with pytest.raises(pps.PpsError):
+        pps.FlexibleCG(pps.BlockGrid.cube(8), form="parity")
