@@ -6,9 +6,12 @@ with f a seeded unit-RMS Gaussian random field, P(k) ~ k^-2 (seed 2), solved by
 BiCGSTAB + Chebyshev(11) (the reference CPU preset) from x = 0.
 
 One step = one full solve.  `value` is the device time per solve of the fastest
-form (MIXED) with the fields resident in HBM; `e2e` is the same solve through
-pps_solve() on pinned host buffers, copies included; the plain FP64 form is timed
-beside it.  Every field is 0.5-1.1 GB, far larger than the 129 MB L2, so no L2 flush
+form, mixed+learned: FP64 iterative refinement around FP32 flexible CG whose
+preconditioner is Chebyshev smoothing plus a U-Net coarse-grid correction (the
+network trained here, outside the timed region, by the library's own kernels).
+`e2e` is the same solve through pps_solve() on pinned host buffers, copies
+included; the reference method (BiCGSTAB + Chebyshev) is timed beside it in mixed
+precision and in plain FP64.  Every field is 0.5-1.1 GB, far larger than the 129 MB L2, so no L2 flush
 is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--size M] [--impl reference]
@@ -33,7 +36,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed FP32/FP64 vs plain FP64), 1 GB300"
+METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed+learned vs plain FP64), 1 GB300"
+NET_GRID = 32   # the U-Net runs as the coarse-grid solver on a 32^3 grid
 TOL = 1e-10
 DEGREE = 11
 # Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload, measured by
@@ -160,6 +164,42 @@ def make_inputs(m: int):
     return x, b
 
 
+def train_network(args, dev: int):
+    """The learned preconditioner's U-Net: linear 3-level 16/32/64 network trained on
+    32^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs; u solved to 1e-12
+    by the plain FP64 solver) with the library's own kernels; it is the coarse-grid
+    solver of the two-grid correction inside flexible CG."""
+    import torch
+
+    import parallelpoissonsolver_gb300 as pps
+    from parallelpoissonsolver_gb300 import learned
+
+    t0 = time.perf_counter()
+    train = learned.make_dataset(NET_GRID, range(10000, 10000 + args.train_samples), device=dev)
+    held = learned.make_dataset(NET_GRID, range(30000, 30000 + 16), device=dev)
+    t_data = time.perf_counter() - t0
+    scale = learned.fit_scale(train)
+    net = pps.UNet((16, 32, 64), seed=1, device=dev, linear=True)
+    t1 = time.perf_counter()
+    losses = learned.train(net, train, scale, args.train_steps, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    errs = learned.evaluate(net, held, scale)
+    info = {"grid": f"{NET_GRID}^3", "channels": [16, 32, 64], "activation": "identity (linear U-Net)",
+            "precision": "BF16 weights/activations, FP32 accumulation (tensor cores)",
+            "train_pairs": len(train), "steps": args.train_steps, "final_loss": float(np.mean(losses[-100:])),
+            "held_out_rel_err_median": float(np.median(errs)), "held_out_rel_err_max": float(np.max(errs)),
+            "data_s": t_data, "train_s": t_train, "scale": scale}
+    return net, scale, info
+
+
+def learned_gain(m: int, scale: float):
+    """(coarsening levels, output gain) to use the 32^3 network on an m^3 grid."""
+    import math
+    k = int(round(math.log2(m / NET_GRID)))
+    return k, scale * ((2 ** k / (m + 1)) / (1.0 / (NET_GRID + 1))) ** 2
+
+
 def run_gpu(args, dist: Dist):
     import torch
 
@@ -169,70 +209,72 @@ def run_gpu(args, dist: Dist):
     torch.cuda.set_device(dev)
     m = args.size
     grid = pps.BlockGrid.cube(m)
-    n_unknowns = m ** 3
     x_h, b_h = make_inputs(m)
     b_d = torch.from_numpy(b_h).to(f"cuda:{dev}")
     x_d = torch.zeros_like(b_d)
     G = b_h.size
     prec = pps.ChebyshevIteration(DEGREE)
 
+    net, scale, net_info = train_network(args, dev)
+    k, gain = learned_gain(m, scale)
+    flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER | pps.LEARNED_POST_SMOOTH
+    head = pps.FlexibleCG(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
+                          inner_tol=args.inner_tol, device=dev)
+    head.set_learned(net, k, gain, flags)
     mixed = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
                          inner_tol=args.inner_tol, device=dev)
     plain = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="fp64", use_graph=False,
                          device=dev)
-
-    tuned = {"mixed": mixed.autotune(), "fp64": plain.autotune()}
+    tuned = {"mixed+learned": head.autotune(), "mixed": mixed.autotune(), "fp64": plain.autotune()}
 
     def solve(s):
         x_d.zero_()
         torch.cuda.current_stream().synchronize()   # the solver runs on its own stream
         st = s.solve_device(x_d.data_ptr(), b_d.data_ptr())
         if st != pps.OK:
-            raise RuntimeError(f"solve failed: {pps.status_string(st)}")
+            raise RuntimeError(f"solve failed: {pps.status_string(st)} {pps.last_error()}")
         return s.stats()
 
     for _ in range(args.warmup):
-        solve(mixed)
+        solve(head)
     torch.cuda.synchronize()
 
-    # ---- timed region: K mixed solves, fields resident in HBM ----
+    # ---- timed region: K mixed+learned solves, fields resident in HBM ----
     dist.barrier()
     torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
     stats = []
     with ClockSampler(dev) as clocks:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            stats.append(solve(mixed))
+            stats.append(solve(head))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     dist.barrier()
     dev_times = [s["seconds_solve"] for s in stats]
     t_step = dist.max(sum(dev_times) / len(dev_times))
-    del stream
-    mixed_x = x_d.clone()
+    head_x = x_d.clone()
 
-    # ---- plain FP64 form, same workload ----
-    plain_stats = []
-    for _ in range(max(1, args.plain_steps)):
-        plain_stats.append(solve(plain))
+    # ---- the reference method in mixed precision, and in plain FP64 ----
+    mixed_stats = [solve(mixed) for _ in range(max(1, args.plain_steps))]
+    t_mixed = sum(s["seconds_solve"] for s in mixed_stats) / len(mixed_stats)
+    plain_stats = [solve(plain) for _ in range(max(1, args.plain_steps))]
     t_plain = sum(s["seconds_solve"] for s in plain_stats) / len(plain_stats)
     plain_x = x_d.clone()
-    rel_diff = float(torch.linalg.norm(mixed_x - plain_x) / torch.linalg.norm(plain_x))
+    rel_diff = float(torch.linalg.norm(head_x - plain_x) / torch.linalg.norm(plain_x))
 
     # ---- e2e: the C ABI on pinned host buffers, copies inside the timed region ----
     xp = torch.zeros(b_h.shape, dtype=torch.float64).pin_memory()
     bp = torch.from_numpy(b_h).pin_memory()
     xn, bn = xp.numpy(), bp.numpy()
     e2e = []
-    for k in range(args.steps + 1):
+    for kk in range(args.steps + 1):
         xn[...] = 0.0
         t = time.perf_counter()
-        st = mixed(xn, bn)
+        st = head(xn, bn)
         el = time.perf_counter() - t
         if st != pps.OK:
             raise RuntimeError(f"e2e solve failed: {pps.status_string(st)}")
-        if k > 0:
+        if kk > 0:
             e2e.append(el)
     t_e2e = dist.max(sum(e2e) / len(e2e))
 
@@ -244,8 +286,11 @@ def run_gpu(args, dist: Dist):
     achieved = (sweep_b / sweep_s) / 1e9 if sweep_s > 0 else None
     ratio = traffic_ratio()
     per_launch_alg = sweep_b / sweep_n if sweep_n else None
-    p_sweep_s = sum(s["sweep_seconds"] for s in plain_stats)
-    p_sweep_b = sum(s["sweep_bytes"] for s in plain_stats)
+
+    def summary(s, t):
+        return {"value": t, "unit": "s", "iterations": s["iterations"], "refinements": s["refinements"],
+                "err_true": s["err_true"],
+                "sweep_gbs": (s["sweep_bytes"] / s["sweep_seconds"]) / 1e9 if s["sweep_seconds"] > 0 else None}
 
     out = {
         "metric": METRIC,
@@ -258,28 +303,35 @@ def run_gpu(args, dist: Dist):
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 stencil/smoother/Krylov fields + f64 residual/dots/refinement",
+        "dtype": "f32 stencil/smoother/Krylov fields, bf16 U-Net (fp32 accum), f64 residual/dots/refinement",
         "data": "synthetic: seeded k^-2 Gaussian random field (numpy PCG64 seed 2), unit RMS",
         "config": {
             "workload": f"{m}^3 interior unknowns, h=1/{m + 1}, Dirichlet 0, -lap u = f, f ~ P(k) k^-2 field; "
-                        f"BiCGSTAB + Chebyshev({DEGREE}) preconditioner, stop at ||r||/||b_adj|| <= {TOL:g}",
-            "form": "mixed: FP32 inner BiCGSTAB/Chebyshev with FP64-accurate dots, FP64 iterative refinement",
+                        f"stop at FP64 ||r||/||b_adj|| <= {TOL:g}",
+            "form": "mixed+learned: FP64 iterative refinement around FP32 flexible CG; preconditioner = "
+                    f"Chebyshev({DEGREE}) smoothing + U-Net coarse-grid correction on the {NET_GRID}^3 grid "
+                    f"({k} restrictions) + Chebyshev post-smoothing; learned initial guess",
             "l2": "no flush: every field (0.5-1.1 GB) exceeds the 129 MB L2",
             "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU, single domain",
             "iterations": stats[-1]["iterations"],
             "refinements": stats[-1]["refinements"],
-            "tiles": tuned,
+            "learned_applications": stats[-1]["learned_applications"],
+            "fallback_iteration": stats[-1]["fallback_iteration"],
             "err_true": stats[-1]["err_true"],
+            "network": net_info,
+            "tiles": tuned,
         },
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
-        "plain_fp64": {
-            "value": t_plain, "unit": "s", "iterations": plain_stats[-1]["iterations"],
-            "err_true": plain_stats[-1]["err_true"],
-            "sweep_gbs": (p_sweep_b / p_sweep_s) / 1e9 if p_sweep_s > 0 else None,
+        "forms": {
+            "mixed+learned (FCG)": summary(stats[-1], t_step),
+            "mixed (reference BiCGSTAB + Chebyshev)": summary(mixed_stats[-1], t_mixed),
+            "plain_fp64 (reference BiCGSTAB + Chebyshev)": summary(plain_stats[-1], t_plain),
         },
-        "speedup_mixed_vs_fp64": t_plain / t_step,
-        "mixed_vs_fp64_rel_l2": rel_diff,
+        "plain_fp64": summary(plain_stats[-1], t_plain),
+        "speedup_vs_plain_fp64": t_plain / t_step,
+        "speedup_mixed_only_vs_plain_fp64": t_plain / t_mixed,
+        "vs_plain_fp64_rel_l2": rel_diff,
         "hbm_gbs_solve": stats[-1]["hbm_bytes"] / stats[-1]["seconds_solve"] / 1e9,
         "roofline": {
             "bound": "hbm",
@@ -296,9 +348,56 @@ def run_gpu(args, dist: Dist):
         "clocks": clocks.summary(),
         "wall_s_timed_region": wall,
     }
+    if not args.no_learned_128:
+        out["learned_128"] = run_learned_128(args, dev, net, scale)
+    head.close()
     mixed.close()
     plain.close()
     return out, plain_stats[-1]["iterations"]
+
+
+def run_learned_128(args, dev: int, net, scale: float):
+    """Learned initial guess and preconditioner at 128^3 on held-out seeds (half k^-2
+    fields, half blobs): flexible CG with the network against the reference method
+    (BiCGSTAB + Chebyshev) and against flexible CG without it, all FP64 to 1e-10."""
+    import torch
+
+    import parallelpoissonsolver_gb300 as pps
+    from parallelpoissonsolver_gb300 import learned
+
+    m = 128
+    grid = pps.BlockGrid.cube(m)
+    k, gain = learned_gain(m, scale)
+    forms = {
+        "bicgstab": pps.BiCGSTAB(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64", device=dev),
+        "fcg": pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64", device=dev),
+        "fcg+learned": pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64",
+                                      use_graph=False, device=dev),
+    }
+    forms["fcg+learned"].set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER |
+                                     pps.LEARNED_POST_SMOOTH)
+    res = {n: {"iterations": [], "seconds": [], "err_true": []} for n in forms}
+    for i in range(args.held_out):
+        seed = 30000 + i
+        b = learned.rhs(m, seed, "field" if seed % 2 == 0 else "blobs")
+        bd = torch.from_numpy(b).cuda(dev)
+        for n, s in forms.items():
+            xd = torch.zeros_like(bd)
+            torch.cuda.synchronize()
+            st = s.solve_device(xd.data_ptr(), bd.data_ptr())
+            d = s.stats()
+            res[n]["iterations"].append(d["iterations"] if st == pps.OK else -1)
+            res[n]["seconds"].append(d["seconds_solve"])
+            res[n]["err_true"].append(d["err_true"])
+    for s in forms.values():
+        s.close()
+    out = {"workload": f"{m}^3, Dirichlet 0, {args.held_out} held-out seeds (30000+), FP64 to {TOL:g}"}
+    for n, r in res.items():
+        out[n] = {"mean_iterations": float(np.mean(r["iterations"])), "mean_seconds": float(np.mean(r["seconds"])),
+                  "max_err_true": float(np.max(r["err_true"]))}
+    out["iteration_gain_vs_fcg"] = out["fcg"]["mean_iterations"] / out["fcg+learned"]["mean_iterations"]
+    out["time_gain_vs_bicgstab"] = out["bicgstab"]["mean_seconds"] / out["fcg+learned"]["mean_seconds"]
+    return out
 
 
 def run_batched(args, dist: Dist):
@@ -411,6 +510,10 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=3e-3)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-learned-128", action="store_true")
+    ap.add_argument("--held-out", type=int, default=16)
+    ap.add_argument("--train-samples", type=int, default=256)
+    ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])

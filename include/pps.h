@@ -110,6 +110,8 @@ typedef struct {
     double sweep_seconds;       /* device time of the Chebyshev sweeps (event-timed)        */
     int sweep_launches;         /* sweeps launched                                          */
     double sweep_bytes;         /* algorithmic bytes of those sweeps                        */
+    int learned_applications;   /* network corrections applied (pps_set_learned)           */
+    int fallback_iteration;     /* iteration at which the learned preconditioner was dropped, -1 none */
 } pps_stats;
 
 typedef struct pps_solver pps_solver;
@@ -229,6 +231,9 @@ typedef struct pps_unet pps_unet;
 pps_status pps_unet_create(int c1, int c2, int c3, unsigned long long seed, int device, pps_unet** out);
 pps_status pps_unet_destroy(pps_unet* net);
 int pps_unet_param_count(const pps_unet* net);
+/* Activation of the hidden layers: 0 ReLU (default), 1 identity (the network is then
+ * a learned linear operator with the U-Net's multigrid structure). */
+pps_status pps_unet_set_activation(pps_unet* net, int linear);
 pps_status pps_unet_get_params(const pps_unet* net, float* out);
 pps_status pps_unet_set_params(pps_unet* net, const float* in);
 /* normalize = 1: the input is scaled to unit RMS and the output scaled back. */
@@ -238,9 +243,27 @@ pps_status pps_unet_forward(pps_unet* net, int nx, int ny, int nz, const float* 
  * of pps_unet_param_count floats). */
 pps_status pps_unet_gradients(pps_unet* net, int nx, int ny, int nz, const float* in_dev, const float* target_dev,
                               float* grads, double* loss);
-/* One Adam step (beta1 0.9, beta2 0.999) on the MSE loss of one sample. */
+/* One Adam step (beta1 0.9, beta2 0.999, gradient clipped to global norm 1) on the
+ * MSE loss of one sample. */
 pps_status pps_unet_train_step(pps_unet* net, int nx, int ny, int nz, const float* in_dev, const float* target_dev,
                                float lr, double* loss);
+/* Attaches a trained U-Net to a solver (FP64 or MIXED form, Dirichlet grid whose
+ * unknown extents are multiples of 4*2^coarsen).  flags:
+ *   PPS_LEARNED_INITIAL_GUESS   x += gain * P^k N(R^k b) before the solve;
+ *   PPS_LEARNED_PRECONDITIONER  inside flexible CG, z = Cheb(r) followed by
+ *                               z += gain * P^k N(R^k (r - A z)); the solve falls back
+ *                               to the plain preconditioner for good (restarting the
+ *                               recurrence) as soon as the per-iteration reduction of
+ *                               ||r||, the geometric mean over the last 4 iterations,
+ *                               is worse than 0.5.
+ * R, P: 2x restriction/prolongation, applied `coarsen` times; N: the network with
+ * unit-RMS input scaling.  net = NULL detaches.  The network must outlive its use. */
+#define PPS_LEARNED_INITIAL_GUESS 1
+#define PPS_LEARNED_PRECONDITIONER 2
+#define PPS_LEARNED_NO_FALLBACK 4     /* keep the network for the whole solve (measurements) */
+#define PPS_LEARNED_POST_SMOOTH 8     /* z += Cheb(r - A z) after the correction (two-grid cycle) */
+pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gain, int flags);
+
 /* 2x grid transfers of dense unknown arrays (coarse extents nx, ny, nz; the fine
  * grid has twice as many unknowns per axis, coarse unknown i on fine unknown 2i+1):
  * full-weighting restriction and trilinear prolongation (its transpose / 8). */

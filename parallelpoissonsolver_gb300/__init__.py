@@ -34,6 +34,7 @@ FORM_PARITY_FP64, FORM_FP64, FORM_MIXED = 0, 1, 2
 FORMS = {"parity": FORM_PARITY_FP64, "fp64": FORM_FP64, "mixed": FORM_MIXED}
 PRESET_CPU, PRESET_ALPAKA = 0, 1
 PROBLEM_REFERENCE_DEFAULT, PROBLEM_SINE = 0, 1
+LEARNED_INITIAL_GUESS, LEARNED_PRECONDITIONER, LEARNED_NO_FALLBACK, LEARNED_POST_SMOOTH = 1, 2, 4, 8
 
 # Every symbol include/pps.h declares.
 EXPORTED = [
@@ -46,6 +47,7 @@ EXPORTED = [
     "pps_batch_autotune", "pps_batch_tile", "pps_batch_solve",
     "pps_unet_create", "pps_unet_destroy", "pps_unet_param_count", "pps_unet_get_params", "pps_unet_set_params",
     "pps_unet_forward", "pps_unet_gradients", "pps_unet_train_step", "pps_restrict2", "pps_prolong2",
+    "pps_set_learned", "pps_unet_set_activation",
 ]
 
 
@@ -67,7 +69,8 @@ class PpsStats(C.Structure):
                 ("err_iter", C.c_double), ("err_true", C.c_double), ("norm_b", C.c_double),
                 ("seconds_solve", C.c_double), ("seconds_total", C.c_double), ("seconds_h2d", C.c_double),
                 ("seconds_d2h", C.c_double), ("hbm_bytes", C.c_double), ("kernel_launches", C.c_int),
-                ("sweep_seconds", C.c_double), ("sweep_launches", C.c_int), ("sweep_bytes", C.c_double)]
+                ("sweep_seconds", C.c_double), ("sweep_launches", C.c_int), ("sweep_bytes", C.c_double),
+                ("learned_applications", C.c_int), ("fallback_iteration", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -160,6 +163,8 @@ def load(build_if_missing: bool = False):
     L.pps_unet_gradients.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, C.POINTER(C.c_double)]
     L.pps_unet_train_step.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_float, C.POINTER(C.c_double)]
     L.pps_restrict2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
+    L.pps_set_learned.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+    L.pps_unet_set_activation.argtypes = [vp, C.c_int]
     L.pps_prolong2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_status_string.restype = C.c_char_p
     L.pps_status_string.argtypes = [C.c_int]
@@ -372,6 +377,16 @@ class Solver:
         if st != OK:
             raise PpsError(st, "pps_write_residual_history")
 
+    def set_learned(self, net, coarsen: int = 0, gain: float = 1.0,
+                    flags: int = LEARNED_INITIAL_GUESS | LEARNED_PRECONDITIONER):
+        """Attach a trained UNet (pps_set_learned); net=None detaches.  The solver keeps
+        a reference so the network outlives its use."""
+        st = load().pps_set_learned(self._h, net.handle if net is not None else None, int(coarsen), float(gain),
+                                    int(flags))
+        if st != OK:
+            raise PpsError(st, "pps_set_learned")
+        self._net = net
+
     def tuning_key(self) -> str:
         n = self.grid.npglobal
         return f"{n[0]}x{n[1]}x{n[2]}:form{self.config.form}"
@@ -526,13 +541,15 @@ class UNet:
     the library's own forward/backward kernels.  Arrays are device pointers of dense
     FP32 [nz][ny][nx] fields; extents must be multiples of 4."""
 
-    def __init__(self, channels=(16, 32, 64), seed: int = 0, device: int = 0):
+    def __init__(self, channels=(16, 32, 64), seed: int = 0, device: int = 0, linear: bool = False):
         h = C.c_void_p()
         st = load().pps_unet_create(channels[0], channels[1], channels[2], seed, device, C.byref(h))
         if st != OK:
             raise PpsError(st, "pps_unet_create")
         self._h = h
         self.channels = tuple(channels)
+        self.linear = bool(linear)
+        load().pps_unet_set_activation(h, int(self.linear))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -592,12 +609,12 @@ class UNet:
         return loss.value
 
     def save(self, path: str):
-        np.savez(path, params=self.get_params(), channels=np.array(self.channels))
+        np.savez(path, params=self.get_params(), channels=np.array(self.channels), linear=np.array(int(self.linear)))
 
     @classmethod
     def load_file(cls, path: str, device: int = 0):
         d = np.load(path)
-        net = cls(tuple(int(c) for c in d["channels"]), device=device)
+        net = cls(tuple(int(c) for c in d["channels"]), device=device, linear=bool(int(d["linear"])) if "linear" in d else False)
         net.set_params(d["params"])
         return net
 

@@ -12,6 +12,7 @@
 //                inner BiCGSTAB/CG with FP32 fields and FP64-accurate dots.
 #include "../../include/pps.h"
 #include "pps_internal.h"
+#include "pps_unet_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -131,6 +132,19 @@ struct pps_solver {
     double g_sweep_bytes = 0;
     int g_sweep_launches = 0;
 
+    // learned preconditioner / initial guess (pps_set_learned)
+    pps_unet* net = nullptr;
+    int net_coarsen = 0;
+    float net_gain = 1.0f;
+    int net_flags = 0;
+    bool net_active = false;          // preconditioner in use in the current solve (fallback clears it)
+    std::vector<float*> dn;           // dense levels: dn[0] fine residual ... dn[k] coarsest; dn_e the same sizes
+    std::vector<float*> dn_e;
+    float* dn_r = nullptr;
+    float* dn_z = nullptr;
+    int learned_apps = 0;
+    int fallback_iter = -1;
+
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
     int sweep_ev_used = 0;
@@ -226,6 +240,10 @@ void free_all(pps_solver* s)
         if (s->d_faces[i]) cudaFree(s->d_faces[i]);
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_dot) cudaFreeHost(s->h_dot);
+    for (float* q : s->dn) cudaFree(q);
+    for (float* q : s->dn_e) cudaFree(q);
+    if (s->dn_r) cudaFree(s->dn_r);
+    if (s->dn_z) cudaFree(s->dn_z);
     for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -512,11 +530,62 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
     }
 }
 
-// Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity).
+unet::Dims dense_dims(const pps_solver* s, int level)
+{
+    const Geo& g = s->geo;
+    const int f = 1 << level;
+    return unet::Dims{(g.hi[2] - g.lo[2]) / f, (g.hi[1] - g.lo[1]) / f, (g.hi[0] - g.lo[0]) / f};
+}
+
+// gain * P^k N(R^k res) where res = dn[0] (dense fine); result in dn_e[0].
+void learned_coarse_correction(pps_solver* s)
+{
+    cudaStream_t st = s->stream;
+    const int k = s->net_coarsen;
+    for (int l = 0; l < k; l++) unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
+    const unet::Dims dc = dense_dims(s, k);
+    if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, s->dn[(size_t)k], s->dn_e[(size_t)k], s->net_gain, st) != PPS_OK)
+        throw CudaFail{cudaErrorUnknown};
+    for (int l = k; l > 0; l--) unet::prolong2(dense_dims(s, l), s->dn_e[(size_t)l], s->dn_e[(size_t)l - 1], st);
+    s->learned_apps++;
+}
+
+// Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity),
+// followed, while the learned preconditioner is active, by the network's coarse
+// correction of the remaining residual: z = Cheb(r); z += gain P^k N(R^k (r - A z)).
 template <typename T>
 void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
 {
     fast_precond<T>(s, F, B, X, L);
+    if (!(s->net && s->net_active)) return;
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    unet::field_to_dense<T>(g, B, s->dn_r, st);
+    unet::field_to_dense<T>(g, X, s->dn_z, st);
+    unet::dense_residual(dense_dims(s, 0), s->dn_r, s->dn_z, (float)(1.0 / (g.ds[0] * g.ds[0])),
+                         (float)(1.0 / (g.ds[1] * g.ds[1])), (float)(1.0 / (g.ds[2] * g.ds[2])), s->dn[0], st);
+    learned_coarse_correction(s);
+    unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
+    if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
+        // post-smoothing: z += Cheb(r - A z), through the fields FCG leaves free (r0, Mp)
+        unet::field_to_dense<T>(g, X, s->dn_z, st);
+        unet::dense_residual(dense_dims(s, 0), s->dn_r, s->dn_z, (float)(1.0 / (g.ds[0] * g.ds[0])),
+                             (float)(1.0 / (g.ds[1] * g.ds[1])), (float)(1.0 / (g.ds[2] * g.ds[2])), s->dn[0], st);
+        unet::dense_to_field<T>(g, s->dn[0], F.r0, 1.0f, 0, st);
+        fast_precond<T>(s, F, F.r0, F.Mp, L);
+        unet::field_to_dense<T>(g, F.Mp, s->dn_z, st);
+        unet::dense_to_field<T>(g, s->dn_z, X, 1.0f, 1, st);
+    }
+}
+
+// Learned initial guess: x += gain P^k N(R^k b) at the unknowns.
+template <typename T>
+void learned_initial_guess(pps_solver* s, double* x, const double* b)
+{
+    const Geo& g = s->geo;
+    unet::field_to_dense<double>(g, b, s->dn[0], s->stream);
+    learned_coarse_correction(s);
+    unet::dense_to_field<double>(g, s->dn_e[0], x, 1.0f, 1, s->stream);
 }
 
 // One BiCGSTAB iteration (BiCGSTAB.hpp:133-272) on the fast kernels; xacc is the
@@ -610,8 +679,10 @@ int auto_check_every(const pps_solver* s, int elem_size)
 template <typename T>
 pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launcher& L)
 {
-    const int chunk = auto_check_every(s, (int)sizeof(T));
-    const bool graph = s->cfg.use_graph != 0 && !L.profile;
+    const bool learned = s->net && s->net_active;
+    const int chunk = learned ? 1 : auto_check_every(s, (int)sizeof(T));
+    const bool graph = s->cfg.use_graph != 0 && !L.profile && !learned;
+    std::vector<double> errs;   // residual norms seen by the fallback rule
     for (;;) {
         if (graph) {
             if (!(s->gexec && s->g_key_x == xacc && s->g_form == form && s->g_iters == chunk)) {
@@ -651,6 +722,21 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
         }
         read_state(s);
         if (s->h_st->done) break;
+        if (s->net && s->net_active) {
+            // fall back to the plain preconditioner when the per-iteration reduction,
+            // the geometric mean over the last 4 iterations, is worse than 0.5
+            const double e = s->h_st->err;
+            errs.push_back(e);
+            const size_t w = 4;
+            if (!(s->net_flags & PPS_LEARNED_NO_FALLBACK) && errs.size() > w &&
+                std::pow(e / errs[errs.size() - 1 - w], 1.0 / (double)w) > 0.5) {
+                s->net_active = false;
+                s->fallback_iter = s->h_st->iter;
+                // restart the flexible-CG recurrence on the plain preconditioner: z = M r, p = z
+                precond_any<T>(s, F, F.r, F.z, L);
+                CK(cudaMemcpyAsync(F.p, F.z, sizeof(T) * (size_t)s->geo.ntot, cudaMemcpyDeviceToDevice, s->stream));
+            }
+        }
     }
     return (pps_status)s->h_st->status;
 }
@@ -690,6 +776,10 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     const double normb = norm_badj(s, x, b);
     S.norm_b = normb;
     if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER) && s->cfg.krylov == PPS_KRYLOV_FCG;
+    s->learned_apps = 0;
+    s->fallback_iter = -1;
+    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess<double>(s, x, b);
     const Coef a = op_coef(g);
     state_init(s->d_st, s->d_hist, s->cfg.maxit, s->cfg.tol * normb, 0.0, 0, 0, 1.0 / normb, s->hist_cap, st);
     fast_residual<double>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st);
@@ -730,6 +820,10 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
     const double normb = norm_badj(s, x, b);
     S.norm_b = normb;
     if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER) && s->cfg.krylov == PPS_KRYLOV_FCG;
+    s->learned_apps = 0;
+    s->fallback_iter = -1;
+    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess<float>(s, x, b);
     const Coef a = op_coef(g);
     const double tol_abs = s->cfg.tol * normb;
     s->history.clear();
@@ -963,6 +1057,8 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
     S.sweep_seconds = sw;
     S.sweep_launches = s->sweep_launch_acc;
     S.sweep_bytes = s->sweep_bytes_acc;
+    S.learned_applications = s->learned_apps;
+    S.fallback_iteration = s->fallback_iter;
     return rc;
 }
 
@@ -1390,6 +1486,59 @@ pps_status pps_autotune(pps_solver* s, pps_tuning* out)
         CK(cudaStreamSynchronize(s->stream));
         apply_tuning(s, t);
         if (out) *out = t;
+        return PPS_OK;
+    });
+}
+
+pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gain, int flags)
+{
+    if (!s) return PPS_ERR_INVALID_ARG;
+    return guarded([&]() -> pps_status {
+        CK(cudaSetDevice(s->device));
+        for (float* q : s->dn) cudaFree(q);
+        for (float* q : s->dn_e) cudaFree(q);
+        s->dn.clear();
+        s->dn_e.clear();
+        if (s->dn_r) cudaFree(s->dn_r);
+        if (s->dn_z) cudaFree(s->dn_z);
+        s->dn_r = s->dn_z = nullptr;
+        s->net = nullptr;
+        if (!net) return PPS_OK;   // detach
+        if (s->cfg.form == PPS_FORM_PARITY_FP64) {
+            set_error("the learned preconditioner has no reference counterpart, so no PARITY form");
+            return PPS_ERR_UNSUPPORTED;
+        }
+        if (s->has_neumann) {
+            set_error("the learned preconditioner takes Dirichlet grids only");
+            return PPS_ERR_UNSUPPORTED;
+        }
+        if (coarsen < 0 || coarsen > 5 || !(gain > 0.0) || (flags & ~15) != 0 || (flags & 3) == 0) {
+            set_error("coarsen 0..5, gain > 0, flags must include PPS_LEARNED_INITIAL_GUESS or _PRECONDITIONER");
+            return PPS_ERR_INVALID_ARG;
+        }
+        const Geo& g = s->geo;
+        const int need = 4 << coarsen;
+        for (int d = 0; d < 3; d++)
+            if ((g.hi[d] - g.lo[d]) % need != 0) {
+                set_error("the unknown extents must be multiples of 4 * 2^coarsen for the U-Net");
+                return PPS_ERR_INVALID_ARG;
+            }
+        s->net = net;
+        s->net_coarsen = coarsen;
+        s->net_gain = (float)gain;
+        s->net_flags = flags;
+        for (int l = 0; l <= coarsen; l++) {
+            const unet::Dims d = dense_dims(s, l);
+            const size_t n = (size_t)d.D * d.H * d.W;
+            float *a = nullptr, *e = nullptr;
+            CK(cudaMalloc((void**)&a, sizeof(float) * n));
+            CK(cudaMalloc((void**)&e, sizeof(float) * n));
+            s->dn.push_back(a);
+            s->dn_e.push_back(e);
+        }
+        const size_t n0 = (size_t)s->n_unknowns;
+        CK(cudaMalloc((void**)&s->dn_r, sizeof(float) * n0));
+        CK(cudaMalloc((void**)&s->dn_z, sizeof(float) * n0));
         return PPS_OK;
     });
 }

@@ -71,6 +71,7 @@ struct Acts {
 
 struct pps_unet {
     int c1, c2, c3;
+    int linear = 0;        // 1: identity activations (a learned linear multigrid-like operator)
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<Layer> L;
@@ -157,20 +158,21 @@ void forward(pps_unet* u, const float* in, const float* rms_dev)
     const int c1 = u->c1, c2 = u->c2, c3 = u->c3;
     const long long v1 = (long long)A.s1.D * A.s1.H * A.s1.W;
     dense_to_act(v1, in, rms_dev, A.x0, 16, s);
-    conv(A.s1, A.x0, 16, 0, 16, Wb(u, 0), Bf(u, 0), A.e1a, c1, 0, c1, true, false, s);
-    conv(A.s1, A.e1a, c1, 0, c1, Wb(u, 1), Bf(u, 1), A.cat1, c2 + c1, c2, c1, true, false, s);
+    const bool R = !u->linear;
+    conv(A.s1, A.x0, 16, 0, 16, Wb(u, 0), Bf(u, 0), A.e1a, c1, 0, c1, R, false, s);
+    conv(A.s1, A.e1a, c1, 0, c1, Wb(u, 1), Bf(u, 1), A.cat1, c2 + c1, c2, c1, R, false, s);
     pool2(A.s2, A.cat1, c2 + c1, c2, A.p1, c1, s);
-    conv(A.s2, A.p1, c1, 0, c1, Wb(u, 2), Bf(u, 2), A.e2a, c2, 0, c2, true, false, s);
-    conv(A.s2, A.e2a, c2, 0, c2, Wb(u, 3), Bf(u, 3), A.cat2, c3 + c2, c3, c2, true, false, s);
+    conv(A.s2, A.p1, c1, 0, c1, Wb(u, 2), Bf(u, 2), A.e2a, c2, 0, c2, R, false, s);
+    conv(A.s2, A.e2a, c2, 0, c2, Wb(u, 3), Bf(u, 3), A.cat2, c3 + c2, c3, c2, R, false, s);
     pool2(A.s3, A.cat2, c3 + c2, c3, A.p2, c2, s);
-    conv(A.s3, A.p2, c2, 0, c2, Wb(u, 4), Bf(u, 4), A.e3a, c3, 0, c3, true, false, s);
-    conv(A.s3, A.e3a, c3, 0, c3, Wb(u, 5), Bf(u, 5), A.e3, c3, 0, c3, true, false, s);
+    conv(A.s3, A.p2, c2, 0, c2, Wb(u, 4), Bf(u, 4), A.e3a, c3, 0, c3, R, false, s);
+    conv(A.s3, A.e3a, c3, 0, c3, Wb(u, 5), Bf(u, 5), A.e3, c3, 0, c3, R, false, s);
     up2(A.s2, A.e3, c3, A.cat2, c3 + c2, 0, s);
-    conv(A.s2, A.cat2, c3 + c2, 0, c3 + c2, Wb(u, 6), Bf(u, 6), A.d2a, c2, 0, c2, true, false, s);
-    conv(A.s2, A.d2a, c2, 0, c2, Wb(u, 7), Bf(u, 7), A.d2, c2, 0, c2, true, false, s);
+    conv(A.s2, A.cat2, c3 + c2, 0, c3 + c2, Wb(u, 6), Bf(u, 6), A.d2a, c2, 0, c2, R, false, s);
+    conv(A.s2, A.d2a, c2, 0, c2, Wb(u, 7), Bf(u, 7), A.d2, c2, 0, c2, R, false, s);
     up2(A.s1, A.d2, c2, A.cat1, c2 + c1, 0, s);
-    conv(A.s1, A.cat1, c2 + c1, 0, c2 + c1, Wb(u, 8), Bf(u, 8), A.d1a, c1, 0, c1, true, false, s);
-    conv(A.s1, A.d1a, c1, 0, c1, Wb(u, 9), Bf(u, 9), A.d1, c1, 0, c1, true, false, s);
+    conv(A.s1, A.cat1, c2 + c1, 0, c2 + c1, Wb(u, 8), Bf(u, 8), A.d1a, c1, 0, c1, R, false, s);
+    conv(A.s1, A.d1a, c1, 0, c1, Wb(u, 9), Bf(u, 9), A.d1, c1, 0, c1, R, false, s);
     conv(A.s1, A.d1, c1, 0, c1, Wb(u, 10), Bf(u, 10), A.out, 16, 0, 16, false, true, s);
 }
 
@@ -198,32 +200,32 @@ void backward(pps_unet* u)
     UK(cudaMemsetAsync(u->G, 0, sizeof(float) * u->npad, s));
     // out <- d1
     layer_bwd(u, 10, A.s1, A.d1, c1, 0, A.g_out, 16, 0, A.g_d1, c1, 0);
-    relu_bwd(v1, A.g_d1, c1, 0, A.d1, c1, 0, c1, s);
+    if (!u->linear) relu_bwd(v1, A.g_d1, c1, 0, A.d1, c1, 0, c1, s);
     layer_bwd(u, 9, A.s1, A.d1a, c1, 0, A.g_d1, c1, 0, A.g_d1a, c1, 0);
-    relu_bwd(v1, A.g_d1a, c1, 0, A.d1a, c1, 0, c1, s);
+    if (!u->linear) relu_bwd(v1, A.g_d1a, c1, 0, A.d1a, c1, 0, c1, s);
     layer_bwd(u, 8, A.s1, A.cat1, c2 + c1, 0, A.g_d1a, c1, 0, A.g_cat1, c2 + c1, 0);
     // up slot of cat1 -> d2
     up2_bwd(A.s2, A.g_cat1, c2 + c1, 0, A.g_d2, c2, s);
-    relu_bwd(v2, A.g_d2, c2, 0, A.d2, c2, 0, c2, s);
+    if (!u->linear) relu_bwd(v2, A.g_d2, c2, 0, A.d2, c2, 0, c2, s);
     layer_bwd(u, 7, A.s2, A.d2a, c2, 0, A.g_d2, c2, 0, A.g_d2a, c2, 0);
-    relu_bwd(v2, A.g_d2a, c2, 0, A.d2a, c2, 0, c2, s);
+    if (!u->linear) relu_bwd(v2, A.g_d2a, c2, 0, A.d2a, c2, 0, c2, s);
     layer_bwd(u, 6, A.s2, A.cat2, c3 + c2, 0, A.g_d2a, c2, 0, A.g_cat2, c3 + c2, 0);
     // up slot of cat2 -> e3
     up2_bwd(A.s3, A.g_cat2, c3 + c2, 0, A.g_e3, c3, s);
-    relu_bwd(v3, A.g_e3, c3, 0, A.e3, c3, 0, c3, s);
+    if (!u->linear) relu_bwd(v3, A.g_e3, c3, 0, A.e3, c3, 0, c3, s);
     layer_bwd(u, 5, A.s3, A.e3a, c3, 0, A.g_e3, c3, 0, A.g_e3a, c3, 0);
-    relu_bwd(v3, A.g_e3a, c3, 0, A.e3a, c3, 0, c3, s);
+    if (!u->linear) relu_bwd(v3, A.g_e3a, c3, 0, A.e3a, c3, 0, c3, s);
     layer_bwd(u, 4, A.s3, A.p2, c2, 0, A.g_e3a, c3, 0, A.g_p2, c2, 0);
     // pooling -> skip slot of cat2 (adds to the skip gradient of conv6)
     pool2_bwd(A.s3, A.g_p2, A.g_cat2, c3 + c2, c3, c2, s);
-    relu_bwd(v2, A.g_cat2, c3 + c2, c3, A.cat2, c3 + c2, c3, c2, s);
+    if (!u->linear) relu_bwd(v2, A.g_cat2, c3 + c2, c3, A.cat2, c3 + c2, c3, c2, s);
     layer_bwd(u, 3, A.s2, A.e2a, c2, 0, A.g_cat2, c3 + c2, c3, A.g_e2a, c2, 0);
-    relu_bwd(v2, A.g_e2a, c2, 0, A.e2a, c2, 0, c2, s);
+    if (!u->linear) relu_bwd(v2, A.g_e2a, c2, 0, A.e2a, c2, 0, c2, s);
     layer_bwd(u, 2, A.s2, A.p1, c1, 0, A.g_e2a, c2, 0, A.g_p1, c1, 0);
     pool2_bwd(A.s2, A.g_p1, A.g_cat1, c2 + c1, c2, c1, s);
-    relu_bwd(v1, A.g_cat1, c2 + c1, c2, A.cat1, c2 + c1, c2, c1, s);
+    if (!u->linear) relu_bwd(v1, A.g_cat1, c2 + c1, c2, A.cat1, c2 + c1, c2, c1, s);
     layer_bwd(u, 1, A.s1, A.e1a, c1, 0, A.g_cat1, c2 + c1, c2, A.g_e1a, c1, 0);
-    relu_bwd(v1, A.g_e1a, c1, 0, A.e1a, c1, 0, c1, s);
+    if (!u->linear) relu_bwd(v1, A.g_e1a, c1, 0, A.e1a, c1, 0, c1, s);
     layer_bwd(u, 0, A.s1, A.x0, 16, 0, A.g_e1a, c1, 0, nullptr, 0, 0);
 }
 
@@ -358,6 +360,13 @@ pps_status pps_unet_destroy(pps_unet* u)
 
 int pps_unet_param_count(const pps_unet* u) { return u ? (int)u->nreal : -1; }
 
+pps_status pps_unet_set_activation(pps_unet* u, int linear)
+{
+    if (!u || (linear != 0 && linear != 1)) return PPS_ERR_INVALID_ARG;
+    u->linear = linear;
+    return PPS_OK;
+}
+
 // Flat real-parameter layout: per layer W[27][cin][cout] (tap = kz*9+ky*3+kx) then b[cout].
 static void pack(const pps_unet* u, const std::vector<float>& padded, float* real)
 {
@@ -465,7 +474,9 @@ pps_status pps_unet_train_step(pps_unet* u, int nx, int ny, int nz, const float*
         pps_status rc = loss_and_grads(u, nx, ny, nz, in_dev, target_dev, loss);
         if (rc != PPS_OK) return rc;
         u->step += 1;
-        adam((long long)u->npad, u->P, u->G, u->M, u->V, u->PB, lr, 0.9f, 0.999f, 1e-8f, u->step, u->stream);
+        rms((long long)u->npad, u->G, u->dtmp + 1, u->stream);   // global-norm clipping at 1
+        adam((long long)u->npad, u->P, u->G, u->M, u->V, u->PB, lr, 0.9f, 0.999f, 1e-8f, u->step, u->dtmp + 1, 1.0f,
+             u->stream);
         UK(cudaStreamSynchronize(u->stream));
         return PPS_OK;
     });

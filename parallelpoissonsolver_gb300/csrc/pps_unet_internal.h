@@ -4,6 +4,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "../../include/pps.h"
 #include "pps_internal.h"
 
 namespace pps {
@@ -29,7 +30,7 @@ void up2_bwd(const Dims& dcoarse, const bf16* gout, int ldo, int co0, bf16* gin,
 void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s);
 void mse(long long nv, const float* out, int ldo, const float* t, bf16* G, int ldg, double* loss, cudaStream_t s);
 void adam(long long n, float* p, const float* g, float* m, float* v, bf16* pb, float lr, float b1, float b2, float eps,
-          int step, cudaStream_t s);
+          int step, const float* g_rms, float max_norm, cudaStream_t s);
 void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s);
 void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s);
 void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s);
@@ -40,9 +41,17 @@ template <typename T>
 void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s);
 template <typename T>
 void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s);
+void dense_residual(const Dims& d, const float* r, const float* z, float ix, float iy, float iz, float* out,
+                    cudaStream_t s);
 // 2x full-weighting restriction and trilinear prolongation of dense unknown arrays.
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s);
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
 
 }  // namespace unet
 }  // namespace pps
+
+struct pps_unet;
+// Forward pass of the network on dense [nz][ny][nx] FP32 arrays on stream s:
+// out = gain * rms(in) * N(in / rms(in)).
+pps_status pps_internal_unet_apply(pps_unet* u, int nx, int ny, int nz, const float* in, float* out, float gain,
+                                   cudaStream_t s);

@@ -108,6 +108,7 @@ void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W
         if (relu) k_conv<true, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
         else k_conv<false, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
     }
+    launches_counter_add(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -201,6 +202,7 @@ void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const b
                 float* dW, cudaStream_t s)
 {
     k_conv_wgrad<<<(unsigned)(27 * d.D), 128, 0, s>>>(d, X, ldx, cx0, Cin, G, ldg, cg0, Cout, dW);
+    launches_counter_add(1);
 }
 
 // db[co] += sum_v G[v][co]
@@ -224,6 +226,7 @@ void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* d
     long long blocks = (nv * Cout + 255) / 256;
     if (blocks > 1024) blocks = 1024;
     k_bias_grad<<<(unsigned)blocks, 256, 0, s>>>(nv, G, ldg, cg0, Cout, db);
+    launches_counter_add(1);
 }
 
 // G[v][c] *= (Y[v][c] > 0): ReLU backward through the layer's own output.
@@ -248,6 +251,7 @@ static unsigned eblocks(long long n)
 void relu_bwd(long long nv, bf16* G, int ldg, int cg0, const bf16* Y, int ldy, int cy0, int C, cudaStream_t s)
 {
     k_relu_bwd<<<eblocks(nv * C), 256, 0, s>>>(nv, G, ldg, cg0, Y, ldy, cy0, C);
+    launches_counter_add(1);
 }
 
 // 2x average pooling: out (D/2,H/2,W/2) dense C channels <- in slot of ldi
@@ -271,6 +275,7 @@ __global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0
 void pool2(const Dims& dout, const bf16* in, int ldi, int ci0, bf16* out, int C, cudaStream_t s)
 {
     k_pool2<<<eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s>>>(dout, in, ldi, ci0, out, C);
+    launches_counter_add(1);
 }
 
 // pooling backward: gin slot (fine) += g_out/8 at each of the 8 children
@@ -291,6 +296,7 @@ __global__ void k_pool2_bwd(Dims dout, const bf16* __restrict__ gout, bf16* __re
 void pool2_bwd(const Dims& dout, const bf16* gout, bf16* gin, int ldi, int ci0, int C, cudaStream_t s)
 {
     k_pool2_bwd<<<eblocks((long long)dout.D * 8 * dout.H * dout.W * C), 256, 0, s>>>(dout, gout, gin, ldi, ci0, C);
+    launches_counter_add(1);
 }
 
 // nearest 2x upsampling: out slot (fine) <- in dense (coarse)
@@ -309,6 +315,7 @@ __global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __re
 void up2(const Dims& dfine, const bf16* in, int C, bf16* out, int ldo, int co0, cudaStream_t s)
 {
     k_up2<<<eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s>>>(dfine, in, C, out, ldo, co0);
+    launches_counter_add(1);
 }
 
 // upsampling backward: gin (coarse dense) = sum of the 8 children of gout's slot
@@ -333,6 +340,7 @@ __global__ void k_up2_bwd(Dims dcoarse, const bf16* __restrict__ gout, int ldo, 
 void up2_bwd(const Dims& dcoarse, const bf16* gout, int ldo, int co0, bf16* gin, int C, cudaStream_t s)
 {
     k_up2_bwd<<<eblocks((long long)dcoarse.D * dcoarse.H * dcoarse.W * C), 256, 0, s>>>(dcoarse, gout, ldo, co0, gin, C);
+    launches_counter_add(1);
 }
 
 // Wf[tap'][co][ci] = W[26-tap][ci][co]: the weights of the backward-data convolution.
@@ -348,6 +356,7 @@ __global__ void k_flip(const bf16* __restrict__ W, bf16* __restrict__ Wf, int Ci
 void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s)
 {
     k_flip<<<(27 * Cin * Cout + 255) / 256, 256, 0, s>>>(W, Wf, Cin, Cout);
+    launches_counter_add(1);
 }
 
 // MSE on channel 0 of an FP32 output slab [v][ld]: loss += sum (o - t)^2 / n,
@@ -371,15 +380,23 @@ __global__ void k_mse(long long nv, const float* __restrict__ out, int ldo, cons
 void mse(long long nv, const float* out, int ldo, const float* t, bf16* G, int ldg, double* loss, cudaStream_t s)
 {
     k_mse<<<eblocks(nv), 256, 0, s>>>(nv, out, ldo, t, G, ldg, loss);
+    launches_counter_add(1);
 }
 
-// Adam on FP32 master parameters; refreshes the BF16 copy of the weights.
+// Adam on FP32 master parameters; refreshes the BF16 copy of the weights.  The
+// gradient is first scaled by min(1, max_norm / ||g||) (global-norm clipping), with
+// ||g|| = (*g_rms) * sqrt(n) from k_rms.
 __global__ void k_adam(long long n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, bf16* __restrict__ pb, float lr, float b1, float b2, float eps, float c1,
-                       float c2)
+                       float c2, const float* g_rms, float max_norm)
 {
+    float clip = 1.0f;
+    if (g_rms) {
+        const float norm = *g_rms * sqrtf((float)n);
+        if (norm > max_norm && norm > 0.0f) clip = max_norm / norm;
+    }
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const float gq = g[q];
+        const float gq = g[q] * clip;
         const float mq = b1 * m[q] + (1.0f - b1) * gq;
         const float vq = b2 * v[q] + (1.0f - b2) * gq * gq;
         m[q] = mq;
@@ -392,10 +409,11 @@ __global__ void k_adam(long long n, float* __restrict__ p, const float* __restri
 }
 
 void adam(long long n, float* p, const float* g, float* m, float* v, bf16* pb, float lr, float b1, float b2, float eps,
-          int step, cudaStream_t s)
+          int step, const float* g_rms, float max_norm, cudaStream_t s)
 {
     const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-    k_adam<<<eblocks(n), 256, 0, s>>>(n, p, g, m, v, pb, lr, b1, b2, eps, c1, c2);
+    k_adam<<<eblocks(n), 256, 0, s>>>(n, p, g, m, v, pb, lr, b1, b2, eps, c1, c2, g_rms, max_norm);
+    launches_counter_add(1);
 }
 
 __global__ void k_f32_to_bf16(long long n, const float* __restrict__ a, bf16* __restrict__ b)
@@ -404,7 +422,11 @@ __global__ void k_f32_to_bf16(long long n, const float* __restrict__ a, bf16* __
         b[q] = __float2bfloat16(a[q]);
 }
 
-void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s) { k_f32_to_bf16<<<eblocks(n), 256, 0, s>>>(n, a, b); }
+void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s)
+{
+    k_f32_to_bf16<<<eblocks(n), 256, 0, s>>>(n, a, b);
+    launches_counter_add(1);
+}
 
 // Dense FP32 input [v] -> channel 0 of a BF16 activation [v][ld], scaled by 1/(*rms)
 // (rms == nullptr: scale 1); the other channels zero.
@@ -420,6 +442,7 @@ __global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const
 void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s)
 {
     k_dense_to_act<<<eblocks(nv), 256, 0, s>>>(nv, in, rms, act, ld);
+    launches_counter_add(1);
 }
 
 // channel 0 of an FP32 output slab -> dense FP32, times (*rms) * gain
@@ -434,6 +457,7 @@ __global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int 
 void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s)
 {
     k_out_to_dense<<<eblocks(nv), 256, 0, s>>>(nv, out, ld, rms, gain, dense);
+    launches_counter_add(1);
 }
 
 // rms of a dense FP32 array into *rms (single block, deterministic)
@@ -453,7 +477,11 @@ __global__ void k_rms(long long n, const float* __restrict__ a, float* rms)
     }
 }
 
-void rms(long long n, const float* a, float* out, cudaStream_t s) { k_rms<<<1, 1024, 0, s>>>(n, a, out); }
+void rms(long long n, const float* a, float* out, cudaStream_t s)
+{
+    k_rms<<<1, 1024, 0, s>>>(n, a, out);
+    launches_counter_add(1);
+}
 
 // ---------------------------------------------------------------------------
 // Grid transfers between a solver field (guard-padded layout, Dirichlet unknowns
@@ -491,6 +519,7 @@ void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
 {
     const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
     k_field_to_dense<T><<<eblocks(n), 256, 0, s>>>(g, f, dense);
+    launches_counter_add(1);
 }
 
 template <typename T>
@@ -498,12 +527,42 @@ void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add
 {
     const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
     k_dense_to_field<T><<<eblocks(n), 256, 0, s>>>(g, dense, f, scale, add);
+    launches_counter_add(1);
 }
 
 template void field_to_dense<float>(const Geo&, const float*, float*, cudaStream_t);
 template void field_to_dense<double>(const Geo&, const double*, float*, cudaStream_t);
 template void dense_to_field<float>(const Geo&, const float*, float*, float, int, cudaStream_t);
 template void dense_to_field<double>(const Geo&, const float*, double*, float, int, cudaStream_t);
+
+// out = r - A z on dense unknown arrays of a Dirichlet grid (zero beyond the array):
+// the residual the network's coarse correction works on.
+__global__ void k_dense_residual(Dims d, const float* __restrict__ r, const float* __restrict__ z, float ix, float iy,
+                                 float iz, float* __restrict__ out)
+{
+    const long long n = (long long)d.D * d.H * d.W;
+    const float cc = -2.0f * (ix + iy + iz);
+    const long long sy = d.W, sz = (long long)d.W * d.H;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % d.W), y = (int)((q / d.W) % d.H), zz = (int)(q / sz);
+        const float c = z[q];
+        const float xm = x > 0 ? z[q - 1] : 0.0f, xp = x + 1 < d.W ? z[q + 1] : 0.0f;
+        const float ym = y > 0 ? z[q - sy] : 0.0f, yp = y + 1 < d.H ? z[q + sy] : 0.0f;
+        const float zm = zz > 0 ? z[q - sz] : 0.0f, zp = zz + 1 < d.D ? z[q + sz] : 0.0f;
+        float a = cc * c;
+        a = fmaf(ix, xm + xp, a);
+        a = fmaf(iy, ym + yp, a);
+        a = fmaf(iz, zm + zp, a);
+        out[q] = r[q] - a;
+    }
+}
+
+void dense_residual(const Dims& d, const float* r, const float* z, float ix, float iy, float iz, float* out,
+                    cudaStream_t s)
+{
+    k_dense_residual<<<eblocks((long long)d.D * d.H * d.W), 256, 0, s>>>(d, r, z, ix, iy, iz, out);
+    launches_counter_add(1);
+}
 
 // Full-weighting restriction of dense unknown arrays, fine (2m) -> coarse (m) per
 // axis: coarse unknown I sits on fine unknown 2I+1 (0-based), weights 1/4,1/2,1/4
@@ -536,6 +595,7 @@ __global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __res
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 {
     k_restrict<<<eblocks((long long)dc.D * dc.H * dc.W), 256, 0, s>>>(dc, fine, coarse);
+    launches_counter_add(1);
 }
 
 // Trilinear prolongation, coarse (m) -> fine (2m): fine unknown i takes coarse
@@ -581,6 +641,7 @@ __global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __re
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
     k_prolong<<<eblocks((long long)dc.D * 8 * dc.H * dc.W), 256, 0, s>>>(dc, coarse, fine);
+    launches_counter_add(1);
 }
 
 }  // namespace unet
