@@ -1,15 +1,19 @@
 """One capped solve of the benchmark workload, sized for profiling.
 
     python -m parallelpoissonsolver_gb300.profile_case --size 320 --form mixed --maxit 2
+    python -m parallelpoissonsolver_gb300.profile_case --save-net net.npz          # train the U-Net, save
+    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --maxit 8
 
 Runs `--repeat` solves of the k^-2 random-field workload at `--size`^3 unknowns with
 the iteration cap `--maxit`, so that an ncu capture sees a handful of launches of
 every kernel of the loop on fields larger than L2, and exits 0 whether or not the
-cap stops the solve.
+cap stops the solve.  With --learned, the solver is flexible CG with the saved U-Net
+as its coarse-grid correction (as in the benchmark's headline form).
 """
 from __future__ import annotations
 
 import argparse
+import math
 
 import parallelpoissonsolver_gb300 as pps
 from parallelpoissonsolver_gb300 import workloads
@@ -23,11 +27,36 @@ def main():
     ap.add_argument("--degree", type=int, default=11)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--save-net", default=None, help="train the 32^3 linear U-Net and save it here, then exit")
+    ap.add_argument("--learned", default=None, help="saved U-Net to use as the coarse-grid correction")
     a = ap.parse_args()
+    if a.save_net:
+        from parallelpoissonsolver_gb300 import learned
+        train = learned.make_dataset(32, range(10000, 10256))
+        scale = learned.fit_scale(train)
+        net = pps.UNet((16, 32, 64), seed=1, linear=True)
+        learned.train(net, train, scale, 4000, lr=1e-3)
+        net.save(a.save_net)
+        import numpy as np
+        with np.load(a.save_net) as d:
+            np.savez(a.save_net, scale=np.array(scale), **{k: d[k] for k in d.files})
+        print(f"saved {a.save_net}: scale {scale:.6g}")
+        return
     grid = pps.BlockGrid.cube(a.size)
     b = workloads.random_field(a.size, seed=2)
-    s = pps.BiCGSTAB(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
-                     form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)
+    if a.learned:
+        import numpy as np
+        net = pps.UNet.load_file(a.learned)
+        scale = float(np.load(a.learned)["scale"])
+        k = int(round(math.log2(a.size / 32)))
+        gain = scale * ((2 ** k / (a.size + 1)) / (1.0 / 33)) ** 2
+        s = pps.FlexibleCG(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
+                           form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=False)
+        s.set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER |
+                      pps.LEARNED_POST_SMOOTH | pps.LEARNED_NO_FALLBACK)
+    else:
+        s = pps.BiCGSTAB(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
+                         form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)
     for _ in range(a.repeat):
         x = grid.new_field()
         st = s(x, b.copy(), raise_on_error=True)
