@@ -164,7 +164,9 @@ pps_status pps_write_residual_history(const pps_solver* s, const char* path);
  * out = A u at the unknowns (MatrixFreeOperatorA::operator(), FP64). */
 pps_status pps_apply_operator(pps_solver* s, const double* u, double* out);
 /* X = M^{-1} B: one preconditioner application (ChebyshevIteration::operator()
- * in preconditioner mode, chebyshevIteration.hpp:48-140), in the solver's form. */
+ * in preconditioner mode, chebyshevIteration.hpp:48-140), in the solver's form;
+ * with a network attached by pps_set_learned as preconditioner, the learned cycle
+ * that flexible CG applies. */
 pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
 
 /* Tile shapes of the z-marching kernels (fast forms).  A tile is (32*cx) x ty
@@ -248,7 +250,7 @@ pps_status pps_unet_gradients(pps_unet* net, int nx, int ny, int nz, const float
 pps_status pps_unet_train_step(pps_unet* net, int nx, int ny, int nz, const float* in_dev, const float* target_dev,
                                float lr, double* loss);
 /* Attaches a trained U-Net to a solver (FP64 or MIXED form, Dirichlet grid whose
- * unknown extents are multiples of 4*2^coarsen).  flags:
+ * unknown extents are multiples of 4*2^coarsen, at most 65535 along y and z).  flags:
  *   PPS_LEARNED_INITIAL_GUESS   x += gain * P^k N(R^k b) before the solve;
  *   PPS_LEARNED_PRECONDITIONER  inside flexible CG, z = Cheb(r) followed by
  *                               z += gain * P^k N(R^k (r - A z)); the solve falls back
@@ -266,7 +268,8 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
 
 /* 2x grid transfers of dense unknown arrays (coarse extents nx, ny, nz; the fine
  * grid has twice as many unknowns per axis, coarse unknown i on fine unknown 2i+1):
- * full-weighting restriction and trilinear prolongation (its transpose / 8). */
+ * full-weighting restriction and trilinear prolongation (its transpose / 8).
+ * ny and nz are at most 32767. */
 pps_status pps_restrict2(int nx, int ny, int nz, const float* fine_dev, float* coarse_dev);
 pps_status pps_prolong2(int nx, int ny, int nz, const float* coarse_dev, float* fine_dev);
 

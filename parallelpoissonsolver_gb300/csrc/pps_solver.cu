@@ -138,10 +138,8 @@ struct pps_solver {
     float net_gain = 1.0f;
     int net_flags = 0;
     bool net_active = false;          // preconditioner in use in the current solve (fallback clears it)
-    std::vector<float*> dn;           // dense levels: dn[0] fine residual ... dn[k] coarsest; dn_e the same sizes
+    std::vector<float*> dn;           // dense levels 0..k of the network correction (residual, correction); level 0 only for k = 0
     std::vector<float*> dn_e;
-    float* dn_r = nullptr;
-    float* dn_z = nullptr;
     int learned_apps = 0;
     int fallback_iter = -1;
 
@@ -242,8 +240,6 @@ void free_all(pps_solver* s)
     if (s->h_dot) cudaFreeHost(s->h_dot);
     for (float* q : s->dn) cudaFree(q);
     for (float* q : s->dn_e) cudaFree(q);
-    if (s->dn_r) cudaFree(s->dn_r);
-    if (s->dn_z) cudaFree(s->dn_z);
     for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -537,55 +533,69 @@ unet::Dims dense_dims(const pps_solver* s, int level)
     return unet::Dims{(g.hi[2] - g.lo[2]) / f, (g.hi[1] - g.lo[1]) / f, (g.hi[0] - g.lo[0]) / f};
 }
 
-// gain * P^k N(R^k res) where res = dn[0] (dense fine); result in dn_e[0].
-void learned_coarse_correction(pps_solver* s)
+// X += gain P^k N(R^k (r - A z)) at the unknowns (R^k r when z is null).  For
+// coarsen k >= 1 the first restriction reads the solver fields and the last
+// prolongation adds into X, so no fine-grid dense array exists; levels 1..k are
+// dense arrays dn[l] (restricted residual) and dn_e[l] (correction).
+template <typename T>
+void learned_coarse_correction(pps_solver* s, const T* r, const T* z, T* X)
 {
+    const Geo& g = s->geo;
     cudaStream_t st = s->stream;
     const int k = s->net_coarsen;
-    for (int l = 0; l < k; l++) unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
+    if (k == 0) {
+        if (z) unet::field_residual_dense<T>(g, r, z, s->dn[0], st);
+        else unet::field_to_dense<T>(g, r, s->dn[0], st);
+    } else {
+        unet::field_residual_restrict<T>(g, r, z, dense_dims(s, 1), s->dn[1], st);
+        for (int l = 1; l < k; l++) unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
+    }
     const unet::Dims dc = dense_dims(s, k);
     if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, s->dn[(size_t)k], s->dn_e[(size_t)k], s->net_gain, st) != PPS_OK)
         throw CudaFail{cudaErrorUnknown};
-    for (int l = k; l > 0; l--) unet::prolong2(dense_dims(s, l), s->dn_e[(size_t)l], s->dn_e[(size_t)l - 1], st);
+    if (k == 0) {
+        unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
+    } else {
+        for (int l = k; l > 1; l--) unet::prolong2(dense_dims(s, l), s->dn_e[(size_t)l], s->dn_e[(size_t)l - 1], st);
+        unet::prolong_add_field<T>(g, dense_dims(s, 1), s->dn_e[1], X, st);
+    }
     s->learned_apps++;
 }
 
 // Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity),
-// followed, while the learned preconditioner is active, by the network's coarse
-// correction of the remaining residual: z = Cheb(r); z += gain P^k N(R^k (r - A z)).
+// followed, while the learned preconditioner is active, by a two-grid cycle whose
+// coarse solver is the network:
+//   z = Cheb(r);  z += gain P^k N(R^k (r - A z));  [z += Cheb(r - A z)]
 template <typename T>
 void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
 {
     fast_precond<T>(s, F, B, X, L);
     if (!(s->net && s->net_active)) return;
-    const Geo& g = s->geo;
-    cudaStream_t st = s->stream;
-    unet::field_to_dense<T>(g, B, s->dn_r, st);
-    unet::field_to_dense<T>(g, X, s->dn_z, st);
-    unet::dense_residual(dense_dims(s, 0), s->dn_r, s->dn_z, (float)(1.0 / (g.ds[0] * g.ds[0])),
-                         (float)(1.0 / (g.ds[1] * g.ds[1])), (float)(1.0 / (g.ds[2] * g.ds[2])), s->dn[0], st);
-    learned_coarse_correction(s);
-    unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
+    learned_coarse_correction<T>(s, B, X, X);
     if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
-        // post-smoothing: z += Cheb(r - A z), through the fields FCG leaves free (r0, Mp)
-        unet::field_to_dense<T>(g, X, s->dn_z, st);
-        unet::dense_residual(dense_dims(s, 0), s->dn_r, s->dn_z, (float)(1.0 / (g.ds[0] * g.ds[0])),
-                             (float)(1.0 / (g.ds[1] * g.ds[1])), (float)(1.0 / (g.ds[2] * g.ds[2])), s->dn[0], st);
-        unet::dense_to_field<T>(g, s->dn[0], F.r0, 1.0f, 0, st);
+        // post-smoothing through the fields flexible CG leaves free (r0, Mp)
+        const Geo& g = s->geo;
+        unet::field_residual<T>(g, B, X, F.r0, s->stream);
         fast_precond<T>(s, F, F.r0, F.Mp, L);
-        unet::field_to_dense<T>(g, F.Mp, s->dn_z, st);
-        unet::dense_to_field<T>(g, s->dn_z, X, 1.0f, 1, st);
+        unet::field_axpy<T>(g, X, F.Mp, s->stream);
     }
 }
 
-// Learned initial guess: x += gain P^k N(R^k b) at the unknowns.
+// One application of the preconditioner the flexible-CG iterations use (with the
+// learned cycle when a network is attached as preconditioner).
 template <typename T>
+void precond_once(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+{
+    const bool keep = s->net_active;
+    s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER);
+    precond_any<T>(s, F, B, X, L);
+    s->net_active = keep;
+}
+
+// Learned initial guess: x += gain P^k N(R^k b) at the unknowns.
 void learned_initial_guess(pps_solver* s, double* x, const double* b)
 {
-    const Geo& g = s->geo;
-    unet::field_to_dense<double>(g, b, s->dn[0], s->stream);
-    learned_coarse_correction(s);
-    unet::dense_to_field<double>(g, s->dn_e[0], x, 1.0f, 1, s->stream);
+    learned_coarse_correction<double>(s, b, nullptr, x);
 }
 
 // One BiCGSTAB iteration (BiCGSTAB.hpp:133-272) on the fast kernels; xacc is the
@@ -779,7 +789,7 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER) && s->cfg.krylov == PPS_KRYLOV_FCG;
     s->learned_apps = 0;
     s->fallback_iter = -1;
-    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess<double>(s, x, b);
+    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess(s, x, b);
     const Coef a = op_coef(g);
     state_init(s->d_st, s->d_hist, s->cfg.maxit, s->cfg.tol * normb, 0.0, 0, 0, 1.0 / normb, s->hist_cap, st);
     fast_residual<double>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st);
@@ -823,7 +833,7 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
     s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER) && s->cfg.krylov == PPS_KRYLOV_FCG;
     s->learned_apps = 0;
     s->fallback_iter = -1;
-    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess<float>(s, x, b);
+    if (s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) learned_initial_guess(s, x, b);
     const Coef a = op_coef(g);
     const double tol_abs = s->cfg.tol * normb;
     s->history.clear();
@@ -1451,7 +1461,7 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         if (s->cfg.form == PPS_FORM_FP64) {
             CK(cudaMemcpyAsync(s->f64.r, B, fb, cudaMemcpyHostToDevice, s->stream));
             CK(cudaMemcpyAsync(s->f64.z, X, fb, cudaMemcpyHostToDevice, s->stream));
-            fast_precond<double>(s, s->f64, s->f64.r, s->f64.z, L);
+            precond_once<double>(s, s->f64, s->f64.r, s->f64.z, L);
             CK(cudaMemcpyAsync(X, s->f64.z, fb, cudaMemcpyDeviceToHost, s->stream));
             CK(cudaStreamSynchronize(s->stream));
             return PPS_OK;
@@ -1463,7 +1473,7 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         }
         CK(cudaMemcpyAsync(s->f32.r, hb.data(), sizeof(float) * (size_t)g.ntot, cudaMemcpyHostToDevice, s->stream));
         CK(cudaMemcpyAsync(s->f32.z, hx.data(), sizeof(float) * (size_t)g.ntot, cudaMemcpyHostToDevice, s->stream));
-        fast_precond<float>(s, s->f32, s->f32.r, s->f32.z, L);
+        precond_once<float>(s, s->f32, s->f32.r, s->f32.z, L);
         CK(cudaMemcpyAsync(hx.data(), s->f32.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         for (long long q = 0; q < g.ntot; q++) X[q] = (double)hx[(size_t)q];
@@ -1499,9 +1509,6 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
         for (float* q : s->dn_e) cudaFree(q);
         s->dn.clear();
         s->dn_e.clear();
-        if (s->dn_r) cudaFree(s->dn_r);
-        if (s->dn_z) cudaFree(s->dn_z);
-        s->dn_r = s->dn_z = nullptr;
         s->net = nullptr;
         if (!net) return PPS_OK;   // detach
         if (s->cfg.form == PPS_FORM_PARITY_FP64) {
@@ -1523,22 +1530,26 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
                 set_error("the unknown extents must be multiples of 4 * 2^coarsen for the U-Net");
                 return PPS_ERR_INVALID_ARG;
             }
+        if (g.hi[1] - g.lo[1] > 65535 || g.hi[2] - g.lo[2] > 65535) {
+            set_error("the learned preconditioner takes at most 65535 unknowns along y and z");
+            return PPS_ERR_INVALID_ARG;
+        }
         s->net = net;
         s->net_coarsen = coarsen;
         s->net_gain = (float)gain;
         s->net_flags = flags;
+        // dense levels 1..coarsen (level 0 too when the network runs on the fine grid)
         for (int l = 0; l <= coarsen; l++) {
-            const unet::Dims d = dense_dims(s, l);
-            const size_t n = (size_t)d.D * d.H * d.W;
             float *a = nullptr, *e = nullptr;
-            CK(cudaMalloc((void**)&a, sizeof(float) * n));
-            CK(cudaMalloc((void**)&e, sizeof(float) * n));
+            if (l > 0 || coarsen == 0) {
+                const unet::Dims d = dense_dims(s, l);
+                const size_t n = (size_t)d.D * d.H * d.W;
+                CK(cudaMalloc((void**)&a, sizeof(float) * n));
+                CK(cudaMalloc((void**)&e, sizeof(float) * n));
+            }
             s->dn.push_back(a);
             s->dn_e.push_back(e);
         }
-        const size_t n0 = (size_t)s->n_unknowns;
-        CK(cudaMalloc((void**)&s->dn_r, sizeof(float) * n0));
-        CK(cudaMalloc((void**)&s->dn_z, sizeof(float) * n0));
         return PPS_OK;
     });
 }

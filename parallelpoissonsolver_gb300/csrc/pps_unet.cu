@@ -484,14 +484,14 @@ pps_status pps_unet_train_step(pps_unet* u, int nx, int ny, int nz, const float*
 
 pps_status pps_restrict2(int nx, int ny, int nz, const float* fine_dev, float* coarse_dev)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || !fine_dev || !coarse_dev) return PPS_ERR_INVALID_ARG;
+    if (nx < 1 || ny < 1 || nz < 1 || ny > 32767 || nz > 32767 || !fine_dev || !coarse_dev) return PPS_ERR_INVALID_ARG;
     restrict2(Dims{nz, ny, nx}, fine_dev, coarse_dev, 0);
     return cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess ? PPS_OK : PPS_ERR_CUDA;
 }
 
 pps_status pps_prolong2(int nx, int ny, int nz, const float* coarse_dev, float* fine_dev)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || !fine_dev || !coarse_dev) return PPS_ERR_INVALID_ARG;
+    if (nx < 1 || ny < 1 || nz < 1 || ny > 32767 || nz > 32767 || !fine_dev || !coarse_dev) return PPS_ERR_INVALID_ARG;
     prolong2(Dims{nz, ny, nx}, coarse_dev, fine_dev, 0);
     return cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess ? PPS_OK : PPS_ERR_CUDA;
 }

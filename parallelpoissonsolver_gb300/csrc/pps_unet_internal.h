@@ -41,8 +41,20 @@ template <typename T>
 void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s);
 template <typename T>
 void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s);
-void dense_residual(const Dims& d, const float* r, const float* z, float ix, float iy, float iz, float* out,
-                    cudaStream_t s);
+// Transfers fused with the solver fields (Dirichlet unknowns of Geo g, guard cells
+// zero): dense = r - A z; out = r - A z; x += y; coarse = R(r - A z) (R r when z is
+// null) with the full weighting of restrict2; f += the trilinear prolongation of
+// `coarse` (prolong2's weights).
+template <typename T>
+void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s);
+template <typename T>
+void field_residual(const Geo& g, const T* r, const T* z, T* out, cudaStream_t s);
+template <typename T>
+void field_axpy(const Geo& g, T* x, const T* y, cudaStream_t s);
+template <typename T>
+void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& dc, float* coarse, cudaStream_t s);
+template <typename T>
+void prolong_add_field(const Geo& g, const Dims& dc, const float* coarse, T* f, cudaStream_t s);
 // 2x full-weighting restriction and trilinear prolongation of dense unknown arrays.
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s);
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);

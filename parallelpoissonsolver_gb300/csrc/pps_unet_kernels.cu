@@ -488,45 +488,52 @@ void rms(long long n, const float* a, float* out, cudaStream_t s)
 // 2..n-1 per axis) and dense [z][y][x] arrays of its unknowns.
 // ---------------------------------------------------------------------------
 
+// The transfer kernels below run one thread per unknown (or per coarse column)
+// on a 3-D grid: x along threadIdx/blockIdx.x, y on blockIdx.y, z on blockIdx.z,
+// so no thread divides to find its indices.  Extents along y and z are at most
+// 65535 (checked when the learned preconditioner is attached).
+static dim3 field_grid(int ux, int uy, int uz, int bx) { return dim3((unsigned)((ux + bx - 1) / bx), (unsigned)uy, (unsigned)uz); }
+
+__device__ __forceinline__ long long field_at(const Geo& g, int i, int j, int k)
+{
+    return (g.lo[0] + i) + g.sj * (long long)(g.lo[1] + j) + g.sk * (long long)(g.lo[2] + k);
+}
+
 // dense = field unknowns (type T -> float)
 template <typename T>
 __global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restrict__ dense)
 {
-    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
-    const long long n = (long long)ux * uy * uz;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(q % ux), j = (int)((q / ux) % uy), k = (int)(q / ((long long)ux * uy));
-        dense[q] = (float)f[(g.lo[0] + i) + g.sj * (g.lo[1] + j) + g.sk * (g.lo[2] + k)];
-    }
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= ux) return;
+    dense[((long long)k * uy + j) * ux + i] = (float)f[field_at(g, i, j, k)];
 }
 
 // field unknowns (+)= scale * dense
 template <typename T>
 __global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __restrict__ f, float scale, int add)
 {
-    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
-    const long long n = (long long)ux * uy * uz;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(q % ux), j = (int)((q / ux) % uy), k = (int)(q / ((long long)ux * uy));
-        const long long c = (g.lo[0] + i) + g.sj * (g.lo[1] + j) + g.sk * (g.lo[2] + k);
-        const T v = (T)(scale * dense[q]);
-        f[c] = add ? f[c] + v : v;
-    }
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= ux) return;
+    const long long c = field_at(g, i, j, k);
+    const T v = (T)(scale * dense[((long long)k * uy + j) * ux + i]);
+    f[c] = add ? f[c] + v : v;
 }
 
 template <typename T>
 void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
 {
-    const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
-    k_field_to_dense<T><<<eblocks(n), 256, 0, s>>>(g, f, dense);
+    k_field_to_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+        g, f, dense);
     launches_counter_add(1);
 }
 
 template <typename T>
 void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s)
 {
-    const long long n = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
-    k_dense_to_field<T><<<eblocks(n), 256, 0, s>>>(g, dense, f, scale, add);
+    k_dense_to_field<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+        g, dense, f, scale, add);
     launches_counter_add(1);
 }
 
@@ -535,66 +542,286 @@ template void field_to_dense<double>(const Geo&, const double*, float*, cudaStre
 template void dense_to_field<float>(const Geo&, const float*, float*, float, int, cudaStream_t);
 template void dense_to_field<double>(const Geo&, const float*, double*, float, int, cudaStream_t);
 
-// out = r - A z on dense unknown arrays of a Dirichlet grid (zero beyond the array):
-// the residual the network's coarse correction works on.
-__global__ void k_dense_residual(Dims d, const float* __restrict__ r, const float* __restrict__ z, float ix, float iy,
-                                 float iz, float* __restrict__ out)
+// ---------------------------------------------------------------------------
+// Transfers fused with the solver fields.  The fast fields keep their guard
+// cells (the Dirichlet boundary nodes) at zero, so the 7-point stencil reads them
+// unconditionally.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct StencilW {
+    T ix, iy, iz, diag;   // 1/h^2 per axis and the centre weight -2 (ix + iy + iz)
+};
+template <typename T>
+static StencilW<T> stencil_w(const Geo& g)
 {
-    const long long n = (long long)d.D * d.H * d.W;
-    const float cc = -2.0f * (ix + iy + iz);
-    const long long sy = d.W, sz = (long long)d.W * d.H;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(q % d.W), y = (int)((q / d.W) % d.H), zz = (int)(q / sz);
-        const float c = z[q];
-        const float xm = x > 0 ? z[q - 1] : 0.0f, xp = x + 1 < d.W ? z[q + 1] : 0.0f;
-        const float ym = y > 0 ? z[q - sy] : 0.0f, yp = y + 1 < d.H ? z[q + sy] : 0.0f;
-        const float zm = zz > 0 ? z[q - sz] : 0.0f, zp = zz + 1 < d.D ? z[q + sz] : 0.0f;
-        float a = cc * c;
-        a = fmaf(ix, xm + xp, a);
-        a = fmaf(iy, ym + yp, a);
-        a = fmaf(iz, zm + zp, a);
-        out[q] = r[q] - a;
+    StencilW<T> w;
+    const double ix = 1.0 / (g.ds[0] * g.ds[0]), iy = 1.0 / (g.ds[1] * g.ds[1]), iz = 1.0 / (g.ds[2] * g.ds[2]);
+    w.ix = (T)ix;
+    w.iy = (T)iy;
+    w.iz = (T)iz;
+    w.diag = (T)(-2.0 * (ix + iy + iz));
+    return w;
+}
+
+template <typename T>
+__device__ __forceinline__ T residual_at(const Geo& g, const T* __restrict__ r, const T* __restrict__ z, long long c,
+                                         const StencilW<T>& w)
+{
+    T a = w.diag * z[c];
+    a += w.ix * (z[c - 1] + z[c + 1]);
+    a += w.iy * (z[c - g.sj] + z[c + g.sj]);
+    a += w.iz * (z[c - g.sk] + z[c + g.sk]);
+    return r[c] - a;
+}
+
+// dense = r - A z at the unknowns.
+template <typename T>
+__global__ void k_field_residual_dense(Geo g, const T* __restrict__ r, const T* __restrict__ z, StencilW<T> w,
+                                       float* __restrict__ dense)
+{
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= ux) return;
+    dense[((long long)k * uy + j) * ux + i] = (float)residual_at<T>(g, r, z, field_at(g, i, j, k), w);
+}
+
+// out = r - A z at the unknowns.
+template <typename T>
+__global__ void k_field_residual(Geo g, const T* __restrict__ r, const T* __restrict__ z, StencilW<T> w,
+                                 T* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.hi[0] - g.lo[0]) return;
+    const long long c = field_at(g, i, blockIdx.y, blockIdx.z);
+    out[c] = residual_at<T>(g, r, z, c, w);
+}
+
+// x += y at the unknowns.
+template <typename T>
+__global__ void k_field_axpy(Geo g, T* __restrict__ x, const T* __restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.hi[0] - g.lo[0]) return;
+    const long long c = field_at(g, i, blockIdx.y, blockIdx.z);
+    x[c] += y[c];
+}
+
+// Full-weighting restriction (the weights of k_restrict: 1/4, 1/2, 1/4 per axis
+// over fine 2c, 2c+1, 2c+2) of the residual r - A z of the solver fields, straight
+// into the coarse dense array; with HAS_Z false the restricted field is r itself.
+// One thread per coarse (x, y) column walks `zc` coarse planes, keeping the three z
+// planes of its 3 x 3 fine points in registers: per pair of fine planes it loads
+// 9 z, 9 r and the 12 in-plane neighbours, and each fine value is read from DRAM
+// once (the fine-grid residual is never stored).
+template <typename T, bool HAS_Z>
+__global__ void __launch_bounds__(128) k_field_residual_restrict(Geo g, const T* __restrict__ r,
+                                                                 const T* __restrict__ z, StencilW<T> w, Dims dc,
+                                                                 int zc, float* __restrict__ coarse)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dc.W || y >= dc.H) return;
+    const int z0 = blockIdx.z * zc, z1 = min(dc.D, z0 + zc);
+    if (z0 >= z1) return;
+    const int uz = 2 * dc.D;
+    // the third fine column / row lies on the boundary node for the last coarse column / row
+    const bool on_x2 = 2 * x + 2 < 2 * dc.W, on_y2 = 2 * y + 2 < 2 * dc.H;
+    const long long sj = g.sj;
+    const T wt[3] = {(T)0.25, (T)0.5, (T)0.25};
+    T zm[3][3], zcn[3][3], zp[3][3];   // z at fine planes f-1, f, f+1 of the 3 x 3 fine points
+
+    auto load_plane = [&](int k, T (&pl)[3][3]) {
+        const long long c = field_at(g, 2 * x, 2 * y, k);
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) pl[b][a] = z[c + b * sj + a];
+    };
+    // weighted 3 x 3 sum of the residual on fine plane f (zcn holds plane f)
+    auto plane_sum = [&](int f) -> T {
+        const long long c = field_at(g, 2 * x, 2 * y, f);
+        T acc = (T)0;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            if (b == 2 && !on_y2) continue;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (a == 2 && !on_x2) continue;
+                const long long o = c + b * sj + a;
+                T res = r[o];
+                if (HAS_Z) {
+                    const T left = a > 0 ? zcn[b][a - 1] : z[o - 1];
+                    const T right = a < 2 ? zcn[b][a + 1] : z[o + 1];
+                    const T down = b > 0 ? zcn[b - 1][a] : z[o - sj];
+                    const T up = b < 2 ? zcn[b + 1][a] : z[o + sj];
+                    T av = w.diag * zcn[b][a];
+                    av += w.ix * (left + right);
+                    av += w.iy * (down + up);
+                    av += w.iz * (zm[b][a] + zp[b][a]);
+                    res -= av;
+                }
+                acc += wt[b] * wt[a] * res;
+            }
+        }
+        return acc;
+    };
+    auto shift = [&](int knext) {
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                zm[b][a] = zcn[b][a];
+                zcn[b][a] = zp[b][a];
+            }
+        if (HAS_Z) load_plane(knext, zp);
+    };
+
+    const int f0 = 2 * z0;   // < uz
+    if (HAS_Z) {
+        load_plane(f0 - 1, zm);
+        load_plane(f0, zcn);
+        load_plane(f0 + 1, zp);
+    }
+    T prev = plane_sum(f0);
+    long long out = ((long long)z0 * dc.H + y) * dc.W + x;
+    const long long cstride = (long long)dc.H * dc.W;
+    for (int cz = z0; cz < z1; cz++, out += cstride) {
+        shift(2 * cz + 2);                     // now at plane 2cz+1; plane 2cz+2 <= uz is in the field
+        const T mid = plane_sum(2 * cz + 1);
+        T next = (T)0;
+        if (2 * cz + 2 < uz) {
+            shift(2 * cz + 3);                 // 2cz+3 <= uz
+            next = plane_sum(2 * cz + 2);
+        }
+        coarse[out] = (float)(wt[0] * prev + wt[1] * mid + wt[2] * next);
+        prev = next;
     }
 }
 
-void dense_residual(const Dims& d, const float* r, const float* z, float ix, float iy, float iz, float* out,
-                    cudaStream_t s)
+// field unknowns += trilinear prolongation of a coarse dense array with half the
+// unknowns per axis (the weights of k_prolong: fine i takes coarse (i-1)/2 when i
+// is odd, the mean of coarse i/2-1 and i/2 otherwise, zero beyond the grid).
+template <typename T>
+__global__ void k_prolong_add_field(Geo g, Dims dc, const float* __restrict__ coarse, T* __restrict__ f)
 {
-    k_dense_residual<<<eblocks((long long)d.D * d.H * d.W), 256, 0, s>>>(d, r, z, ix, iy, iz, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= g.hi[0] - g.lo[0]) return;
+    const int idx[3] = {i, j, k};
+    const int ext[3] = {dc.W, dc.H, dc.D};
+    int i0[3], i1[3];
+    float w0[3], w1[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (idx[d] & 1) {
+            i0[d] = i1[d] = idx[d] >> 1;
+            w0[d] = 1.0f;
+            w1[d] = 0.0f;
+        } else {
+            i0[d] = (idx[d] >> 1) - 1;
+            i1[d] = idx[d] >> 1;
+            w0[d] = i0[d] >= 0 ? 0.5f : 0.0f;
+            w1[d] = i1[d] < ext[d] ? 0.5f : 0.0f;
+        }
+        if (w0[d] == 0.0f) i0[d] = i1[d];
+        if (w1[d] == 0.0f) i1[d] = i0[d];
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+                const float wv = (a ? w1[2] : w0[2]) * (b ? w1[1] : w0[1]) * (cc ? w1[0] : w0[0]);
+                if (wv == 0.0f) continue;
+                const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = cc ? i1[0] : i0[0];
+                s += wv * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
+            }
+    const long long c = field_at(g, i, j, k);
+    f[c] += (T)s;
+}
+
+template <typename T>
+void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s)
+{
+    k_field_residual_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+        g, r, z, stencil_w<T>(g), dense);
     launches_counter_add(1);
 }
+template <typename T>
+void field_residual(const Geo& g, const T* r, const T* z, T* out, cudaStream_t s)
+{
+    k_field_residual<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+        g, r, z, stencil_w<T>(g), out);
+    launches_counter_add(1);
+}
+template <typename T>
+void field_axpy(const Geo& g, T* x, const T* y, cudaStream_t s)
+{
+    k_field_axpy<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(g, x, y);
+    launches_counter_add(1);
+}
+template <typename T>
+void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& dc, float* coarse, cudaStream_t s)
+{
+    const int zc = 8;
+    const dim3 block(32, 4);
+    const dim3 grid((unsigned)((dc.W + 31) / 32), (unsigned)((dc.H + 3) / 4), (unsigned)((dc.D + zc - 1) / zc));
+    if (z) k_field_residual_restrict<T, true><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse);
+    else k_field_residual_restrict<T, false><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse);
+    launches_counter_add(1);
+}
+template <typename T>
+void prolong_add_field(const Geo& g, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
+{
+    k_prolong_add_field<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+        g, dc, coarse, f);
+    launches_counter_add(1);
+}
+template void field_residual_dense<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
+template void field_residual_dense<double>(const Geo&, const double*, const double*, float*, cudaStream_t);
+template void field_residual<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
+template void field_residual<double>(const Geo&, const double*, const double*, double*, cudaStream_t);
+template void field_axpy<float>(const Geo&, float*, const float*, cudaStream_t);
+template void field_axpy<double>(const Geo&, double*, const double*, cudaStream_t);
+template void field_residual_restrict<float>(const Geo&, const float*, const float*, const Dims&, float*, cudaStream_t);
+template void field_residual_restrict<double>(const Geo&, const double*, const double*, const Dims&, float*,
+                                              cudaStream_t);
+template void prolong_add_field<float>(const Geo&, const Dims&, const float*, float*, cudaStream_t);
+template void prolong_add_field<double>(const Geo&, const Dims&, const float*, double*, cudaStream_t);
 
 // Full-weighting restriction of dense unknown arrays, fine (2m) -> coarse (m) per
 // axis: coarse unknown I sits on fine unknown 2I+1 (0-based), weights 1/4,1/2,1/4
 // per axis; fine values beyond the grid are the Dirichlet zero.
 __global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __restrict__ coarse)
 {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= dc.W) return;
     const int Wf = dc.W * 2, Hf = dc.H * 2, Df = dc.D * 2;
-    const long long n = (long long)dc.D * dc.H * dc.W;
     const float w1[3] = {0.25f, 0.5f, 0.25f};
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(q % dc.W), y = (int)((q / dc.W) % dc.H), z = (int)(q / ((long long)dc.W * dc.H));
-        float s = 0.0f;
-        for (int a = 0; a < 3; a++) {
-            const int zz = 2 * z + a;
-            if (zz >= Df) continue;
-            for (int b = 0; b < 3; b++) {
-                const int yy = 2 * y + b;
-                if (yy >= Hf) continue;
-                for (int c = 0; c < 3; c++) {
-                    const int xx = 2 * x + c;
-                    if (xx >= Wf) continue;
-                    s += w1[a] * w1[b] * w1[c] * fine[((long long)zz * Hf + yy) * Wf + xx];
-                }
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int zz = 2 * z + a;
+        if (zz >= Df) continue;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int yy = 2 * y + b;
+            if (yy >= Hf) continue;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int xx = 2 * x + c;
+                if (xx >= Wf) continue;
+                s += w1[a] * w1[b] * w1[c] * fine[((long long)zz * Hf + yy) * Wf + xx];
             }
         }
-        coarse[q] = s;
     }
+    coarse[((long long)z * dc.H + y) * dc.W + x] = s;
 }
 
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 {
-    k_restrict<<<eblocks((long long)dc.D * dc.H * dc.W), 256, 0, s>>>(dc, fine, coarse);
+    k_restrict<<<field_grid(dc.W, dc.H, dc.D, 128), 128, 0, s>>>(dc, fine, coarse);
     launches_counter_add(1);
 }
 
@@ -603,44 +830,44 @@ void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 // otherwise (zero beyond the grid); the transpose of k_restrict up to a factor 8.
 __global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine)
 {
-    const int Wf = dc.W * 2, Hf = dc.H * 2, Df = dc.D * 2;
-    const long long n = (long long)Df * Hf * Wf;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(q % Wf), y = (int)((q / Wf) % Hf), z = (int)(q / ((long long)Wf * Hf));
-        int i0[3], i1[3];
-        float w0[3], w1v[3];
-        const int idx[3] = {x, y, z};
-        const int nc[3] = {dc.W, dc.H, dc.D};
-        for (int d = 0; d < 3; d++) {
-            if (idx[d] & 1) {
-                i0[d] = (idx[d] - 1) / 2;
-                i1[d] = i0[d];
-                w0[d] = 1.0f;
-                w1v[d] = 0.0f;
-            } else {
-                i0[d] = idx[d] / 2 - 1;
-                i1[d] = idx[d] / 2;
-                w0[d] = 0.5f;
-                w1v[d] = 0.5f;
-            }
-            (void)nc;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    const int Wf = dc.W * 2, Hf = dc.H * 2;
+    if (x >= Wf) return;
+    const int idx[3] = {x, y, z};
+    int i0[3], i1[3];
+    float w0[3], w1v[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (idx[d] & 1) {
+            i0[d] = idx[d] >> 1;
+            i1[d] = i0[d];
+            w0[d] = 1.0f;
+            w1v[d] = 0.0f;
+        } else {
+            i0[d] = (idx[d] >> 1) - 1;
+            i1[d] = idx[d] >> 1;
+            w0[d] = 0.5f;
+            w1v[d] = 0.5f;
         }
-        float s = 0.0f;
-        for (int a = 0; a < 2; a++)
-            for (int b = 0; b < 2; b++)
-                for (int c = 0; c < 2; c++) {
-                    const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = c ? i1[0] : i0[0];
-                    const float w = (a ? w1v[2] : w0[2]) * (b ? w1v[1] : w0[1]) * (c ? w1v[0] : w0[0]);
-                    if (w == 0.0f || zz < 0 || yy < 0 || xx < 0 || zz >= dc.D || yy >= dc.H || xx >= dc.W) continue;
-                    s += w * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
-                }
-        fine[q] = s;
     }
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = c ? i1[0] : i0[0];
+                const float w = (a ? w1v[2] : w0[2]) * (b ? w1v[1] : w0[1]) * (c ? w1v[0] : w0[0]);
+                if (w == 0.0f || zz < 0 || yy < 0 || xx < 0 || zz >= dc.D || yy >= dc.H || xx >= dc.W) continue;
+                s += w * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
+            }
+    fine[((long long)z * Hf + y) * Wf + x] = s;
 }
 
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<eblocks((long long)dc.D * 8 * dc.H * dc.W), 256, 0, s>>>(dc, coarse, fine);
+    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine);
     launches_counter_add(1);
 }
 

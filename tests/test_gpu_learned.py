@@ -86,3 +86,58 @@ def test_set_learned_rejects_unsupported(gpu):
     with pytest.raises(pps.PpsError):
         pps.BiCGSTAB(pps.BlockGrid.cube(32), form="parity").set_learned(net, 0, 1.0, FLAGS)
     net.close()
+
+
+def _restrict_1d(nf):
+    """Full weighting along one axis: coarse c on fine 2c+1, weights 1/4, 1/2, 1/4."""
+    r = np.zeros((nf // 2, nf))
+    for c in range(nf // 2):
+        for a, w in enumerate((0.25, 0.5, 0.25)):
+            if 2 * c + a < nf:
+                r[c, 2 * c + a] = w
+    return r
+
+
+def _along_axes(mats, f):
+    return np.einsum("ai,bj,ck,ijk->abc", mats[0], mats[1], mats[2], f, optimize=True)
+
+
+@pytest.mark.parametrize("form,m", [("fp64", 64), ("fp64", 128), ("mixed", 64)])
+def test_learned_cycle_matches_its_composition(gpu, form, m):
+    """apply_preconditioner with the network attached is the two-grid cycle
+    z = Cheb(r); z += gain P^k N(R^k (r - A z)); z += Cheb(r - A z), rebuilt here from
+    the plain Chebyshev application, the operator, numpy transfers and the network."""
+    net = pps.UNet((16, 32, 64), seed=3, linear=True)
+    k = int(round(math.log2(m / 32)))
+    gain = 0.7
+    grid = pps.BlockGrid.cube(m)
+    b = learned.rhs(m, 30020, "field")
+    plain = pps.FlexibleCG(grid, pps.ChebyshevIteration(11), form=form)
+    s = pps.FlexibleCG(grid, pps.ChebyshevIteration(11), form=form)
+    s.set_learned(net, k, gain, pps.LEARNED_PRECONDITIONER | pps.LEARNED_POST_SMOOTH)
+    got = s.apply_preconditioner(b.copy())
+
+    inner = (slice(2, m + 2),) * 3
+    z = plain.apply_preconditioner(b.copy())
+    res = np.zeros_like(b)
+    res[inner] = (b - plain.apply_operator(z))[inner]
+    coarse = res[inner]
+    for _ in range(k):
+        n = coarse.shape[0]
+        coarse = _along_axes([_restrict_1d(n)] * 3, coarse)
+    cin = torch.from_numpy(np.ascontiguousarray(coarse, np.float32)).cuda()
+    cout = torch.empty_like(cin)
+    net.forward(coarse.shape, cin.data_ptr(), cout.data_ptr(), normalize=True)
+    corr = gain * cout.cpu().numpy().astype(np.float64)
+    for _ in range(k):
+        n = corr.shape[0]
+        corr = _along_axes([2.0 * _restrict_1d(2 * n).T] * 3, corr)
+    z[inner] += corr
+    res2 = np.zeros_like(b)
+    res2[inner] = (b - plain.apply_operator(z))[inner]
+    z = z + plain.apply_preconditioner(res2)
+    tol = 1e-4 if form == "fp64" else 2e-3
+    assert rel_l2(got[inner], z[inner]) < tol
+    s.close()
+    plain.close()
+    net.close()
