@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed+learned vs plain FP64), 1 GB300"
 NET_GRID = 32   # the U-Net runs as the coarse-grid solver on a 32^3 grid
+# multigrid V-cycle of the learned preconditioner: Chebyshev smoother degree on the
+# solver's grid, on the intermediate levels, and the smoothing interval ratio
+VCYCLE = (5, 8, 8.0)
 TOL = 1e-10
 DEGREE = 11
 # Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload, measured by
@@ -168,7 +171,7 @@ def train_network(args, dev: int):
     """The learned preconditioner's U-Net: linear 3-level 16/32/64 network trained on
     32^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs; u solved to 1e-12
     by the plain FP64 solver) with the library's own kernels; it is the coarse-grid
-    solver of the two-grid correction inside flexible CG."""
+    solver of the multigrid V-cycle inside flexible CG."""
     import torch
 
     import parallelpoissonsolver_gb300 as pps
@@ -217,10 +220,11 @@ def run_gpu(args, dist: Dist):
 
     net, scale, net_info = train_network(args, dev)
     k, gain = learned_gain(m, scale)
-    flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER | pps.LEARNED_POST_SMOOTH
+    flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER
     head = pps.FlexibleCG(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
-                          inner_tol=args.inner_tol, device=dev)
+                          inner_tol=args.learned_inner_tol, device=dev)
     head.set_learned(net, k, gain, flags)
+    head.set_learned_cycle(*VCYCLE)
     mixed = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
                          inner_tol=args.inner_tol, device=dev)
     plain = pps.BiCGSTAB(grid, prec, tolerance=TOL, max_iteration=20000, form="fp64", use_graph=False,
@@ -308,9 +312,11 @@ def run_gpu(args, dist: Dist):
         "config": {
             "workload": f"{m}^3 interior unknowns, h=1/{m + 1}, Dirichlet 0, -lap u = f, f ~ P(k) k^-2 field; "
                         f"stop at FP64 ||r||/||b_adj|| <= {TOL:g}",
-            "form": "mixed+learned: FP64 iterative refinement around FP32 flexible CG; preconditioner = "
-                    f"Chebyshev({DEGREE}) smoothing + U-Net coarse-grid correction on the {NET_GRID}^3 grid "
-                    f"({k} restrictions) + Chebyshev post-smoothing; learned initial guess",
+            "form": "mixed+learned: FP64 iterative refinement around FP32 flexible CG (inner tolerance "
+                    f"{args.learned_inner_tol:g}); preconditioner = multigrid V-cycle over {k + 1} levels: "
+                    f"Chebyshev({VCYCLE[0]}) smoothing on the {m}^3 grid, Chebyshev({VCYCLE[1]}) pre- and "
+                    f"post-smoothing on each intermediate level (interval [lmax/{VCYCLE[2]:g}, lmax]), the U-Net "
+                    f"as the {NET_GRID}^3 coarse solver; learned initial guess",
             "l2": "no flush: every field (0.5-1.1 GB) exceeds the 129 MB L2",
             "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU, single domain",
             "iterations": stats[-1]["iterations"],
@@ -373,9 +379,13 @@ def run_learned_128(args, dev: int, net, scale: float):
         "fcg": pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64", device=dev),
         "fcg+learned": pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64",
                                       use_graph=False, device=dev),
+        "fcg+learned-vcycle": pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64",
+                                             use_graph=False, device=dev),
     }
     forms["fcg+learned"].set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER |
                                      pps.LEARNED_POST_SMOOTH)
+    forms["fcg+learned-vcycle"].set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER)
+    forms["fcg+learned-vcycle"].set_learned_cycle(*VCYCLE)
     res = {n: {"iterations": [], "seconds": [], "err_true": []} for n in forms}
     for i in range(args.held_out):
         seed = 30000 + i
@@ -395,8 +405,8 @@ def run_learned_128(args, dev: int, net, scale: float):
     for n, r in res.items():
         out[n] = {"mean_iterations": float(np.mean(r["iterations"])), "mean_seconds": float(np.mean(r["seconds"])),
                   "max_err_true": float(np.max(r["err_true"]))}
-    out["iteration_gain_vs_fcg"] = out["fcg"]["mean_iterations"] / out["fcg+learned"]["mean_iterations"]
-    out["time_gain_vs_bicgstab"] = out["bicgstab"]["mean_seconds"] / out["fcg+learned"]["mean_seconds"]
+    out["iteration_gain_vs_fcg"] = out["fcg"]["mean_iterations"] / out["fcg+learned-vcycle"]["mean_iterations"]
+    out["time_gain_vs_bicgstab"] = out["bicgstab"]["mean_seconds"] / out["fcg+learned-vcycle"]["mean_seconds"]
     return out
 
 
@@ -509,6 +519,7 @@ def main():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=3e-3)
+    ap.add_argument("--learned-inner-tol", type=float, default=3e-4)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=16)

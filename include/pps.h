@@ -56,7 +56,7 @@ typedef struct {
 
 /* BiCGSTAB (BiCGSTAB.hpp), CG (baseCG.hpp), and flexible CG (no reference
  * counterpart: BaseCG with a Polak-Ribiere beta, for preconditioners that change
- * between applications, FP64 and MIXED forms only). */
+ * between applications, FP64 and MIXED forms, Dirichlet grids only). */
 typedef enum { PPS_KRYLOV_BICGSTAB = 0, PPS_KRYLOV_CG = 1, PPS_KRYLOV_FCG = 2 } pps_krylov;
 typedef enum { PPS_PREC_NONE = 0, PPS_PREC_CHEBYSHEV = 1 } pps_precond;
 
@@ -265,6 +265,18 @@ pps_status pps_unet_train_step(pps_unet* net, int nx, int ny, int nz, const floa
 #define PPS_LEARNED_NO_FALLBACK 4     /* keep the network for the whole solve (measurements) */
 #define PPS_LEARNED_POST_SMOOTH 8     /* z += Cheb(r - A z) after the correction (two-grid cycle) */
 pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gain, int flags);
+
+/* Multigrid form of the learned preconditioner (no reference counterpart).  With
+ * fine_degree >= 2 and coarsen >= 1, each application is a V-cycle over the levels
+ * 0..coarsen whose coarsest solver is the network: Chebyshev smoothing on
+ * [lambda_max/ratio, lambda_max] of each level's 7-point operator (spacings 2^l ds),
+ * full-weighting restriction of the residual, trilinear prolongation of the
+ * correction and post-smoothing (on the solver's grid with PPS_LEARNED_POST_SMOOTH).
+ * Degrees count as cheb_degree does (the recurrence's output is s_{n-2}):
+ * fine_degree on the solver's grid, coarse_degree on levels 1..coarsen-1 (0: no
+ * smoothing there).  fine_degree = 0 (the default) keeps the two-grid cycle around
+ * the solver's own Chebyshev preconditioner. */
+pps_status pps_set_learned_cycle(pps_solver* s, int fine_degree, int coarse_degree, double ratio);
 
 /* 2x grid transfers of dense unknown arrays (coarse extents nx, ny, nz; the fine
  * grid has twice as many unknowns per axis, coarse unknown i on fine unknown 2i+1):

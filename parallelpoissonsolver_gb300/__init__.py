@@ -47,7 +47,7 @@ EXPORTED = [
     "pps_batch_autotune", "pps_batch_tile", "pps_batch_solve",
     "pps_unet_create", "pps_unet_destroy", "pps_unet_param_count", "pps_unet_get_params", "pps_unet_set_params",
     "pps_unet_forward", "pps_unet_gradients", "pps_unet_train_step", "pps_restrict2", "pps_prolong2",
-    "pps_set_learned", "pps_unet_set_activation",
+    "pps_set_learned", "pps_unet_set_activation", "pps_set_learned_cycle",
 ]
 
 
@@ -164,6 +164,7 @@ def load(build_if_missing: bool = False):
     L.pps_unet_train_step.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, C.c_float, C.POINTER(C.c_double)]
     L.pps_restrict2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_set_learned.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+    L.pps_set_learned_cycle.argtypes = [vp, C.c_int, C.c_int, C.c_double]
     L.pps_unet_set_activation.argtypes = [vp, C.c_int]
     L.pps_prolong2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_status_string.restype = C.c_char_p
@@ -386,6 +387,15 @@ class Solver:
         if st != OK:
             raise PpsError(st, "pps_set_learned")
         self._net = net
+
+    def set_learned_cycle(self, fine_degree: int, coarse_degree: int = 0, ratio: float = 8.0):
+        """Multigrid form of the learned preconditioner (pps_set_learned_cycle): a
+        V-cycle with Chebyshev smoothers of these degrees on [lambda_max/ratio,
+        lambda_max] of every level and the network on the coarsest; fine_degree 0
+        keeps the two-grid cycle around the solver's own Chebyshev preconditioner."""
+        st = load().pps_set_learned_cycle(self._h, int(fine_degree), int(coarse_degree), float(ratio))
+        if st != OK:
+            raise PpsError(st, "pps_set_learned_cycle")
 
     def tuning_key(self) -> str:
         n = self.grid.npglobal

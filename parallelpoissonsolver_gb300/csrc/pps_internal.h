@@ -62,7 +62,9 @@ enum FinKind : int {
     FIN_CG_ALPHA = 6,   // CG alpha = rz / pAp
     FIN_CG_CONV = 7,    // CG beta = rz_new / rz, err, stop test
     FIN_STORE = 8,      // only store sums[] (used by tests and true residuals)
-    FIN_FCG_CONV = 9    // flexible CG: Polak-Ribiere beta, err, stop test
+    FIN_FCG_CONV = 9,   // flexible CG: Polak-Ribiere beta = -alpha z.Ap / rho0, rho0 = z.r, err, stop test
+    FIN_FCG_ALPHA = 10, // flexible CG: alpha = rho0 / pAp
+    FIN_FCG_SETUP = 11  // flexible CG (re)start: rho0 = z.r, beta = 0 (the next p is z)
 };
 
 struct RedCtx {
@@ -198,10 +200,13 @@ template <typename T>
 void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const DevState* st, cudaStream_t s);
 // Flexible CG (no reference counterpart; BaseCG's loop with a Polak-Ribiere beta).
 template <typename T>
-void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, T* r_old, const T* Ap,
+void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap,
                         const DevState* st, cudaStream_t s);
 template <typename T>
-void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* r_old, RedCtx rc, cudaStream_t s);
+void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s);
+template <typename T>
+void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
+                        RedCtx rc, cudaStream_t s);
 
 // FP64 true residual r = b - A x written as TR (also into r0 and p when given),
 // with sum r^2 in FP64.

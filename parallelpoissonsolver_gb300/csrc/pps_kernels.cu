@@ -594,11 +594,26 @@ __device__ void finalize(const RedCtx& rc, const double* tot)
         }
         break;
     }
+    case FIN_FCG_ALPHA: {
+        st->alpha = st->rho0 / tot[0];        // z.r / p.Ap
+        if (!isfinite(st->alpha)) {
+            st->status = 2;
+            st->done = 1;
+        }
+        break;
+    }
+    case FIN_FCG_SETUP: {
+        st->rho0 = tot[0];                    // z.r
+        st->beta = 0.0;
+        break;
+    }
     case FIN_FCG_CONV: {
         // flexible CG, Polak-Ribiere: beta = z_new.(r_new - r_old) / (z_old.r_old)
+        // with r_new - r_old = -alpha Ap
         const double err = sqrt(tot[2]);
         st->err = err;
-        st->beta = (tot[0] - tot[1]) / st->rho0;
+        st->beta = -st->alpha * tot[1] / st->rho0;
+        st->rho0 = tot[0];
         st->iter += 1;
         if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
         if (!isfinite(err)) {
@@ -1044,11 +1059,51 @@ __global__ void __launch_bounds__(256) k_cg_update_p(Geo g, Shape sh, T* __restr
     }
 }
 
-// FCG: x += alpha*p; r_old = r; r -= alpha*Ap
+// FCG: p_out = z + beta*p_in (z itself when beta = 0, the (re)start); Ap = A p_out;
+// sums p_out.Ap.  The direction update rides on the stencil: each thread forms
+// p_out at the 7 points from z and p_in, so p_in and p_out must be distinct fields.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_p_stencil(Geo g, Shape sh, const T* __restrict__ z,
+                                                       const T* __restrict__ pin, T* __restrict__ pout,
+                                                       T* __restrict__ Ap, Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a1;
+    if (q.active) {
+        const T cc = (T)cf.cc, cx = (T)cf.cx, cy = (T)cf.cy, cz = (T)cf.cz;
+        const bool restart = rc.st->beta == 0.0;
+        const T be = (T)rc.st->beta;
+        const long long sj = g.sj, sk = g.sk;
+        auto pv = [&](long long c) -> T { return restart ? z[c] : fmx(be, pin[c], z[c]); };
+        long long c = q.c;
+        T um = pv(c - sk), uc = pv(c);
+#pragma unroll 2
+        for (int k = q.k0; k < q.k1; k++) {
+            const T up = pv(c + sk);
+            const T sx = pv(c - 1) + pv(c + 1);
+            const T sy = pv(c - sj) + pv(c + sj);
+            T a = cc * uc;
+            a = fmx(cx, sx, a);
+            a = fmx(cy, sy, a);
+            a = fmx(cz, um + up, a);
+            pout[c] = uc;
+            Ap[c] = a;
+            a1.add(uc, a);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[1] = {a1.value()};
+    reduce_finalize<1>(v, rc);
+}
+
+// FCG: x += alpha*p; r -= alpha*Ap
 template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
-                                                       T* __restrict__ r, T* __restrict__ r_old,
-                                                       const T* __restrict__ Ap, const DevState* st)
+                                                       T* __restrict__ r, const T* __restrict__ Ap,
+                                                       const DevState* st)
 {
     EARLY_EXIT(&st->done);
     const Col q = column(g, sh);
@@ -1058,17 +1113,16 @@ __global__ void __launch_bounds__(256) k_fcg_update_xr(Geo g, Shape sh, T* __res
 #pragma unroll 4
     for (int k = q.k0; k < q.k1; k++) {
         x[c] = fmx(a, p[c], x[c]);
-        const T rv = r[c];
-        r_old[c] = rv;
-        r[c] = fmx(-a, Ap[c], rv);
+        r[c] = fmx(-a, Ap[c], r[c]);
         c += g.sk;
     }
 }
 
-// FCG: sums z.r, z.r_old, r.r after the (possibly nonlinear) preconditioner
+// FCG: sums z.r, z.Ap, r.r after the (possibly nonlinear) preconditioner; with
+// r_new - r_old = -alpha Ap the Polak-Ribiere numerator is -alpha z.Ap
 template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_dot(Geo g, Shape sh, const T* __restrict__ r, const T* __restrict__ z,
-                                                 const T* __restrict__ r_old, RedCtx rc)
+                                                 const T* __restrict__ Ap, RedCtx rc)
 {
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
@@ -1079,7 +1133,7 @@ __global__ void __launch_bounds__(256) k_fcg_dot(Geo g, Shape sh, const T* __res
         for (int k = q.k0; k < q.k1; k++) {
             const T rv = r[c], zv = z[c];
             a1.add(zv, rv);
-            a2.add(zv, r_old[c]);
+            if (Ap) a2.add(zv, Ap[c]);
             a3.add(rv, rv);
             c += g.sk;
         }
@@ -1273,16 +1327,23 @@ void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const Dev
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
-void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, T* r_old, const T* Ap,
-                        const DevState* st, cudaStream_t s)
+void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+                        cudaStream_t s)
 {
-    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, r_old, Ap, st);
+    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, st);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
-void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* r_old, RedCtx rc, cudaStream_t s)
+void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s)
 {
-    k_fcg_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, r_old, rc);
+    k_fcg_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, Ap, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
+                        RedCtx rc, cudaStream_t s)
+{
+    k_fcg_p_stencil<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename TR>
@@ -1339,9 +1400,11 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
                                        cudaStream_t);                                                            \
     template void fast_cg_dot_rz<T>(const Geo&, const Shape&, const T*, const T*, RedCtx, cudaStream_t);         \
     template void fast_cg_update_p<T>(const Geo&, const Shape&, T*, const T*, const DevState*, cudaStream_t);    \
-    template void fast_fcg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, T*, const T*,                \
-                                        const DevState*, cudaStream_t);                                          \
+    template void fast_fcg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, const DevState*,   \
+                                        cudaStream_t);                                                           \
     template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
+    template void fast_fcg_p_stencil<T>(const Geo&, const Shape&, const T*, const T*, T*, T*, const Coef&,       \
+                                        RedCtx, cudaStream_t);                                                   \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
                                    const Coef&, RedCtx, cudaStream_t);                                           \
     template void fill_field<T>(T*, long long, T, cudaStream_t);

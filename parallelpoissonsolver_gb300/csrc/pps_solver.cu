@@ -142,6 +142,13 @@ struct pps_solver {
     std::vector<float*> dn_e;
     int learned_apps = 0;
     int fallback_iter = -1;
+    // multigrid form of the learned cycle (pps_set_learned_cycle): smoother degrees
+    // of the fine and the coarse levels (fine 0: the two-grid cycle), interval ratio;
+    // dt: residuals of levels 1..k-1; cY, cZ, cW: Chebyshev buffers of those levels
+    int cyc_fine = 0, cyc_coarse = 0;
+    double cyc_ratio = 8.0;
+    std::vector<float*> dt;
+    float *cY = nullptr, *cZ = nullptr, *cW = nullptr;
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
@@ -173,10 +180,10 @@ RedCtx red(pps_solver* s, int kind)
 }
 
 // A(u) = cc*u + c_d*(pairs) with c_d = 1/h_d^2  (matrixFreeOperatorA.hpp:34-38)
-Coef op_coef(const Geo& g)
+Coef op_coef_ds(const double ds[3])
 {
     Coef c;
-    const double ix = 1.0 / (g.ds[0] * g.ds[0]), iy = 1.0 / (g.ds[1] * g.ds[1]), iz = 1.0 / (g.ds[2] * g.ds[2]);
+    const double ix = 1.0 / (ds[0] * ds[0]), iy = 1.0 / (ds[1] * ds[1]), iz = 1.0 / (ds[2] * ds[2]);
     c.cc = -2.0 * (ix + iy + iz);
     c.cx = ix;
     c.cy = iy;
@@ -185,6 +192,11 @@ Coef op_coef(const Geo& g)
     c.cw = 0;
     c.scale = 1.0;
     return c;
+}
+
+Coef op_coef(const Geo& g)
+{
+    return op_coef_ds(g.ds);
 }
 
 long long face_count(const pps_solver* s, int f)
@@ -240,6 +252,8 @@ void free_all(pps_solver* s)
     if (s->h_dot) cudaFreeHost(s->h_dot);
     for (float* q : s->dn) cudaFree(q);
     for (float* q : s->dn_e) cudaFree(q);
+    for (float* q : s->dt) cudaFree(q);
+    for (float* q : {s->cY, s->cZ, s->cW}) cudaFree(q);
     for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -402,28 +416,55 @@ double bytes_of(long long n, int words)
     return (double)n * words * sizeof(T);
 }
 
-// Pre-folded Chebyshev coefficients for the fast kernels.
-Coef cheb_s01_coef(const pps_solver* s, double rhoCurr)
+// A Chebyshev polynomial in the reference's form (chebyshevIteration.hpp:22-26,
+// 48-140): interval parameters theta, delta, sigma = theta/delta and degree n;
+// the output is -s_{n-2}.
+struct ChebP {
+    double theta, delta, sigma;
+    int n;
+};
+
+ChebP cheb_of(const pps_solver* s)
 {
-    const Coef a = op_coef(s->geo);
-    const double t = 2 * rhoCurr / s->delta;   // Y = t*(2B + A(B)/theta)
+    return ChebP{s->theta, s->delta, s->sigma, s->cfg.cheb_degree};
+}
+
+// The same recurrence as a smoother on [lambda_max / ratio, lambda_max] of the
+// operator with spacings ds (lambda_max = sum_d 4 / ds_d^2, the bound the
+// sine formula approaches): the high-frequency part of the spectrum only.
+ChebP smoother_of(const double ds[3], double ratio, int n)
+{
+    double lmax = 0;
+    for (int d = 0; d < 3; d++) lmax += 4.0 / (ds[d] * ds[d]);
+    const double lo = lmax / ratio;
+    ChebP p;
+    p.theta = (lo + lmax) * 0.5;
+    p.delta = (lo - lmax) * 0.5;
+    p.sigma = p.theta / p.delta;
+    p.n = n;
+    return p;
+}
+
+// Pre-folded Chebyshev coefficients for the fast kernels (a: the operator's).
+Coef cheb_s01_coef(const Coef& a, const ChebP& p, double rhoCurr)
+{
+    const double t = 2 * rhoCurr / p.delta;   // Y = t*(2B + A(B)/theta)
     Coef c;
-    c.cc = t * (2.0 + a.cc / s->theta);
-    c.cx = t * a.cx / s->theta;
-    c.cy = t * a.cy / s->theta;
-    c.cz = t * a.cz / s->theta;
+    c.cc = t * (2.0 + a.cc / p.theta);
+    c.cx = t * a.cx / p.theta;
+    c.cy = t * a.cy / p.theta;
+    c.cz = t * a.cz / p.theta;
     c.cb = 0;
     c.cw = 0;
     c.scale = 1.0;
     return c;
 }
 
-Coef cheb_sweep_coef(const pps_solver* s, double rhoCurr, double rhoOld, double scale)
+Coef cheb_sweep_coef(const Coef& a, const ChebP& p, double rhoCurr, double rhoOld, double scale)
 {
-    const Coef a = op_coef(s->geo);
-    const double tod = 2.0 / s->delta;   // W = rc*(2 sigma Y + 2/delta (B + A Y) - ro Z)
+    const double tod = 2.0 / p.delta;   // W = rc*(2 sigma Y + 2/delta (B + A Y) - ro Z)
     Coef c;
-    c.cc = rhoCurr * (2.0 * s->sigma + tod * a.cc);
+    c.cc = rhoCurr * (2.0 * p.sigma + tod * a.cc);
     c.cx = rhoCurr * tod * a.cx;
     c.cy = rhoCurr * tod * a.cy;
     c.cz = rhoCurr * tod * a.cz;
@@ -444,23 +485,35 @@ struct Launcher {
 // sweeps of the reference are dead (its output is s_{n-2}, chebyshevIteration.hpp:
 // 114-125), so sweeps run for i = 2..n-2 and the last one writes X = -s_{n-2}.
 template <typename T>
+void fast_cheb(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const ChebP& p);
+
+template <typename T>
 void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+{
+    const Geo& g = s->geo;
+    if (s->cfg.precond == PPS_PREC_NONE) {
+        CK(cudaMemcpyAsync(X, B, sizeof(T) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, s->stream));
+        L.bytes += bytes_of<T>(g.ntot, 2);
+        return;
+    }
+    fast_cheb<T>(s, F, B, X, L, cheb_of(s));
+}
+
+// X = -s_{n-2} of the Chebyshev recurrence p on B (the preconditioner, or a smoother).
+template <typename T>
+void fast_cheb(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const ChebP& p)
 {
     const Geo& g = s->geo;
     cudaStream_t st = s->stream;
     const long long N = s->n_unknowns;
     const int* done = &s->d_st->done;
-    if (s->cfg.precond == PPS_PREC_NONE) {
-        CK(cudaMemcpyAsync(X, B, sizeof(T) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
-        L.bytes += bytes_of<T>(g.ntot, 2);
-        return;
-    }
     if (s->has_neumann) {
         neumann_fill<T>(g, B, faces_of(s), 0, 1.0, st);
         L.launches += 2;
     }
-    const int n = s->cfg.cheb_degree;
-    const double sigma = s->sigma;
+    const Coef a = op_coef(g);
+    const int n = p.n;
+    const double sigma = p.sigma;
     double rhoOld = 1 / sigma;
     double rhoCurr = 1 / (2 * sigma - rhoOld);
     if (n == 1) {
@@ -470,13 +523,13 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
         return;
     }
     if (n == 2) {
-        fast_scale_copy<T>(g, s->shape, B, X, -1.0 / s->theta, done, st);
+        fast_scale_copy<T>(g, s->shape, B, X, -1.0 / p.theta, done, st);
         L.bytes += bytes_of<T>(N, 2);
         L.launches++;
         return;
     }
     const Shape& shc = s->shape_cheb;
-    Coef c01 = cheb_s01_coef(s, rhoCurr);
+    Coef c01 = cheb_s01_coef(a, p, rhoCurr);
     if (n == 3) {
         c01.scale = -1.0;
         fast_cheb_s01<T>(g, shc, B, X, c01, done, st);
@@ -500,11 +553,11 @@ void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
             L.launches += 2;
         }
         const bool last = (it == n - 2);
-        Coef c = cheb_sweep_coef(s, rhoCurr, rhoOld, last ? -1.0 : 1.0);
+        Coef c = cheb_sweep_coef(a, p, rhoCurr, rhoOld, last ? -1.0 : 1.0);
         const bool first = (it == 2);
         if (first) {
             // Z = s0 = B/theta: fold it into the B coefficient instead of storing s0
-            c.cb += c.cw / s->theta;
+            c.cb += c.cw / p.theta;
             c.cw = 0.0;
         }
         fast_cheb_sweep<T>(g, shc, Y, B, first ? nullptr : Z, last ? X : W, c, done, st);
@@ -557,27 +610,146 @@ void learned_coarse_correction(pps_solver* s, const T* r, const T* z, T* X)
         unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
     } else {
         for (int l = k; l > 1; l--) unet::prolong2(dense_dims(s, l), s->dn_e[(size_t)l], s->dn_e[(size_t)l - 1], st);
-        unet::prolong_add_field<T>(g, dense_dims(s, 1), s->dn_e[1], X, st);
+        unet::prolong_add_field<T>(g, s->shape, dense_dims(s, 1), s->dn_e[1], X, st);
+    }
+    s->learned_apps++;
+}
+
+unet::DCoef dcoef(const Coef& c)
+{
+    return unet::DCoef{(float)c.cc, (float)c.cx, (float)c.cy, (float)c.cz, (float)c.cb, (float)c.cw, (float)c.scale};
+}
+
+// Spacings of level l (2^l times the solver's).
+void level_ds(const pps_solver* s, int l, double ds[3])
+{
+    for (int d = 0; d < 3; d++) ds[d] = s->geo.ds[d] * (double)(1 << l);
+}
+
+// out = b - A_l z on dense level l (A_l: the 7-point operator with level-l spacings).
+void dense_residual(pps_solver* s, int l, const float* b, const float* z, float* out)
+{
+    double ds[3];
+    level_ds(s, l, ds);
+    Coef a = op_coef_ds(ds);
+    const Coef r{-a.cc, -a.cx, -a.cy, -a.cz, 1.0, 0.0, 1.0};
+    unet::dense_sweep(dense_dims(s, l), z, b, nullptr, out, dcoef(r), false, s->stream);
+}
+
+// X (+)= -s_{n-2}: the Chebyshev smoother of dense level l on B (the recurrence of
+// fast_cheb, on [lambda_max/ratio, lambda_max] of A_l).
+void dense_cheb(pps_solver* s, int l, const float* B, float* X, bool acc)
+{
+    double ds[3];
+    level_ds(s, l, ds);
+    const Coef a = op_coef_ds(ds);
+    const ChebP p = smoother_of(ds, s->cyc_ratio, s->cyc_coarse);
+    const unet::Dims d = dense_dims(s, l);
+    cudaStream_t st = s->stream;
+    const int n = p.n;
+    if (n == 2) {
+        const Coef c{1.0 / p.theta, 0, 0, 0, 0, 0, -1.0};
+        unet::dense_sweep(d, B, nullptr, nullptr, X, dcoef(c), acc, st);
+        return;
+    }
+    double rhoOld = 1 / p.sigma;
+    double rhoCurr = 1 / (2 * p.sigma - rhoOld);
+    Coef c01 = cheb_s01_coef(a, p, rhoCurr);
+    if (n == 3) {
+        c01.scale = -1.0;
+        unet::dense_sweep(d, B, nullptr, nullptr, X, dcoef(c01), acc, st);
+        return;
+    }
+    float *Y = s->cY, *Z = s->cZ, *W = s->cW;
+    unet::dense_sweep(d, B, nullptr, nullptr, Y, dcoef(c01), false, st);
+    for (int it = 2; it <= n - 2; it++) {
+        rhoOld = rhoCurr;
+        rhoCurr = 1 / (2 * p.sigma - rhoOld);
+        const bool last = (it == n - 2), first = (it == 2);
+        Coef c = cheb_sweep_coef(a, p, rhoCurr, rhoOld, last ? -1.0 : 1.0);
+        if (first) {
+            c.cb += c.cw / p.theta;
+            c.cw = 0.0;
+        }
+        unet::dense_sweep(d, Y, B, first ? nullptr : Z, last ? X : W, dcoef(c), last && acc, st);
+        if (!last) {
+            float* t = Z;
+            Z = Y;
+            Y = W;
+            W = t;
+        }
+    }
+}
+
+// The multigrid form of the learned cycle, a V-cycle over levels 0..k whose
+// coarsest solver is the network:
+//   level 0 (solver fields): X = S_0 B;  r_1 = R (B - A X)
+//   level l = 1..k-1:        z_l = S_l r_l;  r_{l+1} = R (r_l - A_l z_l)
+//   level k:                 z_k = gain N(r_k)
+//   level l = k-1..1:        z_l += P z_{l+1};  z_l += S_l (r_l - A_l z_l)
+//   level 0:                 X += P z_1;  [X += S_0 (B - A X)]
+// S_l: Chebyshev smoothers on the high-frequency end of each level's spectrum;
+// dn[l] holds r_l, dn_e[l] holds z_l.
+template <typename T>
+void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+{
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    const int k = s->net_coarsen;
+    const ChebP pf = smoother_of(g.ds, s->cyc_ratio, s->cyc_fine);
+    fast_cheb<T>(s, F, B, X, L, pf);
+    unet::field_residual_restrict<T>(g, B, X, dense_dims(s, 1), s->dn[1], st);
+    for (int l = 1; l < k; l++) {
+        if (s->cyc_coarse > 0) {
+            dense_cheb(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], false);
+            dense_residual(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], s->dt[(size_t)l]);
+            unet::restrict2(dense_dims(s, l + 1), s->dt[(size_t)l], s->dn[(size_t)l + 1], st);
+        } else {
+            unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
+        }
+    }
+    const unet::Dims dc = dense_dims(s, k);
+    if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, s->dn[(size_t)k], s->dn_e[(size_t)k], s->net_gain, st) != PPS_OK)
+        throw CudaFail{cudaErrorUnknown};
+    for (int l = k - 1; l >= 1; l--) {
+        if (s->cyc_coarse > 0) {
+            unet::prolong2_add(dense_dims(s, l + 1), s->dn_e[(size_t)l + 1], s->dn_e[(size_t)l], st);
+            dense_residual(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], s->dt[(size_t)l]);
+            dense_cheb(s, l, s->dt[(size_t)l], s->dn_e[(size_t)l], true);
+        } else {
+            unet::prolong2(dense_dims(s, l + 1), s->dn_e[(size_t)l + 1], s->dn_e[(size_t)l], st);
+        }
+    }
+    unet::prolong_add_field<T>(g, s->shape, dense_dims(s, 1), s->dn_e[1], X, st);
+    if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
+        unet::field_residual<T>(g, s->shape, B, X, F.r0, st);
+        fast_cheb<T>(s, F, F.r0, F.Mp, L, pf);
+        unet::field_axpy<T>(g, s->shape, X, F.Mp, st);
     }
     s->learned_apps++;
 }
 
 // Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity),
-// followed, while the learned preconditioner is active, by a two-grid cycle whose
-// coarse solver is the network:
+// or, while the learned preconditioner is active, a cycle whose coarse solver is
+// the network: the two-grid cycle around the solver's own preconditioner
 //   z = Cheb(r);  z += gain P^k N(R^k (r - A z));  [z += Cheb(r - A z)]
+// or the multigrid V-cycle of learned_vcycle.
 template <typename T>
 void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
 {
+    if (s->net && s->net_active && s->cyc_fine > 0 && s->net_coarsen >= 1) {
+        learned_vcycle<T>(s, F, B, X, L);
+        return;
+    }
     fast_precond<T>(s, F, B, X, L);
     if (!(s->net && s->net_active)) return;
     learned_coarse_correction<T>(s, B, X, X);
     if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
         // post-smoothing through the fields flexible CG leaves free (r0, Mp)
         const Geo& g = s->geo;
-        unet::field_residual<T>(g, B, X, F.r0, s->stream);
+        unet::field_residual<T>(g, s->shape, B, X, F.r0, s->stream);
         fast_precond<T>(s, F, F.r0, F.Mp, L);
-        unet::field_axpy<T>(g, X, F.Mp, s->stream);
+        unet::field_axpy<T>(g, s->shape, X, F.Mp, s->stream);
     }
 }
 
@@ -639,9 +811,11 @@ void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     L.launches += 4;
 }
 
-// One flexible-CG iteration: CG with beta = z_new.(r_new - r_old) / (z_old.r_old), so
-// the preconditioner may change from one application to the next.  r_old lives in
-// the Az field, which CG does not use.
+// One flexible-CG iteration: CG with the Polak-Ribiere beta = z_new.(r_new - r_old) /
+// (z_old.r_old), so the preconditioner may change from one application to the next.
+// With r_new - r_old = -alpha Ap no old residual is kept; the direction update
+// p = z + beta p rides on the stencil kernel, which writes the new direction into
+// the other of the fields p and Az (swapped here after every iteration).
 template <typename T>
 void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
 {
@@ -650,13 +824,23 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     cudaStream_t st = s->stream;
     const long long N = s->n_unknowns;
     const Coef a = op_coef(g);
-    fast_cg_stencil_dot<T>(g, sh, F.p, F.r, F.z, F.AMp, a, red(s, FIN_CG_ALPHA), st);
-    fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.Az, F.AMp, s->d_st, st);
+    fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
+    std::swap(F.p, F.Az);
+    fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
     precond_any<T>(s, F, F.r, F.z, L);
-    fast_fcg_dot<T>(g, sh, F.r, F.z, F.Az, red(s, FIN_FCG_CONV), st);
-    fast_cg_update_p<T>(g, sh, F.p, F.z, s->d_st, st);
-    L.bytes += bytes_of<T>(N, 4 + 7 + 3 + 3);
-    L.launches += 4;
+    fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
+    L.bytes += bytes_of<T>(N, 4 + 6 + 3);
+    L.launches += 3;
+}
+
+// Flexible-CG (re)start after z = M r: rho0 = z.r and beta = 0, so the next
+// iteration's direction is z.
+template <typename T>
+void fcg_setup(pps_solver* s, Fields<T>& F, Launcher& L)
+{
+    fast_fcg_dot<T>(s->geo, s->shape, F.r, F.z, nullptr, red(s, FIN_FCG_SETUP), s->stream);
+    L.bytes += bytes_of<T>(s->n_unknowns, 2);
+    L.launches += 1;
 }
 
 template <typename T>
@@ -690,7 +874,10 @@ template <typename T>
 pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launcher& L)
 {
     const bool learned = s->net && s->net_active;
-    const int chunk = learned ? 1 : auto_check_every(s, (int)sizeof(T));
+    int chunk = learned ? 1 : auto_check_every(s, (int)sizeof(T));
+    // flexible CG swaps its direction fields every iteration: a captured chunk must
+    // hold an even number of iterations to leave them where the capture found them
+    if (s->cfg.krylov == PPS_KRYLOV_FCG && !learned) chunk += chunk & 1;
     const bool graph = s->cfg.use_graph != 0 && !L.profile && !learned;
     std::vector<double> errs;   // residual norms seen by the fallback rule
     for (;;) {
@@ -744,7 +931,7 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
                 s->fallback_iter = s->h_st->iter;
                 // restart the flexible-CG recurrence on the plain preconditioner: z = M r, p = z
                 precond_any<T>(s, F, F.r, F.z, L);
-                CK(cudaMemcpyAsync(F.p, F.z, sizeof(T) * (size_t)s->geo.ntot, cudaMemcpyDeviceToDevice, s->stream));
+                fcg_setup<T>(s, F, L);
             }
         }
     }
@@ -797,9 +984,12 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     pps_status rc = PPS_OK;
     read_state(s);
     if (!s->h_st->done) {
-        if (s->cfg.krylov == PPS_KRYLOV_CG || s->cfg.krylov == PPS_KRYLOV_FCG) {
+        if (s->cfg.krylov == PPS_KRYLOV_CG) {
             precond_any<double>(s, F, F.r, F.z, L);
             CK(cudaMemcpyAsync(F.p, F.z, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        } else if (s->cfg.krylov == PPS_KRYLOV_FCG) {
+            precond_any<double>(s, F, F.r, F.z, L);
+            fcg_setup<double>(s, F, L);
         }
         rc = run_iterations<double>(s, F, x, PPS_FORM_FP64, L);
     } else {
@@ -858,9 +1048,12 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         }
         if (ref == s->cfg.max_refinements || remaining <= 0) break;
         fill_field<float>(F.e, g.ntot, 0.0f, st);
-        if (s->cfg.krylov == PPS_KRYLOV_CG || s->cfg.krylov == PPS_KRYLOV_FCG) {
+        if (s->cfg.krylov == PPS_KRYLOV_CG) {
             precond_any<float>(s, F, F.r, F.z, L);
             CK(cudaMemcpyAsync(F.p, F.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        } else if (s->cfg.krylov == PPS_KRYLOV_FCG) {
+            precond_any<float>(s, F, F.r, F.z, L);
+            fcg_setup<float>(s, F, L);
         }
         pps_status irc = run_iterations<float>(s, F, F.e, PPS_FORM_MIXED, L);
         const int it = s->h_st->iter;
@@ -930,7 +1123,7 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
     const long long N = s->n_unknowns;
     const int reps = N > (1LL << 24) ? 5 : 20;
     state_init(s->d_st, s->d_hist, 1, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
-    const Coef c = cheb_sweep_coef(s, 0.5, 0.5, 1.0);
+    const Coef c = cheb_sweep_coef(op_coef(g), cheb_of(s), 0.5, 0.5, 1.0);
     double best_us = 1e30;
     for (int ty : kTys)
         for (int cx : kCxs)
@@ -1000,6 +1193,9 @@ pps_status validate(const pps_grid* g, const pps_config* c)
         if (g->bcs[f] != 0 && g->bcs[f] != 1) { set_error("bcs must be 0 (Dirichlet) or 1 (Neumann)"); return PPS_ERR_INVALID_ARG; }
     if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG && c->krylov != PPS_KRYLOV_FCG) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
     if (c->krylov == PPS_KRYLOV_FCG && c->form == PPS_FORM_PARITY_FP64) { set_error("flexible CG has no reference counterpart, so no PARITY form"); return PPS_ERR_UNSUPPORTED; }
+    if (c->krylov == PPS_KRYLOV_FCG)
+        for (int f = 0; f < 6; f++)
+            if (g->bcs[f] != 0) { set_error("flexible CG takes Dirichlet grids only"); return PPS_ERR_UNSUPPORTED; }
     if (c->precond != PPS_PREC_NONE && c->precond != PPS_PREC_CHEBYSHEV) { set_error("unknown precond"); return PPS_ERR_INVALID_ARG; }
     if (c->precond == PPS_PREC_CHEBYSHEV && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
     if (c->maxit < 0 || c->maxit > 100000000) { set_error("maxit out of range"); return PPS_ERR_INVALID_ARG; }
@@ -1507,8 +1703,12 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
         CK(cudaSetDevice(s->device));
         for (float* q : s->dn) cudaFree(q);
         for (float* q : s->dn_e) cudaFree(q);
+        for (float* q : s->dt) cudaFree(q);
+        for (float* q : {s->cY, s->cZ, s->cW}) cudaFree(q);
         s->dn.clear();
         s->dn_e.clear();
+        s->dt.clear();
+        s->cY = s->cZ = s->cW = nullptr;
         s->net = nullptr;
         if (!net) return PPS_OK;   // detach
         if (s->cfg.form == PPS_FORM_PARITY_FP64) {
@@ -1550,8 +1750,40 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
             s->dn.push_back(a);
             s->dn_e.push_back(e);
         }
+        // residuals of the intermediate levels 1..coarsen-1 and the Chebyshev buffers
+        // of the multigrid cycle (sized for level 1)
+        for (int l = 0; l < coarsen; l++) {
+            float* t = nullptr;
+            if (l > 0) {
+                const unet::Dims d = dense_dims(s, l);
+                CK(cudaMalloc((void**)&t, sizeof(float) * (size_t)d.D * d.H * d.W));
+            }
+            s->dt.push_back(t);
+        }
+        if (coarsen >= 2) {
+            const unet::Dims d = dense_dims(s, 1);
+            const size_t n = (size_t)d.D * d.H * d.W;
+            CK(cudaMalloc((void**)&s->cY, sizeof(float) * n));
+            CK(cudaMalloc((void**)&s->cZ, sizeof(float) * n));
+            CK(cudaMalloc((void**)&s->cW, sizeof(float) * n));
+        }
         return PPS_OK;
     });
+}
+
+pps_status pps_set_learned_cycle(pps_solver* s, int fine_degree, int coarse_degree, double ratio)
+{
+    if (!s) return PPS_ERR_INVALID_ARG;
+    const bool fine_ok = fine_degree == 0 || (fine_degree >= 2 && fine_degree <= 64);
+    const bool coarse_ok = coarse_degree == 0 || (coarse_degree >= 2 && coarse_degree <= 64);
+    if (!fine_ok || !coarse_ok || !(ratio > 1.0)) {
+        set_error("smoother degrees 0 or 2..64, ratio > 1");
+        return PPS_ERR_INVALID_ARG;
+    }
+    s->cyc_fine = fine_degree;
+    s->cyc_coarse = coarse_degree;
+    s->cyc_ratio = ratio;
+    return PPS_OK;
 }
 
 pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out)

@@ -44,20 +44,31 @@ void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add
 // Transfers fused with the solver fields (Dirichlet unknowns of Geo g, guard cells
 // zero): dense = r - A z; out = r - A z; x += y; coarse = R(r - A z) (R r when z is
 // null) with the full weighting of restrict2; f += the trilinear prolongation of
-// `coarse` (prolong2's weights).
+// `coarse` (prolong2's weights).  Shape: the z-marching column tiles (cx = 1).
 template <typename T>
 void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s);
 template <typename T>
-void field_residual(const Geo& g, const T* r, const T* z, T* out, cudaStream_t s);
+void field_residual(const Geo& g, const Shape& sh, const T* r, const T* z, T* out, cudaStream_t s);
 template <typename T>
-void field_axpy(const Geo& g, T* x, const T* y, cudaStream_t s);
+void field_axpy(const Geo& g, const Shape& sh, T* x, const T* y, cudaStream_t s);
 template <typename T>
 void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& dc, float* coarse, cudaStream_t s);
 template <typename T>
-void prolong_add_field(const Geo& g, const Dims& dc, const float* coarse, T* f, cudaStream_t s);
-// 2x full-weighting restriction and trilinear prolongation of dense unknown arrays.
+void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s);
+// 2x full-weighting restriction and trilinear prolongation of dense unknown arrays
+// (prolong2_add: fine += P coarse).
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s);
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
+void prolong2_add(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
+
+// Coarse levels of the learned multigrid cycle (dense arrays, zero beyond the edges):
+// W (+)= scale (cc Y + cx (Y[x-1] + Y[x+1]) + cy (..y..) + cz (..z..) + cb B + cw Z);
+// B and Z may be null.
+struct DCoef {
+    float cc, cx, cy, cz, cb, cw, scale;
+};
+void dense_sweep(const Dims& d, const float* Y, const float* B, const float* Z, float* W, const DCoef& c, bool acc,
+                 cudaStream_t s);
 
 }  // namespace unet
 }  // namespace pps

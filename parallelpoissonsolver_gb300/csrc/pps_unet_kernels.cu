@@ -586,25 +586,61 @@ __global__ void k_field_residual_dense(Geo g, const T* __restrict__ r, const T* 
     dense[((long long)k * uy + j) * ux + i] = (float)residual_at<T>(g, r, z, field_at(g, i, j, k), w);
 }
 
-// out = r - A z at the unknowns.
-template <typename T>
-__global__ void k_field_residual(Geo g, const T* __restrict__ r, const T* __restrict__ z, StencilW<T> w,
-                                 T* __restrict__ out)
+// The field kernels below march along z over the column tiles of a Shape (32 x ty
+// columns per block, kchunk planes per thread, one column per thread), like the
+// solver's own z-marching kernels.
+struct ZCol {
+    int i, j, k0, k1;   // column (i, j) of unknowns, planes [k0, k1)
+    long long c;        // field index of (i, j, k0)
+    bool active;
+};
+
+__device__ __forceinline__ ZCol zcolumn(const Geo& g, const Shape& sh)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.hi[0] - g.lo[0]) return;
-    const long long c = field_at(g, i, blockIdx.y, blockIdx.z);
-    out[c] = residual_at<T>(g, r, z, c, w);
+    ZCol q;
+    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
+    q.i = g.lo[0] + bx * 32 + threadIdx.x;
+    q.j = g.lo[1] + by * sh.ty + threadIdx.y;
+    q.k0 = g.lo[2] + blockIdx.y * sh.kchunk;
+    q.k1 = min(q.k0 + sh.kchunk, g.hi[2]);
+    q.active = q.i < g.hi[0] && q.j < g.hi[1];
+    q.c = q.i + g.sj * q.j + g.sk * q.k0;
+    return q;
+}
+
+static dim3 zgrid(const Shape& sh) { return dim3((unsigned)(sh.ntx * sh.nty), (unsigned)sh.nchunks, 1); }
+static dim3 zblock(const Shape& sh) { return dim3(32, (unsigned)sh.ty, 1); }
+
+// out = r - A z at the unknowns (z planes k-1, k, k+1 kept in registers).
+template <typename T>
+__global__ void __launch_bounds__(256) k_field_residual(Geo g, Shape sh, const T* __restrict__ r,
+                                                        const T* __restrict__ z, StencilW<T> w, T* __restrict__ out)
+{
+    const ZCol q = zcolumn(g, sh);
+    if (!q.active) return;
+    const long long sj = g.sj, sk = g.sk;
+    long long c = q.c;
+    T zm = z[c - sk], zc = z[c];
+    for (int k = q.k0; k < q.k1; k++, c += sk) {
+        const T zp = z[c + sk];
+        T a = w.diag * zc;
+        a += w.ix * (z[c - 1] + z[c + 1]);
+        a += w.iy * (z[c - sj] + z[c + sj]);
+        a += w.iz * (zm + zp);
+        out[c] = r[c] - a;
+        zm = zc;
+        zc = zp;
+    }
 }
 
 // x += y at the unknowns.
 template <typename T>
-__global__ void k_field_axpy(Geo g, T* __restrict__ x, const T* __restrict__ y)
+__global__ void __launch_bounds__(256) k_field_axpy(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ y)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.hi[0] - g.lo[0]) return;
-    const long long c = field_at(g, i, blockIdx.y, blockIdx.z);
-    x[c] += y[c];
+    const ZCol q = zcolumn(g, sh);
+    if (!q.active) return;
+    long long c = q.c;
+    for (int k = q.k0; k < q.k1; k++, c += g.sk) x[c] += y[c];
 }
 
 // Full-weighting restriction (the weights of k_restrict: 1/4, 1/2, 1/4 per axis
@@ -701,44 +737,61 @@ __global__ void __launch_bounds__(128) k_field_residual_restrict(Geo g, const T*
 // field unknowns += trilinear prolongation of a coarse dense array with half the
 // unknowns per axis (the weights of k_prolong: fine i takes coarse (i-1)/2 when i
 // is odd, the mean of coarse i/2-1 and i/2 otherwise, zero beyond the grid).
+// Each thread marches its column along z and interpolates every coarse plane in
+// (x, y) once (4 loads), so a fine point costs about 2 coarse loads.
 template <typename T>
-__global__ void k_prolong_add_field(Geo g, Dims dc, const float* __restrict__ coarse, T* __restrict__ f)
+__global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
+                                                           T* __restrict__ f)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-    if (i >= g.hi[0] - g.lo[0]) return;
-    const int idx[3] = {i, j, k};
-    const int ext[3] = {dc.W, dc.H, dc.D};
-    int i0[3], i1[3];
-    float w0[3], w1[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        if (idx[d] & 1) {
-            i0[d] = i1[d] = idx[d] >> 1;
-            w0[d] = 1.0f;
-            w1[d] = 0.0f;
-        } else {
-            i0[d] = (idx[d] >> 1) - 1;
-            i1[d] = idx[d] >> 1;
-            w0[d] = i0[d] >= 0 ? 0.5f : 0.0f;
-            w1[d] = i1[d] < ext[d] ? 0.5f : 0.0f;
-        }
-        if (w0[d] == 0.0f) i0[d] = i1[d];
-        if (w1[d] == 0.0f) i1[d] = i0[d];
+    const ZCol q = zcolumn(g, sh);
+    if (!q.active) return;
+    const int ii = q.i - g.lo[0], jj = q.j - g.lo[1];
+    int xa, xb, ya, yb;   // coarse indices along x and y
+    float wxa, wxb, wya, wyb;
+    if (ii & 1) {
+        xa = xb = ii >> 1;
+        wxa = 1.0f;
+        wxb = 0.0f;
+    } else {
+        xa = (ii >> 1) - 1;
+        xb = ii >> 1;
+        wxa = xa >= 0 ? 0.5f : 0.0f;
+        wxb = 0.5f;
+        if (xa < 0) xa = xb;
     }
-    float s = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-            for (int cc = 0; cc < 2; cc++) {
-                const float wv = (a ? w1[2] : w0[2]) * (b ? w1[1] : w0[1]) * (cc ? w1[0] : w0[0]);
-                if (wv == 0.0f) continue;
-                const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = cc ? i1[0] : i0[0];
-                s += wv * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
-            }
-    const long long c = field_at(g, i, j, k);
-    f[c] += (T)s;
+    if (jj & 1) {
+        ya = yb = jj >> 1;
+        wya = 1.0f;
+        wyb = 0.0f;
+    } else {
+        ya = (jj >> 1) - 1;
+        yb = jj >> 1;
+        wya = ya >= 0 ? 0.5f : 0.0f;
+        wyb = 0.5f;
+        if (ya < 0) ya = yb;
+    }
+    const long long plane = (long long)dc.H * dc.W;
+    const long long oaa = (long long)ya * dc.W + xa, oab = (long long)ya * dc.W + xb;
+    const long long oba = (long long)yb * dc.W + xa, obb = (long long)yb * dc.W + xb;
+    auto interp = [&](int cz) -> float {   // bilinear value of coarse plane cz at this column
+        const float* p = coarse + (long long)cz * plane;
+        return wya * (wxa * p[oaa] + wxb * p[oab]) + wyb * (wxa * p[oba] + wxb * p[obb]);
+    };
+    const int kk0 = q.k0 - g.lo[2], kk1 = q.k1 - g.lo[2];
+    int cz = kk0 >> 1;
+    float vm = cz >= 1 ? interp(cz - 1) : 0.0f;   // coarse planes cz-1 and cz
+    float v0 = interp(cz);
+    long long c = q.c;
+    for (int kk = kk0; kk < kk1; kk++, c += g.sk) {
+        if (!(kk & 1)) {
+            f[c] += (T)(0.5f * (vm + v0));
+        } else {
+            f[c] += (T)v0;
+            vm = v0;
+            cz++;
+            v0 = cz < dc.D ? interp(cz) : 0.0f;
+        }
+    }
 }
 
 template <typename T>
@@ -749,16 +802,15 @@ void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cu
     launches_counter_add(1);
 }
 template <typename T>
-void field_residual(const Geo& g, const T* r, const T* z, T* out, cudaStream_t s)
+void field_residual(const Geo& g, const Shape& sh, const T* r, const T* z, T* out, cudaStream_t s)
 {
-    k_field_residual<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
-        g, r, z, stencil_w<T>(g), out);
+    k_field_residual<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, r, z, stencil_w<T>(g), out);
     launches_counter_add(1);
 }
 template <typename T>
-void field_axpy(const Geo& g, T* x, const T* y, cudaStream_t s)
+void field_axpy(const Geo& g, const Shape& sh, T* x, const T* y, cudaStream_t s)
 {
-    k_field_axpy<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(g, x, y);
+    k_field_axpy<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, x, y);
     launches_counter_add(1);
 }
 template <typename T>
@@ -772,23 +824,73 @@ void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& d
     launches_counter_add(1);
 }
 template <typename T>
-void prolong_add_field(const Geo& g, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
+void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
 {
-    k_prolong_add_field<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
-        g, dc, coarse, f);
+    k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f);
     launches_counter_add(1);
 }
 template void field_residual_dense<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
 template void field_residual_dense<double>(const Geo&, const double*, const double*, float*, cudaStream_t);
-template void field_residual<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
-template void field_residual<double>(const Geo&, const double*, const double*, double*, cudaStream_t);
-template void field_axpy<float>(const Geo&, float*, const float*, cudaStream_t);
-template void field_axpy<double>(const Geo&, double*, const double*, cudaStream_t);
+template void field_residual<float>(const Geo&, const Shape&, const float*, const float*, float*, cudaStream_t);
+template void field_residual<double>(const Geo&, const Shape&, const double*, const double*, double*, cudaStream_t);
+template void field_axpy<float>(const Geo&, const Shape&, float*, const float*, cudaStream_t);
+template void field_axpy<double>(const Geo&, const Shape&, double*, const double*, cudaStream_t);
 template void field_residual_restrict<float>(const Geo&, const float*, const float*, const Dims&, float*, cudaStream_t);
 template void field_residual_restrict<double>(const Geo&, const double*, const double*, const Dims&, float*,
                                               cudaStream_t);
-template void prolong_add_field<float>(const Geo&, const Dims&, const float*, float*, cudaStream_t);
-template void prolong_add_field<double>(const Geo&, const Dims&, const float*, double*, cudaStream_t);
+template void prolong_add_field<float>(const Geo&, const Shape&, const Dims&, const float*, float*, cudaStream_t);
+template void prolong_add_field<double>(const Geo&, const Shape&, const Dims&, const float*, double*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Coarse levels of the learned multigrid cycle: dense [z][y][x] arrays with the
+// Dirichlet zero beyond the array edges.
+// ---------------------------------------------------------------------------
+
+// W (+)= scale * (cc Y + cx (Y[x-1] + Y[x+1]) + cy (Y[y-1] + Y[y+1]) + cz (Y[z-1] + Y[z+1])
+//                 + cb B + cw Z)
+// One sweep of the Chebyshev recurrence (or, with the operator's negated
+// coefficients and cb = 1, the residual B - A Y).  Z may be null (cw unused).
+__global__ void __launch_bounds__(128) k_dense_sweep(Dims d, int kchunk, const float* __restrict__ Y,
+                                                    const float* __restrict__ B, const float* __restrict__ Z,
+                                                    float* __restrict__ W, DCoef c, int acc)
+{
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= d.W || y >= d.H) return;
+    const int z0 = blockIdx.z * kchunk, z1 = min(d.D, z0 + kchunk);
+    const long long sy = d.W, sz = (long long)d.W * d.H;
+    const bool hx0 = x > 0, hx1 = x + 1 < d.W, hy0 = y > 0, hy1 = y + 1 < d.H;
+    long long q = (long long)z0 * sz + (long long)y * sy + x;
+    float ym = z0 > 0 ? Y[q - sz] : 0.0f, yc = Y[q];
+    for (int z = z0; z < z1; z++, q += sz) {
+        const float yp = z + 1 < d.D ? Y[q + sz] : 0.0f;
+        const float sx = (hx0 ? Y[q - 1] : 0.0f) + (hx1 ? Y[q + 1] : 0.0f);
+        const float syy = (hy0 ? Y[q - sy] : 0.0f) + (hy1 ? Y[q + sy] : 0.0f);
+        float v = c.cc * yc;
+        v = fmaf(c.cx, sx, v);
+        v = fmaf(c.cy, syy, v);
+        v = fmaf(c.cz, ym + yp, v);
+        if (B) v = fmaf(c.cb, B[q], v);
+        if (Z) v = fmaf(c.cw, Z[q], v);
+        v *= c.scale;
+        W[q] = acc ? W[q] + v : v;
+        ym = yc;
+        yc = yp;
+    }
+}
+
+void dense_sweep(const Dims& d, const float* Y, const float* B, const float* Z, float* W, const DCoef& c, bool acc,
+                 cudaStream_t s)
+{
+    // 32 x 4 columns per block, z split into chunks for about 16 blocks per SM
+    const int tx = (d.W + 31) / 32, ty = (d.H + 3) / 4;
+    long long chunks = (152LL * 16 + (long long)tx * ty - 1) / ((long long)tx * ty);
+    if (chunks < 1) chunks = 1;
+    if (chunks > d.D) chunks = d.D;
+    const int kchunk = (int)((d.D + chunks - 1) / chunks);
+    const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((d.D + kchunk - 1) / kchunk));
+    k_dense_sweep<<<grid, dim3(32, 4), 0, s>>>(d, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
+    launches_counter_add(1);
+}
 
 // Full-weighting restriction of dense unknown arrays, fine (2m) -> coarse (m) per
 // axis: coarse unknown I sits on fine unknown 2I+1 (0-based), weights 1/4,1/2,1/4
@@ -828,7 +930,7 @@ void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 // Trilinear prolongation, coarse (m) -> fine (2m): fine unknown i takes coarse
 // (i-1)/2 exactly when i is odd (0-based), the mean of its two coarse neighbours
 // otherwise (zero beyond the grid); the transpose of k_restrict up to a factor 8.
-__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine)
+__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine, int add)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     const int Wf = dc.W * 2, Hf = dc.H * 2;
@@ -862,12 +964,19 @@ __global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __re
                 if (w == 0.0f || zz < 0 || yy < 0 || xx < 0 || zz >= dc.D || yy >= dc.H || xx >= dc.W) continue;
                 s += w * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
             }
-    fine[((long long)z * Hf + y) * Wf + x] = s;
+    const long long q = ((long long)z * Hf + y) * Wf + x;
+    fine[q] = add ? fine[q] + s : s;
 }
 
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine);
+    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 0);
+    launches_counter_add(1);
+}
+
+void prolong2_add(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
+{
+    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 1);
     launches_counter_add(1);
 }
 

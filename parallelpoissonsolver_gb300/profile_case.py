@@ -3,12 +3,14 @@
     python -m parallelpoissonsolver_gb300.profile_case --size 320 --form mixed --maxit 2
     python -m parallelpoissonsolver_gb300.profile_case --save-net net.npz          # train the U-Net, save
     python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --maxit 8
+    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 3,4,8 --maxit 20000
 
 Runs `--repeat` solves of the k^-2 random-field workload at `--size`^3 unknowns with
 the iteration cap `--maxit`, so that an ncu capture sees a handful of launches of
 every kernel of the loop on fields larger than L2, and exits 0 whether or not the
 cap stops the solve.  With --learned, the solver is flexible CG with the saved U-Net
-as its coarse-grid correction (as in the benchmark's headline form).
+as its coarse-grid correction (as in the benchmark's headline form); --cycle
+F,C,RATIO selects the multigrid V-cycle with those smoother degrees.
 """
 from __future__ import annotations
 
@@ -29,6 +31,9 @@ def main():
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--save-net", default=None, help="train the 32^3 linear U-Net and save it here, then exit")
     ap.add_argument("--learned", default=None, help="saved U-Net to use as the coarse-grid correction")
+    ap.add_argument("--cycle", default=None, help="fine,coarse,ratio of the multigrid V-cycle (with --learned)")
+    ap.add_argument("--inner-tol", type=float, default=3e-3)
+    ap.add_argument("--refinements", type=int, default=1)
     a = ap.parse_args()
     if a.save_net:
         from parallelpoissonsolver_gb300 import learned
@@ -51,9 +56,13 @@ def main():
         k = int(round(math.log2(a.size / 32)))
         gain = scale * ((2 ** k / (a.size + 1)) / (1.0 / 33)) ** 2
         s = pps.FlexibleCG(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
-                           form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=False)
+                           form=a.form, inner_maxit=a.maxit, max_refinements=a.refinements, use_graph=False,
+                           inner_tol=a.inner_tol)
         s.set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER |
                       pps.LEARNED_POST_SMOOTH | pps.LEARNED_NO_FALLBACK)
+        if a.cycle:
+            fd, cd, ratio = a.cycle.split(",")
+            s.set_learned_cycle(int(fd), int(cd), float(ratio))
     else:
         s = pps.BiCGSTAB(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
                          form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)

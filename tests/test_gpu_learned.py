@@ -141,3 +141,89 @@ def test_learned_cycle_matches_its_composition(gpu, form, m):
     s.close()
     plain.close()
     net.close()
+
+
+def _lap(u, h):
+    """The 7-point operator (u- - 2u + u+)/h^2 per axis, zero beyond the array."""
+    p = np.pad(u, 1)
+    out = -6.0 * u
+    for ax in range(3):
+        sl_m = [slice(1, -1)] * 3
+        sl_p = [slice(1, -1)] * 3
+        sl_m[ax] = slice(0, -2)
+        sl_p[ax] = slice(2, None)
+        out = out + p[tuple(sl_m)] + p[tuple(sl_p)]
+    return out / (h * h)
+
+
+def _cheb_smoother(b, h, ratio, n):
+    """-s_{n-2} of the preconditioner's Chebyshev recurrence on [lmax/ratio, lmax]."""
+    lmax = 12.0 / (h * h)
+    lo = lmax / ratio
+    theta, delta = (lo + lmax) / 2, (lo - lmax) / 2
+    sigma = theta / delta
+    if n == 2:
+        return -b / theta
+    rho_old = 1 / sigma
+    rho = 1 / (2 * sigma - rho_old)
+    s_prev = b / theta
+    s = (2 * rho / delta) * (2 * b + _lap(b, h) / theta)
+    for _ in range(2, n - 1):
+        rho_old, rho = rho, 1 / (2 * sigma - rho)
+        s, s_prev = rho * (2 * sigma * s + (2 / delta) * (b + _lap(s, h))) - rho * rho_old * s_prev, s
+    return -s
+
+
+@pytest.mark.parametrize("form,m,fd,cd", [("fp64", 128, 3, 4), ("fp64", 64, 4, 0), ("mixed", 128, 3, 4)])
+def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
+    """The multigrid form of the learned cycle, rebuilt level by level in numpy:
+    Chebyshev smoothing on [lmax/ratio, lmax] of each level (spacing 2^l h), residual
+    restriction, the network on the coarsest level, prolongation, post-smoothing."""
+    net = pps.UNet((16, 32, 64), seed=4, linear=True)
+    k = int(round(math.log2(m / 32)))
+    gain, ratio = 0.6, 8.0
+    grid = pps.BlockGrid.cube(m)
+    b = learned.rhs(m, 30021, "blobs")
+    s = pps.FlexibleCG(grid, pps.ChebyshevIteration(11), form=form)
+    s.set_learned(net, k, gain, pps.LEARNED_PRECONDITIONER | pps.LEARNED_POST_SMOOTH)
+    s.set_learned_cycle(fd, cd, ratio)
+    got = s.apply_preconditioner(b.copy())
+
+    inner = (slice(2, m + 2),) * 3
+    h = 1.0 / (m + 1)
+    r0 = b[inner].copy()
+
+    def restrict(f):
+        return _along_axes([_restrict_1d(f.shape[0])] * 3, f)
+
+    def prolong(c):
+        return _along_axes([2.0 * _restrict_1d(2 * c.shape[0]).T] * 3, c)
+
+    def network(r):
+        cin = torch.from_numpy(np.ascontiguousarray(r, np.float32)).cuda()
+        cout = torch.empty_like(cin)
+        net.forward(r.shape, cin.data_ptr(), cout.data_ptr(), normalize=True)
+        return gain * cout.cpu().numpy().astype(np.float64)
+
+    X = _cheb_smoother(r0, h, ratio, fd)
+    r = restrict(r0 - _lap(X, h))
+    rs, zs = [None], [None]
+    for lvl in range(1, k):
+        hl = h * 2 ** lvl
+        z = _cheb_smoother(r, hl, ratio, cd) if cd else np.zeros_like(r)
+        rs.append(r)
+        zs.append(z)
+        r = restrict(r - _lap(z, hl)) if cd else restrict(r)
+    e = network(r)
+    for lvl in range(k - 1, 0, -1):
+        hl = h * 2 ** lvl
+        z = zs[lvl] + prolong(e)
+        if cd:
+            z = z + _cheb_smoother(rs[lvl] - _lap(z, hl), hl, ratio, cd)
+        e = z
+    X = X + prolong(e)
+    X = X + _cheb_smoother(r0 - _lap(X, h), h, ratio, fd)
+    tol = 1e-4 if form == "fp64" else 2e-3
+    assert rel_l2(got[inner], X) < tol
+    s.close()
+    net.close()

@@ -301,6 +301,30 @@ def test_flexible_cg_converges(gpu, oracle, form):
     assert abs(s.get_num_iteration_final() - cg.get_num_iteration_final()) <= 3
 
 
+@pytest.mark.parametrize("check_every", [1, 3, 4])
+def test_flexible_cg_graph_replay_matches_direct_launches(gpu, check_every):
+    """Flexible CG alternates its direction fields; graph chunks of any requested
+    length must replay exactly what direct launches compute."""
+    from parallelpoissonsolver_gb300 import workloads
+    m = 48
+    b = workloads.random_field(m, seed=7, slope=-2.0)
+    out = []
+    for graph in (False, True):
+        s = pps.FlexibleCG(pps.BlockGrid.cube(m), pps.ChebyshevIteration(11), tolerance=1e-10, form="fp64",
+                           use_graph=graph, check_every=check_every)
+        x = np.zeros_like(b)
+        assert s(x, b.copy()) == pps.OK
+        out.append((x, s.get_num_iteration_final()))
+        s.close()
+    assert out[0][1] == out[1][1]
+    assert same_bits(out[0][0], out[1][0])
+
+
+def test_flexible_cg_rejects_neumann_grids(gpu):
+    with pytest.raises(pps.PpsError):
+        pps.FlexibleCG(pps.BlockGrid(npglobal=(10, 10, 10), ds=(0.1,) * 3, bcs=(1, 0, 0, 0, 0, 0)), form="fp64")
+
+
 def test_flexible_cg_has_no_parity_form(gpu):
     with pytest.raises(pps.PpsError):
         pps.FlexibleCG(pps.BlockGrid.cube(8), form="parity")
