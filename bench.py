@@ -40,7 +40,7 @@ METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed+learned vs plain FP64), 1
 NET_GRID = 32   # the U-Net runs as the coarse-grid solver on a 32^3 grid
 # multigrid V-cycle of the learned preconditioner: Chebyshev smoother degree on the
 # solver's grid, on the intermediate levels, and the smoothing interval ratio
-VCYCLE = (5, 8, 8.0)
+VCYCLE = (5, 4, 8.0)
 TOL = 1e-10
 DEGREE = 11
 # Iterations the reference BiCGSTAB+Chebyshev(11) needs on this workload, measured by
@@ -167,19 +167,20 @@ def make_inputs(m: int):
     return x, b
 
 
-def train_network(args, dev: int):
+def train_network(args, dev: int, coarsen: int):
     """The learned preconditioner's U-Net: linear 3-level 16/32/64 network trained on
-    32^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs; u solved to 1e-12
-    by the plain FP64 solver) with the library's own kernels; it is the coarse-grid
-    solver of the multigrid V-cycle inside flexible CG."""
+    32^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs) with the library's
+    own kernels; u solves the operator of the multigrid cycle's coarsest level after
+    `coarsen` coarsenings (its upper wall 2^-coarsen spacings above the last unknown),
+    exactly.  The network is that level's solver inside flexible CG."""
     import torch
 
     import parallelpoissonsolver_gb300 as pps
     from parallelpoissonsolver_gb300 import learned
 
     t0 = time.perf_counter()
-    train = learned.make_dataset(NET_GRID, range(10000, 10000 + args.train_samples), device=dev)
-    held = learned.make_dataset(NET_GRID, range(30000, 30000 + 16), device=dev)
+    train = learned.make_dataset(NET_GRID, range(10000, 10000 + args.train_samples), device=dev, coarsen=coarsen)
+    held = learned.make_dataset(NET_GRID, range(30000, 30000 + 16), device=dev, coarsen=coarsen)
     t_data = time.perf_counter() - t0
     scale = learned.fit_scale(train)
     net = pps.UNet((16, 32, 64), seed=1, device=dev, linear=True)
@@ -192,7 +193,7 @@ def train_network(args, dev: int):
             "precision": "BF16 weights/activations, FP32 accumulation (tensor cores)",
             "train_pairs": len(train), "steps": args.train_steps, "final_loss": float(np.mean(losses[-100:])),
             "held_out_rel_err_median": float(np.median(errs)), "held_out_rel_err_max": float(np.max(errs)),
-            "data_s": t_data, "train_s": t_train, "scale": scale}
+            "data_s": t_data, "train_s": t_train, "scale": scale, "coarsen": coarsen}
     return net, scale, info
 
 
@@ -218,9 +219,9 @@ def run_gpu(args, dist: Dist):
     G = b_h.size
     prec = pps.ChebyshevIteration(DEGREE)
 
-    net, scale, net_info = train_network(args, dev)
+    net, scale, net_info = train_network(args, dev, learned_gain(m, 1.0)[0])
     k, gain = learned_gain(m, scale)
-    flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER
+    flags = pps.LEARNED_PRECONDITIONER
     head = pps.FlexibleCG(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
                           inner_tol=args.learned_inner_tol, device=dev)
     head.set_learned(net, k, gain, flags)
@@ -314,9 +315,10 @@ def run_gpu(args, dist: Dist):
                         f"stop at FP64 ||r||/||b_adj|| <= {TOL:g}",
             "form": "mixed+learned: FP64 iterative refinement around FP32 flexible CG (inner tolerance "
                     f"{args.learned_inner_tol:g}); preconditioner = multigrid V-cycle over {k + 1} levels: "
-                    f"Chebyshev({VCYCLE[0]}) smoothing on the {m}^3 grid, Chebyshev({VCYCLE[1]}) pre- and "
-                    f"post-smoothing on each intermediate level (interval [lmax/{VCYCLE[2]:g}, lmax]), the U-Net "
-                    f"as the {NET_GRID}^3 coarse solver; learned initial guess",
+                    f"Chebyshev({VCYCLE[0]}) smoothing on the {m}^3 grid (interval [lmax/{VCYCLE[2]:g}, lmax]), "
+                    f"Jacobi-scaled Chebyshev({VCYCLE[1]}) pre- and post-smoothing on each intermediate level "
+                    f"(interval [2/{VCYCLE[2]:g}, 2] of D^-1 A_l, A_l with the upper wall one fine spacing above "
+                    f"the last unknown), the U-Net trained for that operator as the {NET_GRID}^3 coarse solver",
             "l2": "no flush: every field (0.5-1.1 GB) exceeds the 129 MB L2",
             "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU, single domain",
             "iterations": stats[-1]["iterations"],
@@ -355,16 +357,17 @@ def run_gpu(args, dist: Dist):
         "wall_s_timed_region": wall,
     }
     if not args.no_learned_128:
-        out["learned_128"] = run_learned_128(args, dev, net, scale)
+        out["learned_128"] = run_learned_128(args, dev)
     head.close()
     mixed.close()
     plain.close()
     return out, plain_stats[-1]["iterations"]
 
 
-def run_learned_128(args, dev: int, net, scale: float):
+def run_learned_128(args, dev: int):
     """Learned initial guess and preconditioner at 128^3 on held-out seeds (half k^-2
-    fields, half blobs): flexible CG with the network against the reference method
+    fields, half blobs): flexible CG with the network (two-grid cycle and multigrid
+    V-cycle; the network trained for two coarsenings) against the reference method
     (BiCGSTAB + Chebyshev) and against flexible CG without it, all FP64 to 1e-10."""
     import torch
 
@@ -373,6 +376,7 @@ def run_learned_128(args, dev: int, net, scale: float):
 
     m = 128
     grid = pps.BlockGrid.cube(m)
+    net, scale, _ = train_network(args, dev, learned_gain(m, 1.0)[0])
     k, gain = learned_gain(m, scale)
     forms = {
         "bicgstab": pps.BiCGSTAB(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, form="fp64", device=dev),
@@ -401,6 +405,7 @@ def run_learned_128(args, dev: int, net, scale: float):
             res[n]["err_true"].append(d["err_true"])
     for s in forms.values():
         s.close()
+    net.close()
     out = {"workload": f"{m}^3, Dirichlet 0, {args.held_out} held-out seeds (30000+), FP64 to {TOL:g}"}
     for n, r in res.items():
         out[n] = {"mean_iterations": float(np.mean(r["iterations"])), "mean_seconds": float(np.mean(r["seconds"])),

@@ -269,9 +269,13 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
 /* Multigrid form of the learned preconditioner (no reference counterpart).  With
  * fine_degree >= 2 and coarsen >= 1, each application is a V-cycle over the levels
  * 0..coarsen whose coarsest solver is the network: Chebyshev smoothing on
- * [lambda_max/ratio, lambda_max] of each level's 7-point operator (spacings 2^l ds),
- * full-weighting restriction of the residual, trilinear prolongation of the
- * correction and post-smoothing (on the solver's grid with PPS_LEARNED_POST_SMOOTH).
+ * [lambda_max/ratio, lambda_max] of the solver's operator, full-weighting restriction
+ * of the residual, on each coarse level l a Jacobi-scaled Chebyshev smoother on
+ * [2/ratio, 2] of D^-1 A_l (A_l: the 7-point operator with spacings 2^l ds, whose
+ * upper wall lies one fine spacing above the last unknown, as the coarsening of an
+ * even grid places it; D = -diag A_l), trilinear prolongation of the correction and
+ * post-smoothing (on the solver's grid with PPS_LEARNED_POST_SMOOTH).  The network
+ * should be trained for the coarsest level's operator.
  * Degrees count as cheb_degree does (the recurrence's output is s_{n-2}):
  * fine_degree on the solver's grid, coarse_degree on levels 1..coarsen-1 (0: no
  * smoothing there).  fine_degree = 0 (the default) keeps the two-grid cycle around

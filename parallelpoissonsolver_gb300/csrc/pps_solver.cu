@@ -615,68 +615,71 @@ void learned_coarse_correction(pps_solver* s, const T* r, const T* z, T* X)
     s->learned_apps++;
 }
 
-unet::DCoef dcoef(const Coef& c)
+// Operator of coarse level l (2^l times the solver's spacing, the upper wall one
+// fine spacing above the last unknown of each axis).
+unet::DLevel level_op(const pps_solver* s, int l)
 {
-    return unet::DCoef{(float)c.cc, (float)c.cx, (float)c.cy, (float)c.cz, (float)c.cb, (float)c.cw, (float)c.scale};
+    unet::DLevel L;
+    for (int d = 0; d < 3; d++) {
+        const double h = s->geo.ds[d], H = h * (double)(1 << l);
+        L.ih2[d] = (float)(1.0 / (H * H));
+        L.last_m[d] = (float)(2.0 / (H * (H + h)));
+        L.last_c[d] = (float)(-2.0 / (H * h));
+    }
+    return L;
 }
 
-// Spacings of level l (2^l times the solver's).
-void level_ds(const pps_solver* s, int l, double ds[3])
-{
-    for (int d = 0; d < 3; d++) ds[d] = s->geo.ds[d] * (double)(1 << l);
-}
-
-// out = b - A_l z on dense level l (A_l: the 7-point operator with level-l spacings).
+// out = b - A_l z on coarse level l.
 void dense_residual(pps_solver* s, int l, const float* b, const float* z, float* out)
 {
-    double ds[3];
-    level_ds(s, l, ds);
-    Coef a = op_coef_ds(ds);
-    const Coef r{-a.cc, -a.cx, -a.cy, -a.cz, 1.0, 0.0, 1.0};
-    unet::dense_sweep(dense_dims(s, l), z, b, nullptr, out, dcoef(r), false, s->stream);
+    unet::level_residual(dense_dims(s, l), level_op(s, l), z, b, out, s->stream);
 }
 
-// X (+)= -s_{n-2}: the Chebyshev smoother of dense level l on B (the recurrence of
-// fast_cheb, on [lambda_max/ratio, lambda_max] of A_l).
+// X (+)= -s_{n-2} on coarse level l: the preconditioner's Chebyshev recurrence applied
+// to the Jacobi-scaled operator D^-1 A_l (D = -diag A_l), whose spectrum lies in
+// (0, 2]; smoothing interval [2/ratio, 2].  The scaling absorbs the larger diagonal
+// of the unknowns next to the upper wall.
 void dense_cheb(pps_solver* s, int l, const float* B, float* X, bool acc)
 {
-    double ds[3];
-    level_ds(s, l, ds);
-    const Coef a = op_coef_ds(ds);
-    const ChebP p = smoother_of(ds, s->cyc_ratio, s->cyc_coarse);
+    const unet::DLevel L = level_op(s, l);
     const unet::Dims d = dense_dims(s, l);
     cudaStream_t st = s->stream;
-    const int n = p.n;
+    const int n = s->cyc_coarse;
+    const double hi = 2.0, lo = 2.0 / s->cyc_ratio;
+    const double theta = 0.5 * (lo + hi), delta = 0.5 * (lo - hi), sigma = theta / delta;
+    const float y0 = (float)(1.0 / theta);
     if (n == 2) {
-        const Coef c{1.0 / p.theta, 0, 0, 0, 0, 0, -1.0};
-        unet::dense_sweep(d, B, nullptr, nullptr, X, dcoef(c), acc, st);
+        unet::level_cheb(d, L, nullptr, B, nullptr, X, unet::LCoef{1.0f, 0.0f, 0.0f, 0.0f, -1.0f, y0}, true, acc, st);
         return;
     }
-    double rhoOld = 1 / p.sigma;
-    double rhoCurr = 1 / (2 * p.sigma - rhoOld);
-    Coef c01 = cheb_s01_coef(a, p, rhoCurr);
+    double rhoOld = 1 / sigma;
+    double rhoCurr = 1 / (2 * sigma - rhoOld);
+    // s1 = rho1 (2 sigma s0 + 2/delta D^-1 (B + A s0)), s0 = D^-1 B / theta
+    const float t1 = (float)(rhoCurr * 2.0 / delta);
+    const unet::LCoef c1{(float)(rhoCurr * 2.0 * sigma), t1, t1, 0.0f, n == 3 ? -1.0f : 1.0f, y0};
     if (n == 3) {
-        c01.scale = -1.0;
-        unet::dense_sweep(d, B, nullptr, nullptr, X, dcoef(c01), acc, st);
+        unet::level_cheb(d, L, nullptr, B, nullptr, X, c1, true, acc, st);
         return;
     }
     float *Y = s->cY, *Z = s->cZ, *W = s->cW;
-    unet::dense_sweep(d, B, nullptr, nullptr, Y, dcoef(c01), false, st);
+    unet::level_cheb(d, L, nullptr, B, nullptr, Y, c1, true, false, st);
     for (int it = 2; it <= n - 2; it++) {
         rhoOld = rhoCurr;
-        rhoCurr = 1 / (2 * p.sigma - rhoOld);
+        rhoCurr = 1 / (2 * sigma - rhoOld);
         const bool last = (it == n - 2), first = (it == 2);
-        Coef c = cheb_sweep_coef(a, p, rhoCurr, rhoOld, last ? -1.0 : 1.0);
-        if (first) {
-            c.cb += c.cw / p.theta;
-            c.cw = 0.0;
+        const double t = rhoCurr * 2.0 / delta;
+        double cb = t, cz = -rhoCurr * rhoOld;
+        if (first) {   // Z = s0 = D^-1 B / theta: fold it into the B term
+            cb += cz / theta;
+            cz = 0.0;
         }
-        unet::dense_sweep(d, Y, B, first ? nullptr : Z, last ? X : W, dcoef(c), last && acc, st);
+        const unet::LCoef c{(float)(rhoCurr * 2.0 * sigma), (float)cb, (float)t, (float)cz, last ? -1.0f : 1.0f, y0};
+        unet::level_cheb(d, L, Y, B, first ? nullptr : Z, last ? X : W, c, false, last && acc, st);
         if (!last) {
-            float* t = Z;
+            float* tmp = Z;
             Z = Y;
             Y = W;
-            W = t;
+            W = tmp;
         }
     }
 }

@@ -61,14 +61,27 @@ void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
 void prolong2_add(const Dims& dc, const float* coarse, float* fine, cudaStream_t s);
 
-// Coarse levels of the learned multigrid cycle (dense arrays, zero beyond the edges):
-// W (+)= scale (cc Y + cx (Y[x-1] + Y[x+1]) + cy (..y..) + cz (..z..) + cb B + cw Z);
-// B and Z may be null.
-struct DCoef {
-    float cc, cx, cy, cz, cb, cw, scale;
+// Coarse levels of the learned multigrid cycle.  Level l of an even fine grid puts
+// its unknown c on the fine position 2^l (c+1) h: spacing H = 2^l h, the lower wall
+// H below the first unknown, the upper wall only h above the last one.  The level
+// operator is the 7-point second difference with that gap on the upper side: at the
+// last unknown of an axis the lower neighbour weighs 2/(H (H+h)) and the centre
+// -2/(H h) (the non-uniform three-point formula, wall value 0).
+struct DLevel {
+    float ih2[3];      // 1/H_d^2
+    float last_m[3];   // 2/(H_d (H_d + h_d))
+    float last_c[3];   // -2/(H_d h_d)
 };
-void dense_sweep(const Dims& d, const float* Y, const float* B, const float* Z, float* W, const DCoef& c, bool acc,
-                 cudaStream_t s);
+// Jacobi-scaled Chebyshev step coefficients, D = -diag(A):
+// W (+)= scale (cy Y + D^-1 (cb B + ca A Y) + cz Z); y0 = 1/theta scales D^-1 B into
+// the starting term when `first`.
+struct LCoef {
+    float cy, cb, ca, cz, scale, y0;
+};
+// W = B - A Y on the level
+void level_residual(const Dims& d, const DLevel& L, const float* Y, const float* B, float* W, cudaStream_t s);
+void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, const float* Z, float* W,
+                const LCoef& c, bool first, bool acc, cudaStream_t s);
 
 }  // namespace unet
 }  // namespace pps

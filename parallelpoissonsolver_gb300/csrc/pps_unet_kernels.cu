@@ -846,49 +846,97 @@ template void prolong_add_field<double>(const Geo&, const Shape&, const Dims&, c
 // Dirichlet zero beyond the array edges.
 // ---------------------------------------------------------------------------
 
-// W (+)= scale * (cc Y + cx (Y[x-1] + Y[x+1]) + cy (Y[y-1] + Y[y+1]) + cz (Y[z-1] + Y[z+1])
-//                 + cb B + cw Z)
-// One sweep of the Chebyshev recurrence (or, with the operator's negated
-// coefficients and cb = 1, the residual B - A Y).  Z may be null (cw unused).
-__global__ void __launch_bounds__(128) k_dense_sweep(Dims d, int kchunk, const float* __restrict__ Y,
+__device__ __forceinline__ float level_diag(const DLevel& L, bool lx, bool ly, bool lz)
+{
+    return (lx ? L.last_c[0] : -2.0f * L.ih2[0]) + (ly ? L.last_c[1] : -2.0f * L.ih2[1]) +
+           (lz ? L.last_c[2] : -2.0f * L.ih2[2]);
+}
+
+// One pass over a coarse level, z-marching:
+//   RESID:  W = B - A Y
+//   CHEB:   W (+)= scale (cy Y + D^-1 (cb B + ca A Y) + cz Z)     (Z may be null)
+// with D = -diag(A).  With `first`, Y is not read: its values are D^-1 B / theta
+// (the recurrence's starting term), formed at each of the 7 points on the fly.
+template <bool CHEB>
+__global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk, const float* __restrict__ Y,
                                                     const float* __restrict__ B, const float* __restrict__ Z,
-                                                    float* __restrict__ W, DCoef c, int acc)
+                                                    float* __restrict__ W, LCoef c, int first, int acc)
 {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= d.W || y >= d.H) return;
     const int z0 = blockIdx.z * kchunk, z1 = min(d.D, z0 + kchunk);
     const long long sy = d.W, sz = (long long)d.W * d.H;
     const bool hx0 = x > 0, hx1 = x + 1 < d.W, hy0 = y > 0, hy1 = y + 1 < d.H;
+    const bool lx = x == d.W - 1, ly = y == d.H - 1;
+    // the axis coefficients at this column: lower and upper neighbour weights
+    const float wxm = lx ? L.last_m[0] : L.ih2[0], wxp = lx ? 0.0f : L.ih2[0];
+    const float wym = ly ? L.last_m[1] : L.ih2[1], wyp = ly ? 0.0f : L.ih2[1];
+    // D^-1 of the x/y neighbours (only used when `first`): their last-flags differ in one axis
+    auto yval = [&](long long q, bool fx, bool fy, bool fz) -> float {
+        if (!first) return Y[q];
+        return B[q] * c.y0 / (-level_diag(L, fx, fy, fz));
+    };
     long long q = (long long)z0 * sz + (long long)y * sy + x;
-    float ym = z0 > 0 ? Y[q - sz] : 0.0f, yc = Y[q];
+    float ym = z0 > 0 ? yval(q - sz, lx, ly, z0 - 1 == d.D - 1) : 0.0f;
+    float yc = yval(q, lx, ly, z0 == d.D - 1);
     for (int z = z0; z < z1; z++, q += sz) {
-        const float yp = z + 1 < d.D ? Y[q + sz] : 0.0f;
-        const float sx = (hx0 ? Y[q - 1] : 0.0f) + (hx1 ? Y[q + 1] : 0.0f);
-        const float syy = (hy0 ? Y[q - sy] : 0.0f) + (hy1 ? Y[q + sy] : 0.0f);
-        float v = c.cc * yc;
-        v = fmaf(c.cx, sx, v);
-        v = fmaf(c.cy, syy, v);
-        v = fmaf(c.cz, ym + yp, v);
-        if (B) v = fmaf(c.cb, B[q], v);
-        if (Z) v = fmaf(c.cw, Z[q], v);
-        v *= c.scale;
+        const bool lz = z == d.D - 1;
+        const float yp = z + 1 < d.D ? yval(q + sz, lx, ly, z + 1 == d.D - 1) : 0.0f;
+        const float xm = hx0 ? yval(q - 1, x - 1 == d.W - 1, ly, lz) : 0.0f;
+        const float xp = hx1 ? yval(q + 1, x + 1 == d.W - 1, ly, lz) : 0.0f;
+        const float ymn = hy0 ? yval(q - sy, lx, y - 1 == d.H - 1, lz) : 0.0f;
+        const float ypn = hy1 ? yval(q + sy, lx, y + 1 == d.H - 1, lz) : 0.0f;
+        const float wzm = lz ? L.last_m[2] : L.ih2[2], wzp = lz ? 0.0f : L.ih2[2];
+        const float dg = level_diag(L, lx, ly, lz);
+        float ay = dg * yc;
+        ay = fmaf(wxm, xm, ay);
+        ay = fmaf(wxp, xp, ay);
+        ay = fmaf(wym, ymn, ay);
+        ay = fmaf(wyp, ypn, ay);
+        ay = fmaf(wzm, ym, ay);
+        ay = fmaf(wzp, yp, ay);
+        const float b = B[q];
+        float v;
+        if (CHEB) {
+            v = c.cy * yc + fmaf(c.cb, b, c.ca * ay) / (-dg);
+            if (Z) v = fmaf(c.cz, Z[q], v);
+            v *= c.scale;
+        } else {
+            v = b - ay;
+        }
         W[q] = acc ? W[q] + v : v;
         ym = yc;
         yc = yp;
     }
 }
 
-void dense_sweep(const Dims& d, const float* Y, const float* B, const float* Z, float* W, const DCoef& c, bool acc,
-                 cudaStream_t s)
+static void level_launch(const Dims& d, int& kchunk, dim3& grid)
 {
     // 32 x 4 columns per block, z split into chunks for about 16 blocks per SM
     const int tx = (d.W + 31) / 32, ty = (d.H + 3) / 4;
     long long chunks = (152LL * 16 + (long long)tx * ty - 1) / ((long long)tx * ty);
     if (chunks < 1) chunks = 1;
     if (chunks > d.D) chunks = d.D;
-    const int kchunk = (int)((d.D + chunks - 1) / chunks);
-    const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((d.D + kchunk - 1) / kchunk));
-    k_dense_sweep<<<grid, dim3(32, 4), 0, s>>>(d, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
+    kchunk = (int)((d.D + chunks - 1) / chunks);
+    grid = dim3((unsigned)tx, (unsigned)ty, (unsigned)((d.D + kchunk - 1) / kchunk));
+}
+
+void level_residual(const Dims& d, const DLevel& L, const float* Y, const float* B, float* W, cudaStream_t s)
+{
+    int kchunk;
+    dim3 grid;
+    level_launch(d, kchunk, grid);
+    k_level_pass<false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, 0, 0);
+    launches_counter_add(1);
+}
+
+void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, const float* Z, float* W,
+                const LCoef& c, bool first, bool acc, cudaStream_t s)
+{
+    int kchunk;
+    dim3 grid;
+    level_launch(d, kchunk, grid);
+    k_level_pass<true><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, first ? 1 : 0, acc ? 1 : 0);
     launches_counter_add(1);
 }
 

@@ -1,11 +1,14 @@
 """Training pipeline of the learned preconditioner.
 
 (f, u) pairs: f is a seeded k^-2 Gaussian random field or a sum of 1-8 Gaussian
-blobs, u the solution of -lap u = f with Dirichlet zero boundaries, solved by the
-plain FP64 GPU solver to ||r||/||b|| <= 1e-12.  The network learns the map from
-b = -f (scaled to unit RMS) to u / (rms(b) * S), S a dataset-wide scale, so that
-gain = S turns its output back into a solution: u ~ S * rms(b) * N(b / rms(b)).
-Training and inference run on the library's own kernels (pps_unet_*).
+blobs, u the solution of -lap u = f with Dirichlet zero boundaries.  Two operators:
+the solver's own grid (u from the plain FP64 GPU solver to ||r||/||b|| <= 1e-12), or,
+for the coarsest level of the multigrid cycle after k coarsenings of an even grid,
+the level operator whose upper wall sits 2^-k spacings above the last unknown (u
+from an exact tensor-product eigen-solve).  The network learns the map from b = -f
+(scaled to unit RMS) to u / (rms(b) * S), S a dataset-wide scale, so that gain = S
+turns its output back into a solution: u ~ S * rms(b) * N(b / rms(b)).  Training
+and inference run on the library's own kernels (pps_unet_*).
 """
 from __future__ import annotations
 
@@ -23,10 +26,54 @@ def rhs(m: int, seed: int, kind: str) -> np.ndarray:
     return workloads.blobs(m, seed)
 
 
-def make_dataset(m: int, seeds, device: int = 0, tol: float = 1e-12):
-    """List of (b, u) dense float32 CUDA tensors of the m^3 unknowns; even seeds are
-    random fields, odd seeds blobs."""
+def level_operator_1d(n: int, gap: float) -> np.ndarray:
+    """Second difference at unit spacing on n unknowns, the lower wall one spacing
+    below the first unknown and the upper wall `gap` spacings above the last (the
+    three-point formula for unequal spacings there); gap = 1 is the uniform grid."""
+    t = np.zeros((n, n))
+    for i in range(n):
+        t[i, i] = -2.0
+        if i > 0:
+            t[i, i - 1] = 1.0
+        if i + 1 < n:
+            t[i, i + 1] = 1.0
+    t[n - 1, n - 2] = 2.0 / (1.0 + gap) if n > 1 else 0.0
+    t[n - 1, n - 1] = -2.0 / gap
+    return t
+
+
+def level_solve(b, h: float, gap: float):
+    """u with A u = b on an n^3 cube, A the sum over axes of level_operator_1d / h^2;
+    b: (..., n, n, n) float64 torch tensor.  Exact: the 1-D operator is diagonalisable
+    (tridiagonal with positive off-diagonal products), so A is in the tensor basis."""
     import torch
+    n = b.shape[-1]
+    w, v = np.linalg.eig(level_operator_1d(n, gap))
+    w, v = w.real, v.real
+    vi = np.linalg.inv(v)
+    V = torch.from_numpy(v).to(b)
+    Vi = torch.from_numpy(vi).to(b)
+    lam = torch.from_numpy(w).to(b) / (h * h)
+    bt = torch.einsum("ai,bj,ck,...ijk->...abc", Vi, Vi, Vi, b)
+    den = lam[:, None, None] + lam[None, :, None] + lam[None, None, :]
+    return torch.einsum("ai,bj,ck,...ijk->...abc", V, V, V, bt / den)
+
+
+def make_dataset(m: int, seeds, device: int = 0, tol: float = 1e-12, coarsen: int | None = None):
+    """List of (b, u) dense float32 CUDA tensors of the m^3 unknowns; even seeds are
+    random fields, odd seeds blobs.  With `coarsen` = k, u solves the coarse-level
+    operator of k coarsenings (upper wall 2^-k spacings above the last unknown)."""
+    import torch
+    if coarsen is not None:
+        out = []
+        inner = (slice(2, m + 2),) * 3
+        h = 1.0 / (m + 1)
+        for sd in seeds:
+            b = torch.from_numpy(np.ascontiguousarray(rhs(m, int(sd), "field" if sd % 2 == 0 else "blobs")[inner]))
+            bd = b.cuda(device)
+            u = level_solve(bd, h, 2.0 ** (-coarsen))
+            out.append((bd.float().contiguous(), u.float().contiguous()))
+        return out
     grid = pps.BlockGrid.cube(m)
     solver = pps.BiCGSTAB(grid, pps.ChebyshevIteration(11), tolerance=tol, max_iteration=20000, form="fp64",
                           device=device)

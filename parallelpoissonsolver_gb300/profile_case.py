@@ -3,7 +3,8 @@
     python -m parallelpoissonsolver_gb300.profile_case --size 320 --form mixed --maxit 2
     python -m parallelpoissonsolver_gb300.profile_case --save-net net.npz          # train the U-Net, save
     python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --maxit 8
-    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 3,4,8 --maxit 20000
+    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 5,8,8 --maxit 20000 \
+        --refinements 12 --inner-tol 3e-4
 
 Runs `--repeat` solves of the k^-2 random-field workload at `--size`^3 unknowns with
 the iteration cap `--maxit`, so that an ncu capture sees a handful of launches of
@@ -30,14 +31,16 @@ def main():
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--save-net", default=None, help="train the 32^3 linear U-Net and save it here, then exit")
+    ap.add_argument("--coarsen", type=int, default=4, help="coarsenings whose coarsest-level operator --save-net learns")
     ap.add_argument("--learned", default=None, help="saved U-Net to use as the coarse-grid correction")
     ap.add_argument("--cycle", default=None, help="fine,coarse,ratio of the multigrid V-cycle (with --learned)")
     ap.add_argument("--inner-tol", type=float, default=3e-3)
+    ap.add_argument("--post-smooth", action="store_true", help="Chebyshev post-smoothing on the solver's grid")
     ap.add_argument("--refinements", type=int, default=1)
     a = ap.parse_args()
     if a.save_net:
         from parallelpoissonsolver_gb300 import learned
-        train = learned.make_dataset(32, range(10000, 10256))
+        train = learned.make_dataset(32, range(10000, 10256), coarsen=a.coarsen)
         scale = learned.fit_scale(train)
         net = pps.UNet((16, 32, 64), seed=1, linear=True)
         learned.train(net, train, scale, 4000, lr=1e-3)
@@ -58,8 +61,10 @@ def main():
         s = pps.FlexibleCG(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
                            form=a.form, inner_maxit=a.maxit, max_refinements=a.refinements, use_graph=False,
                            inner_tol=a.inner_tol)
-        s.set_learned(net, k, gain, pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER |
-                      pps.LEARNED_POST_SMOOTH | pps.LEARNED_NO_FALLBACK)
+        flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER | pps.LEARNED_NO_FALLBACK
+        if a.post_smooth or not a.cycle:
+            flags |= pps.LEARNED_POST_SMOOTH
+        s.set_learned(net, k, gain, flags)
         if a.cycle:
             fd, cd, ratio = a.cycle.split(",")
             s.set_learned_cycle(int(fd), int(cd), float(ratio))

@@ -174,11 +174,57 @@ def _cheb_smoother(b, h, ratio, n):
     return -s
 
 
+def _level_lap(u, H, h):
+    """The coarse-level operator: spacing H, lower wall H below the first unknown,
+    upper wall h above the last (weights 2/(H(H+h)) and -2/(Hh) there)."""
+    out = _lap(u, H)
+    for ax in range(3):
+        last = [slice(None)] * 3
+        prev = [slice(None)] * 3
+        last[ax] = -1
+        prev[ax] = -2
+        out[tuple(last)] += (2.0 / (H * (H + h)) - 1.0 / (H * H)) * u[tuple(prev)] \
+            + (-2.0 / (H * h) + 2.0 / (H * H)) * u[tuple(last)]
+    return out
+
+
+def _level_diag(shape, H, h):
+    d = np.zeros(shape)
+    for ax in range(3):
+        c = np.full(shape[ax], 2.0 / (H * H))
+        c[-1] = 2.0 / (H * h)
+        sh = [1, 1, 1]
+        sh[ax] = shape[ax]
+        d = d + c.reshape(sh)
+    return d
+
+
+def _jacobi_cheb(b, H, h, ratio, n):
+    """-s_{n-2} of the Chebyshev recurrence on D^-1 A (D = -diag A) over [2/ratio, 2]."""
+    dinv = 1.0 / _level_diag(b.shape, H, h)
+    lo, hi = 2.0 / ratio, 2.0
+    theta, delta = (lo + hi) / 2, (lo - hi) / 2
+    sigma = theta / delta
+    bb = dinv * b
+    if n == 2:
+        return -bb / theta
+    rho_old = 1 / sigma
+    rho = 1 / (2 * sigma - rho_old)
+    s_prev = bb / theta
+    s = rho * (2 * sigma * s_prev + (2 / delta) * dinv * (b + _level_lap(s_prev, H, h)))
+    for _ in range(2, n - 1):
+        rho_old, rho = rho, 1 / (2 * sigma - rho)
+        s, s_prev = rho * (2 * sigma * s + (2 / delta) * dinv * (b + _level_lap(s, H, h))) - rho * rho_old * s_prev, s
+    return -s
+
+
 @pytest.mark.parametrize("form,m,fd,cd", [("fp64", 128, 3, 4), ("fp64", 64, 4, 0), ("mixed", 128, 3, 4)])
 def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
     """The multigrid form of the learned cycle, rebuilt level by level in numpy:
-    Chebyshev smoothing on [lmax/ratio, lmax] of each level (spacing 2^l h), residual
-    restriction, the network on the coarsest level, prolongation, post-smoothing."""
+    Chebyshev smoothing on [lmax/ratio, lmax] of the solver's grid, Jacobi-scaled
+    Chebyshev on the coarse levels (spacing 2^l h, upper wall h above the last
+    unknown), residual restriction, the network on the coarsest level, prolongation,
+    post-smoothing."""
     net = pps.UNet((16, 32, 64), seed=4, linear=True)
     k = int(round(math.log2(m / 32)))
     gain, ratio = 0.6, 8.0
@@ -210,16 +256,16 @@ def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
     rs, zs = [None], [None]
     for lvl in range(1, k):
         hl = h * 2 ** lvl
-        z = _cheb_smoother(r, hl, ratio, cd) if cd else np.zeros_like(r)
+        z = _jacobi_cheb(r, hl, h, ratio, cd) if cd else np.zeros_like(r)
         rs.append(r)
         zs.append(z)
-        r = restrict(r - _lap(z, hl)) if cd else restrict(r)
+        r = restrict(r - _level_lap(z, hl, h)) if cd else restrict(r)
     e = network(r)
     for lvl in range(k - 1, 0, -1):
         hl = h * 2 ** lvl
         z = zs[lvl] + prolong(e)
         if cd:
-            z = z + _cheb_smoother(rs[lvl] - _lap(z, hl), hl, ratio, cd)
+            z = z + _jacobi_cheb(rs[lvl] - _level_lap(z, hl, h), hl, h, ratio, cd)
         e = z
     X = X + prolong(e)
     X = X + _cheb_smoother(r0 - _lap(X, h), h, ratio, fd)
