@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time to ||r||/||b|| <= 1e-10 at 512^3 (mixed+learned vs plain FP64), 1 GB300"
-NET_GRID = 32   # the U-Net runs as the coarse-grid solver on a 32^3 grid
+NET_GRID = 16   # the U-Net runs as the coarsest-level solver on a 16^3 grid
 # multigrid V-cycle of the learned preconditioner: Chebyshev smoother degree on the
 # solver's grid, on the intermediate levels, and the smoothing interval ratio
 VCYCLE = (5, 4, 8.0)
@@ -169,7 +169,7 @@ def make_inputs(m: int):
 
 def train_network(args, dev: int, coarsen: int):
     """The learned preconditioner's U-Net: linear 3-level 16/32/64 network trained on
-    32^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs) with the library's
+    16^3 (f, u) pairs (half k^-2 random fields, half Gaussian blobs) with the library's
     own kernels; u solves the operator of the multigrid cycle's coarsest level after
     `coarsen` coarsenings (its upper wall 2^-coarsen spacings above the last unknown),
     exactly.  The network is that level's solver inside flexible CG."""
@@ -198,7 +198,7 @@ def train_network(args, dev: int, coarsen: int):
 
 
 def learned_gain(m: int, scale: float):
-    """(coarsening levels, output gain) to use the 32^3 network on an m^3 grid."""
+    """(coarsening levels, output gain) to use the NET_GRID^3 network on an m^3 grid."""
     import math
     k = int(round(math.log2(m / NET_GRID)))
     return k, scale * ((2 ** k / (m + 1)) / (1.0 / (NET_GRID + 1))) ** 2
@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=3e-3)
-    ap.add_argument("--learned-inner-tol", type=float, default=3e-4)
+    ap.add_argument("--learned-inner-tol", type=float, default=1e-5)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=16)

@@ -207,6 +207,13 @@ void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T
 template <typename T>
 void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
                         RedCtx rc, cudaStream_t s);
+// The same updates and sums over the whole padded array in 16-byte vectors (fields
+// zero on the guard cells, 16-byte aligned).
+template <typename T>
+void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+                             cudaStream_t s);
+template <typename T>
+void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s);
 
 // FP64 true residual r = b - A x written as TR (also into r0 and p when given),
 // with sum r^2 in FP64.

@@ -1142,39 +1142,134 @@ __global__ void __launch_bounds__(256) k_fcg_dot(Geo g, Shape sh, const T* __res
     reduce_finalize<3>(v, rc);
 }
 
+// Flexible CG over the whole padded array in 16-byte vectors.  Every flexible-CG
+// work field is zero on the guard cells (allocated zeroed, written only at the
+// unknowns, Dirichlet grids only), so x += alpha*0 leaves the guard cells of x as
+// they are and they add nothing to the sums.  The caller checks 16-byte alignment.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    typedef float4 type;
+    static constexpr int n = 4;
+    __device__ static float& at(float4& v, int i) { return (&v.x)[i]; }
+};
+template <>
+struct Vec16<double> {
+    typedef double2 type;
+    static constexpr int n = 2;
+    __device__ static double& at(double2& v, int i) { return (&v.x)[i]; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_update_xr_flat(long long n, T* __restrict__ x, const T* __restrict__ p,
+                                                            T* __restrict__ r, const T* __restrict__ Ap,
+                                                            const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    typedef Vec16<T> VT;
+    typedef typename VT::type V;
+    const T a = (T)st->alpha;
+    const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        V xv = reinterpret_cast<const V*>(x)[i], rv = reinterpret_cast<const V*>(r)[i];
+        V pv = reinterpret_cast<const V*>(p)[i], av = reinterpret_cast<const V*>(Ap)[i];
+#pragma unroll
+        for (int e = 0; e < VT::n; e++) {
+            VT::at(xv, e) = fmx(a, VT::at(pv, e), VT::at(xv, e));
+            VT::at(rv, e) = fmx(-a, VT::at(av, e), VT::at(rv, e));
+        }
+        reinterpret_cast<V*>(x)[i] = xv;
+        reinterpret_cast<V*>(r)[i] = rv;
+    }
+    for (long long i = nv * VT::n + t0; i < n; i += stride) {
+        x[i] = fmx(a, p[i], x[i]);
+        r[i] = fmx(-a, Ap[i], r[i]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_dot_flat(long long n, const T* __restrict__ r, const T* __restrict__ z,
+                                                      const T* __restrict__ Ap, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    typedef Vec16<T> VT;
+    typedef typename VT::type V;
+    Acc<T> a1, a2, a3;
+    const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        V rv = reinterpret_cast<const V*>(r)[i], zv = reinterpret_cast<const V*>(z)[i];
+        V av;
+        if (Ap) av = reinterpret_cast<const V*>(Ap)[i];
+#pragma unroll
+        for (int e = 0; e < VT::n; e++) {
+            a1.add(VT::at(zv, e), VT::at(rv, e));
+            if (Ap) a2.add(VT::at(zv, e), VT::at(av, e));
+            a3.add(VT::at(rv, e), VT::at(rv, e));
+        }
+    }
+    for (long long i = nv * VT::n + t0; i < n; i += stride) {
+        a1.add(z[i], r[i]);
+        if (Ap) a2.add(z[i], Ap[i]);
+        a3.add(r[i], r[i]);
+    }
+    double v[3] = {a1.value(), a2.value(), a3.value()};
+    reduce_finalize<3>(v, rc);
+}
+
 // r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
 // stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
-template <typename TR>
+__device__ __forceinline__ unsigned long long bits_of(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+// ISO: equal spacings on the three axes, so the six neighbours share one weight
+// (GB300 runs FP64 at 1/64 of the FP32 rate, and this kernel is bound by it).  The
+// sum of squares of the stored value accumulates in double-float for TR = float.
+template <typename TR, bool ISO>
 __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double* __restrict__ x,
                                                   const double* __restrict__ b, TR* __restrict__ r,
                                                   TR* __restrict__ r0, TR* __restrict__ p, Coef cf, RedCtx rc)
 {
     const Col q = column(g, sh);
-    double s = 0.0;
+    Acc<TR> acc;
     if (q.active) {
         const long long sj = g.sj, sk = g.sk;
         long long c = q.c;
         double um = x[c - sk], uc = x[c];
         for (int k = q.k0; k < q.k1; k++) {
             const double up = x[c + sk];
-            const double sx = x[c - 1] + x[c + 1];
-            const double sy = x[c - sj] + x[c + sj];
-            double a = cf.cc * uc;
-            a = fmx(cf.cx, sx, a);
-            a = fmx(cf.cy, sy, a);
-            a = fmx(cf.cz, um + up, a);
-            const double rv = b[c] - a;
+            const double xw = x[c - 1], xe = x[c + 1], xs = x[c - sj], xn = x[c + sj];
+            // where all seven values are zero (a zero initial guess) A x = 0: test the
+            // bit patterns on the integer pipe and skip the FP64 stencil
+            const unsigned long long nz = (bits_of(um) | bits_of(uc) | bits_of(up) | bits_of(xw) | bits_of(xe) |
+                                           bits_of(xs) | bits_of(xn)) << 1;
+            double rv = b[c];
+            if (nz != 0ull) {
+                const double sx = xw + xe;
+                const double sy = xs + xn;
+                double a;
+                if (ISO) {
+                    a = fmx(cf.cx, (sx + sy) + (um + up), cf.cc * uc);
+                } else {
+                    a = cf.cc * uc;
+                    a = fmx(cf.cx, sx, a);
+                    a = fmx(cf.cy, sy, a);
+                    a = fmx(cf.cz, um + up, a);
+                }
+                rv -= a;
+            }
             const TR rs = (TR)rv;
             r[c] = rs;
             if (r0) r0[c] = rs;
             if (p) p[c] = rs;
-            s = fmx(rv, rv, s);
+            acc.add(rs, rs);
             um = uc;
             uc = up;
             c += sk;
         }
     }
-    double v[1] = {s};
+    double v[1] = {acc.value()};
     reduce_finalize<1>(v, rc);
 }
 
@@ -1340,6 +1435,19 @@ void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
+void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+                             cudaStream_t s)
+{
+    k_fcg_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, p, r, Ap, st);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s)
+{
+    k_fcg_dot_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, r, z, Ap, rc);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
 void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
                         RedCtx rc, cudaStream_t s)
 {
@@ -1350,7 +1458,10 @@ template <typename TR>
 void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
                    const Coef& a, RedCtx rc, cudaStream_t s)
 {
-    k_residual<TR><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+    if (a.cx == a.cy && a.cx == a.cz)
+        k_residual<TR, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+    else
+        k_residual<TR, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
@@ -1405,6 +1516,10 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
     template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
     template void fast_fcg_p_stencil<T>(const Geo&, const Shape&, const T*, const T*, T*, T*, const Coef&,       \
                                         RedCtx, cudaStream_t);                                                   \
+    template void fast_fcg_update_xr_flat<T>(const Geo&, const Shape&, T*, const T*, T*, const T*,               \
+                                             const DevState*, cudaStream_t);                                     \
+    template void fast_fcg_dot_flat<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx,          \
+                                       cudaStream_t);                                                            \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
                                    const Coef&, RedCtx, cudaStream_t);                                           \
     template void fill_field<T>(T*, long long, T, cudaStream_t);

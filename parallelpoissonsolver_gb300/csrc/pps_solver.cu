@@ -814,6 +814,11 @@ void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     L.launches += 4;
 }
 
+bool aligned16(const void* p)
+{
+    return ((uintptr_t)p & 15u) == 0;
+}
+
 // One flexible-CG iteration: CG with the Polak-Ribiere beta = z_new.(r_new - r_old) /
 // (z_old.r_old), so the preconditioner may change from one application to the next.
 // With r_new - r_old = -alpha Ap no old residual is kept; the direction update
@@ -829,9 +834,12 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     const Coef a = op_coef(g);
     fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
     std::swap(F.p, F.Az);
-    fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
+    const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
+    if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
+    else fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
     precond_any<T>(s, F, F.r, F.z, L);
-    fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
+    if (flat) fast_fcg_dot_flat<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
+    else fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
     L.bytes += bytes_of<T>(N, 4 + 6 + 3);
     L.launches += 3;
 }

@@ -23,8 +23,8 @@ constexpr int TILE_V = 64;   // voxels (along x) per conv block: 4 warps x 16
 
 // ---------------------------------------------------------------------------
 // Convolution, forward: Y[v][co] = act(bias[co] + sum_tap sum_ci X[v+off(tap)][ci] W[tap][ci][co])
-// Cin, Cout multiples of 16, Cout <= 96.  One block: 64 consecutive voxels of one
-// (z, y) row, all output channels.
+// Cin, Cout multiples of 16, Cout <= 96.  One block: 64 consecutive voxels in
+// (z, y, x) order (several rows of a small grid), all output channels.
 // ---------------------------------------------------------------------------
 template <bool RELU, bool OUT_F32>
 __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
@@ -34,32 +34,30 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
     __shared__ __align__(32) bf16 sA[TILE_V * 16];
     __shared__ __align__(32) bf16 sB[16 * 96];
     __shared__ __align__(32) float sC[TILE_V * 96];
-    const int ntx = (d.W + TILE_V - 1) / TILE_V;
-    const int xt = blockIdx.x % ntx;
-    const int y = (blockIdx.x / ntx) % d.H;
-    const int z = blockIdx.x / (ntx * d.H);
-    const int x0 = xt * TILE_V;
+    const long long nvox = (long long)d.D * d.H * d.W;
+    const long long v0 = (long long)blockIdx.x * TILE_V;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int nfrag = Cout / 16;
+    // the voxel whose A-tile row this thread fills (two threads per voxel)
+    const int va = tid >> 1, ha = tid & 1;
+    const long long lva = v0 + va;
+    const bool va_in = lva < nvox;
+    const int xa = (int)(lva % d.W), ya = (int)((lva / d.W) % d.H), za = (int)(lva / ((long long)d.W * d.H));
     wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[6];
 #pragma unroll
     for (int f = 0; f < 6; f++) wmma::fill_fragment(acc[f], 0.0f);
 
     for (int tap = 0; tap < 27; tap++) {
         const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int zz = z + dz, yy = y + dy;
-        const bool row_ok = zz >= 0 && zz < d.D && yy >= 0 && yy < d.H;
+        const int zz = za + dz, yy = ya + dy, xx = xa + dx;
+        const bool ok = va_in && zz >= 0 && zz < d.D && yy >= 0 && yy < d.H && xx >= 0 && xx < d.W;
+        const long long src_v = ((long long)zz * d.H + yy) * d.W + xx;
         for (int c0 = 0; c0 < Cin; c0 += 16) {
             // A tile: 64 voxels x 16 channels; each thread moves 8 channels (16 B)
             {
-                const int v = tid >> 1, h = tid & 1;
-                const int xx = x0 + v + dx;
                 uint4 val = make_uint4(0, 0, 0, 0);
-                if (row_ok && xx >= 0 && xx < d.W && x0 + v < d.W) {
-                    const bf16* src = X + ((long long)(zz * d.H + yy) * d.W + xx) * ldx + cx0 + c0 + 8 * h;
-                    val = *reinterpret_cast<const uint4*>(src);
-                }
-                *reinterpret_cast<uint4*>(&sA[v * 16 + 8 * h]) = val;
+                if (ok) val = *reinterpret_cast<const uint4*>(X + src_v * ldx + cx0 + c0 + 8 * ha);
+                *reinterpret_cast<uint4*>(&sA[va * 16 + 8 * ha]) = val;
             }
             // B tile: 16 input channels x Cout
             for (int q = tid; q < 16 * Cout / 8; q += 128) {
@@ -87,10 +85,10 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
     __syncthreads();
     for (int q = tid; q < TILE_V * Cout; q += 128) {
         const int v = q / Cout, co = q % Cout;
-        if (x0 + v >= d.W) continue;
+        if (v0 + v >= nvox) continue;
         float val = sC[v * 96 + co] + (bias ? bias[co] : 0.0f);
         if (RELU) val = fmaxf(val, 0.0f);
-        const long long o = ((long long)(z * d.H + y) * d.W + x0 + v) * ldy + cy0 + co;
+        const long long o = (v0 + v) * ldy + cy0 + co;
         if (OUT_F32) reinterpret_cast<float*>(Yv)[o] = val;
         else reinterpret_cast<bf16*>(Yv)[o] = __float2bfloat16(val);
     }
@@ -99,8 +97,7 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
           int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
 {
-    const int ntx = (d.W + TILE_V - 1) / TILE_V;
-    const unsigned blocks = (unsigned)(ntx * d.H * d.D);
+    const unsigned blocks = (unsigned)(((long long)d.D * d.H * d.W + TILE_V - 1) / TILE_V);
     if (out_f32) {
         if (relu) k_conv<true, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
         else k_conv<false, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
@@ -777,21 +774,32 @@ __global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims
         const float* p = coarse + (long long)cz * plane;
         return wya * (wxa * p[oaa] + wxb * p[oab]) + wyb * (wxa * p[oba] + wxb * p[obb]);
     };
-    const int kk0 = q.k0 - g.lo[2], kk1 = q.k1 - g.lo[2];
-    int cz = kk0 >> 1;
+    const long long sk = g.sk;
+    const int kk1 = q.k1 - g.lo[2];
+    int kk = q.k0 - g.lo[2];
+    int cz = kk >> 1;
     float vm = cz >= 1 ? interp(cz - 1) : 0.0f;   // coarse planes cz-1 and cz
     float v0 = interp(cz);
     long long c = q.c;
-    for (int kk = kk0; kk < kk1; kk++, c += g.sk) {
-        if (!(kk & 1)) {
-            f[c] += (T)(0.5f * (vm + v0));
-        } else {
-            f[c] += (T)v0;
-            vm = v0;
-            cz++;
-            v0 = cz < dc.D ? interp(cz) : 0.0f;
-        }
+    if (kk & 1) {   // odd first plane: coarse plane cz alone
+        f[c] += (T)v0;
+        c += sk;
+        kk++;
+        vm = v0;
+        cz++;
+        v0 = cz < dc.D ? interp(cz) : 0.0f;
     }
+    // plane pairs (2cz, 2cz+1): the mean of coarse planes cz-1, cz, then cz alone
+    for (; kk + 1 < kk1; kk += 2, c += 2 * sk) {
+        const float vn = cz + 1 < dc.D ? interp(cz + 1) : 0.0f;
+        const T f0 = f[c], f1 = f[c + sk];
+        f[c] = f0 + (T)(0.5f * (vm + v0));
+        f[c + sk] = f1 + (T)v0;
+        vm = v0;
+        v0 = vn;
+        cz++;
+    }
+    if (kk < kk1) f[c] += (T)(0.5f * (vm + v0));   // a last even plane
 }
 
 template <typename T>

@@ -3,8 +3,8 @@
     python -m parallelpoissonsolver_gb300.profile_case --size 320 --form mixed --maxit 2
     python -m parallelpoissonsolver_gb300.profile_case --save-net net.npz          # train the U-Net, save
     python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --maxit 8
-    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 5,8,8 --maxit 20000 \
-        --refinements 12 --inner-tol 3e-4
+    python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 5,4,8 --maxit 20000 \
+        --refinements 12 --inner-tol 1e-5
 
 Runs `--repeat` solves of the k^-2 random-field workload at `--size`^3 unknowns with
 the iteration cap `--maxit`, so that an ncu capture sees a handful of launches of
@@ -30,8 +30,9 @@ def main():
     ap.add_argument("--degree", type=int, default=11)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--graph", action="store_true")
-    ap.add_argument("--save-net", default=None, help="train the 32^3 linear U-Net and save it here, then exit")
-    ap.add_argument("--coarsen", type=int, default=4, help="coarsenings whose coarsest-level operator --save-net learns")
+    ap.add_argument("--save-net", default=None, help="train the linear U-Net and save it here, then exit")
+    ap.add_argument("--net-grid", type=int, default=16, help="edge of the network's grid")
+    ap.add_argument("--coarsen", type=int, default=5, help="coarsenings whose coarsest-level operator --save-net learns")
     ap.add_argument("--learned", default=None, help="saved U-Net to use as the coarse-grid correction")
     ap.add_argument("--cycle", default=None, help="fine,coarse,ratio of the multigrid V-cycle (with --learned)")
     ap.add_argument("--inner-tol", type=float, default=3e-3)
@@ -40,14 +41,14 @@ def main():
     a = ap.parse_args()
     if a.save_net:
         from parallelpoissonsolver_gb300 import learned
-        train = learned.make_dataset(32, range(10000, 10256), coarsen=a.coarsen)
+        train = learned.make_dataset(a.net_grid, range(10000, 10256), coarsen=a.coarsen)
         scale = learned.fit_scale(train)
         net = pps.UNet((16, 32, 64), seed=1, linear=True)
         learned.train(net, train, scale, 4000, lr=1e-3)
         net.save(a.save_net)
         import numpy as np
         with np.load(a.save_net) as d:
-            np.savez(a.save_net, scale=np.array(scale), **{k: d[k] for k in d.files})
+            np.savez(a.save_net, scale=np.array(scale), net_grid=np.array(a.net_grid), **{k: d[k] for k in d.files})
         print(f"saved {a.save_net}: scale {scale:.6g}")
         return
     grid = pps.BlockGrid.cube(a.size)
@@ -55,13 +56,17 @@ def main():
     if a.learned:
         import numpy as np
         net = pps.UNet.load_file(a.learned)
-        scale = float(np.load(a.learned)["scale"])
-        k = int(round(math.log2(a.size / 32)))
-        gain = scale * ((2 ** k / (a.size + 1)) / (1.0 / 33)) ** 2
+        saved = np.load(a.learned)
+        scale = float(saved["scale"])
+        ng = int(saved["net_grid"]) if "net_grid" in saved.files else 32
+        k = int(round(math.log2(a.size / ng)))
+        gain = scale * ((2 ** k / (a.size + 1)) / (1.0 / (ng + 1))) ** 2
         s = pps.FlexibleCG(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
                            form=a.form, inner_maxit=a.maxit, max_refinements=a.refinements, use_graph=False,
                            inner_tol=a.inner_tol)
-        flags = pps.LEARNED_INITIAL_GUESS | pps.LEARNED_PRECONDITIONER | pps.LEARNED_NO_FALLBACK
+        flags = pps.LEARNED_PRECONDITIONER | pps.LEARNED_NO_FALLBACK
+        if not a.cycle:
+            flags |= pps.LEARNED_INITIAL_GUESS
         if a.post_smooth or not a.cycle:
             flags |= pps.LEARNED_POST_SMOOTH
         s.set_learned(net, k, gain, flags)
