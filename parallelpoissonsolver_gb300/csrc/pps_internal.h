@@ -219,10 +219,12 @@ void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, co
 // with sum r^2 in FP64.
 template <typename TR>
 void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
-                   const Coef& a, RedCtx rc, cudaStream_t s);
+                   const Coef& a, RedCtx rc, cudaStream_t s, bool x_zero = false);
+// Number of entries of a whole FP64 field that are not +-0 (into sums[0]).
+void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx rc, cudaStream_t s);
 // ||b_adj||^2 over the unknowns, b_adj formed on the fly (FP64).
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
-                    cudaStream_t s);
+                    cudaStream_t s, bool x_zero = false);
 // x += scale * e at the unknowns (FP64 += FP32).
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState* st,
                          cudaStream_t s);

@@ -1221,44 +1221,59 @@ __global__ void __launch_bounds__(256) k_fcg_dot_flat(long long n, const T* __re
 
 // r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
 // stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
-__device__ __forceinline__ unsigned long long bits_of(double v) { return (unsigned long long)__double_as_longlong(v); }
+// Counts the entries of a whole field (guard layers included) whose bit pattern is
+// not +-0, in 16-byte vectors.
+__global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double* __restrict__ x, RedCtx rc)
+{
+    double cnt = 0.0;
+    const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        const longlong2 v = reinterpret_cast<const longlong2*>(x)[i];
+        cnt += ((unsigned long long)v.x << 1 != 0ull) + ((unsigned long long)v.y << 1 != 0ull);
+    }
+    for (long long i = nv * 2 + t0; i < n; i += stride) cnt += ((unsigned long long)__double_as_longlong(x[i]) << 1) != 0ull;
+    double v[1] = {cnt};
+    reduce_finalize<1>(v, rc);
+}
 
 // ISO: equal spacings on the three axes, so the six neighbours share one weight
 // (GB300 runs FP64 at 1/64 of the FP32 rate, and this kernel is bound by it).  The
 // sum of squares of the stored value accumulates in double-float for TR = float.
-template <typename TR, bool ISO>
+template <typename TR, bool ISO, bool XZERO>
 __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double* __restrict__ x,
                                                   const double* __restrict__ b, TR* __restrict__ r,
                                                   TR* __restrict__ r0, TR* __restrict__ p, Coef cf, RedCtx rc)
 {
     const Col q = column(g, sh);
     Acc<TR> acc;
-    if (q.active) {
+    if (XZERO && q.active) {   // x = 0 on every point the stencil reads: r = b
+        long long c = q.c;
+        for (int k = q.k0; k < q.k1; k++, c += g.sk) {
+            const TR rs = (TR)b[c];
+            r[c] = rs;
+            if (r0) r0[c] = rs;
+            if (p) p[c] = rs;
+            acc.add(rs, rs);
+        }
+    } else if (q.active) {
         const long long sj = g.sj, sk = g.sk;
         long long c = q.c;
         double um = x[c - sk], uc = x[c];
         for (int k = q.k0; k < q.k1; k++) {
             const double up = x[c + sk];
-            const double xw = x[c - 1], xe = x[c + 1], xs = x[c - sj], xn = x[c + sj];
-            // where all seven values are zero (a zero initial guess) A x = 0: test the
-            // bit patterns on the integer pipe and skip the FP64 stencil
-            const unsigned long long nz = (bits_of(um) | bits_of(uc) | bits_of(up) | bits_of(xw) | bits_of(xe) |
-                                           bits_of(xs) | bits_of(xn)) << 1;
-            double rv = b[c];
-            if (nz != 0ull) {
-                const double sx = xw + xe;
-                const double sy = xs + xn;
-                double a;
-                if (ISO) {
-                    a = fmx(cf.cx, (sx + sy) + (um + up), cf.cc * uc);
-                } else {
-                    a = cf.cc * uc;
-                    a = fmx(cf.cx, sx, a);
-                    a = fmx(cf.cy, sy, a);
-                    a = fmx(cf.cz, um + up, a);
-                }
-                rv -= a;
+            const double sx = x[c - 1] + x[c + 1];
+            const double sy = x[c - sj] + x[c + sj];
+            double a;
+            if (ISO) {
+                a = fmx(cf.cx, (sx + sy) + (um + up), cf.cc * uc);
+            } else {
+                a = cf.cc * uc;
+                a = fmx(cf.cx, sx, a);
+                a = fmx(cf.cy, sy, a);
+                a = fmx(cf.cz, um + up, a);
             }
+            const double rv = b[c] - a;
             const TR rs = (TR)rv;
             r[c] = rs;
             if (r0) r0[c] = rs;
@@ -1273,7 +1288,9 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
     reduce_finalize<1>(v, rc);
 }
 
-// sum b_adj^2 over the unknowns (normalizeProblemToFieldBNorm, iterativeSolverBase.hpp:171-234)
+// sum b_adj^2 over the unknowns (normalizeProblemToFieldBNorm, iterativeSolverBase.hpp:171-234);
+// XZERO: Dirichlet grid with x = 0 everywhere, so b_adj = b
+template <bool XZERO>
 __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double* __restrict__ b,
                                                    const double* __restrict__ x, Faces f, RedCtx rc)
 {
@@ -1282,7 +1299,7 @@ __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double
     if (q.active) {
         long long c = q.c;
         for (int k = q.k0; k < q.k1; k++) {
-            const double v = badj_exact(g, b, x, f, c, q.i, q.j, k);
+            const double v = XZERO ? b[c] : badj_exact(g, b, x, f, c, q.i, q.j, k);
             s = fmx(v, v, s);
             c += g.sk;
         }
@@ -1454,20 +1471,28 @@ void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin,
     k_fcg_p_stencil<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
+void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx rc, cudaStream_t s)
+{
+    k_count_nonzero<<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, rc);
+    PPS_COUNT_LAUNCH();
+}
 template <typename TR>
 void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
-                   const Coef& a, RedCtx rc, cudaStream_t s)
+                   const Coef& a, RedCtx rc, cudaStream_t s, bool x_zero)
 {
-    if (a.cx == a.cy && a.cx == a.cz)
-        k_residual<TR, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+    if (x_zero)
+        k_residual<TR, true, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+    else if (a.cx == a.cy && a.cx == a.cz)
+        k_residual<TR, true, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
     else
-        k_residual<TR, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+        k_residual<TR, false, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
-                    cudaStream_t s)
+                    cudaStream_t s, bool x_zero)
 {
-    k_norm_badj<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
+    if (x_zero) k_norm_badj<true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
+    else k_norm_badj<false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s)
@@ -1521,7 +1546,7 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
     template void fast_fcg_dot_flat<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx,          \
                                        cudaStream_t);                                                            \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
-                                   const Coef&, RedCtx, cudaStream_t);                                           \
+                                   const Coef&, RedCtx, cudaStream_t, bool);                                     \
     template void fill_field<T>(T*, long long, T, cudaStream_t);
 
 PPS_INST(double)

@@ -16,7 +16,7 @@ struct Dims {
 
 typedef __nv_bfloat16 bf16;
 
-// 3x3x3 zero-padded convolution on tensor cores (Cin, Cout multiples of 16, Cout <= 96).
+// 3x3x3 zero-padded convolution on tensor cores (Cin, Cout multiples of 16).
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
           int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s);
 void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* G, int ldg, int cg0, int Cout,

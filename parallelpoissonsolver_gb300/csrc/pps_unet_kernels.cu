@@ -23,72 +23,65 @@ constexpr int TILE_V = 64;   // voxels (along x) per conv block: 4 warps x 16
 
 // ---------------------------------------------------------------------------
 // Convolution, forward: Y[v][co] = act(bias[co] + sum_tap sum_ci X[v+off(tap)][ci] W[tap][ci][co])
-// Cin, Cout multiples of 16, Cout <= 96.  One block: 64 consecutive voxels in
-// (z, y, x) order (several rows of a small grid), all output channels.
+// Cin, Cout multiples of 16.  One block: one 16 x 16 output fragment (16 consecutive
+// voxels in (z, y, x) order, 16 output channels).  The K = 27 * Cin/16 steps of
+// 16 x 16 x 16 are dealt round-robin to the 4 warps, so each warp's dependent chain
+// is a quarter of K (the grids are small: at 16^3 latency, not the tensor pipe, is
+// the limit); each warp stages its A tile in its own shared slot (warp-level sync
+// only), reads the weight fragment straight from global memory, prefetches the
+// next A tile into registers, and the four partial fragments are summed at the end.
 // ---------------------------------------------------------------------------
+constexpr int CONV_V = 16;   // voxels per block
+
 template <bool RELU, bool OUT_F32>
 __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
                                               const bf16* __restrict__ Wt, const float* __restrict__ bias,
                                               void* __restrict__ Yv, int ldy, int cy0, int Cout)
 {
-    __shared__ __align__(32) bf16 sA[TILE_V * 16];
-    __shared__ __align__(32) bf16 sB[16 * 96];
-    __shared__ __align__(32) float sC[TILE_V * 96];
+    __shared__ __align__(32) bf16 sA[4][CONV_V * 16];
+    __shared__ __align__(32) float sC[4][16 * 16];
     const long long nvox = (long long)d.D * d.H * d.W;
-    const long long v0 = (long long)blockIdx.x * TILE_V;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int nfrag = Cout / 16;
-    // the voxel whose A-tile row this thread fills (two threads per voxel)
-    const int va = tid >> 1, ha = tid & 1;
+    const long long v0 = (long long)blockIdx.x * CONV_V;
+    const int co0 = blockIdx.y * 16;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // this lane's voxel row of the A tile and its 8-channel half
+    const int va = lane >> 1, ha = lane & 1;
     const long long lva = v0 + va;
     const bool va_in = lva < nvox;
     const int xa = (int)(lva % d.W), ya = (int)((lva / d.W) % d.H), za = (int)(lva / ((long long)d.W * d.H));
-    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc[6];
-#pragma unroll
-    for (int f = 0; f < 6; f++) wmma::fill_fragment(acc[f], 0.0f);
-
-    for (int tap = 0; tap < 27; tap++) {
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int zz = za + dz, yy = ya + dy, xx = xa + dx;
-        const bool ok = va_in && zz >= 0 && zz < d.D && yy >= 0 && yy < d.H && xx >= 0 && xx < d.W;
-        const long long src_v = ((long long)zz * d.H + yy) * d.W + xx;
-        for (int c0 = 0; c0 < Cin; c0 += 16) {
-            // A tile: 64 voxels x 16 channels; each thread moves 8 channels (16 B)
-            {
-                uint4 val = make_uint4(0, 0, 0, 0);
-                if (ok) val = *reinterpret_cast<const uint4*>(X + src_v * ldx + cx0 + c0 + 8 * ha);
-                *reinterpret_cast<uint4*>(&sA[va * 16 + 8 * ha]) = val;
-            }
-            // B tile: 16 input channels x Cout
-            for (int q = tid; q < 16 * Cout / 8; q += 128) {
-                const int row = q / (Cout / 8), col8 = q % (Cout / 8);
-                const bf16* src = Wt + ((long long)tap * Cin + c0 + row) * Cout + 8 * col8;
-                *reinterpret_cast<uint4*>(&sB[row * 96 + 8 * col8]) = *reinterpret_cast<const uint4*>(src);
-            }
-            __syncthreads();
-            wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
-            wmma::load_matrix_sync(a, sA + warp * 16 * 16, 16);
-#pragma unroll
-            for (int f = 0; f < 6; f++) {
-                if (f < nfrag) {
-                    wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> bfr;
-                    wmma::load_matrix_sync(bfr, sB + f * 16, 96);
-                    wmma::mma_sync(acc[f], a, bfr, acc[f]);
-                }
-            }
-            __syncthreads();
-        }
+    const int csteps = Cin / 16, ksteps = 27 * csteps;
+    auto load_a = [&](int t) -> uint4 {
+        const int tap = t / csteps, c0 = (t - tap * csteps) * 16;
+        const int zz = za + tap / 9 - 1, yy = ya + (tap / 3) % 3 - 1, xx = xa + tap % 3 - 1;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (va_in && zz >= 0 && zz < d.D && yy >= 0 && yy < d.H && xx >= 0 && xx < d.W)
+            val = *reinterpret_cast<const uint4*>(X + (((long long)zz * d.H + yy) * d.W + xx) * ldx + cx0 + c0 + 8 * ha);
+        return val;
+    };
+    wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
+    wmma::fill_fragment(acc, 0.0f);
+    int t = warp;
+    uint4 next = t < ksteps ? load_a(t) : make_uint4(0, 0, 0, 0);
+    for (; t < ksteps; t += 4) {
+        *reinterpret_cast<uint4*>(&sA[warp][va * 16 + 8 * ha]) = next;
+        __syncwarp();
+        if (t + 4 < ksteps) next = load_a(t + 4);
+        const int tap = t / csteps, c0 = (t - tap * csteps) * 16;
+        wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
+        wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> bfr;
+        wmma::load_matrix_sync(a, sA[warp], 16);
+        wmma::load_matrix_sync(bfr, Wt + ((long long)tap * Cin + c0) * Cout + co0, Cout);
+        wmma::mma_sync(acc, a, bfr, acc);
+        __syncwarp();
     }
-#pragma unroll
-    for (int f = 0; f < 6; f++)
-        if (f < nfrag) wmma::store_matrix_sync(sC + warp * 16 * 96 + f * 16, acc[f], 96, wmma::mem_row_major);
+    wmma::store_matrix_sync(sC[warp], acc, 16, wmma::mem_row_major);
     __syncthreads();
-    for (int q = tid; q < TILE_V * Cout; q += 128) {
-        const int v = q / Cout, co = q % Cout;
+    for (int q = threadIdx.x; q < CONV_V * 16; q += 128) {
+        const int v = q >> 4, co = q & 15;
         if (v0 + v >= nvox) continue;
-        float val = sC[v * 96 + co] + (bias ? bias[co] : 0.0f);
+        float val = sC[0][q] + sC[1][q] + sC[2][q] + sC[3][q] + (bias ? bias[co0 + co] : 0.0f);
         if (RELU) val = fmaxf(val, 0.0f);
-        const long long o = (v0 + v) * ldy + cy0 + co;
+        const long long o = (v0 + v) * ldy + cy0 + co0 + co;
         if (OUT_F32) reinterpret_cast<float*>(Yv)[o] = val;
         else reinterpret_cast<bf16*>(Yv)[o] = __float2bfloat16(val);
     }
@@ -97,13 +90,13 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
           int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
 {
-    const unsigned blocks = (unsigned)(((long long)d.D * d.H * d.W + TILE_V - 1) / TILE_V);
+    const dim3 grid((unsigned)(((long long)d.D * d.H * d.W + CONV_V - 1) / CONV_V), (unsigned)(Cout / 16));
     if (out_f32) {
-        if (relu) k_conv<true, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
-        else k_conv<false, true><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        if (relu) k_conv<true, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        else k_conv<false, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
     } else {
-        if (relu) k_conv<true, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
-        else k_conv<false, false><<<blocks, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        if (relu) k_conv<true, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        else k_conv<false, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
     }
     launches_counter_add(1);
 }
@@ -854,21 +847,24 @@ template void prolong_add_field<double>(const Geo&, const Shape&, const Dims&, c
 // Dirichlet zero beyond the array edges.
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ float level_diag(const DLevel& L, bool lx, bool ly, bool lz)
+// -diag(A) at a point whose last-unknown flags along x, y, z are lx, ly, lz
+__device__ __forceinline__ float level_negdiag(const DLevel& L, bool lx, bool ly, bool lz)
 {
-    return (lx ? L.last_c[0] : -2.0f * L.ih2[0]) + (ly ? L.last_c[1] : -2.0f * L.ih2[1]) +
-           (lz ? L.last_c[2] : -2.0f * L.ih2[2]);
+    return (lx ? -L.last_c[0] : 2.0f * L.ih2[0]) + (ly ? -L.last_c[1] : 2.0f * L.ih2[1]) +
+           (lz ? -L.last_c[2] : 2.0f * L.ih2[2]);
 }
 
 // One pass over a coarse level, z-marching:
 //   RESID:  W = B - A Y
 //   CHEB:   W (+)= scale (cy Y + D^-1 (cb B + ca A Y) + cz Z)     (Z may be null)
-// with D = -diag(A).  With `first`, Y is not read: its values are D^-1 B / theta
-// (the recurrence's starting term), formed at each of the 7 points on the fly.
-template <bool CHEB>
+// with D = -diag(A).  FIRST: Y is not read; its values are D^-1 B / theta (the
+// recurrence's starting term), formed at each of the 7 points on the fly.  The
+// D^-1 a thread needs (its own point and its four in-plane neighbours, inside the
+// grid or on the last plane) are set up once per column.
+template <bool CHEB, bool FIRST>
 __global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk, const float* __restrict__ Y,
                                                     const float* __restrict__ B, const float* __restrict__ Z,
-                                                    float* __restrict__ W, LCoef c, int first, int acc)
+                                                    float* __restrict__ W, LCoef c, int acc)
 {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= d.W || y >= d.H) return;
@@ -879,24 +875,39 @@ __global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk
     // the axis coefficients at this column: lower and upper neighbour weights
     const float wxm = lx ? L.last_m[0] : L.ih2[0], wxp = lx ? 0.0f : L.ih2[0];
     const float wym = ly ? L.last_m[1] : L.ih2[1], wyp = ly ? 0.0f : L.ih2[1];
-    // D^-1 of the x/y neighbours (only used when `first`): their last-flags differ in one axis
-    auto yval = [&](long long q, bool fx, bool fy, bool fz) -> float {
-        if (!first) return Y[q];
-        return B[q] * c.y0 / (-level_diag(L, fx, fy, fz));
-    };
+    // D^-1 (times 1/theta for the starting term) per point kind, [0]: inside, [1]: last plane
+    float di[2], dxm[2], dxp[2], dym[2], dyp[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        di[e] = 1.0f / level_negdiag(L, lx, ly, e);
+        if (FIRST) {
+            dxm[e] = c.y0 / level_negdiag(L, false, ly, e);
+            dxp[e] = c.y0 / level_negdiag(L, x + 1 == d.W - 1, ly, e);
+            dym[e] = c.y0 / level_negdiag(L, lx, false, e);
+            dyp[e] = c.y0 / level_negdiag(L, lx, y + 1 == d.H - 1, e);
+        }
+    }
+    auto yc_of = [&](long long q, int e) -> float { return FIRST ? B[q] * c.y0 * di[e] : Y[q]; };
     long long q = (long long)z0 * sz + (long long)y * sy + x;
-    float ym = z0 > 0 ? yval(q - sz, lx, ly, z0 - 1 == d.D - 1) : 0.0f;
-    float yc = yval(q, lx, ly, z0 == d.D - 1);
+    float ym = z0 > 0 ? yc_of(q - sz, 0) : 0.0f;
+    float yc = yc_of(q, z0 == d.D - 1);
     for (int z = z0; z < z1; z++, q += sz) {
-        const bool lz = z == d.D - 1;
-        const float yp = z + 1 < d.D ? yval(q + sz, lx, ly, z + 1 == d.D - 1) : 0.0f;
-        const float xm = hx0 ? yval(q - 1, x - 1 == d.W - 1, ly, lz) : 0.0f;
-        const float xp = hx1 ? yval(q + 1, x + 1 == d.W - 1, ly, lz) : 0.0f;
-        const float ymn = hy0 ? yval(q - sy, lx, y - 1 == d.H - 1, lz) : 0.0f;
-        const float ypn = hy1 ? yval(q + sy, lx, y + 1 == d.H - 1, lz) : 0.0f;
+        const int lz = z == d.D - 1;
+        const float yp = z + 1 < d.D ? yc_of(q + sz, z + 1 == d.D - 1) : 0.0f;
+        float xm, xp, ymn, ypn;
+        if (FIRST) {
+            xm = hx0 ? B[q - 1] * dxm[lz] : 0.0f;
+            xp = hx1 ? B[q + 1] * dxp[lz] : 0.0f;
+            ymn = hy0 ? B[q - sy] * dym[lz] : 0.0f;
+            ypn = hy1 ? B[q + sy] * dyp[lz] : 0.0f;
+        } else {
+            xm = hx0 ? Y[q - 1] : 0.0f;
+            xp = hx1 ? Y[q + 1] : 0.0f;
+            ymn = hy0 ? Y[q - sy] : 0.0f;
+            ypn = hy1 ? Y[q + sy] : 0.0f;
+        }
         const float wzm = lz ? L.last_m[2] : L.ih2[2], wzp = lz ? 0.0f : L.ih2[2];
-        const float dg = level_diag(L, lx, ly, lz);
-        float ay = dg * yc;
+        float ay = -level_negdiag(L, lx, ly, lz) * yc;
         ay = fmaf(wxm, xm, ay);
         ay = fmaf(wxp, xp, ay);
         ay = fmaf(wym, ymn, ay);
@@ -906,7 +917,8 @@ __global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk
         const float b = B[q];
         float v;
         if (CHEB) {
-            v = c.cy * yc + fmaf(c.cb, b, c.ca * ay) / (-dg);
+            v = fmaf(c.cb, b, c.ca * ay) * di[lz];
+            v = fmaf(c.cy, yc, v);
             if (Z) v = fmaf(c.cz, Z[q], v);
             v *= c.scale;
         } else {
@@ -934,7 +946,7 @@ void level_residual(const Dims& d, const DLevel& L, const float* Y, const float*
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    k_level_pass<false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, 0, 0);
+    k_level_pass<false, false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, 0);
     launches_counter_add(1);
 }
 
@@ -944,7 +956,8 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    k_level_pass<true><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, first ? 1 : 0, acc ? 1 : 0);
+    if (first) k_level_pass<true, true><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
+    else k_level_pass<true, false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
     launches_counter_add(1);
 }
 
