@@ -101,10 +101,14 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()   # let the sampler start before the timed region does
+            while not self.lines and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.lines.clear()
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -343,7 +347,8 @@ def run_gpu(args, dist: Dist):
         "hbm_gbs_solve": stats[-1]["hbm_bytes"] / stats[-1]["seconds_solve"] / 1e9,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_cheb_sweep<float> (Chebyshev sweep, 16 B per unknown)",
+            "kernel": "k_cheb_sweep<float> (Chebyshev sweeps of the fine-grid smoother: 12 B per unknown for "
+                      "the first, 16 B for the others)",
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
@@ -519,7 +524,7 @@ def cpu_sample(m: int, iterations_needed: int | None, threads: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=1)
