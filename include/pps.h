@@ -177,6 +177,9 @@ typedef struct {
     int cheb_ty, cheb_cx, cheb_waves;
     int other_ty, other_waves;
     double cheb_us, other_us;
+    int cheb_fused;             /* 1: Chebyshev applications of degree 4 or 5 on Dirichlet grids
+                                   run all their steps in one temporally blocked pass
+                                   (bit-identical); 0 (default): one launch per step */
 } pps_tuning;
 
 /* Autotuner (no reference counterpart; the reference fixes its launch shapes,

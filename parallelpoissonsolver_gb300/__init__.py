@@ -78,7 +78,8 @@ class PpsStats(C.Structure):
 
 class PpsTuning(C.Structure):
     _fields_ = [("cheb_ty", C.c_int), ("cheb_cx", C.c_int), ("cheb_waves", C.c_int), ("other_ty", C.c_int),
-                ("other_waves", C.c_int), ("cheb_us", C.c_double), ("other_us", C.c_double)]
+                ("other_waves", C.c_int), ("cheb_us", C.c_double), ("other_us", C.c_double),
+                ("cheb_fused", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -87,7 +88,7 @@ class PpsTuning(C.Structure):
     def from_dict(cls, d):
         t = cls()
         for k, _ in cls._fields_:
-            setattr(t, k, d[k])
+            setattr(t, k, d.get(k, 0) if k == "cheb_fused" else d[k])
         return t
 
 

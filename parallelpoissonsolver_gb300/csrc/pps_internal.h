@@ -168,6 +168,11 @@ void neumann_fill(const Geo& g, T* field, Faces f, int field_mode, double normb,
 template <typename T>
 void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& cy, const int* done, cudaStream_t s);
 // One sweep; Z == nullptr for the first sweep (s0 folded into the B coefficient).
+// s1..s_nsteps of the Chebyshev recurrence in one pass (nsteps 2 or 3): c[0] makes
+// s1 from B, c[t-1] step t (the last one's scale is the output's -1); X = the last
+// step.  Bit-identical to fast_cheb_s01 + fast_cheb_sweep launches.  Dirichlet only.
+template <typename T>
+void fast_cheb_fused(const Geo& g, int nsteps, const T* B, T* X, const Coef* c, const int* done, cudaStream_t s);
 template <typename T>
 void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, const T* Z, T* W, const Coef& c,
                      const int* done, cudaStream_t s);

@@ -13,6 +13,8 @@
 //              Krylov scalars on the device (no host round trip).
 #include "pps_internal.h"
 
+#include <algorithm>
+
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -825,6 +827,108 @@ __global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __
     }
 }
 
+// Several Chebyshev steps in one pass (temporal blocking).  The steps s1..s_NS of
+// the recurrence above (s1 from B, then sweeps; the last writes X = -s_NS) run as a
+// wavefront along z over a tile of 32 x 8 columns: when B plane j is loaded, step t
+// computes its plane j - 2t from planes of step t-1 (B for t = 1) that earlier
+// iterations left in shared memory, so one barrier per plane orders everything.
+// Step t covers the tile plus a halo of NS - t columns (the halo of B is NS), so the
+// tile's outputs need no other block's work; step values off the unknowns are zero,
+// as the guard cells of the unfused work fields are, and B is read as stored, its
+// guard layer included.  The arithmetic is the unfused kernels' (same coefficients,
+// same operand order), so the result is bit-identical to k_cheb_s01 followed by
+// NS - 1 k_cheb_sweep launches.  Dirichlet grids only.
+template <typename T>
+struct ChebStages {
+    CT<T> c[4];   // c[0]: s1 from B; c[t-1]: step t (c[NS-1] carries the -1 of the output)
+};
+
+constexpr int FUSE_TX = 32, FUSE_TY = 8;
+
+template <int NS>
+struct FuseDims {
+    // step t (0: B) covers (32 + 2h) x (8 + 2h) columns, h = NS - t
+    __host__ __device__ static constexpr int w(int t) { return FUSE_TX + 2 * (NS - t); }
+    __host__ __device__ static constexpr int h(int t) { return FUSE_TY + 2 * (NS - t); }
+    __host__ __device__ static constexpr int sz(int t) { return w(t) * h(t); }
+    // ring depths: B is read back to plane j - 2NS (the last step's B term) and written
+    // at j; step t (1 <= t < NS) is written at j - 2t and read back to j - 2t - 3
+    // (step t+1's stencil) and j - 2t - 4 (step t+2's Z term)
+    __host__ __device__ static constexpr int depth(int t) { return t == 0 ? 2 * NS + 1 : (t + 2 <= NS ? 5 : 4); }
+    __host__ __device__ static constexpr int off(int t) { return t == 0 ? 0 : off(t - 1) + depth(t - 1) * sz(t - 1); }
+    __host__ __device__ static constexpr int total() { return off(NS); }
+};
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(256) k_cheb_fused(Geo g, int ntx, int kchunk, const T* __restrict__ B,
+                                                    T* __restrict__ X, ChebStages<T> cs, const int* done)
+{
+    EARLY_EXIT(done);
+    typedef FuseDims<NS> FD;
+    extern __shared__ __align__(16) unsigned char fuse_smem[];
+    T* sm = reinterpret_cast<T*>(fuse_smem);
+    const int tid = threadIdx.x + FUSE_TX * threadIdx.y;
+    const int i0 = g.lo[0] + (blockIdx.x % ntx) * FUSE_TX;
+    const int j0 = g.lo[1] + (blockIdx.x / ntx) * FUSE_TY;
+    const int kb = g.lo[2] + blockIdx.y * kchunk;
+    const int ke = min(kb + kchunk, g.hi[2]);
+    const int base = kb - NS;   // first B plane; ring slots count planes from here
+    const long long sj = g.sj, sk = g.sk;
+    auto inside = [&](int i, int j, int k) {
+        return i >= g.lo[0] && i < g.hi[0] && j >= g.lo[1] && j < g.hi[1] && k >= g.lo[2] && k < g.hi[2];
+    };
+    auto plane_of = [&](int t, int p) -> T* { return sm + FD::off(t) + ((p - base) % FD::depth(t)) * FD::sz(t); };
+    // B planes kb-NS .. ke+NS-1; step t's plane lags the loaded one by 2t
+    for (int jp = base; jp < ke + 2 * NS; jp++) {
+        if (jp < ke + NS) {
+            T* dst = plane_of(0, jp);
+            for (int q = tid; q < FD::sz(0); q += 256) {
+                const int a = q % FD::w(0), b = q / FD::w(0);
+                const int i = i0 - NS + a, j = j0 - NS + b;
+                const bool stored = i >= g.lo[0] - 1 && i <= g.hi[0] && j >= g.lo[1] - 1 && j <= g.hi[1] &&
+                                    jp >= g.lo[2] - 1 && jp <= g.hi[2];
+                dst[q] = stored ? B[i + sj * j + sk * jp] : T(0);
+            }
+        }
+#pragma unroll
+        for (int t = 1; t <= NS; t++) {
+            const int p = jp - 2 * t;   // plane of step t; its inputs were written by earlier iterations
+            if (p >= kb - (NS - t) && p < ke + (NS - t)) {
+                const CT<T> cf = cs.c[t - 1];
+                const int wi = FD::w(t), wp = FD::w(t - 1);
+                const T* ym = plane_of(t - 1, p - 1);
+                const T* yc = plane_of(t - 1, p);
+                const T* yp = plane_of(t - 1, p + 1);
+                const T* bb = plane_of(0, p);
+                const T* zz = t >= 3 ? plane_of(t - 2, p) : nullptr;
+                T* out = t < NS ? plane_of(t, p) : nullptr;
+                const int npos = t < NS ? FD::sz(t) : FUSE_TX * FUSE_TY;
+                for (int q = tid; q < npos; q += 256) {
+                    const int a = t < NS ? q % wi : q % FUSE_TX;
+                    const int b = t < NS ? q / wi : q / FUSE_TX;
+                    const int i = i0 - (NS - t) + a, j = j0 - (NS - t) + b;
+                    T v = T(0);
+                    if (inside(i, j, p)) {
+                        const int e = (b + 1) * wp + (a + 1);   // (i, j) in step t-1's region
+                        const T sx = yc[e - 1] + yc[e + 1];
+                        const T sy = yc[e - wp] + yc[e + wp];
+                        T w = cf.cc * yc[e];
+                        w = fmx(cf.cx, sx, w);
+                        w = fmx(cf.cy, sy, w);
+                        w = fmx(cf.cz, ym[e] + yp[e], w);
+                        if (t >= 2) w = fmx(cf.cb, bb[(b + t) * FD::w(0) + (a + t)], w);
+                        if (t >= 3) w = fmx(cf.cw, zz[(b + 2) * FD::w(t - 2) + (a + 2)], w);
+                        v = w;
+                    }
+                    if (t < NS) out[q] = v;
+                    else if (p >= kb && p < ke && inside(i, j, p)) X[i + sj * j + sk * p] = v;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_scale_copy(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ X, T a,
                                                     const int* done)
@@ -1374,6 +1478,38 @@ void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, cons
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
+void fast_cheb_fused(const Geo& g, int nsteps, const T* B, T* X, const Coef* c, const int* done, cudaStream_t s)
+{
+    ChebStages<T> cs;
+    for (int t = 0; t < nsteps && t < 4; t++) cs.c[t] = cast_coef<T>(c[t]);
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
+    const int ntx = (ux + FUSE_TX - 1) / FUSE_TX, nty = (uy + FUSE_TY - 1) / FUSE_TY;
+    const long long tiles = (long long)ntx * nty;
+    // z chunks: about 8 blocks per SM, each chunk at most 128 planes (the wavefront
+    // re-reads 2*nsteps planes per chunk)
+    long long chunks = std::max((152LL * 8 + tiles - 1) / tiles, (long long)((uz + 127) / 128));
+    chunks = std::max(1LL, std::min(chunks, (long long)uz));
+    const int kchunk = (int)((uz + chunks - 1) / chunks);
+    const dim3 grid((unsigned)tiles, (unsigned)((uz + kchunk - 1) / kchunk));
+    const dim3 block(FUSE_TX, FUSE_TY);
+    // the dynamic shared-memory opt-in, once per device and instantiation (a host call)
+    static unsigned long long attr_set = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !(attr_set & (1ull << dev))) {
+        cudaFuncSetAttribute(k_cheb_fused<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(T) * FuseDims<2>::total()));
+        cudaFuncSetAttribute(k_cheb_fused<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(T) * FuseDims<3>::total()));
+        attr_set |= 1ull << dev;
+    }
+    if (nsteps == 2)
+        k_cheb_fused<T, 2><<<grid, block, sizeof(T) * FuseDims<2>::total(), s>>>(g, ntx, kchunk, B, X, cs, done);
+    else
+        k_cheb_fused<T, 3><<<grid, block, sizeof(T) * FuseDims<3>::total(), s>>>(g, ntx, kchunk, B, X, cs, done);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
 void fast_scale_copy(const Geo& g, const Shape& sh, const T* B, T* X, double a, const int* done, cudaStream_t s)
 {
     k_scale_copy<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, X, (T)a, done);
@@ -1541,6 +1677,7 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
     template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
     template void fast_fcg_p_stencil<T>(const Geo&, const Shape&, const T*, const T*, T*, T*, const Coef&,       \
                                         RedCtx, cudaStream_t);                                                   \
+    template void fast_cheb_fused<T>(const Geo&, int, const T*, T*, const Coef*, const int*, cudaStream_t);      \
     template void fast_fcg_update_xr_flat<T>(const Geo&, const Shape&, T*, const T*, T*, const T*,               \
                                              const DevState*, cudaStream_t);                                     \
     template void fast_fcg_dot_flat<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx,          \

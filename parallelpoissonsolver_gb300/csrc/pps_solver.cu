@@ -537,6 +537,33 @@ void fast_cheb(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const ChebP
         L.launches++;
         return;
     }
+    if (!s->has_neumann && s->tuning.cheb_fused && (n == 4 || n == 5)) {
+        // all n-2 steps in one temporally blocked pass: B read once, X written once
+        Coef cs[3];
+        cs[0] = c01;
+        for (int it = 2; it <= n - 2; it++) {
+            rhoOld = rhoCurr;
+            rhoCurr = 1 / (2 * sigma - rhoOld);
+            Coef c = cheb_sweep_coef(a, p, rhoCurr, rhoOld, it == n - 2 ? -1.0 : 1.0);
+            if (it == 2) {
+                c.cb += c.cw / p.theta;
+                c.cw = 0.0;
+            }
+            cs[it - 1] = c;
+        }
+        const bool prof = L.profile && s->sweep_ev_used + 2 <= (int)s->sweep_ev.size();
+        if (prof) CK(cudaEventRecord(s->sweep_ev[s->sweep_ev_used], st));
+        fast_cheb_fused<T>(g, n - 2, B, X, cs, done, st);
+        if (prof) {
+            CK(cudaEventRecord(s->sweep_ev[s->sweep_ev_used + 1], st));
+            s->sweep_ev_used += 2;
+        }
+        L.bytes += bytes_of<T>(N, 2);
+        L.launches++;
+        s->sweep_bytes_acc += bytes_of<T>(N, 2);
+        s->sweep_launch_acc++;
+        return;
+    }
     T* Y = F.Y;
     T* Z = F.Z;
     T* W = F.W;
@@ -1205,7 +1232,7 @@ bool tuning_valid(const pps_tuning* t)
         return false;
     };
     return in(t->cheb_ty, kTys, 3) && in(t->cheb_cx, kCxs, 2) && in(t->cheb_waves, kWaves, 4) &&
-           in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4);
+           in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4) && (t->cheb_fused == 0 || t->cheb_fused == 1);
 }
 
 pps_status validate(const pps_grid* g, const pps_config* c)
@@ -1384,6 +1411,7 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         s->tuning.other_waves = 4;
         s->tuning.cheb_us = 0.0;
         s->tuning.other_us = 0.0;
+        s->tuning.cheb_fused = 0;
         // computeEigenvalues, global bounds (blockGrid.hpp:322-339)
         double eigMin = 0, eigMax = 0;
         for (int i = 0; i < 3; i++) {

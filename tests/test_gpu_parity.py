@@ -301,6 +301,31 @@ def test_flexible_cg_converges(gpu, oracle, form):
     assert abs(s.get_num_iteration_final() - cg.get_num_iteration_final()) <= 3
 
 
+@pytest.mark.parametrize("form,degree", [("fp64", 4), ("fp64", 5), ("mixed", 4), ("mixed", 5)])
+def test_fused_chebyshev_is_bit_identical(gpu, form, degree):
+    """The temporally blocked Chebyshev pass (all steps of a degree-4/5 application in
+    one kernel) against one launch per step: the same bits for one application on a
+    ragged grid with nonzero boundary data, and for a whole solve."""
+    rng = np.random.default_rng(11)
+    grid = pps.BlockGrid(npglobal=(37, 29, 45), ds=(0.03, 0.035, 0.025))
+    b = rng.standard_normal(grid.shape)
+    out = []
+    for fused in (1, 0):
+        s = pps.BiCGSTAB(grid, pps.ChebyshevIteration(degree), tolerance=1e-10, max_iteration=3000, form=form,
+                         use_graph=False)
+        s.set_tuning({**s.tuning(), "cheb_fused": fused})
+        z = s.apply_preconditioner(b.copy())
+        x = np.zeros_like(b)
+        st = s(x, b.copy())
+        out.append((z, x, st, s.get_num_iteration_final(), s.history()))
+        s.close()
+    assert same_bits(out[0][0], out[1][0])
+    assert out[0][2] == out[1][2]       # (degree 4 can break BiCGSTAB down; identically)
+    assert out[0][3] == out[1][3] > 0
+    assert same_bits(out[0][1], out[1][1])
+    assert same_bits(out[0][4], out[1][4])
+
+
 @pytest.mark.parametrize("check_every", [1, 3, 4])
 def test_flexible_cg_graph_replay_matches_direct_launches(gpu, check_every):
     """Flexible CG alternates its direction fields; graph chunks of any requested
