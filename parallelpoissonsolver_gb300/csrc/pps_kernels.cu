@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __
 
 // Several Chebyshev steps in one pass (temporal blocking).  The steps s1..s_NS of
 // the recurrence above (s1 from B, then sweeps; the last writes X = -s_NS) run as a
-// wavefront along z over a tile of 32 x 8 columns: when B plane j is loaded, step t
+// wavefront along z over a tile of 32 x 16 columns: when B plane j is loaded, step t
 // computes its plane j - 2t from planes of step t-1 (B for t = 1) that earlier
 // iterations left in shared memory, so one barrier per plane orders everything.
 // Step t covers the tile plus a halo of NS - t columns (the halo of B is NS), so the
@@ -843,11 +843,11 @@ struct ChebStages {
     CT<T> c[4];   // c[0]: s1 from B; c[t-1]: step t (c[NS-1] carries the -1 of the output)
 };
 
-constexpr int FUSE_TX = 32, FUSE_TY = 8;
+constexpr int FUSE_TX = 32, FUSE_TY = 16;
 
 template <int NS>
 struct FuseDims {
-    // step t (0: B) covers (32 + 2h) x (8 + 2h) columns, h = NS - t
+    // step t (0: B) covers (32 + 2h) x (16 + 2h) columns, h = NS - t
     __host__ __device__ static constexpr int w(int t) { return FUSE_TX + 2 * (NS - t); }
     __host__ __device__ static constexpr int h(int t) { return FUSE_TY + 2 * (NS - t); }
     __host__ __device__ static constexpr int sz(int t) { return w(t) * h(t); }
@@ -865,6 +865,10 @@ __global__ void __launch_bounds__(256) k_cheb_fused(Geo g, int ntx, int kchunk, 
 {
     EARLY_EXIT(done);
     typedef FuseDims<NS> FD;
+    constexpr int NT = 256;
+    constexpr int NB = (FD::sz(0) + NT - 1) / NT;                 // B items per thread
+    constexpr int NI = (FD::sz(1) + NT - 1) / NT;                 // step items per thread (the widest step)
+    constexpr int NO = (FUSE_TX * FUSE_TY + NT - 1) / NT;         // output items per thread
     extern __shared__ __align__(16) unsigned char fuse_smem[];
     T* sm = reinterpret_cast<T*>(fuse_smem);
     const int tid = threadIdx.x + FUSE_TX * threadIdx.y;
@@ -873,55 +877,96 @@ __global__ void __launch_bounds__(256) k_cheb_fused(Geo g, int ntx, int kchunk, 
     const int kb = g.lo[2] + blockIdx.y * kchunk;
     const int ke = min(kb + kchunk, g.hi[2]);
     const int base = kb - NS;   // first B plane; ring slots count planes from here
-    const long long sj = g.sj, sk = g.sk;
-    auto inside = [&](int i, int j, int k) {
-        return i >= g.lo[0] && i < g.hi[0] && j >= g.lo[1] && j < g.hi[1] && k >= g.lo[2] && k < g.hi[2];
-    };
+    const long long sk = g.sk;
+
+    // Everything that does not depend on the plane is set up once per thread: the
+    // B items' global column offsets, and for every step item its neighbour indices
+    // in the previous step's region, in B's region and in step t-2's region.
+    long long bofs[NB];
+    bool bxy[NB];
+#pragma unroll
+    for (int r = 0; r < NB; r++) {
+        const int q = tid + NT * r;
+        const int a = q % FD::w(0), b = q / FD::w(0);
+        const int i = i0 - NS + a, j = j0 - NS + b;
+        bxy[r] = q < FD::sz(0) && i >= g.lo[0] - 1 && i <= g.hi[0] && j >= g.lo[1] - 1 && j <= g.hi[1];
+        bofs[r] = bxy[r] ? (long long)i + g.sj * j : 0;
+    }
+    int ie[NS][NI], ib[NS][NI], iz[NS][NI];
+    bool ixy[NS][NI];
+    long long xofs[NO];
+#pragma unroll
+    for (int t = 1; t <= NS; t++) {
+        const int wi = t < NS ? FD::w(t) : FUSE_TX;
+        const int npos = t < NS ? FD::sz(t) : FUSE_TX * FUSE_TY;
+        const int hal = NS - t;
+#pragma unroll
+        for (int r = 0; r < NI; r++) {
+            const int q = tid + NT * r;
+            const int a = q % wi, b = q / wi;
+            const int i = i0 - hal + a, j = j0 - hal + b;
+            ixy[t - 1][r] = q < npos && i >= g.lo[0] && i < g.hi[0] && j >= g.lo[1] && j < g.hi[1];
+            ie[t - 1][r] = (b + 1) * FD::w(t - 1) + (a + 1);
+            ib[t - 1][r] = (b + t) * FD::w(0) + (a + t);
+            iz[t - 1][r] = t >= 3 ? (b + 2) * FD::w(t >= 3 ? t - 2 : 0) + (a + 2) : 0;
+            if (t == NS && r < NO) xofs[r] = (long long)i + g.sj * j;
+        }
+    }
     auto plane_of = [&](int t, int p) -> T* { return sm + FD::off(t) + ((p - base) % FD::depth(t)) * FD::sz(t); };
-    // B planes kb-NS .. ke+NS-1; step t's plane lags the loaded one by 2t
+
+    // B plane jp+1 is fetched into registers while the steps of iteration jp run, so
+    // the global-memory latency overlaps the shared-memory work
+    T breg[NB];
+    auto fetch = [&](int jp) {
+        const bool zs = jp >= g.lo[2] - 1 && jp <= g.hi[2];
+        const long long zo = sk * jp;
+#pragma unroll
+        for (int r = 0; r < NB; r++) breg[r] = (bxy[r] && zs) ? B[bofs[r] + zo] : T(0);
+    };
+    fetch(base);
     for (int jp = base; jp < ke + 2 * NS; jp++) {
         if (jp < ke + NS) {
             T* dst = plane_of(0, jp);
-            for (int q = tid; q < FD::sz(0); q += 256) {
-                const int a = q % FD::w(0), b = q / FD::w(0);
-                const int i = i0 - NS + a, j = j0 - NS + b;
-                const bool stored = i >= g.lo[0] - 1 && i <= g.hi[0] && j >= g.lo[1] - 1 && j <= g.hi[1] &&
-                                    jp >= g.lo[2] - 1 && jp <= g.hi[2];
-                dst[q] = stored ? B[i + sj * j + sk * jp] : T(0);
+#pragma unroll
+            for (int r = 0; r < NB; r++) {
+                const int q = tid + NT * r;
+                if (q < FD::sz(0)) dst[q] = breg[r];
             }
+            if (jp + 1 < ke + NS) fetch(jp + 1);
         }
 #pragma unroll
         for (int t = 1; t <= NS; t++) {
             const int p = jp - 2 * t;   // plane of step t; its inputs were written by earlier iterations
             if (p >= kb - (NS - t) && p < ke + (NS - t)) {
                 const CT<T> cf = cs.c[t - 1];
-                const int wi = FD::w(t), wp = FD::w(t - 1);
+                const int wp = FD::w(t - 1);
                 const T* ym = plane_of(t - 1, p - 1);
                 const T* yc = plane_of(t - 1, p);
                 const T* yp = plane_of(t - 1, p + 1);
                 const T* bb = plane_of(0, p);
-                const T* zz = t >= 3 ? plane_of(t - 2, p) : nullptr;
-                T* out = t < NS ? plane_of(t, p) : nullptr;
+                const T* zz = plane_of(t >= 3 ? t - 2 : 0, p);
+                T* out = plane_of(t < NS ? t : 0, p);
+                const bool zin = p >= g.lo[2] && p < g.hi[2];
                 const int npos = t < NS ? FD::sz(t) : FUSE_TX * FUSE_TY;
-                for (int q = tid; q < npos; q += 256) {
-                    const int a = t < NS ? q % wi : q % FUSE_TX;
-                    const int b = t < NS ? q / wi : q / FUSE_TX;
-                    const int i = i0 - (NS - t) + a, j = j0 - (NS - t) + b;
+#pragma unroll
+                for (int r = 0; r < NI; r++) {
+                    const int q = tid + NT * r;
+                    if (q >= npos) continue;
                     T v = T(0);
-                    if (inside(i, j, p)) {
-                        const int e = (b + 1) * wp + (a + 1);   // (i, j) in step t-1's region
+                    if (ixy[t - 1][r] && zin) {
+                        const int e = ie[t - 1][r];
                         const T sx = yc[e - 1] + yc[e + 1];
                         const T sy = yc[e - wp] + yc[e + wp];
                         T w = cf.cc * yc[e];
                         w = fmx(cf.cx, sx, w);
                         w = fmx(cf.cy, sy, w);
                         w = fmx(cf.cz, ym[e] + yp[e], w);
-                        if (t >= 2) w = fmx(cf.cb, bb[(b + t) * FD::w(0) + (a + t)], w);
-                        if (t >= 3) w = fmx(cf.cw, zz[(b + 2) * FD::w(t - 2) + (a + 2)], w);
+                        if (t >= 2) w = fmx(cf.cb, bb[ib[t - 1][r]], w);
+                        if (t >= 3) w = fmx(cf.cw, zz[iz[t - 1][r]], w);
                         v = w;
                     }
                     if (t < NS) out[q] = v;
-                    else if (p >= kb && p < ke && inside(i, j, p)) X[i + sj * j + sk * p] = v;
+                    else if (r < NO && p >= kb && p < ke && ixy[t - 1][r]) X[xofs[r] + sk * p] = v;
                 }
             }
         }
@@ -1491,7 +1536,7 @@ void fast_cheb_fused(const Geo& g, int nsteps, const T* B, T* X, const Coef* c, 
     chunks = std::max(1LL, std::min(chunks, (long long)uz));
     const int kchunk = (int)((uz + chunks - 1) / chunks);
     const dim3 grid((unsigned)tiles, (unsigned)((uz + kchunk - 1) / kchunk));
-    const dim3 block(FUSE_TX, FUSE_TY);
+    const dim3 block(FUSE_TX, 256 / FUSE_TX);
     // the dynamic shared-memory opt-in, once per device and instantiation (a host call)
     static unsigned long long attr_set = 0;
     int dev = 0;

@@ -856,15 +856,15 @@ __device__ __forceinline__ float level_negdiag(const DLevel& L, bool lx, bool ly
 
 // One pass over a coarse level, z-marching:
 //   RESID:  W = B - A Y
-//   CHEB:   W (+)= scale (cy Y + D^-1 (cb B + ca A Y) + cz Z)     (Z may be null)
+//   CHEB:   W (+)= scale (cy Y + D^-1 (cb B + ca A Y) + cz Z)     (HASZ: with Z)
 // with D = -diag(A).  FIRST: Y is not read; its values are D^-1 B / theta (the
-// recurrence's starting term), formed at each of the 7 points on the fly.  The
-// D^-1 a thread needs (its own point and its four in-plane neighbours, inside the
-// grid or on the last plane) are set up once per column.
-template <bool CHEB, bool FIRST>
-__global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk, const float* __restrict__ Y,
+// recurrence's starting term), formed at each of the 7 points on the fly.  A
+// column's coefficients (and D^-1 of its own and neighbouring points) are fixed
+// except on the last plane, which is peeled off the plane loop.
+template <bool CHEB, bool FIRST, bool HASZ, bool ACC>
+__global__ void __launch_bounds__(256) k_level_pass(Dims d, DLevel L, int kchunk, const float* __restrict__ Y,
                                                     const float* __restrict__ B, const float* __restrict__ Z,
-                                                    float* __restrict__ W, LCoef c, int acc)
+                                                    float* __restrict__ W, LCoef c)
 {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= d.W || y >= d.H) return;
@@ -872,42 +872,41 @@ __global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk
     const long long sy = d.W, sz = (long long)d.W * d.H;
     const bool hx0 = x > 0, hx1 = x + 1 < d.W, hy0 = y > 0, hy1 = y + 1 < d.H;
     const bool lx = x == d.W - 1, ly = y == d.H - 1;
-    // the axis coefficients at this column: lower and upper neighbour weights
-    const float wxm = lx ? L.last_m[0] : L.ih2[0], wxp = lx ? 0.0f : L.ih2[0];
-    const float wym = ly ? L.last_m[1] : L.ih2[1], wyp = ly ? 0.0f : L.ih2[1];
-    // D^-1 (times 1/theta for the starting term) per point kind, [0]: inside, [1]: last plane
-    float di[2], dxm[2], dxp[2], dym[2], dyp[2];
+    // neighbour weights of this column (zero where the neighbour is the wall)
+    const float wxm = hx0 ? (lx ? L.last_m[0] : L.ih2[0]) : 0.0f, wxp = hx1 ? L.ih2[0] : 0.0f;
+    const float wym = hy0 ? (ly ? L.last_m[1] : L.ih2[1]) : 0.0f, wyp = hy1 ? L.ih2[1] : 0.0f;
+    // per plane kind e (0: inside, 1: the last plane): -diag, D^-1, and for FIRST the
+    // starting-term scales of the neighbours (D^-1/theta at each of them)
+    float ndg[2], di[2], fc[2], fxm[2], fxp[2], fym[2], fyp[2];
 #pragma unroll
     for (int e = 0; e < 2; e++) {
-        di[e] = 1.0f / level_negdiag(L, lx, ly, e);
+        ndg[e] = level_negdiag(L, lx, ly, e);
+        di[e] = 1.0f / ndg[e];
         if (FIRST) {
-            dxm[e] = c.y0 / level_negdiag(L, false, ly, e);
-            dxp[e] = c.y0 / level_negdiag(L, x + 1 == d.W - 1, ly, e);
-            dym[e] = c.y0 / level_negdiag(L, lx, false, e);
-            dyp[e] = c.y0 / level_negdiag(L, lx, y + 1 == d.H - 1, e);
+            fc[e] = c.y0 * di[e];
+            fxm[e] = hx0 ? c.y0 / level_negdiag(L, false, ly, e) : 0.0f;
+            fxp[e] = hx1 ? c.y0 / level_negdiag(L, x + 1 == d.W - 1, ly, e) : 0.0f;
+            fym[e] = hy0 ? c.y0 / level_negdiag(L, lx, false, e) : 0.0f;
+            fyp[e] = hy1 ? c.y0 / level_negdiag(L, lx, y + 1 == d.H - 1, e) : 0.0f;
         }
     }
-    auto yc_of = [&](long long q, int e) -> float { return FIRST ? B[q] * c.y0 * di[e] : Y[q]; };
+    const float* S = FIRST ? B : Y;   // the stencil's field
+    // the value of the stencil's field at column offset q on plane kind e
+    auto val = [&](long long q, float f) -> float { return FIRST ? S[q] * f : S[q]; };
     long long q = (long long)z0 * sz + (long long)y * sy + x;
-    float ym = z0 > 0 ? yc_of(q - sz, 0) : 0.0f;
-    float yc = yc_of(q, z0 == d.D - 1);
-    for (int z = z0; z < z1; z++, q += sz) {
-        const int lz = z == d.D - 1;
-        const float yp = z + 1 < d.D ? yc_of(q + sz, z + 1 == d.D - 1) : 0.0f;
-        float xm, xp, ymn, ypn;
-        if (FIRST) {
-            xm = hx0 ? B[q - 1] * dxm[lz] : 0.0f;
-            xp = hx1 ? B[q + 1] * dxp[lz] : 0.0f;
-            ymn = hy0 ? B[q - sy] * dym[lz] : 0.0f;
-            ypn = hy1 ? B[q + sy] * dyp[lz] : 0.0f;
-        } else {
-            xm = hx0 ? Y[q - 1] : 0.0f;
-            xp = hx1 ? Y[q + 1] : 0.0f;
-            ymn = hy0 ? Y[q - sy] : 0.0f;
-            ypn = hy1 ? Y[q + sy] : 0.0f;
-        }
-        const float wzm = lz ? L.last_m[2] : L.ih2[2], wzp = lz ? 0.0f : L.ih2[2];
-        float ay = -level_negdiag(L, lx, ly, lz) * yc;
+    const int zlast = d.D - 1;
+    float ym = z0 > 0 ? val(q - sz, fc[0]) : 0.0f;
+    float yc = val(q, z0 == zlast ? fc[1] : fc[0]);
+    auto point = [&](int e, float yp) {
+        // in-plane neighbours: the stencil field is read directly (the weights above
+        // hold the wall); FIRST scales each by its own D^-1/theta
+        const float xm = hx0 ? val(q - 1, fxm[e]) : 0.0f;
+        const float xp = hx1 ? val(q + 1, fxp[e]) : 0.0f;
+        const float ymn = hy0 ? val(q - sy, fym[e]) : 0.0f;
+        const float ypn = hy1 ? val(q + sy, fyp[e]) : 0.0f;
+        const float wzm = e ? L.last_m[2] : L.ih2[2];
+        const float wzp = e ? 0.0f : L.ih2[2];
+        float ay = -ndg[e] * yc;
         ay = fmaf(wxm, xm, ay);
         ay = fmaf(wxp, xp, ay);
         ay = fmaf(wym, ymn, ay);
@@ -917,24 +916,34 @@ __global__ void __launch_bounds__(128) k_level_pass(Dims d, DLevel L, int kchunk
         const float b = B[q];
         float v;
         if (CHEB) {
-            v = fmaf(c.cb, b, c.ca * ay) * di[lz];
+            v = fmaf(c.cb, b, c.ca * ay) * di[e];
             v = fmaf(c.cy, yc, v);
-            if (Z) v = fmaf(c.cz, Z[q], v);
+            if (HASZ) v = fmaf(c.cz, Z[q], v);
             v *= c.scale;
         } else {
             v = b - ay;
         }
-        W[q] = acc ? W[q] + v : v;
+        if (ACC) v += W[q];
+        W[q] = v;
+    };
+    const int zend = min(z1, zlast);   // planes before the last one
+    int z = z0;
+#pragma unroll 2
+    for (; z < zend; z++) {
+        const float yp = val(q + sz, z + 1 == zlast ? fc[1] : fc[0]);
+        point(0, yp);
         ym = yc;
         yc = yp;
+        q += sz;
     }
+    if (z < z1) point(1, 0.0f);   // the last plane: upper wall one fine spacing above
 }
 
 static void level_launch(const Dims& d, int& kchunk, dim3& grid)
 {
-    // 32 x 4 columns per block, z split into chunks for about 16 blocks per SM
-    const int tx = (d.W + 31) / 32, ty = (d.H + 3) / 4;
-    long long chunks = (152LL * 16 + (long long)tx * ty - 1) / ((long long)tx * ty);
+    // 32 x 8 columns per block, z split into chunks for about 8 blocks per SM
+    const int tx = (d.W + 31) / 32, ty = (d.H + 7) / 8;
+    long long chunks = (152LL * 8 + (long long)tx * ty - 1) / ((long long)tx * ty);
     if (chunks < 1) chunks = 1;
     if (chunks > d.D) chunks = d.D;
     kchunk = (int)((d.D + chunks - 1) / chunks);
@@ -946,7 +955,7 @@ void level_residual(const Dims& d, const DLevel& L, const float* Y, const float*
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    k_level_pass<false, false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, 0);
+    k_level_pass<false, false, false, false><<<grid, dim3(32, 8), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{});
     launches_counter_add(1);
 }
 
@@ -956,8 +965,17 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    if (first) k_level_pass<true, true><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
-    else k_level_pass<true, false><<<grid, dim3(32, 4), 0, s>>>(d, L, kchunk, Y, B, Z, W, c, acc ? 1 : 0);
+    const dim3 blk(32, 8);
+    if (first) {
+        if (acc) k_level_pass<true, true, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        else k_level_pass<true, true, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+    } else if (Z) {
+        if (acc) k_level_pass<true, false, true, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        else k_level_pass<true, false, true, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+    } else {
+        if (acc) k_level_pass<true, false, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        else k_level_pass<true, false, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+    }
     launches_counter_add(1);
 }
 
