@@ -131,6 +131,8 @@ struct pps_solver {
     int g_launches = 0;
     double g_sweep_bytes = 0;
     int g_sweep_launches = 0;
+    bool g_learned = false;   // captured with the learned preconditioner active
+    int g_learned_apps = 0;
 
     // learned preconditioner / initial guess (pps_set_learned)
     pps_unet* net = nullptr;
@@ -911,16 +913,19 @@ int auto_check_every(const pps_solver* s, int elem_size)
 template <typename T>
 pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launcher& L)
 {
-    const bool learned = s->net && s->net_active;
-    int chunk = learned ? 1 : auto_check_every(s, (int)sizeof(T));
+    // with the learned preconditioner the host looks at the residual every two
+    // iterations (the fallback rule), otherwise at the automatic polling interval
+    int chunk = s->net && s->net_active ? 2 : auto_check_every(s, (int)sizeof(T));
     // flexible CG swaps its direction fields every iteration: a captured chunk must
     // hold an even number of iterations to leave them where the capture found them
-    if (s->cfg.krylov == PPS_KRYLOV_FCG && !learned) chunk += chunk & 1;
-    const bool graph = s->cfg.use_graph != 0 && !L.profile && !learned;
-    std::vector<double> errs;   // residual norms seen by the fallback rule
+    if (s->cfg.krylov == PPS_KRYLOV_FCG) chunk += chunk & 1;
+    const bool graph = s->cfg.use_graph != 0 && !L.profile;
+    std::vector<std::pair<int, double>> errs;   // (iteration, residual norm) seen by the fallback rule
     for (;;) {
+        const bool learned = s->net && s->net_active;
         if (graph) {
-            if (!(s->gexec && s->g_key_x == xacc && s->g_form == form && s->g_iters == chunk)) {
+            if (!(s->gexec && s->g_key_x == xacc && s->g_form == form && s->g_iters == chunk &&
+                  s->g_learned == learned)) {
                 if (s->gexec) {
                     cudaGraphExecDestroy(s->gexec);
                     s->gexec = nullptr;
@@ -929,6 +934,7 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
                 Launcher LG{s, false};
                 const double sb = s->sweep_bytes_acc;
                 const int sl = s->sweep_launch_acc;
+                const int la = s->learned_apps;
                 const int c0 = launches_counter();
                 CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
                 for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, LG);
@@ -946,25 +952,35 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
                 s->g_sweep_launches = s->sweep_launch_acc - sl;
                 s->sweep_bytes_acc = sb;
                 s->sweep_launch_acc = sl;
+                s->g_learned = learned;
+                s->g_learned_apps = s->learned_apps - la;
+                s->learned_apps = la;
             }
             CK(cudaGraphLaunch(s->gexec, s->stream));
             L.bytes += s->g_bytes;
             launches_counter_add(s->g_launches);
             s->sweep_bytes_acc += s->g_sweep_bytes;
             s->sweep_launch_acc += s->g_sweep_launches;
+            s->learned_apps += s->g_learned_apps;
         } else {
             for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, L);
         }
         read_state(s);
         if (s->h_st->done) break;
-        if (s->net && s->net_active) {
+        if (learned) {
             // fall back to the plain preconditioner when the per-iteration reduction,
-            // the geometric mean over the last 4 iterations, is worse than 0.5
+            // the geometric mean over at least the last 4 iterations, is worse than 0.5
             const double e = s->h_st->err;
-            errs.push_back(e);
-            const size_t w = 4;
-            if (!(s->net_flags & PPS_LEARNED_NO_FALLBACK) && errs.size() > w &&
-                std::pow(e / errs[errs.size() - 1 - w], 1.0 / (double)w) > 0.5) {
+            const int it = s->h_st->iter;
+            errs.emplace_back(it, e);
+            int back = -1;   // the latest sample at least 4 iterations old
+            for (int q = (int)errs.size() - 1; q >= 0; q--)
+                if (it - errs[(size_t)q].first >= 4) {
+                    back = q;
+                    break;
+                }
+            if (!(s->net_flags & PPS_LEARNED_NO_FALLBACK) && back >= 0 &&
+                std::pow(e / errs[(size_t)back].second, 1.0 / (double)(it - errs[(size_t)back].first)) > 0.5) {
                 s->net_active = false;
                 s->fallback_iter = s->h_st->iter;
                 // restart the flexible-CG recurrence on the plain preconditioner: z = M r, p = z
@@ -1757,6 +1773,10 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
     if (!s) return PPS_ERR_INVALID_ARG;
     return guarded([&]() -> pps_status {
         CK(cudaSetDevice(s->device));
+        if (s->gexec) {   // a captured iteration holds the old buffers and settings
+            cudaGraphExecDestroy(s->gexec);
+            s->gexec = nullptr;
+        }
         for (float* q : s->dn) cudaFree(q);
         for (float* q : s->dn_e) cudaFree(q);
         for (float* q : s->dt) cudaFree(q);
@@ -1839,6 +1859,10 @@ pps_status pps_set_learned_cycle(pps_solver* s, int fine_degree, int coarse_degr
     s->cyc_fine = fine_degree;
     s->cyc_coarse = coarse_degree;
     s->cyc_ratio = ratio;
+    if (s->gexec) {   // a captured iteration holds the old cycle
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
     return PPS_OK;
 }
 
