@@ -1370,6 +1370,34 @@ __global__ void __launch_bounds__(256) k_fcg_dot_flat(long long n, const T* __re
 
 // r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
 // stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
+// A double as m * 2^(e - 1075) with |m| < 2^53 (subnormals: e = 1, no hidden bit).
+struct MI {
+    long long m;
+    int e;
+};
+__device__ __forceinline__ MI msplit(double v)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int ex = (int)((u >> 52) & 0x7ffu);
+    unsigned long long mag = u & 0xFFFFFFFFFFFFFull;
+    MI r;
+    if (ex != 0) {
+        mag |= 1ull << 52;
+        r.e = ex;
+    } else {
+        r.e = 1;
+    }
+    r.m = (u >> 63) ? -(long long)mag : (long long)mag;
+    return r;
+}
+// m * 2^(e - E) for E >= e, truncated toward zero
+__device__ __forceinline__ long long malign(const MI& a, int E)
+{
+    const int sh = min(E - a.e, 63);
+    const long long mag = (a.m < 0 ? -a.m : a.m) >> sh;
+    return a.m < 0 ? -mag : mag;
+}
+
 // Counts the entries of a whole field (guard layers included) whose bit pattern is
 // not +-0, in 16-byte vectors.
 __global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double* __restrict__ x, RedCtx rc)
@@ -1405,6 +1433,39 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
             if (p) p[c] = rs;
             acc.add(rs, rs);
         }
+    } else if (ISO && q.active) {
+        // Equal spacings: A x = cx (sum of the six neighbours - 6 x).  The seven values
+        // are aligned to the largest one's exponent as 53-bit integers, so the second
+        // difference is exact in int64 on the integer pipe; one conversion and one FMA
+        // remain on the FP64 pipe (instead of eight operations).  Truncating the
+        // smaller values' low bits costs at most 2^-53 of the largest, the rounding
+        // the FP64 stencil has anyway.
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        MI um = msplit(x[c - sk]), uc = msplit(x[c]);
+        for (int k = q.k0; k < q.k1; k++) {
+            const MI up = msplit(x[c + sk]);
+            const MI w = msplit(x[c - 1]), e = msplit(x[c + 1]), sv = msplit(x[c - sj]), nv = msplit(x[c + sj]);
+            const int E = max(max(max(um.e, uc.e), max(up.e, w.e)), max(max(e.e, sv.e), nv.e));
+            double rv;
+            if (E == 2047) {   // an Inf or NaN: let FP64 arithmetic propagate it
+                rv = b[c] - cf.cx * (x[c - 1] + x[c + 1] + x[c - sj] + x[c + sj] + x[c - sk] + x[c + sk] - 6.0 * x[c]);
+            } else {
+                const long long D = malign(w, E) + malign(e, E) + malign(sv, E) + malign(nv, E) + malign(um, E) +
+                                    malign(up, E) - 6 * malign(uc, E);
+                // A x = cx * D * 2^(E - 1075); below 2^-1022 it is far under b's rounding
+                const double scale = E >= 53 ? __longlong_as_double((long long)(E - 52) << 52) : 0.0;
+                rv = fmx(-(cf.cx * scale), __ll2double_rn(D), b[c]);
+            }
+            const TR rs = (TR)rv;
+            r[c] = rs;
+            if (r0) r0[c] = rs;
+            if (p) p[c] = rs;
+            acc.add(rs, rs);
+            um = uc;
+            uc = up;
+            c += sk;
+        }
     } else if (q.active) {
         const long long sj = g.sj, sk = g.sk;
         long long c = q.c;
@@ -1414,9 +1475,7 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
             const double sx = x[c - 1] + x[c + 1];
             const double sy = x[c - sj] + x[c + sj];
             double a;
-            if (ISO) {
-                a = fmx(cf.cx, (sx + sy) + (um + up), cf.cc * uc);
-            } else {
+            {
                 a = cf.cc * uc;
                 a = fmx(cf.cx, sx, a);
                 a = fmx(cf.cy, sy, a);
