@@ -62,9 +62,10 @@ enum FinKind : int {
     FIN_CG_ALPHA = 6,   // CG alpha = rz / pAp
     FIN_CG_CONV = 7,    // CG beta = rz_new / rz, err, stop test
     FIN_STORE = 8,      // only store sums[] (used by tests and true residuals)
-    FIN_FCG_CONV = 9,   // flexible CG: Polak-Ribiere beta = -alpha z.Ap / rho0, rho0 = z.r, err, stop test
+    FIN_FCG_CONV = 9,   // flexible CG: Polak-Ribiere beta = -alpha z.Ap / rho0, rho0 = z.r
     FIN_FCG_ALPHA = 10, // flexible CG: alpha = rho0 / pAp
-    FIN_FCG_SETUP = 11  // flexible CG (re)start: rho0 = z.r, beta = 0 (the next p is z)
+    FIN_FCG_SETUP = 11, // flexible CG (re)start: rho0 = z.r, beta = 0 (the next p is z)
+    FIN_FCG_RES = 12    // flexible CG: err = ||r|| after the x, r update, iteration count, stop test
 };
 
 struct RedCtx {
@@ -205,8 +206,8 @@ template <typename T>
 void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const DevState* st, cudaStream_t s);
 // Flexible CG (no reference counterpart; BaseCG's loop with a Polak-Ribiere beta).
 template <typename T>
-void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap,
-                        const DevState* st, cudaStream_t s);
+void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
+                        cudaStream_t s);
 template <typename T>
 void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s);
 template <typename T>
@@ -215,7 +216,7 @@ void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin,
 // The same updates and sums over the whole padded array in 16-byte vectors (fields
 // zero on the guard cells, 16-byte aligned).
 template <typename T>
-void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
                              cudaStream_t s);
 template <typename T>
 void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s);

@@ -609,13 +609,10 @@ __device__ void finalize(const RedCtx& rc, const double* tot)
         st->beta = 0.0;
         break;
     }
-    case FIN_FCG_CONV: {
-        // flexible CG, Polak-Ribiere: beta = z_new.(r_new - r_old) / (z_old.r_old)
-        // with r_new - r_old = -alpha Ap
-        const double err = sqrt(tot[2]);
+    case FIN_FCG_RES: {
+        // flexible CG after x, r: the recursive residual norm and the stop test
+        const double err = sqrt(tot[0]);
         st->err = err;
-        st->beta = -st->alpha * tot[1] / st->rho0;
-        st->rho0 = tot[0];
         st->iter += 1;
         if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
         if (!isfinite(err)) {
@@ -627,7 +624,15 @@ __device__ void finalize(const RedCtx& rc, const double* tot)
         } else if (st->iter >= st->maxit) {
             st->status = 1;
             st->done = 1;
-        } else if (!isfinite(st->beta)) {
+        }
+        break;
+    }
+    case FIN_FCG_CONV: {
+        // flexible CG, Polak-Ribiere: beta = z_new.(r_new - r_old) / (z_old.r_old)
+        // with r_new - r_old = -alpha Ap
+        st->beta = -st->alpha * tot[1] / st->rho0;
+        st->rho0 = tot[0];
+        if (!isfinite(st->beta)) {
             st->status = 2;
             st->done = 1;
         }
@@ -1248,23 +1253,29 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil(Geo g, Shape sh, const T*
     reduce_finalize<1>(v, rc);
 }
 
-// FCG: x += alpha*p; r -= alpha*Ap
+// FCG: x += alpha*p; r -= alpha*Ap; sum r.r (the convergence test, before the
+// preconditioner, which a converged iteration then skips)
 template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
-                                                       T* __restrict__ r, const T* __restrict__ Ap,
-                                                       const DevState* st)
+                                                       T* __restrict__ r, const T* __restrict__ Ap, RedCtx rc)
 {
-    EARLY_EXIT(&st->done);
+    EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
-    if (!q.active) return;
-    const T a = (T)st->alpha;
-    long long c = q.c;
+    Acc<T> rr;
+    if (q.active) {
+        const T a = (T)rc.st->alpha;
+        long long c = q.c;
 #pragma unroll 4
-    for (int k = q.k0; k < q.k1; k++) {
-        x[c] = fmx(a, p[c], x[c]);
-        r[c] = fmx(-a, Ap[c], r[c]);
-        c += g.sk;
+        for (int k = q.k0; k < q.k1; k++) {
+            x[c] = fmx(a, p[c], x[c]);
+            const T rn = fmx(-a, Ap[c], r[c]);
+            r[c] = rn;
+            rr.add(rn, rn);
+            c += g.sk;
+        }
     }
+    double v[1] = {rr.value()};
+    reduce_finalize<1>(v, rc);
 }
 
 // FCG: sums z.r, z.Ap, r.r after the (possibly nonlinear) preconditioner; with
@@ -1312,13 +1323,13 @@ struct Vec16<double> {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_update_xr_flat(long long n, T* __restrict__ x, const T* __restrict__ p,
-                                                            T* __restrict__ r, const T* __restrict__ Ap,
-                                                            const DevState* st)
+                                                            T* __restrict__ r, const T* __restrict__ Ap, RedCtx rc)
 {
-    EARLY_EXIT(&st->done);
+    EARLY_EXIT(&rc.st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
-    const T a = (T)st->alpha;
+    const T a = (T)rc.st->alpha;
+    Acc<T> rr;
     const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     for (long long i = t0; i < nv; i += stride) {
@@ -1328,14 +1339,19 @@ __global__ void __launch_bounds__(256) k_fcg_update_xr_flat(long long n, T* __re
         for (int e = 0; e < VT::n; e++) {
             VT::at(xv, e) = fmx(a, VT::at(pv, e), VT::at(xv, e));
             VT::at(rv, e) = fmx(-a, VT::at(av, e), VT::at(rv, e));
+            rr.add(VT::at(rv, e), VT::at(rv, e));
         }
         reinterpret_cast<V*>(x)[i] = xv;
         reinterpret_cast<V*>(r)[i] = rv;
     }
     for (long long i = nv * VT::n + t0; i < n; i += stride) {
         x[i] = fmx(a, p[i], x[i]);
-        r[i] = fmx(-a, Ap[i], r[i]);
+        const T rn = fmx(-a, Ap[i], r[i]);
+        r[i] = rn;
+        rr.add(rn, rn);
     }
+    double v[1] = {rr.value()};
+    reduce_finalize<1>(v, rc);
 }
 
 template <typename T>
@@ -1679,10 +1695,10 @@ void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const Dev
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
-void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
                         cudaStream_t s)
 {
-    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, st);
+    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1692,10 +1708,10 @@ void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
-void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
+void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
                              cudaStream_t s)
 {
-    k_fcg_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, p, r, Ap, st);
+    k_fcg_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, p, r, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1776,14 +1792,14 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
                                        cudaStream_t);                                                            \
     template void fast_cg_dot_rz<T>(const Geo&, const Shape&, const T*, const T*, RedCtx, cudaStream_t);         \
     template void fast_cg_update_p<T>(const Geo&, const Shape&, T*, const T*, const DevState*, cudaStream_t);    \
-    template void fast_fcg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, const DevState*,   \
+    template void fast_fcg_update_xr<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, RedCtx,            \
                                         cudaStream_t);                                                           \
     template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
     template void fast_fcg_p_stencil<T>(const Geo&, const Shape&, const T*, const T*, T*, T*, const Coef&,       \
                                         RedCtx, cudaStream_t);                                                   \
     template void fast_cheb_fused<T>(const Geo&, int, const T*, T*, const Coef*, const int*, cudaStream_t);      \
-    template void fast_fcg_update_xr_flat<T>(const Geo&, const Shape&, T*, const T*, T*, const T*,               \
-                                             const DevState*, cudaStream_t);                                     \
+    template void fast_fcg_update_xr_flat<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, RedCtx,       \
+                                             cudaStream_t);                                                      \
     template void fast_fcg_dot_flat<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx,          \
                                        cudaStream_t);                                                            \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \

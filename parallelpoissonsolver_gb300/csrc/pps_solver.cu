@@ -864,8 +864,8 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
     std::swap(F.p, F.Az);
     const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
-    if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
-    else fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
+    if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
+    else fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
     precond_any<T>(s, F, F.r, F.z, L);
     if (flat) fast_fcg_dot_flat<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
     else fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
@@ -921,6 +921,12 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
     if (s->cfg.krylov == PPS_KRYLOV_FCG) chunk += chunk & 1;
     const bool graph = s->cfg.use_graph != 0 && !L.profile;
     std::vector<std::pair<int, double>> errs;   // (iteration, residual norm) seen by the fallback rule
+    // inside the iterations the learned cycle's kernels return at once after the stop
+    // test (a converged iteration skips its preconditioner)
+    unet::set_stop_flag(&s->d_st->done);
+    struct ClearStop {
+        ~ClearStop() { unet::set_stop_flag(nullptr); }
+    } clear_stop;
     for (;;) {
         const bool learned = s->net && s->net_active;
         if (graph) {

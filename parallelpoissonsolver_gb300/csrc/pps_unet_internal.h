@@ -14,6 +14,10 @@ struct Dims {
     int D, H, W;   // z, y, x extents of an activation grid
 };
 
+// Device stop flag that the forward and transfer kernels check on entry (a set flag
+// makes them return at once); null (the default) while training or outside a solve.
+void set_stop_flag(const int* done);
+
 typedef __nv_bfloat16 bf16;
 
 // 3x3x3 zero-padded convolution on tensor cores (Cin, Cout multiples of 16).

@@ -16,6 +16,12 @@
 namespace pps {
 namespace unet {
 
+// The stop flag the forward and transfer kernels check on entry: a solver sets it to
+// its device stop flag while it runs the learned cycle, so a cycle launched (or
+// replayed) after the iteration converged costs no more than its launches.
+static thread_local const int* g_stop = nullptr;
+void set_stop_flag(const int* done) { g_stop = done; }
+
 using namespace nvcuda;
 typedef __nv_bfloat16 bf16;
 
@@ -36,8 +42,9 @@ constexpr int CONV_V = 16;   // voxels per block
 template <bool RELU, bool OUT_F32>
 __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
                                               const bf16* __restrict__ Wt, const float* __restrict__ bias,
-                                              void* __restrict__ Yv, int ldy, int cy0, int Cout)
+                                              void* __restrict__ Yv, int ldy, int cy0, int Cout, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     __shared__ __align__(32) bf16 sA[4][CONV_V * 16];
     __shared__ __align__(32) float sC[4][16 * 16];
     const long long nvox = (long long)d.D * d.H * d.W;
@@ -92,11 +99,11 @@ void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W
 {
     const dim3 grid((unsigned)(((long long)d.D * d.H * d.W + CONV_V - 1) / CONV_V), (unsigned)(Cout / 16));
     if (out_f32) {
-        if (relu) k_conv<true, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
-        else k_conv<false, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        if (relu) k_conv<true, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else k_conv<false, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
     } else {
-        if (relu) k_conv<true, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
-        else k_conv<false, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout);
+        if (relu) k_conv<true, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else k_conv<false, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
     }
     launches_counter_add(1);
 }
@@ -245,8 +252,9 @@ void relu_bwd(long long nv, bf16* G, int ldg, int cg0, const bf16* Y, int ldy, i
 }
 
 // 2x average pooling: out (D/2,H/2,W/2) dense C channels <- in slot of ldi
-__global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0, bf16* __restrict__ out, int C)
+__global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0, bf16* __restrict__ out, int C, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const long long n = (long long)dout.D * dout.H * dout.W * C;
     const int Hi = dout.H * 2, Wi = dout.W * 2;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -264,7 +272,7 @@ __global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0
 
 void pool2(const Dims& dout, const bf16* in, int ldi, int ci0, bf16* out, int C, cudaStream_t s)
 {
-    k_pool2<<<eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s>>>(dout, in, ldi, ci0, out, C);
+    k_pool2<<<eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s>>>(dout, in, ldi, ci0, out, C, g_stop);
     launches_counter_add(1);
 }
 
@@ -290,8 +298,9 @@ void pool2_bwd(const Dims& dout, const bf16* gout, bf16* gin, int ldi, int ci0, 
 }
 
 // nearest 2x upsampling: out slot (fine) <- in dense (coarse)
-__global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __restrict__ out, int ldo, int co0)
+__global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __restrict__ out, int ldo, int co0, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const long long n = (long long)dfine.D * dfine.H * dfine.W * C;
     const int Hc = dfine.H / 2, Wc = dfine.W / 2;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -304,7 +313,7 @@ __global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __re
 
 void up2(const Dims& dfine, const bf16* in, int C, bf16* out, int ldo, int co0, cudaStream_t s)
 {
-    k_up2<<<eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s>>>(dfine, in, C, out, ldo, co0);
+    k_up2<<<eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s>>>(dfine, in, C, out, ldo, co0, g_stop);
     launches_counter_add(1);
 }
 
@@ -420,8 +429,9 @@ void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s)
 
 // Dense FP32 input [v] -> channel 0 of a BF16 activation [v][ld], scaled by 1/(*rms)
 // (rms == nullptr: scale 1); the other channels zero.
-__global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const float* rms, bf16* __restrict__ act, int ld)
+__global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const float* rms, bf16* __restrict__ act, int ld, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const float sc = rms ? (*rms > 0.0f ? 1.0f / *rms : 0.0f) : 1.0f;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
         act[v * ld] = __float2bfloat16(in[v] * sc);
@@ -431,14 +441,15 @@ __global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const
 
 void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s)
 {
-    k_dense_to_act<<<eblocks(nv), 256, 0, s>>>(nv, in, rms, act, ld);
+    k_dense_to_act<<<eblocks(nv), 256, 0, s>>>(nv, in, rms, act, ld, g_stop);
     launches_counter_add(1);
 }
 
 // channel 0 of an FP32 output slab -> dense FP32, times (*rms) * gain
 __global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int ld, const float* rms, float gain,
-                               float* __restrict__ dense)
+                               float* __restrict__ dense, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const float sc = (rms ? *rms : 1.0f) * gain;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x)
         dense[v] = out[v * ld] * sc;
@@ -446,13 +457,14 @@ __global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int 
 
 void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s)
 {
-    k_out_to_dense<<<eblocks(nv), 256, 0, s>>>(nv, out, ld, rms, gain, dense);
+    k_out_to_dense<<<eblocks(nv), 256, 0, s>>>(nv, out, ld, rms, gain, dense, g_stop);
     launches_counter_add(1);
 }
 
 // rms of a dense FP32 array into *rms (single block, deterministic)
-__global__ void k_rms(long long n, const float* __restrict__ a, float* rms)
+__global__ void k_rms(long long n, const float* __restrict__ a, float* rms, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     __shared__ double sm[32];
     double s = 0.0;
     for (long long q = threadIdx.x; q < n; q += blockDim.x) s += (double)a[q] * (double)a[q];
@@ -469,7 +481,7 @@ __global__ void k_rms(long long n, const float* __restrict__ a, float* rms)
 
 void rms(long long n, const float* a, float* out, cudaStream_t s)
 {
-    k_rms<<<1, 1024, 0, s>>>(n, a, out);
+    k_rms<<<1, 1024, 0, s>>>(n, a, out, g_stop);
     launches_counter_add(1);
 }
 
@@ -491,8 +503,9 @@ __device__ __forceinline__ long long field_at(const Geo& g, int i, int j, int k)
 
 // dense = field unknowns (type T -> float)
 template <typename T>
-__global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restrict__ dense)
+__global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restrict__ dense, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= ux) return;
@@ -501,8 +514,9 @@ __global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restri
 
 // field unknowns (+)= scale * dense
 template <typename T>
-__global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __restrict__ f, float scale, int add)
+__global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __restrict__ f, float scale, int add, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= ux) return;
@@ -515,7 +529,7 @@ template <typename T>
 void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
 {
     k_field_to_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
-        g, f, dense);
+        g, f, dense, g_stop);
     launches_counter_add(1);
 }
 
@@ -523,7 +537,7 @@ template <typename T>
 void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s)
 {
     k_dense_to_field<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
-        g, dense, f, scale, add);
+        g, dense, f, scale, add, g_stop);
     launches_counter_add(1);
 }
 
@@ -568,8 +582,9 @@ __device__ __forceinline__ T residual_at(const Geo& g, const T* __restrict__ r, 
 // dense = r - A z at the unknowns.
 template <typename T>
 __global__ void k_field_residual_dense(Geo g, const T* __restrict__ r, const T* __restrict__ z, StencilW<T> w,
-                                       float* __restrict__ dense)
+                                       float* __restrict__ dense, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= ux) return;
@@ -604,8 +619,9 @@ static dim3 zblock(const Shape& sh) { return dim3(32, (unsigned)sh.ty, 1); }
 // out = r - A z at the unknowns (z planes k-1, k, k+1 kept in registers).
 template <typename T>
 __global__ void __launch_bounds__(256) k_field_residual(Geo g, Shape sh, const T* __restrict__ r,
-                                                        const T* __restrict__ z, StencilW<T> w, T* __restrict__ out)
+                                                        const T* __restrict__ z, StencilW<T> w, T* __restrict__ out, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
     const long long sj = g.sj, sk = g.sk;
@@ -625,8 +641,9 @@ __global__ void __launch_bounds__(256) k_field_residual(Geo g, Shape sh, const T
 
 // x += y at the unknowns.
 template <typename T>
-__global__ void __launch_bounds__(256) k_field_axpy(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ y)
+__global__ void __launch_bounds__(256) k_field_axpy(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ y, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
     long long c = q.c;
@@ -643,8 +660,9 @@ __global__ void __launch_bounds__(256) k_field_axpy(Geo g, Shape sh, T* __restri
 template <typename T, bool HAS_Z>
 __global__ void __launch_bounds__(128) k_field_residual_restrict(Geo g, const T* __restrict__ r,
                                                                  const T* __restrict__ z, StencilW<T> w, Dims dc,
-                                                                 int zc, float* __restrict__ coarse)
+                                                                 int zc, float* __restrict__ coarse, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dc.W || y >= dc.H) return;
     const int z0 = blockIdx.z * zc, z1 = min(dc.D, z0 + zc);
@@ -731,8 +749,9 @@ __global__ void __launch_bounds__(128) k_field_residual_restrict(Geo g, const T*
 // (x, y) once (4 loads), so a fine point costs about 2 coarse loads.
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
-                                                           T* __restrict__ f)
+                                                           T* __restrict__ f, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
     const int ii = q.i - g.lo[0], jj = q.j - g.lo[1];
@@ -799,19 +818,19 @@ template <typename T>
 void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s)
 {
     k_field_residual_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
-        g, r, z, stencil_w<T>(g), dense);
+        g, r, z, stencil_w<T>(g), dense, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
 void field_residual(const Geo& g, const Shape& sh, const T* r, const T* z, T* out, cudaStream_t s)
 {
-    k_field_residual<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, r, z, stencil_w<T>(g), out);
+    k_field_residual<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, r, z, stencil_w<T>(g), out, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
 void field_axpy(const Geo& g, const Shape& sh, T* x, const T* y, cudaStream_t s)
 {
-    k_field_axpy<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, x, y);
+    k_field_axpy<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, x, y, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
@@ -820,14 +839,14 @@ void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& d
     const int zc = 8;
     const dim3 block(32, 4);
     const dim3 grid((unsigned)((dc.W + 31) / 32), (unsigned)((dc.H + 3) / 4), (unsigned)((dc.D + zc - 1) / zc));
-    if (z) k_field_residual_restrict<T, true><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse);
-    else k_field_residual_restrict<T, false><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse);
+    if (z) k_field_residual_restrict<T, true><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
+    else k_field_residual_restrict<T, false><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
 void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
 {
-    k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f);
+    k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
     launches_counter_add(1);
 }
 template void field_residual_dense<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
@@ -864,8 +883,9 @@ __device__ __forceinline__ float level_negdiag(const DLevel& L, bool lx, bool ly
 template <bool CHEB, bool FIRST, bool HASZ, bool ACC>
 __global__ void __launch_bounds__(256) k_level_pass(Dims d, DLevel L, int kchunk, const float* __restrict__ Y,
                                                     const float* __restrict__ B, const float* __restrict__ Z,
-                                                    float* __restrict__ W, LCoef c)
+                                                    float* __restrict__ W, LCoef c, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= d.W || y >= d.H) return;
     const int z0 = blockIdx.z * kchunk, z1 = min(d.D, z0 + kchunk);
@@ -955,7 +975,7 @@ void level_residual(const Dims& d, const DLevel& L, const float* Y, const float*
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    k_level_pass<false, false, false, false><<<grid, dim3(32, 8), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{});
+    k_level_pass<false, false, false, false><<<grid, dim3(32, 8), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, g_stop);
     launches_counter_add(1);
 }
 
@@ -967,14 +987,14 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
     level_launch(d, kchunk, grid);
     const dim3 blk(32, 8);
     if (first) {
-        if (acc) k_level_pass<true, true, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
-        else k_level_pass<true, true, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        if (acc) k_level_pass<true, true, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else k_level_pass<true, true, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
     } else if (Z) {
-        if (acc) k_level_pass<true, false, true, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
-        else k_level_pass<true, false, true, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        if (acc) k_level_pass<true, false, true, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else k_level_pass<true, false, true, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
     } else {
-        if (acc) k_level_pass<true, false, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
-        else k_level_pass<true, false, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c);
+        if (acc) k_level_pass<true, false, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else k_level_pass<true, false, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
     }
     launches_counter_add(1);
 }
@@ -982,8 +1002,9 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
 // Full-weighting restriction of dense unknown arrays, fine (2m) -> coarse (m) per
 // axis: coarse unknown I sits on fine unknown 2I+1 (0-based), weights 1/4,1/2,1/4
 // per axis; fine values beyond the grid are the Dirichlet zero.
-__global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __restrict__ coarse)
+__global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __restrict__ coarse, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= dc.W) return;
     const int Wf = dc.W * 2, Hf = dc.H * 2, Df = dc.D * 2;
@@ -1010,15 +1031,16 @@ __global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __res
 
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 {
-    k_restrict<<<field_grid(dc.W, dc.H, dc.D, 128), 128, 0, s>>>(dc, fine, coarse);
+    k_restrict<<<field_grid(dc.W, dc.H, dc.D, 128), 128, 0, s>>>(dc, fine, coarse, g_stop);
     launches_counter_add(1);
 }
 
 // Trilinear prolongation, coarse (m) -> fine (2m): fine unknown i takes coarse
 // (i-1)/2 exactly when i is odd (0-based), the mean of its two coarse neighbours
 // otherwise (zero beyond the grid); the transpose of k_restrict up to a factor 8.
-__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine, int add)
+__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine, int add, const int* __restrict__ stop)
 {
+    if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     const int Wf = dc.W * 2, Hf = dc.H * 2;
     if (x >= Wf) return;
@@ -1057,13 +1079,13 @@ __global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __re
 
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 0);
+    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 0, g_stop);
     launches_counter_add(1);
 }
 
 void prolong2_add(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 1);
+    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 1, g_stop);
     launches_counter_add(1);
 }
 
