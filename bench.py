@@ -422,6 +422,61 @@ def run_learned_128(args, dev: int):
     return out
 
 
+def run_large(args, dev: int):
+    """Config 5 (opt-in, --large): one 1024^3 Dirichlet solve of 64 Gaussian charges on a
+    k^-3 background, the mixed + learned V-cycle (network on the 16^3 level, six
+    coarsenings) against the plain FP64 BiCGSTAB + Chebyshev path, both to 1e-10."""
+    import math
+
+    import torch
+
+    import parallelpoissonsolver_gb300 as pps
+    from parallelpoissonsolver_gb300 import workloads
+
+    m = 1024
+    grid = pps.BlockGrid.cube(m)
+    b_d = workloads.charges_device(m, device=f"cuda:{dev}")
+    x_d = torch.zeros_like(b_d)
+    k = int(round(math.log2(m / NET_GRID)))
+    net, scale, info = train_network(args, dev, k)
+    _, gain = learned_gain(m, scale)
+
+    def solve(s):
+        x_d.zero_()
+        torch.cuda.synchronize()
+        st = s.solve_device(x_d.data_ptr(), b_d.data_ptr())
+        return pps.status_string(st), s.stats()
+
+    head = pps.FlexibleCG(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, max_iteration=20000, form="mixed",
+                          use_graph=True, inner_tol=args.learned_inner_tol, device=dev)
+    head.set_learned(net, k, gain, pps.LEARNED_PRECONDITIONER)
+    head.set_learned_cycle(*VCYCLE)
+    head.autotune()
+    solve(head)   # warm-up
+    runs = [solve(head) for _ in range(2)]
+    head_x = x_d.clone()
+    head.close()
+    plain = pps.BiCGSTAB(grid, pps.ChebyshevIteration(DEGREE), tolerance=TOL, max_iteration=20000, form="fp64",
+                         use_graph=True, device=dev)
+    st_p, d_p = solve(plain)
+    plain.close()
+    rel = float(torch.linalg.norm(head_x - x_d) / torch.linalg.norm(x_d))
+    net.close()
+    t_head = sum(d["seconds_solve"] for _, d in runs) / len(runs)
+    return {
+        "workload": f"{m}^3 interior unknowns, Dirichlet 0, 64 Gaussian charges (width 2h, amplitude +-1) on a "
+                    f"k^-3 random-field background at 0.1 RMS; stop at FP64 ||r||/||b_adj|| <= {TOL:g}",
+        "mixed+learned": {"status": runs[-1][0], "value": t_head, "unit": "s",
+                          "iterations": runs[-1][1]["iterations"], "refinements": runs[-1][1]["refinements"],
+                          "err_true": runs[-1][1]["err_true"], "network_coarsen": k,
+                          "network_held_out_rel_err_median": info["held_out_rel_err_median"]},
+        "plain_fp64": {"status": st_p, "value": d_p["seconds_solve"], "unit": "s", "iterations": d_p["iterations"],
+                       "err_true": d_p["err_true"]},
+        "speedup_vs_plain_fp64": d_p["seconds_solve"] / t_head,
+        "vs_plain_fp64_rel_l2": rel,
+    }
+
+
 def run_batched(args, dist: Dist):
     """256 independent Dirichlet problems, edges uniform on {32,48,64,96,128}, each f a
     seeded sum of 1-8 Gaussian blobs; MIXED form to 1e-10 in one batch (one launch per
@@ -533,6 +588,7 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=3e-3)
     ap.add_argument("--learned-inner-tol", type=float, default=1e-5)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--large", action="store_true", help="also run the 1024^3 charges solve (several minutes)")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=16)
     ap.add_argument("--train-samples", type=int, default=256)
@@ -568,6 +624,8 @@ def main():
     out, iters_fp64 = run_gpu(args, dist)
     if not args.no_batched:
         out["batched"] = run_batched(args, dist)
+    if args.large:
+        out["large_1024"] = run_large(args, dist.local)
     if dist.rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_sample(args.size, REFERENCE_ITERATIONS.get(args.size) or iters_fp64, threads)

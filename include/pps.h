@@ -261,7 +261,7 @@ pps_status pps_unet_train_step(pps_unet* net, int nx, int ny, int nz, const floa
  *                               recurrence) as soon as the per-iteration reduction of
  *                               ||r||, the geometric mean over the last 4 iterations,
  *                               is worse than 0.5.
- * R, P: 2x restriction/prolongation, applied `coarsen` times; N: the network with
+ * R, P: 2x restriction/prolongation, applied `coarsen` (0..8) times; N: the network with
  * unit-RMS input scaling.  net = NULL detaches.  The network must outlive its use. */
 #define PPS_LEARNED_INITIAL_GUESS 1
 #define PPS_LEARNED_PRECONDITIONER 2

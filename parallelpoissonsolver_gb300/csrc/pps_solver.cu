@@ -1801,8 +1801,8 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
             set_error("the learned preconditioner takes Dirichlet grids only");
             return PPS_ERR_UNSUPPORTED;
         }
-        if (coarsen < 0 || coarsen > 5 || !(gain > 0.0) || (flags & ~15) != 0 || (flags & 3) == 0) {
-            set_error("coarsen 0..5, gain > 0, flags must include PPS_LEARNED_INITIAL_GUESS or _PRECONDITIONER");
+        if (coarsen < 0 || coarsen > 8 || !(gain > 0.0) || (flags & ~15) != 0 || (flags & 3) == 0) {
+            set_error("coarsen 0..8, gain > 0, flags must include PPS_LEARNED_INITIAL_GUESS or _PRECONDITIONER");
             return PPS_ERR_INVALID_ARG;
         }
         const Geo& g = s->geo;

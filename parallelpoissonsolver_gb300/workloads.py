@@ -27,24 +27,33 @@ def _interior(m: int, values: np.ndarray) -> np.ndarray:
     return b
 
 
+def _random_field_tensor(m: int, seed: int, slope: float, dev):
+    """The random field of random_field_values as a float64 torch tensor on `dev`."""
+    import torch
+    rng = np.random.default_rng(seed)
+    t = torch.from_numpy(rng.standard_normal((m, m, m))).to(dev)
+    F = torch.fft.rfftn(t)
+    del t
+    kz = torch.fft.fftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
+    kx = torch.fft.rfftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
+    k2 = kz[:, None, None] ** 2 + kz[None, :, None] ** 2 + kx[None, None, :] ** 2
+    amp = torch.where(k2 > 0, k2 ** (slope / 4.0), torch.zeros_like(k2))
+    F = F * amp
+    del amp, k2
+    out = torch.fft.irfftn(F, s=(m, m, m))
+    del F
+    return out / torch.sqrt(torch.mean(out * out))
+
+
 def random_field_values(m: int, seed: int, slope: float = -2.0, device=None) -> np.ndarray:
     """m^3 unit-RMS Gaussian random field with P(k) ~ k^slope (float64, z,y,x order)."""
-    rng = np.random.default_rng(seed)
-    noise = rng.standard_normal((m, m, m))
     try:
         import torch
         dev = device if device is not None else ("cuda" if torch.cuda.is_available() else "cpu")
-        t = torch.from_numpy(noise).to(dev)
-        F = torch.fft.rfftn(t)
-        kz = torch.fft.fftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
-        kx = torch.fft.rfftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
-        k2 = kz[:, None, None] ** 2 + kz[None, :, None] ** 2 + kx[None, None, :] ** 2
-        amp = torch.where(k2 > 0, k2 ** (slope / 4.0), torch.zeros_like(k2))
-        F = F * amp
-        out = torch.fft.irfftn(F, s=(m, m, m))
-        out = out / torch.sqrt(torch.mean(out * out))
-        return out.cpu().numpy()
+        return _random_field_tensor(m, seed, slope, dev).cpu().numpy()
     except ImportError:
+        rng = np.random.default_rng(seed)
+        noise = rng.standard_normal((m, m, m))
         F = np.fft.rfftn(noise)
         kz = np.fft.fftfreq(m, d=1.0 / m)
         kx = np.fft.rfftfreq(m, d=1.0 / m)
@@ -99,6 +108,27 @@ def charges(m: int, seed: int = 5, count: int = 64, background_rms: float = 0.1)
         gz = np.exp(-((c - cz) ** 2) / (2 * w * w))
         f += a * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
     return _interior(m, -f)
+
+
+def charges_device(m: int, seed: int = 5, count: int = 64, background_rms: float = 0.1, device="cuda"):
+    """charges() built on the GPU as a guard-padded float64 torch tensor (the 1024^3
+    case: 8.6 GB per field)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (m + 1)
+    c = torch.arange(1, m + 1, dtype=torch.float64, device=device) * h
+    f = background_rms * _random_field_tensor(m, seed + 1000, -3.0, device)
+    w = 2 * h
+    for _ in range(count):
+        cx, cy, cz = rng.uniform(0.0, 1.0, 3)
+        a = rng.choice([-1.0, 1.0])
+        gx = torch.exp(-((c - cx) ** 2) / (2 * w * w))
+        gy = torch.exp(-((c - cy) ** 2) / (2 * w * w))
+        gz = torch.exp(-((c - cz) ** 2) / (2 * w * w))
+        f.add_(a * gz[:, None, None] * gy[None, :, None] * gx[None, None, :])
+    b = torch.zeros((m + 4,) * 3, dtype=torch.float64, device=device)
+    b[2:m + 2, 2:m + 2, 2:m + 2] = -f
+    return b
 
 
 def edges_config3(count: int = 256, seed: int = 3):
