@@ -25,8 +25,8 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libppsref.so")
 REF_INCLUDE = "/root/reference/solverPoissonMPI_CPU/include"
 
-BICGSTAB, CG = 0, 1
-PREC_NONE, PREC_CHEBYSHEV = 0, 1
+BICGSTAB, CG, CHEBYSHEV_MAIN = 0, 1, 2
+PREC_NONE, PREC_CHEBYSHEV, PREC_BICGSTAB = 0, 1, 2
 
 
 class OraGrid(C.Structure):
@@ -36,12 +36,14 @@ class OraGrid(C.Structure):
 class OraConfig(C.Structure):
     _fields_ = [("krylov", C.c_int), ("precond", C.c_int), ("cheb_degree", C.c_int), ("cheb_eps", C.c_double),
                 ("rescale_min", C.c_double), ("rescale_max", C.c_double), ("tol", C.c_double),
-                ("maxit", C.c_int), ("threads", C.c_int)]
+                ("maxit", C.c_int), ("threads", C.c_int), ("prec_tol", C.c_double), ("prec_maxit", C.c_int),
+                ("prec_inner", C.c_int)]
 
 
 class OraStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("err_iter", C.c_double), ("err_true", C.c_double),
-                ("norm_b", C.c_double), ("seconds_loop", C.c_double), ("seconds_total", C.c_double)]
+                ("norm_b", C.c_double), ("seconds_loop", C.c_double), ("seconds_total", C.c_double),
+                ("prec_iterations", C.c_int)]
 
 
 @dataclass
@@ -101,12 +103,18 @@ class Config:
     tol: float = 1e-10
     maxit: int = 1700
     threads: int = 1
+    # PREC_BICGSTAB: the inner BiCGSTAB's toll_ and maxIteration, and its own
+    # preconditioner (PREC_NONE, or PREC_CHEBYSHEV with the fields above)
+    prec_tol: float = 1e-6
+    prec_maxit: int = 150
+    prec_inner: int = PREC_NONE
 
     def c(self):
         k = OraConfig()
         k.krylov, k.precond, k.cheb_degree = self.krylov, self.precond, self.cheb_degree
         k.cheb_eps, k.rescale_min, k.rescale_max = self.cheb_eps, self.rescale_min, self.rescale_max
         k.tol, k.maxit, k.threads = self.tol, self.maxit, self.threads
+        k.prec_tol, k.prec_maxit, k.prec_inner = self.prec_tol, self.prec_maxit, self.prec_inner
         return k
 
 
@@ -123,6 +131,7 @@ class Result:
     seconds_loop: float
     seconds_total: float
     history: np.ndarray = field(repr=False, default=None)
+    prec_iterations: int = 0
 
 
 def build(ref: bool | None = None, quiet: bool = True) -> None:
@@ -177,6 +186,10 @@ def ref_lib():
                                 C.c_double, C.c_double, C.c_int, dp, dp, C.c_void_p, C.POINTER(C.c_int), dp,
                                 C.c_void_p]
         L.ref_solve.restype = C.c_int
+        L.ref_solve2.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, ip, dp, dp, ip,
+                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, C.c_void_p,
+                                 C.POINTER(C.c_int), dp, C.c_void_p]
+        L.ref_solve2.restype = C.c_int
         L.ref_set_problem.argtypes = [ip, dp, dp, ip, C.c_int, dp, dp]
         L.ref_table.argtypes = [ip, C.c_int]
         _ref = L
@@ -223,13 +236,15 @@ def solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, neumann=None) -
     if rc != 0:
         raise ValueError("oracle rejected the configuration")
     return Result(st.iterations, st.err_iter, st.err_true, st.norm_b, st.seconds_loop, st.seconds_total,
-                  hist[: st.iterations + 1].copy())
+                  hist[: st.iterations + 1].copy(), st.prec_iterations)
 
 
 def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: int = 0, neumann=None) -> Result:
     """The reference's own classes, in place on x and b.  The reference plugin
     evaluates Neumann data from built-in problem `problem`, or looks it up in the
-    face arrays `neumann` when they are given."""
+    face arrays `neumann` when they are given.  With PREC_BICGSTAB the inner solver's
+    tolerance is an integer multiple of the main one (a template argument there), so
+    cfg.prec_tol must equal that multiple times cfg.tol exactly."""
     L = ref_lib()
     hist = np.full(cfg.maxit + 1, -1.0)
     it = C.c_int(0)
@@ -237,10 +252,15 @@ def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: in
     ptrs, keep = _neumann_ptrs(grid, neumann)
     if neumann is not None:
         problem = 2
-    rc = L.ref_solve(cfg.krylov, cfg.precond, cfg.cheb_degree, cfg.maxit, np.array(grid.np, np.int32),
-                     np.array(grid.ds, np.float64), np.array(grid.origin, np.float64), np.array(grid.bcs, np.int32),
-                     cfg.tol, cfg.cheb_eps, cfg.rescale_min, cfg.rescale_max, problem, x, b, hist.ctypes.data,
-                     C.byref(it), errs, ptrs)
+    pratio = 0
+    if cfg.krylov != CHEBYSHEV_MAIN and cfg.precond == PREC_BICGSTAB:
+        pratio = int(round(cfg.prec_tol / cfg.tol))
+        if float(pratio) * cfg.tol != cfg.prec_tol:
+            raise ValueError("prec_tol must be an integer multiple of tol for the reference")
+    rc = L.ref_solve2(cfg.krylov, cfg.precond, cfg.cheb_degree, cfg.maxit, cfg.prec_maxit, pratio, cfg.prec_inner,
+                      np.array(grid.np, np.int32), np.array(grid.ds, np.float64), np.array(grid.origin, np.float64),
+                      np.array(grid.bcs, np.int32), cfg.tol, cfg.cheb_eps, cfg.rescale_min, cfg.rescale_max, problem,
+                      x, b, hist.ctypes.data, C.byref(it), errs, ptrs)
     if rc == -2:
         raise KeyError("combination not instantiated in oracle/_ref")
     n = it.value

@@ -310,50 +310,54 @@ static void cheb_apply(const grid_t* G, cheb_t* C, double* B, double* X)
     }
 }
 
-static void precond_apply(const grid_t* G, int precond, cheb_t* C, double* B, double* X)
-{
-    if (precond == ORA_PREC_CHEBYSHEV) cheb_apply(G, C, B, X);
-    else memcpy(X, B, sizeof(double) * (size_t)G->ntot);   /* NoneSolver */
-}
+/* The seven work fields of one BiCGSTAB object (BiCGSTAB.hpp:23-37). */
+typedef struct {
+    double *pk, *rk, *r0, *Mpk, *AMpk, *zk, *Azk;
+} bicg_t;
 
-/* BiCGSTAB::operator() main loop (BiCGSTAB.hpp:55-322). */
-static int solve_bicgstab(const grid_t* G, const ora_config* cf, cheb_t* C, double* x, double* b,
-                          const double* const* neumann, double* hist, ora_stats* st)
+static int bicg_alloc(bicg_t* W, const grid_t* G)
 {
     const size_t nb = sizeof(double) * (size_t)G->ntot;
-    double* pk = (double*)calloc(1, nb);
-    double* rk = (double*)calloc(1, nb);
-    double* r0 = (double*)calloc(1, nb);
-    double* Mpk = (double*)calloc(1, nb);
-    double* AMpk = (double*)calloc(1, nb);
-    double* zk = (double*)calloc(1, nb);
-    double* Azk = (double*)calloc(1, nb);
-    if (!pk || !rk || !r0 || !Mpk || !AMpk || !zk || !Azk) return -1;
+    W->pk = (double*)calloc(1, nb); W->rk = (double*)calloc(1, nb); W->r0 = (double*)calloc(1, nb);
+    W->Mpk = (double*)calloc(1, nb); W->AMpk = (double*)calloc(1, nb);
+    W->zk = (double*)calloc(1, nb); W->Azk = (double*)calloc(1, nb);
+    return (W->pk && W->rk && W->r0 && W->Mpk && W->AMpk && W->zk && W->Azk) ? 0 : -1;
+}
 
-    const double toll = cf->tol;
+static void bicg_free(bicg_t* W)
+{
+    free(W->pk); free(W->rk); free(W->r0); free(W->Mpk); free(W->AMpk); free(W->zk); free(W->Azk);
+}
+
+/* A preconditioner object: the T_Preconditioner template argument of a solver
+ * (inputParam.hpp:24-33).  Kind ORA_PREC_BICGSTAB is a BiCGSTAB object with
+ * isMainLoop == false and communicationOFF, whose own preconditioner is `inner`. */
+typedef struct prec_s prec_t;
+struct prec_s {
+    int kind;
+    cheb_t C;            /* ORA_PREC_CHEBYSHEV */
+    bicg_t W;            /* ORA_PREC_BICGSTAB: its work fields */
+    prec_t* inner;       /* ORA_PREC_BICGSTAB: its preconditioner (none or Chebyshev) */
+    double toll;         /* ORA_PREC_BICGSTAB: toll_ (tolerance * tollScalingFactor) */
+    int maxit;           /* ORA_PREC_BICGSTAB: maxIteration */
+    long iterations;     /* ORA_PREC_BICGSTAB: inner iterations, summed over applications */
+};
+
+static void precond_apply(const grid_t* G, prec_t* P, double* B, double* X);
+
+/* The iteration loop of BiCGSTAB::operator() (BiCGSTAB.hpp:131-292).  On entry rk,
+ * pk and r0 hold the initial residual and x the initial iterate; P is the solver's
+ * preconditioner.  hist (main loop only) receives the recursive norms. */
+static int bicgstab_loop(const grid_t* G, prec_t* P, bicg_t* W, double* x, double toll, int maxit,
+                         double* hist, double* err_iter)
+{
+    double* pk = W->pk; double* rk = W->rk; double* r0 = W->r0; double* Mpk = W->Mpk;
+    double* AMpk = W->AMpk; double* zk = W->zk; double* Azk = W->Azk;
     double alphak = 1, betak = 1, omegak = 1, rho0 = 1, rho1 = 1;
     double pSum1, pSum2;
     int iter = 0;
-
-    reset_neumann(G, x, 1, neumann, 1.0);              /* normFieldB_ is 1 here */
-    const double normb = normalize(G, x, b, neumann);
-    st->norm_b = normb;
-    st->err_true = true_residual(G, x, b, rk, neumann, normb);
-    if (hist) hist[0] = st->err_true;
-    st->err_iter = -1.0;
-    st->iterations = 0;
-    st->seconds_loop = 0.0;
-    if (st->err_true < toll) {
-        /* The reference returns here without undoing the normalisation. */
-        goto out;
-    }
-    memcpy(pk, rk, nb);
-    memcpy(r0, rk, nb);
-    rho0 = 1;
-    rho1 = rho0;
-    const double t0 = now_s();
-    while (iter < cf->maxit) {
-        precond_apply(G, cf->precond, C, pk, Mpk);
+    while (iter < maxit) {
+        precond_apply(G, P, pk, Mpk);
         reset_neumann(G, Mpk, 0, NULL, 1.0);
         FOR_UNKNOWNS_PAR(G, { AMpk[c] = opA(G, Mpk, c); });
         pSum2 = dot_serial(G, r0, AMpk);
@@ -362,7 +366,7 @@ static int solve_bicgstab(const grid_t* G, const ora_config* cf, cheb_t* C, doub
             const double a = alphak;
             FOR_UNKNOWNS_PAR(G, { rk[c] = rk[c] - a * AMpk[c]; });
         }
-        precond_apply(G, cf->precond, C, rk, zk);
+        precond_apply(G, P, rk, zk);
         reset_neumann(G, zk, 0, NULL, 1.0);
         FOR_UNKNOWNS_PAR(G, { Azk[c] = opA(G, zk, c); });
         dot2_serial(G, rk, Azk, Azk, Azk, &pSum1, &pSum2);
@@ -373,7 +377,7 @@ static int solve_bicgstab(const grid_t* G, const ora_config* cf, cheb_t* C, doub
             FOR_UNKNOWNS_PAR(G, { rk[c] = rk[c] - w * Azk[c]; });
         }
         dot2_serial(G, r0, rk, rk, rk, &pSum1, &pSum2);
-        st->err_iter = sqrt(pSum2);
+        *err_iter = sqrt(pSum2);
         rho1 = pSum1;
         betak = rho1 / rho0 * alphak / omegak;
         rho0 = rho1;
@@ -382,22 +386,92 @@ static int solve_bicgstab(const grid_t* G, const ora_config* cf, cheb_t* C, doub
             FOR_UNKNOWNS_PAR(G, { pk[c] = rk[c] + be * (pk[c] - w * AMpk[c]); });
         }
         iter++;
-        if (hist) hist[iter] = st->err_iter;
-        if (st->err_iter < toll) break;
+        if (hist) hist[iter] = *err_iter;
+        if (*err_iter < toll) break;
     }
-    st->iterations = iter;
+    return iter;
+}
+
+static void zero_work(const grid_t* G, bicg_t* W)
+{
+    const size_t nb = sizeof(double) * (size_t)G->ntot;
+    memset(W->pk, 0, nb); memset(W->rk, 0, nb); memset(W->r0, 0, nb); memset(W->Mpk, 0, nb);
+    memset(W->AMpk, 0, nb); memset(W->zk, 0, nb); memset(W->Azk, 0, nb);
+}
+
+/* BiCGSTAB::operator() as a preconditioner: isMainLoop == false, communicationOFF
+ * (BiCGSTAB.hpp:55-322).  X = 0; B is normalised in place by its own norm over the
+ * unknowns (normalizeProblemToFieldBNorm<false>, iterativeSolverBase.hpp:171-234, no
+ * boundary adjustment); the loop runs to toll on that system; X and B are scaled
+ * back at the end, so B comes back as (B / n) * n. */
+static void bicg_precond(const grid_t* G, prec_t* P, double* B, double* X)
+{
+    bicg_t* W = &P->W;
+    zero_work(G, W);                                              /* :60-66 */
+    memset(X, 0, sizeof(double) * (size_t)G->ntot);              /* :94-97 */
+    const double normb = sqrt(dot_serial(G, B, B));
+    FOR_ALL_PAR(G, { X[c] /= normb; B[c] /= normb; });
+    /* computeErrorOperatorA<false,...>: resetNeumanBCs<false,true> is the mirror copy */
+    reset_neumann(G, X, 0, NULL, 1.0);
+    {
+        double* rk = W->rk;
+        FOR_UNKNOWNS_PAR(G, { rk[c] = B[c] - opA(G, X, c); });
+    }
+    const double errC = sqrt(dot_serial(G, W->rk, W->rk));
+    if (errC < P->toll) return;          /* :117-121: X and B stay normalised */
+    const size_t nb = sizeof(double) * (size_t)G->ntot;
+    memcpy(W->pk, W->rk, nb);
+    memcpy(W->r0, W->rk, nb);
+    double err = 0;
+    P->iterations += bicgstab_loop(G, P->inner, W, X, P->toll, P->maxit, NULL, &err);
+    reset_neumann(G, X, 0, NULL, 1.0);
+    FOR_ALL_PAR(G, { X[c] *= normb; B[c] *= normb; });
+}
+
+static void precond_apply(const grid_t* G, prec_t* P, double* B, double* X)
+{
+    if (P->kind == ORA_PREC_CHEBYSHEV) cheb_apply(G, &P->C, B, X);
+    else if (P->kind == ORA_PREC_BICGSTAB) bicg_precond(G, P, B, X);
+    else memcpy(X, B, sizeof(double) * (size_t)G->ntot);   /* NoneSolver */
+}
+
+/* BiCGSTAB::operator() main loop (BiCGSTAB.hpp:55-322). */
+static int solve_bicgstab(const grid_t* G, const ora_config* cf, prec_t* P, double* x, double* b,
+                          const double* const* neumann, double* hist, ora_stats* st)
+{
+    bicg_t W;
+    if (bicg_alloc(&W, G) != 0) { bicg_free(&W); return -1; }
+    const size_t nb = sizeof(double) * (size_t)G->ntot;
+    const double toll = cf->tol;
+
+    reset_neumann(G, x, 1, neumann, 1.0);              /* normFieldB_ is 1 here */
+    const double normb = normalize(G, x, b, neumann);
+    st->norm_b = normb;
+    st->err_true = true_residual(G, x, b, W.rk, neumann, normb);
+    if (hist) hist[0] = st->err_true;
+    st->err_iter = -1.0;
+    st->iterations = 0;
+    st->seconds_loop = 0.0;
+    if (st->err_true < toll) {
+        /* The reference returns here without undoing the normalisation. */
+        bicg_free(&W);
+        return 0;
+    }
+    memcpy(W.pk, W.rk, nb);
+    memcpy(W.r0, W.rk, nb);
+    const double t0 = now_s();
+    st->iterations = bicgstab_loop(G, P, &W, x, toll, cf->maxit, hist, &st->err_iter);
     reset_neumann(G, x, 1, neumann, normb);
     st->seconds_loop = now_s() - t0;
-    st->err_true = true_residual(G, x, b, rk, neumann, normb);
+    st->err_true = true_residual(G, x, b, W.rk, neumann, normb);
     FOR_ALL_PAR(G, { x[c] *= normb; b[c] *= normb; });
-out:
-    free(pk); free(rk); free(r0); free(Mpk); free(AMpk); free(zk); free(Azk);
+    bicg_free(&W);
     return 0;
 }
 
 /* BaseCG::operator() main loop (baseCG.hpp:44-260). orderNeumanBcs == 2, so the
  * reference skips its Neumann resets inside this loop (baseCG.hpp:123-124, 237-238). */
-static int solve_cg(const grid_t* G, const ora_config* cf, cheb_t* C, double* x, double* b,
+static int solve_cg(const grid_t* G, const ora_config* cf, prec_t* P, double* x, double* b,
                     const double* const* neumann, double* hist, ora_stats* st)
 {
     const size_t nb = sizeof(double) * (size_t)G->ntot;
@@ -420,7 +494,7 @@ static int solve_cg(const grid_t* G, const ora_config* cf, cheb_t* C, double* x,
     st->seconds_loop = 0.0;
     if (st->err_true < toll) goto out;
 
-    precond_apply(G, cf->precond, C, rk, zk);
+    precond_apply(G, P, rk, zk);
     memcpy(pk, zk, nb);
     const double t0 = now_s();
     while (iter < cf->maxit) {
@@ -434,7 +508,7 @@ static int solve_cg(const grid_t* G, const ora_config* cf, cheb_t* C, double* x,
                 rk[c] = rk[c] - a * Apk[c];
             });
         }
-        precond_apply(G, cf->precond, C, rk, zk);
+        precond_apply(G, P, rk, zk);
         dot2_serial(G, rk, zk, rk, rk, &pSum2, &pSumRk);
         betak = pSum2 / pSum1;
         st->err_iter = sqrt(pSumRk);
@@ -455,6 +529,47 @@ out:
     return 0;
 }
 
+/* ChebyshevIteration::operator() as the main solver: isMainLoop == true
+ * (chebyshevIteration.hpp:48-140).  A copy of b is adjusted for the boundary data
+ * and the polynomial of degree maxIteration is applied to it, overwriting x at the
+ * unknowns (the initial guess is not used); there is no convergence test and no
+ * normalisation (normFieldB_ stays 1), so both errors are the absolute true
+ * residual ||b - A x||.  norm_b is reported for the caller only. */
+static int solve_cheb_main(const grid_t* G, const ora_config* cf, cheb_t* C, double* x, double* b,
+                           const double* const* neumann, ora_stats* st)
+{
+    const size_t nb = sizeof(double) * (size_t)G->ntot;
+    double* bt = (double*)malloc(nb);
+    double* r = (double*)calloc(1, nb);
+    if (!bt || !r) { free(bt); free(r); return -1; }
+    memcpy(bt, b, nb);
+    adjust_b(G, x, bt, neumann);
+    st->norm_b = sqrt(dot_serial(G, bt, bt));
+    const double t0 = now_s();
+    cheb_apply(G, C, bt, x);
+    st->seconds_loop = now_s() - t0;
+    st->err_true = true_residual(G, x, b, r, neumann, 1.0);
+    st->err_iter = st->err_true;
+    st->iterations = cf->cheb_degree;
+    free(bt);
+    free(r);
+    return 0;
+}
+
+static int prec_init(prec_t* P, int kind, const grid_t* G, const ora_grid* g, const ora_config* c)
+{
+    memset(P, 0, sizeof(*P));
+    P->kind = kind;
+    if (kind == ORA_PREC_CHEBYSHEV) return cheb_init(&P->C, G, g, c);
+    return 0;
+}
+
+static void prec_free(prec_t* P)
+{
+    if (P->kind == ORA_PREC_CHEBYSHEV) cheb_free(&P->C);
+    if (P->kind == ORA_PREC_BICGSTAB) bicg_free(&P->W);
+}
+
 int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
               const double* const* neumann, double* history, ora_stats* st)
 {
@@ -462,14 +577,38 @@ int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
     if (!g || !c || !x || !b || !st) return -1;
     if (make_grid(g, c->threads, &G) != 0) return -1;
     if (c->maxit < 0 || c->cheb_degree < 1) return -1;
-    if (c->krylov != ORA_BICGSTAB && c->krylov != ORA_CG) return -1;
+    if (c->krylov != ORA_BICGSTAB && c->krylov != ORA_CG && c->krylov != ORA_CHEBYSHEV_MAIN) return -1;
+    if (c->precond < ORA_PREC_NONE || c->precond > ORA_PREC_BICGSTAB) return -1;
+    if (c->precond == ORA_PREC_BICGSTAB &&
+        (c->prec_maxit < 0 || (c->prec_inner != ORA_PREC_NONE && c->prec_inner != ORA_PREC_CHEBYSHEV)))
+        return -1;
     const double t0 = now_s();
-    cheb_t C;
-    memset(&C, 0, sizeof(C));
-    if (c->precond == ORA_PREC_CHEBYSHEV && cheb_init(&C, &G, g, c) != 0) return -1;
-    int rc = c->krylov == ORA_BICGSTAB ? solve_bicgstab(&G, c, &C, x, b, neumann, history, st)
-                                       : solve_cg(&G, c, &C, x, b, neumann, history, st);
-    if (c->precond == ORA_PREC_CHEBYSHEV) cheb_free(&C);
+    int rc = 0;
+    memset(st, 0, sizeof(*st));
+    if (c->krylov == ORA_CHEBYSHEV_MAIN) {
+        cheb_t C;
+        if (cheb_init(&C, &G, g, c) != 0) { cheb_free(&C); return -1; }
+        rc = solve_cheb_main(&G, c, &C, x, b, neumann, st);
+        cheb_free(&C);
+        st->seconds_total = now_s() - t0;
+        return rc;
+    }
+    prec_t P, Pin;
+    const int kind = c->precond;
+    if (prec_init(&P, kind, &G, g, c) != 0) { prec_free(&P); return -1; }
+    if (kind == ORA_PREC_BICGSTAB) {
+        if (prec_init(&Pin, c->prec_inner, &G, g, c) != 0 || bicg_alloc(&P.W, &G) != 0) {
+            prec_free(&Pin); prec_free(&P); return -1;
+        }
+        P.inner = &Pin;
+        P.toll = c->prec_tol;
+        P.maxit = c->prec_maxit;
+    }
+    rc = c->krylov == ORA_BICGSTAB ? solve_bicgstab(&G, c, &P, x, b, neumann, history, st)
+                                   : solve_cg(&G, c, &P, x, b, neumann, history, st);
+    st->prec_iterations = P.iterations;
+    if (kind == ORA_PREC_BICGSTAB) prec_free(&Pin);
+    prec_free(&P);
     st->seconds_total = now_s() - t0;
     return rc;
 }

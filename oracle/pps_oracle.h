@@ -9,7 +9,10 @@
  *   BlockGrid index limits / eigenvalue bounds   include/blockGrid.hpp:184-222, 301-340
  *   MatrixFreeOperatorA                          include/matrixFreeOperatorA.hpp:22-39
  *   ChebyshevIteration (preconditioner mode)     include/chebyshevIteration.hpp:19-34, 48-140
+ *   ChebyshevIteration (main solver, isMainLoop)  include/chebyshevIteration.hpp:48-140
  *   BiCGSTAB main loop                           include/BiCGSTAB.hpp:55-322
+ *   BiCGSTAB as a preconditioner (isMainLoop false, communicationOFF)
+ *                                                include/BiCGSTAB.hpp:55-322, inputParam.hpp:30
  *   BaseCG main loop                             include/baseCG.hpp:44-260
  *   NoneSolver                                   include/noneSolver.hpp:15-27
  *   normalisation / true residual / BC handling  include/iterativeSolverBase.hpp:62-234, 236-280, 429-534
@@ -38,11 +41,11 @@ typedef struct {
 } ora_grid;
 
 enum { ORA_BICGSTAB = 0, ORA_CG = 1, ORA_CHEBYSHEV_MAIN = 2 };
-enum { ORA_PREC_NONE = 0, ORA_PREC_CHEBYSHEV = 1 };
+enum { ORA_PREC_NONE = 0, ORA_PREC_CHEBYSHEV = 1, ORA_PREC_BICGSTAB = 2 };
 
 typedef struct {
-    int krylov;           /* ORA_BICGSTAB / ORA_CG                                  */
-    int precond;          /* ORA_PREC_NONE / ORA_PREC_CHEBYSHEV                      */
+    int krylov;           /* ORA_BICGSTAB / ORA_CG / ORA_CHEBYSHEV_MAIN              */
+    int precond;          /* ORA_PREC_NONE / ORA_PREC_CHEBYSHEV / ORA_PREC_BICGSTAB  */
     int cheb_degree;      /* Chebyshev maxIteration (chebyshevMax)                  */
     double cheb_eps;      /* epsilon                                                */
     double rescale_min;   /* rescaleEigMin                                          */
@@ -50,6 +53,11 @@ typedef struct {
     double tol;           /* tolerance * tollScalingFactor                          */
     int maxit;            /* maxIteration of the Krylov loop                        */
     int threads;          /* OpenMP threads for element-wise passes (sums stay serial) */
+    /* ORA_PREC_BICGSTAB: the inner BiCGSTAB object's toll_, maxIteration and its own
+     * preconditioner (ORA_PREC_NONE or ORA_PREC_CHEBYSHEV with the fields above). */
+    double prec_tol;
+    int prec_maxit;
+    int prec_inner;
 } ora_config;
 
 typedef struct {
@@ -59,12 +67,16 @@ typedef struct {
     double norm_b;        /* ||b_adj|| over the unknowns                            */
     double seconds_loop;  /* wall time of the Krylov loop (getDurationSolver)       */
     double seconds_total; /* wall time of the whole call                            */
+    int prec_iterations;  /* ORA_PREC_BICGSTAB: inner iterations, summed              */
 } ora_stats;
 
 /* Full solve in place on x (in/out) and b (scaled and unscaled in place, as the
- * reference does).  neumann[f] (f = 2*dir + side) holds du/d(dir) at the data nodes
- * of Neumann face f, laid out with the lower remaining axis fastest; NULL entries
- * mean zero flux.  history needs maxit+1 doubles (may be NULL).
+ * reference does).  ORA_CHEBYSHEV_MAIN applies the polynomial of degree cheb_degree
+ * (always Chebyshev, `precond` is not used), leaves b untouched and reports the
+ * absolute true residual in err_iter and err_true.  neumann[f] (f = 2*dir + side)
+ * holds du/d(dir) at the data nodes of Neumann face f, laid out with the lower
+ * remaining axis fastest; NULL entries mean zero flux.  history needs maxit+1
+ * doubles (may be NULL).
  * Returns 0, or -1 on an invalid argument. */
 int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
               const double* const* neumann, double* history, ora_stats* st);

@@ -105,8 +105,14 @@ int run(const RefArgs* a, double* x, double* b, double* hist, RefOut* out)
 
 typedef int (*run_fn)(const RefArgs*, double*, double*, double*, RefOut*);
 
+/* (krylov, precond, degree, maxit) as in the oracle's enums; for precond 2 (a BiCGSTAB
+ * object as the preconditioner, isMainLoop false) also its maxIteration (pmaxit), its
+ * tolerance template argument (pratio: toll_ = pratio * tollScalingFactor, i.e.
+ * pratio times the main tolerance) and its own preconditioner (pinner 0 none, 1
+ * Chebyshev of `degree`).  krylov 2 is ChebyshevIteration as the main solver. */
 struct Entry {
     int krylov, precond, degree, maxit;
+    int pmaxit, pratio, pinner;
     run_fn fn;
 };
 
@@ -114,11 +120,22 @@ template <int MAXIT, class P>
 using BiCG = BiCGSTAB<3, T_data, 1, MAXIT, true, true, P>;
 template <int MAXIT, class P>
 using CG = BaseCG<3, T_data, 1, MAXIT, true, true, P>;
+/* inputParam.hpp:30: BiCGSTAB<..., isbiCGMainLoop2 (false), communicationOFF, T_NoneSolver> */
+template <int PRATIO, int PMAXIT, class P>
+using BiCGPrec = BiCGSTAB<3, T_data, PRATIO, PMAXIT, false, false, P>;
+/* ALP/include/inputParam.hpp:37: the Chebyshev iteration as the main solver */
+template <int DEG>
+using ChebMain = ChebyshevIteration<3, T_data, 10000, DEG, true, true, NoneP>;
 
-#define BICG_CHEB(DEG, MAXIT) {0, 1, DEG, MAXIT, &run<BiCG<MAXIT, ChebP<DEG>>, MAXIT>}
-#define BICG_NONE(MAXIT) {0, 0, 0, MAXIT, &run<BiCG<MAXIT, NoneP>, MAXIT>}
-#define CG_CHEB(DEG, MAXIT) {1, 1, DEG, MAXIT, &run<CG<MAXIT, ChebP<DEG>>, MAXIT>}
-#define CG_NONE(MAXIT) {1, 0, 0, MAXIT, &run<CG<MAXIT, NoneP>, MAXIT>}
+#define BICG_CHEB(DEG, MAXIT) {0, 1, DEG, MAXIT, 0, 0, 0, &run<BiCG<MAXIT, ChebP<DEG>>, MAXIT>}
+#define BICG_NONE(MAXIT) {0, 0, 0, MAXIT, 0, 0, 0, &run<BiCG<MAXIT, NoneP>, MAXIT>}
+#define CG_CHEB(DEG, MAXIT) {1, 1, DEG, MAXIT, 0, 0, 0, &run<CG<MAXIT, ChebP<DEG>>, MAXIT>}
+#define CG_NONE(MAXIT) {1, 0, 0, MAXIT, 0, 0, 0, &run<CG<MAXIT, NoneP>, MAXIT>}
+#define BICG_BICG(MAXIT, PR, PM) {0, 2, 0, MAXIT, PM, PR, 0, &run<BiCG<MAXIT, BiCGPrec<PR, PM, NoneP>>, MAXIT>}
+#define BICG_BICG_CHEB(MAXIT, PR, PM, DEG) \
+    {0, 2, DEG, MAXIT, PM, PR, 1, &run<BiCG<MAXIT, BiCGPrec<PR, PM, ChebP<DEG>>>, MAXIT>}
+#define CG_BICG(MAXIT, PR, PM) {1, 2, 0, MAXIT, PM, PR, 0, &run<CG<MAXIT, BiCGPrec<PR, PM, NoneP>>, MAXIT>}
+#define CHEB_MAIN(DEG) {2, 1, DEG, DEG, 0, 0, 0, &run<ChebMain<DEG>, DEG>}
 
 const Entry kTable[] = {
     BICG_CHEB(1, 1700), BICG_CHEB(2, 1700), BICG_CHEB(3, 1700), BICG_CHEB(4, 1700),
@@ -126,6 +143,9 @@ const Entry kTable[] = {
     BICG_CHEB(11, 3), BICG_CHEB(24, 3), BICG_CHEB(11, 20000), BICG_CHEB(24, 1000),
     BICG_NONE(1700), BICG_NONE(20000),
     CG_CHEB(2, 1700), CG_CHEB(11, 1700), CG_CHEB(11, 20000), CG_NONE(1700), CG_NONE(20000),
+    BICG_BICG(1700, 100, 150), BICG_BICG(1700, 100, 3), BICG_BICG(1700, 100000000, 500),
+    BICG_BICG_CHEB(1700, 100, 150, 11), CG_BICG(1700, 100, 150),
+    CHEB_MAIN(1), CHEB_MAIN(2), CHEB_MAIN(3), CHEB_MAIN(4), CHEB_MAIN(11), CHEB_MAIN(24), CHEB_MAIN(80),
 };
 
 }  // namespace
@@ -133,12 +153,13 @@ const Entry kTable[] = {
 extern "C" {
 
 /* Solve in place with the reference's classes.  `problem` selects what the
- * plugin evaluates for Neumann data (2: the tabulated `faces`).  Returns 0, or -2
- * when the (krylov, precond, degree, maxit) combination was not instantiated. */
-int ref_solve(int krylov, int precond, int degree, int maxit, const int* np, const double* ds,
-              const double* origin, const int* bcs, double tol, double eps, double rescale_min,
-              double rescale_max, int problem, double* x, double* b, double* hist, int* iterations,
-              double* errs /* err_iter, err_true, seconds_loop, seconds_call */, const double* const* faces)
+ * plugin evaluates for Neumann data (2: the tabulated `faces`).  pmaxit, pratio and
+ * pinner select the inner BiCGSTAB of precond 2 (see Entry).  Returns 0, or -2 when
+ * the combination was not instantiated. */
+int ref_solve2(int krylov, int precond, int degree, int maxit, int pmaxit, int pratio, int pinner, const int* np,
+               const double* ds, const double* origin, const int* bcs, double tol, double eps, double rescale_min,
+               double rescale_max, int problem, double* x, double* b, double* hist, int* iterations,
+               double* errs /* err_iter, err_true, seconds_loop, seconds_call */, const double* const* faces)
 {
     for (int f = 0; f < 6; f++) ppsOracleFaces[f] = faces ? faces[f] : nullptr;
     RefArgs a;
@@ -146,15 +167,33 @@ int ref_solve(int krylov, int precond, int degree, int maxit, const int* np, con
     for (int f = 0; f < 6; f++) a.bcs[f] = bcs[f];
     a.tol = tol; a.eps = eps; a.rescale_min = rescale_min; a.rescale_max = rescale_max; a.problem = problem;
     for (const Entry& e : kTable) {
-        if (e.krylov == krylov && e.precond == precond && e.maxit == maxit && (precond == 0 || e.degree == degree)) {
+        bool match;
+        if (krylov == 2) {
+            match = e.krylov == 2 && e.degree == degree;
+        } else {
+            match = e.krylov == krylov && e.precond == precond && e.maxit == maxit &&
+                    (precond == 0 || (precond == 2 && pinner == 0) || e.degree == degree);
+            if (precond == 2) match = match && e.pmaxit == pmaxit && e.pratio == pratio && e.pinner == pinner;
+        }
+        if (match) {
             RefOut o;
-            int rc = e.fn(&a, x, b, hist, &o);
+            /* the Chebyshev main loop keeps no history; its degree may exceed the caller's maxit */
+            int rc = e.fn(&a, x, b, krylov == 2 ? nullptr : hist, &o);
             *iterations = o.iterations;
             errs[0] = o.err_iter; errs[1] = o.err_true; errs[2] = o.seconds_loop; errs[3] = o.seconds_call;
             return rc;
         }
     }
     return -2;
+}
+
+int ref_solve(int krylov, int precond, int degree, int maxit, const int* np, const double* ds,
+              const double* origin, const int* bcs, double tol, double eps, double rescale_min,
+              double rescale_max, int problem, double* x, double* b, double* hist, int* iterations,
+              double* errs, const double* const* faces)
+{
+    return ref_solve2(krylov, precond, degree, maxit, 0, 0, 0, np, ds, origin, bcs, tol, eps, rescale_min,
+                      rescale_max, problem, x, b, hist, iterations, errs, faces);
 }
 
 /* The instantiated (krylov, precond, degree, maxit) combinations, 4 ints each. */

@@ -14,6 +14,14 @@ and how its input fields are made:
                     solution, which exercises the reference's early return
                     (BiCGSTAB.hpp:118-122).
 
+The compositions of inputParam.hpp beyond the default: krylov 2 is
+ChebyshevIteration as the main solver (isMainLoop true, ALP/include/inputParam.hpp:37,
+used with the eigenvalue rescaling set to 1 as its comment asks); precond 2 is a
+BiCGSTAB object as the preconditioner (isMainLoop false, CPU/include/inputParam.hpp:30)
+with tolerance prec_tol, cap prec_maxit and its own preconditioner prec_inner
+(0 none, 1 Chebyshev).  The CPU preset's inner tolerance is tollPreconditionerSolver *
+tollScalingFactor = 1e4 * 1e-10, a hundred times the main one (solverSetup.hpp:22-33).
+
 `store` = "full" keeps input and output fields; "summary" keeps iteration count,
 residual history, checksums and a sample of the solution.
 """
@@ -70,6 +78,37 @@ CASES = [
     dict(name="problem0_m64", **cube(64), bcs=(0,) * 6, cfg=cfg(), inputs=("problem", 0), store="summary"),
     dict(name="problem0_m64_tol1e13", **cube(64), bcs=(0,) * 6, cfg=cfg(tol=1e-13, maxit=20000),
          inputs=("problem", 0), store="summary"),
+]
+
+PREC_BICG = dict(precond=2, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150, prec_inner=0)
+CHEB_MAIN = dict(krylov=2, cheb_eps=0.0, rescale_min=1.0, rescale_max=1.0)
+
+CASES += [
+    dict(name="bicgstab_precond_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(**PREC_BICG), inputs=("random", 20),
+         store="full"),
+    dict(name="bicgstab_precond_neumann_ragged", np=(9, 8, 10), ds=(0.1, 0.1, 0.1), origin=(0.0, 0.0, 0.0),
+         bcs=(0, 1, 1, 0, 0, 1), cfg=cfg(**PREC_BICG), inputs=("random", 21), store="full"),
+    dict(name="bicgstab_precond_cap3_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(**{**PREC_BICG, "prec_maxit": 3}),
+         inputs=("random", 22), store="full"),
+    dict(name="bicgstab_precond_chebyshev_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(**{**PREC_BICG, "prec_inner": 1}),
+         inputs=("random", 23), store="full"),
+    dict(name="cg_bicgstab_precond_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(krylov=1, **PREC_BICG),
+         inputs=("random", 24), store="full"),
+    dict(name="bicgstab_precond_alpaka_m8", **cube(8), bcs=(0,) * 6,
+         cfg=cfg(**{**PREC_BICG, "tol": 1e-10, "prec_tol": 1e8 * 1e-10, "prec_maxit": 500}), inputs=("random", 25),
+         store="full"),
+    dict(name="chebyshev_main_d80_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(cheb_degree=80, **CHEB_MAIN),
+         inputs=("random", 26), store="full"),
+    dict(name="chebyshev_main_d24_neumann_m8", **cube(8), bcs=(0, 1, 0, 1, 0, 1), cfg=cfg(cheb_degree=24, **CHEB_MAIN),
+         inputs=("problem", 0), store="full"),
+    dict(name="chebyshev_main_d1_m6", **cube(6), bcs=(0,) * 6, cfg=cfg(cheb_degree=1, **CHEB_MAIN),
+         inputs=("random", 27), store="full"),
+    dict(name="chebyshev_main_d2_m6", **cube(6), bcs=(0,) * 6, cfg=cfg(cheb_degree=2, **CHEB_MAIN),
+         inputs=("random", 28), store="full"),
+    dict(name="chebyshev_main_d3_m6", **cube(6), bcs=(0,) * 6, cfg=cfg(cheb_degree=3, **CHEB_MAIN),
+         inputs=("random", 29), store="full"),
+    dict(name="chebyshev_main_cpu_preset_m8", **cube(8), bcs=(0, 0, 1, 0, 0, 0), cfg=cfg(krylov=2, cheb_degree=11),
+         inputs=("random", 30), store="full"),
 ]
 
 BY_NAME = {c["name"]: c for c in CASES}

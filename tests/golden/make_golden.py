@@ -7,7 +7,7 @@ sample).  It also checks, before writing, that the C restatement in
 oracle/pps_oracle.c reproduces every output bit for bit.
 
 Usage (needs the reference sources, so it runs where they are mounted):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case name ...]     (default: every case)
 """
 from __future__ import annotations
 
@@ -85,7 +85,10 @@ def run_case(case):
 
 def main():
     O.build(ref=True)
+    names = set(sys.argv[1:])
     for case in CASES:
+        if names and case["name"] not in names:
+            continue
         out = run_case(case)
         path = os.path.join(HERE, case["name"] + ".npz")
         np.savez_compressed(path, **out)
