@@ -26,7 +26,7 @@ REF_PATH = os.path.join(HERE, "_ref", "libppsref.so")
 REF_INCLUDE = "/root/reference/solverPoissonMPI_CPU/include"
 
 BICGSTAB, CG, CHEBYSHEV_MAIN = 0, 1, 2
-PREC_NONE, PREC_CHEBYSHEV, PREC_BICGSTAB = 0, 1, 2
+PREC_NONE, PREC_CHEBYSHEV, PREC_BICGSTAB, PREC_CG = 0, 1, 2, 3
 
 
 class OraGrid(C.Structure):
@@ -103,7 +103,7 @@ class Config:
     tol: float = 1e-10
     maxit: int = 1700
     threads: int = 1
-    # PREC_BICGSTAB: the inner BiCGSTAB's toll_ and maxIteration, and its own
+    # PREC_BICGSTAB / PREC_CG: the inner solver's toll_ and maxIteration, and its own
     # preconditioner (PREC_NONE, or PREC_CHEBYSHEV with the fields above)
     prec_tol: float = 1e-6
     prec_maxit: int = 150
@@ -242,9 +242,9 @@ def solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, neumann=None) -
 def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: int = 0, neumann=None) -> Result:
     """The reference's own classes, in place on x and b.  The reference plugin
     evaluates Neumann data from built-in problem `problem`, or looks it up in the
-    face arrays `neumann` when they are given.  With PREC_BICGSTAB the inner solver's
-    tolerance is an integer multiple of the main one (a template argument there), so
-    cfg.prec_tol must equal that multiple times cfg.tol exactly."""
+    face arrays `neumann` when they are given.  With an inner solver (PREC_BICGSTAB,
+    PREC_CG) its tolerance is an integer multiple of the main one (a template
+    argument there), so cfg.prec_tol must equal that multiple times cfg.tol exactly."""
     L = ref_lib()
     hist = np.full(cfg.maxit + 1, -1.0)
     it = C.c_int(0)
@@ -253,7 +253,7 @@ def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: in
     if neumann is not None:
         problem = 2
     pratio = 0
-    if cfg.krylov != CHEBYSHEV_MAIN and cfg.precond == PREC_BICGSTAB:
+    if cfg.krylov != CHEBYSHEV_MAIN and cfg.precond in (PREC_BICGSTAB, PREC_CG):
         pratio = int(round(cfg.prec_tol / cfg.tol))
         if float(pratio) * cfg.tol != cfg.prec_tol:
             raise ValueError("prec_tol must be an integer multiple of tol for the reference")

@@ -330,17 +330,18 @@ static void bicg_free(bicg_t* W)
 }
 
 /* A preconditioner object: the T_Preconditioner template argument of a solver
- * (inputParam.hpp:24-33).  Kind ORA_PREC_BICGSTAB is a BiCGSTAB object with
- * isMainLoop == false and communicationOFF, whose own preconditioner is `inner`. */
+ * (inputParam.hpp:24-33).  Kinds ORA_PREC_BICGSTAB and ORA_PREC_CG are a BiCGSTAB or
+ * BaseCG object with isMainLoop == false and communicationOFF, whose own
+ * preconditioner is `inner` (the CG one uses pk, rk, AMpk as Apk and zk of W). */
 typedef struct prec_s prec_t;
 struct prec_s {
     int kind;
     cheb_t C;            /* ORA_PREC_CHEBYSHEV */
-    bicg_t W;            /* ORA_PREC_BICGSTAB: its work fields */
-    prec_t* inner;       /* ORA_PREC_BICGSTAB: its preconditioner (none or Chebyshev) */
-    double toll;         /* ORA_PREC_BICGSTAB: toll_ (tolerance * tollScalingFactor) */
-    int maxit;           /* ORA_PREC_BICGSTAB: maxIteration */
-    long iterations;     /* ORA_PREC_BICGSTAB: inner iterations, summed over applications */
+    bicg_t W;            /* inner solver: its work fields */
+    prec_t* inner;       /* inner solver: its preconditioner (none or Chebyshev) */
+    double toll;         /* inner solver: toll_ (tolerance * tollScalingFactor) */
+    int maxit;           /* inner solver: maxIteration */
+    long iterations;     /* inner solver: iterations, summed over applications */
 };
 
 static void precond_apply(const grid_t* G, prec_t* P, double* B, double* X);
@@ -428,10 +429,71 @@ static void bicg_precond(const grid_t* G, prec_t* P, double* B, double* X)
     FOR_ALL_PAR(G, { X[c] *= normb; B[c] *= normb; });
 }
 
+/* The iteration loop of BaseCG::operator() (baseCG.hpp:115-228).  On entry rk holds
+ * the initial residual, zk its preconditioned value and pk = zk.  orderNeumanBcs ==
+ * 2, so the reference skips its Neumann resets inside this loop (baseCG.hpp:123-124,
+ * 237-238). */
+static int cg_loop(const grid_t* G, prec_t* P, double* pk, double* rk, double* Apk, double* zk, double* x,
+                   double toll, int maxit, double* hist, double* err_iter)
+{
+    double alphak = 1, betak = 1, pSum1, pSum2, pSumRk;
+    int iter = 0;
+    while (iter < maxit) {
+        FOR_UNKNOWNS_PAR(G, { Apk[c] = opA(G, pk, c); });
+        dot2_serial(G, rk, zk, pk, Apk, &pSum1, &pSum2);
+        alphak = pSum1 / pSum2;
+        {
+            const double a = alphak;
+            FOR_UNKNOWNS_PAR(G, {
+                x[c] = x[c] + a * pk[c];
+                rk[c] = rk[c] - a * Apk[c];
+            });
+        }
+        precond_apply(G, P, rk, zk);
+        dot2_serial(G, rk, zk, rk, rk, &pSum2, &pSumRk);
+        betak = pSum2 / pSum1;
+        *err_iter = sqrt(pSumRk);
+        {
+            const double be = betak;
+            FOR_UNKNOWNS_PAR(G, { pk[c] = zk[c] + be * pk[c]; });
+        }
+        iter++;
+        if (hist) hist[iter] = *err_iter;
+        if (*err_iter < toll) break;
+    }
+    return iter;
+}
+
+/* BaseCG::operator() as a preconditioner: isMainLoop == false, communicationOFF
+ * (baseCG.hpp:44-260, composed at inputParam.hpp:29).  As bicg_precond, except
+ * that z = M r and p = z start the loop and X gets no Neumann reset at the end. */
+static void cg_precond(const grid_t* G, prec_t* P, double* B, double* X)
+{
+    bicg_t* W = &P->W;
+    const size_t nb = sizeof(double) * (size_t)G->ntot;
+    memset(W->pk, 0, nb); memset(W->rk, 0, nb); memset(W->AMpk, 0, nb); memset(W->zk, 0, nb);  /* :49-52 */
+    memset(X, 0, nb);                                                                           /* :81-84 */
+    const double normb = sqrt(dot_serial(G, B, B));
+    FOR_ALL_PAR(G, { X[c] /= normb; B[c] /= normb; });
+    reset_neumann(G, X, 0, NULL, 1.0);
+    {
+        double* rk = W->rk;
+        FOR_UNKNOWNS_PAR(G, { rk[c] = B[c] - opA(G, X, c); });
+    }
+    const double errC = sqrt(dot_serial(G, W->rk, W->rk));
+    if (errC < P->toll) return;          /* :104-108: X and B stay normalised */
+    precond_apply(G, P->inner, W->rk, W->zk);
+    memcpy(W->pk, W->zk, nb);
+    double err = 0;
+    P->iterations += cg_loop(G, P->inner, W->pk, W->rk, W->AMpk, W->zk, X, P->toll, P->maxit, NULL, &err);
+    FOR_ALL_PAR(G, { X[c] *= normb; B[c] *= normb; });
+}
+
 static void precond_apply(const grid_t* G, prec_t* P, double* B, double* X)
 {
     if (P->kind == ORA_PREC_CHEBYSHEV) cheb_apply(G, &P->C, B, X);
     else if (P->kind == ORA_PREC_BICGSTAB) bicg_precond(G, P, B, X);
+    else if (P->kind == ORA_PREC_CG) cg_precond(G, P, B, X);
     else memcpy(X, B, sizeof(double) * (size_t)G->ntot);   /* NoneSolver */
 }
 
@@ -469,8 +531,7 @@ static int solve_bicgstab(const grid_t* G, const ora_config* cf, prec_t* P, doub
     return 0;
 }
 
-/* BaseCG::operator() main loop (baseCG.hpp:44-260). orderNeumanBcs == 2, so the
- * reference skips its Neumann resets inside this loop (baseCG.hpp:123-124, 237-238). */
+/* BaseCG::operator() main loop (baseCG.hpp:44-260). */
 static int solve_cg(const grid_t* G, const ora_config* cf, prec_t* P, double* x, double* b,
                     const double* const* neumann, double* hist, ora_stats* st)
 {
@@ -479,10 +540,8 @@ static int solve_cg(const grid_t* G, const ora_config* cf, prec_t* P, double* x,
     double* rk = (double*)calloc(1, nb);
     double* Apk = (double*)calloc(1, nb);
     double* zk = (double*)calloc(1, nb);
-    if (!pk || !rk || !Apk || !zk) return -1;
+    if (!pk || !rk || !Apk || !zk) { free(pk); free(rk); free(Apk); free(zk); return -1; }
     const double toll = cf->tol;
-    double alphak = 1, betak = 1, pSum1, pSum2, pSumRk;
-    int iter = 0;
 
     reset_neumann(G, x, 1, neumann, 1.0);
     const double normb = normalize(G, x, b, neumann);
@@ -496,32 +555,11 @@ static int solve_cg(const grid_t* G, const ora_config* cf, prec_t* P, double* x,
 
     precond_apply(G, P, rk, zk);
     memcpy(pk, zk, nb);
-    const double t0 = now_s();
-    while (iter < cf->maxit) {
-        FOR_UNKNOWNS_PAR(G, { Apk[c] = opA(G, pk, c); });
-        dot2_serial(G, rk, zk, pk, Apk, &pSum1, &pSum2);
-        alphak = pSum1 / pSum2;
-        {
-            const double a = alphak;
-            FOR_UNKNOWNS_PAR(G, {
-                x[c] = x[c] + a * pk[c];
-                rk[c] = rk[c] - a * Apk[c];
-            });
-        }
-        precond_apply(G, P, rk, zk);
-        dot2_serial(G, rk, zk, rk, rk, &pSum2, &pSumRk);
-        betak = pSum2 / pSum1;
-        st->err_iter = sqrt(pSumRk);
-        {
-            const double be = betak;
-            FOR_UNKNOWNS_PAR(G, { pk[c] = zk[c] + be * pk[c]; });
-        }
-        iter++;
-        if (hist) hist[iter] = st->err_iter;
-        if (st->err_iter < toll) break;
+    {
+        const double t0 = now_s();
+        st->iterations = cg_loop(G, P, pk, rk, Apk, zk, x, toll, cf->maxit, hist, &st->err_iter);
+        st->seconds_loop = now_s() - t0;
     }
-    st->iterations = iter;
-    st->seconds_loop = now_s() - t0;
     st->err_true = true_residual(G, x, b, rk, neumann, normb);
     FOR_ALL_PAR(G, { x[c] *= normb; b[c] *= normb; });
 out:
@@ -567,7 +605,7 @@ static int prec_init(prec_t* P, int kind, const grid_t* G, const ora_grid* g, co
 static void prec_free(prec_t* P)
 {
     if (P->kind == ORA_PREC_CHEBYSHEV) cheb_free(&P->C);
-    if (P->kind == ORA_PREC_BICGSTAB) bicg_free(&P->W);
+    if (P->kind == ORA_PREC_BICGSTAB || P->kind == ORA_PREC_CG) bicg_free(&P->W);
 }
 
 int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
@@ -578,8 +616,9 @@ int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
     if (make_grid(g, c->threads, &G) != 0) return -1;
     if (c->maxit < 0 || c->cheb_degree < 1) return -1;
     if (c->krylov != ORA_BICGSTAB && c->krylov != ORA_CG && c->krylov != ORA_CHEBYSHEV_MAIN) return -1;
-    if (c->precond < ORA_PREC_NONE || c->precond > ORA_PREC_BICGSTAB) return -1;
-    if (c->precond == ORA_PREC_BICGSTAB &&
+    if (c->precond < ORA_PREC_NONE || c->precond > ORA_PREC_CG) return -1;
+    const int nested = c->precond == ORA_PREC_BICGSTAB || c->precond == ORA_PREC_CG;
+    if (nested &&
         (c->prec_maxit < 0 || (c->prec_inner != ORA_PREC_NONE && c->prec_inner != ORA_PREC_CHEBYSHEV)))
         return -1;
     const double t0 = now_s();
@@ -596,7 +635,7 @@ int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
     prec_t P, Pin;
     const int kind = c->precond;
     if (prec_init(&P, kind, &G, g, c) != 0) { prec_free(&P); return -1; }
-    if (kind == ORA_PREC_BICGSTAB) {
+    if (nested) {
         if (prec_init(&Pin, c->prec_inner, &G, g, c) != 0 || bicg_alloc(&P.W, &G) != 0) {
             prec_free(&Pin); prec_free(&P); return -1;
         }
@@ -606,8 +645,8 @@ int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
     }
     rc = c->krylov == ORA_BICGSTAB ? solve_bicgstab(&G, c, &P, x, b, neumann, history, st)
                                    : solve_cg(&G, c, &P, x, b, neumann, history, st);
-    st->prec_iterations = P.iterations;
-    if (kind == ORA_PREC_BICGSTAB) prec_free(&Pin);
+    st->prec_iterations = (int)P.iterations;
+    if (nested) prec_free(&Pin);
     prec_free(&P);
     st->seconds_total = now_s() - t0;
     return rc;

@@ -14,6 +14,8 @@
  *   BiCGSTAB as a preconditioner (isMainLoop false, communicationOFF)
  *                                                include/BiCGSTAB.hpp:55-322, inputParam.hpp:30
  *   BaseCG main loop                             include/baseCG.hpp:44-260
+ *   BaseCG as a preconditioner (isMainLoop false, communicationOFF)
+ *                                                include/baseCG.hpp:44-260, inputParam.hpp:29
  *   NoneSolver                                   include/noneSolver.hpp:15-27
  *   normalisation / true residual / BC handling  include/iterativeSolverBase.hpp:62-234, 236-280, 429-534
  *
@@ -41,11 +43,11 @@ typedef struct {
 } ora_grid;
 
 enum { ORA_BICGSTAB = 0, ORA_CG = 1, ORA_CHEBYSHEV_MAIN = 2 };
-enum { ORA_PREC_NONE = 0, ORA_PREC_CHEBYSHEV = 1, ORA_PREC_BICGSTAB = 2 };
+enum { ORA_PREC_NONE = 0, ORA_PREC_CHEBYSHEV = 1, ORA_PREC_BICGSTAB = 2, ORA_PREC_CG = 3 };
 
 typedef struct {
     int krylov;           /* ORA_BICGSTAB / ORA_CG / ORA_CHEBYSHEV_MAIN              */
-    int precond;          /* ORA_PREC_NONE / ORA_PREC_CHEBYSHEV / ORA_PREC_BICGSTAB  */
+    int precond;          /* ORA_PREC_NONE / _CHEBYSHEV / _BICGSTAB / _CG           */
     int cheb_degree;      /* Chebyshev maxIteration (chebyshevMax)                  */
     double cheb_eps;      /* epsilon                                                */
     double rescale_min;   /* rescaleEigMin                                          */
@@ -53,8 +55,9 @@ typedef struct {
     double tol;           /* tolerance * tollScalingFactor                          */
     int maxit;            /* maxIteration of the Krylov loop                        */
     int threads;          /* OpenMP threads for element-wise passes (sums stay serial) */
-    /* ORA_PREC_BICGSTAB: the inner BiCGSTAB object's toll_, maxIteration and its own
-     * preconditioner (ORA_PREC_NONE or ORA_PREC_CHEBYSHEV with the fields above). */
+    /* ORA_PREC_BICGSTAB / ORA_PREC_CG: the inner solver object's toll_, maxIteration
+     * and its own preconditioner (ORA_PREC_NONE or ORA_PREC_CHEBYSHEV with the fields
+     * above). */
     double prec_tol;
     int prec_maxit;
     int prec_inner;
@@ -67,7 +70,7 @@ typedef struct {
     double norm_b;        /* ||b_adj|| over the unknowns                            */
     double seconds_loop;  /* wall time of the Krylov loop (getDurationSolver)       */
     double seconds_total; /* wall time of the whole call                            */
-    int prec_iterations;  /* ORA_PREC_BICGSTAB: inner iterations, summed              */
+    int prec_iterations;  /* inner solver: iterations, summed over applications      */
 } ora_stats;
 
 /* Full solve in place on x (in/out) and b (scaled and unscaled in place, as the

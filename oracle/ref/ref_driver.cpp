@@ -105,8 +105,9 @@ int run(const RefArgs* a, double* x, double* b, double* hist, RefOut* out)
 
 typedef int (*run_fn)(const RefArgs*, double*, double*, double*, RefOut*);
 
-/* (krylov, precond, degree, maxit) as in the oracle's enums; for precond 2 (a BiCGSTAB
- * object as the preconditioner, isMainLoop false) also its maxIteration (pmaxit), its
+/* (krylov, precond, degree, maxit) as in the oracle's enums; for precond 2 or 3 (a
+ * BiCGSTAB or BaseCG object as the preconditioner, isMainLoop false) also its
+ * maxIteration (pmaxit), its
  * tolerance template argument (pratio: toll_ = pratio * tollScalingFactor, i.e.
  * pratio times the main tolerance) and its own preconditioner (pinner 0 none, 1
  * Chebyshev of `degree`).  krylov 2 is ChebyshevIteration as the main solver. */
@@ -123,6 +124,9 @@ using CG = BaseCG<3, T_data, 1, MAXIT, true, true, P>;
 /* inputParam.hpp:30: BiCGSTAB<..., isbiCGMainLoop2 (false), communicationOFF, T_NoneSolver> */
 template <int PRATIO, int PMAXIT, class P>
 using BiCGPrec = BiCGSTAB<3, T_data, PRATIO, PMAXIT, false, false, P>;
+/* inputParam.hpp:29: BaseCG<..., isbiCGMainLoop2 (false), communicationOFF, T_Preconditioner2> */
+template <int PRATIO, int PMAXIT, class P>
+using CGPrec = BaseCG<3, T_data, PRATIO, PMAXIT, false, false, P>;
 /* ALP/include/inputParam.hpp:37: the Chebyshev iteration as the main solver */
 template <int DEG>
 using ChebMain = ChebyshevIteration<3, T_data, 10000, DEG, true, true, NoneP>;
@@ -135,6 +139,9 @@ using ChebMain = ChebyshevIteration<3, T_data, 10000, DEG, true, true, NoneP>;
 #define BICG_BICG_CHEB(MAXIT, PR, PM, DEG) \
     {0, 2, DEG, MAXIT, PM, PR, 1, &run<BiCG<MAXIT, BiCGPrec<PR, PM, ChebP<DEG>>>, MAXIT>}
 #define CG_BICG(MAXIT, PR, PM) {1, 2, 0, MAXIT, PM, PR, 0, &run<CG<MAXIT, BiCGPrec<PR, PM, NoneP>>, MAXIT>}
+#define BICG_CGP_CHEB(MAXIT, PR, PM, DEG) \
+    {0, 3, DEG, MAXIT, PM, PR, 1, &run<BiCG<MAXIT, CGPrec<PR, PM, ChebP<DEG>>>, MAXIT>}
+#define BICG_CGP(MAXIT, PR, PM) {0, 3, 0, MAXIT, PM, PR, 0, &run<BiCG<MAXIT, CGPrec<PR, PM, NoneP>>, MAXIT>}
 #define CHEB_MAIN(DEG) {2, 1, DEG, DEG, 0, 0, 0, &run<ChebMain<DEG>, DEG>}
 
 const Entry kTable[] = {
@@ -145,6 +152,7 @@ const Entry kTable[] = {
     CG_CHEB(2, 1700), CG_CHEB(11, 1700), CG_CHEB(11, 20000), CG_NONE(1700), CG_NONE(20000),
     BICG_BICG(1700, 100, 150), BICG_BICG(1700, 100, 3), BICG_BICG(1700, 100000000, 500),
     BICG_BICG_CHEB(1700, 100, 150, 11), CG_BICG(1700, 100, 150),
+    BICG_CGP_CHEB(1700, 100, 150, 11), BICG_CGP(1700, 100, 150), BICG_CGP_CHEB(1700, 100, 3, 11),
     CHEB_MAIN(1), CHEB_MAIN(2), CHEB_MAIN(3), CHEB_MAIN(4), CHEB_MAIN(11), CHEB_MAIN(24), CHEB_MAIN(80),
 };
 
@@ -171,9 +179,10 @@ int ref_solve2(int krylov, int precond, int degree, int maxit, int pmaxit, int p
         if (krylov == 2) {
             match = e.krylov == 2 && e.degree == degree;
         } else {
+            const bool nested = precond == 2 || precond == 3;
             match = e.krylov == krylov && e.precond == precond && e.maxit == maxit &&
-                    (precond == 0 || (precond == 2 && pinner == 0) || e.degree == degree);
-            if (precond == 2) match = match && e.pmaxit == pmaxit && e.pratio == pratio && e.pinner == pinner;
+                    (precond == 0 || (nested && pinner == 0) || e.degree == degree);
+            if (nested) match = match && e.pmaxit == pmaxit && e.pratio == pratio && e.pinner == pinner;
         }
         if (match) {
             RefOut o;

@@ -17,9 +17,9 @@ and how its input fields are made:
 The compositions of inputParam.hpp beyond the default: krylov 2 is
 ChebyshevIteration as the main solver (isMainLoop true, ALP/include/inputParam.hpp:37,
 used with the eigenvalue rescaling set to 1 as its comment asks); precond 2 is a
-BiCGSTAB object as the preconditioner (isMainLoop false, CPU/include/inputParam.hpp:30)
-with tolerance prec_tol, cap prec_maxit and its own preconditioner prec_inner
-(0 none, 1 Chebyshev).  The CPU preset's inner tolerance is tollPreconditionerSolver *
+BiCGSTAB object as the preconditioner (isMainLoop false, CPU/include/inputParam.hpp:30),
+precond 3 a BaseCG object (inputParam.hpp:29), each with tolerance prec_tol, cap
+prec_maxit and its own preconditioner prec_inner (0 none, 1 Chebyshev).  The CPU preset's inner tolerance is tollPreconditionerSolver *
 tollScalingFactor = 1e4 * 1e-10, a hundred times the main one (solverSetup.hpp:22-33).
 
 `store` = "full" keeps input and output fields; "summary" keeps iteration count,
@@ -96,6 +96,14 @@ CASES += [
          inputs=("random", 24), store="full"),
     dict(name="bicgstab_precond_alpaka_m8", **cube(8), bcs=(0,) * 6,
          cfg=cfg(**{**PREC_BICG, "tol": 1e-10, "prec_tol": 1e8 * 1e-10, "prec_maxit": 500}), inputs=("random", 25),
+         store="full"),
+    dict(name="bicgstab_cg_precond_chebyshev_m8", **cube(8), bcs=(0,) * 6,
+         cfg=cfg(**{**PREC_BICG, "precond": 3, "prec_inner": 1}), inputs=("random", 31), store="full"),
+    dict(name="bicgstab_cg_precond_neumann_ragged", np=(9, 8, 10), ds=(0.1, 0.1, 0.1), origin=(0.0, 0.0, 0.0),
+         bcs=(1, 0, 0, 1, 1, 0), cfg=cfg(**{**PREC_BICG, "precond": 3, "prec_inner": 1}), inputs=("random", 32),
+         store="full"),
+    dict(name="bicgstab_cg_precond_cap3_m8", **cube(8), bcs=(0,) * 6,
+         cfg=cfg(**{**PREC_BICG, "precond": 3, "prec_inner": 1, "prec_maxit": 3}), inputs=("random", 33),
          store="full"),
     dict(name="chebyshev_main_d80_m8", **cube(8), bcs=(0,) * 6, cfg=cfg(cheb_degree=80, **CHEB_MAIN),
          inputs=("random", 26), store="full"),

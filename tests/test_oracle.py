@@ -90,6 +90,8 @@ def test_set_problem_matches_reference(oracle):
     (107, (0, 1, 0, 0, 1, 0), dict(precond=2, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150)),
     (108, (0,) * 6, dict(precond=2, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150, prec_inner=1)),
     (109, (0,) * 6, dict(krylov=1, precond=2, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150)),
+    (112, (0,) * 6, dict(precond=3, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150, prec_inner=1)),
+    (113, (0, 0, 1, 0, 0, 1), dict(precond=3, tol=1e-8, prec_tol=100.0 * 1e-8, prec_maxit=150)),
     (110, (0,) * 6, dict(krylov=2, cheb_degree=80, cheb_eps=0.0, rescale_min=1.0, rescale_max=1.0)),
     (111, (1, 0, 0, 1, 0, 0), dict(krylov=2, cheb_degree=24, cheb_eps=0.0, rescale_min=1.0, rescale_max=1.0)),
 ])
