@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define PPS_ABI_VERSION 1
+#define PPS_ABI_VERSION 2
 
 typedef enum {
     PPS_OK = 0,
@@ -54,11 +54,28 @@ typedef struct {
     int bcs[6];                 /* x- x+ y- y+ z- z+ : 0 Dirichlet, 1 Neumann            */
 } pps_grid;
 
-/* BiCGSTAB (BiCGSTAB.hpp), CG (baseCG.hpp), and flexible CG (no reference
- * counterpart: BaseCG with a Polak-Ribiere beta, for preconditioners that change
- * between applications, FP64 and MIXED forms, Dirichlet grids only). */
-typedef enum { PPS_KRYLOV_BICGSTAB = 0, PPS_KRYLOV_CG = 1, PPS_KRYLOV_FCG = 2 } pps_krylov;
-typedef enum { PPS_PREC_NONE = 0, PPS_PREC_CHEBYSHEV = 1 } pps_precond;
+/* Main solvers (T_Solver): BiCGSTAB (BiCGSTAB.hpp), CG (baseCG.hpp), flexible CG
+ * (no reference counterpart: BaseCG with a Polak-Ribiere beta, for preconditioners
+ * that change between applications, FP64 and MIXED forms, Dirichlet grids only),
+ * and the Chebyshev iteration as the main solver (ChebyshevIteration with
+ * isMainLoop true, chebyshevIteration.hpp:48-140, chebyshevIterationAlpaka.hpp:
+ * 320-587): the polynomial of degree cheb_degree applied once to the adjusted b,
+ * overwriting x at the unknowns, with no convergence test (`precond` is not used;
+ * the reference asks for rescale_min = rescale_max = 1 in this use,
+ * ALP/include/inputParam.hpp:21). */
+typedef enum {
+    PPS_KRYLOV_BICGSTAB = 0,
+    PPS_KRYLOV_CG = 1,
+    PPS_KRYLOV_FCG = 2,
+    PPS_KRYLOV_CHEBYSHEV = 3
+} pps_krylov;
+/* Preconditioners (T_Preconditioner): none (noneSolver.hpp), the Chebyshev
+ * polynomial (chebyshevIteration.hpp, isMainLoop false), or an inner solve from
+ * X = 0 on B / ||B|| to precond_tol or precond_maxit iterations, itself
+ * preconditioned by precond_inner: BiCGSTAB (BiCGSTAB.hpp with isMainLoop false,
+ * CPU/include/inputParam.hpp:30, ALP/include/inputParam.hpp:31-33) or CG (baseCG.hpp
+ * with isMainLoop false, CPU/include/inputParam.hpp:29). */
+typedef enum { PPS_PREC_NONE = 0, PPS_PREC_CHEBYSHEV = 1, PPS_PREC_BICGSTAB = 2, PPS_PREC_CG = 3 } pps_precond;
 
 typedef enum {
     /* FP64 with the reference's expression order and serial reductions: results are
@@ -90,6 +107,13 @@ typedef struct {
                                    0 = automatic.  Results do not depend on it.             */
     int use_graph;              /* replay the iteration as a CUDA graph (fast forms)        */
     int device;                 /* CUDA device ordinal                                      */
+    /* PPS_PREC_BICGSTAB, PPS_PREC_CG: the inner solver's toll_ (tollPreconditionerSolver *
+     * tollScalingFactor, on its ||r||/||B||, 0 < precond_tol < 1), maxIteration
+     * (iterMaxPreconditioner) and its own preconditioner (PPS_PREC_NONE, or
+     * PPS_PREC_CHEBYSHEV with the cheb_* fields above). */
+    double precond_tol;
+    int precond_maxit;
+    int precond_inner;
 } pps_config;
 
 typedef enum { PPS_PRESET_CPU = 0, PPS_PRESET_ALPAKA = 1 } pps_preset;
@@ -112,6 +136,9 @@ typedef struct {
     double sweep_bytes;         /* algorithmic bytes of those sweeps                        */
     int learned_applications;   /* network corrections applied (pps_set_learned)           */
     int fallback_iteration;     /* iteration at which the learned preconditioner was dropped, -1 none */
+    int precond_iterations;     /* inner solver: its iterations summed over the
+                                   applications (numIterationPreconditionerFinal_,
+                                   BiCGstabAlpaka.hpp:214,290)                              */
 } pps_stats;
 
 typedef struct pps_solver pps_solver;
@@ -127,7 +154,8 @@ typedef struct {
 typedef enum { PPS_PROBLEM_REFERENCE_DEFAULT = 0, PPS_PROBLEM_SINE = 1 } pps_builtin_problem;
 
 /* Defaults of the reference presets: CPU (n=11, eps=1e-4, rescale 500, tol 1e-8,
- * maxit 1700) or alpaka (n=24, eps=0, rescale 100, tol 1e-10, maxit 1000). */
+ * maxit 1700; inner BiCGSTAB preconditioner tol 1e-6, maxit 150) or alpaka (n=24,
+ * eps=0, rescale 100, tol 1e-10, maxit 1000; inner tol 1e-2, maxit 500). */
 pps_status pps_config_default(pps_config* cfg, int preset);
 
 /* Solver constructor (BiCGSTAB.hpp:18-39 with the ChebyshevIteration member,
@@ -147,7 +175,12 @@ pps_status pps_set_neumann(pps_solver* s, int face, const double* values);
 /* operator()(x, b, A) (BiCGSTAB.hpp:55-322, BiCGstabAlpaka.hpp:68-475): solves in
  * place on host arrays; x is in/out (Dirichlet nodes hold the boundary values),
  * b is input (PARITY form: scaled and unscaled in place exactly like the reference).
- * Returns PPS_OK, PPS_NOT_CONVERGED, PPS_BREAKDOWN or an error. */
+ * Returns PPS_OK, PPS_NOT_CONVERGED, PPS_BREAKDOWN or an error.
+ * PPS_KRYLOV_CHEBYSHEV: iterations = cheb_degree, err_iter = err_true = the
+ * absolute ||b - A x|| (the reference does not normalise in this use), history one
+ * entry holding it; PPS_OK when it is below tol * norm_b, else PPS_NOT_CONVERGED.
+ * The MIXED form applies the polynomial in FP32 to the FP64 residual up to
+ * max_refinements + 1 times, stopping at tol (iterations: degree x passes). */
 pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats);
 /* The same with device pointers (fields already resident in HBM). */
 pps_status pps_solve_device(pps_solver* s, double* x_dev, double* b_dev, pps_stats* stats);

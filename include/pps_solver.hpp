@@ -13,6 +13,14 @@
 // checkSolutionLocalGlobal keep the reference's signatures and meaning
 // (BiCGSTAB.hpp:18-55, iterativeSolverBase.hpp:51-55, 283-425).  The grid must be a
 // single rank (nranks 1x1x1): libpps runs one domain on one GPU.
+//
+// The other compositions of inputParam.hpp read the same way:
+//   pps::BiCGSTAB<..., true, true, pps::BiCGSTAB<..., false, false, T_NoneSolver>>
+//       an inner BiCGSTAB solve as the preconditioner (CPU/include/inputParam.hpp:30);
+//   pps::BiCGSTAB<..., true, true, pps::BaseCG<..., false, false, T_Preconditioner2>>
+//       an inner CG solve preconditioned by Chebyshev (inputParam.hpp:29);
+//   pps::ChebyshevIteration<..., chebyshevMax, true, true, T_NoneSolver>
+//       the Chebyshev iteration as the main solver (ALP/include/inputParam.hpp:37).
 #ifndef PPS_SOLVER_HPP
 #define PPS_SOLVER_HPP
 
@@ -22,6 +30,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "pps.h"
 
@@ -62,7 +71,7 @@ struct NoneSolver {
 
 template <int DIM, typename T_data, int tolerance, int maxIteration, bool isMainLoop, bool communicationON,
           typename T_Preconditioner>
-struct ChebyshevIteration {
+struct ChebyshevTag {
     static constexpr int precond = PPS_PREC_CHEBYSHEV;
     static constexpr int degree = maxIteration;
 };
@@ -92,6 +101,14 @@ class KrylovSolver {
     static_assert(sizeof(T_data) == sizeof(double), "fields are double precision");
 
 public:
+    // As the T_Preconditioner of another solver (isMainLoop false): an inner solve
+    // of this kind, tolerance and cap, preconditioned by its own T_Preconditioner.
+    static constexpr int precond = KRYLOV == PPS_KRYLOV_CG ? PPS_PREC_CG : PPS_PREC_BICGSTAB;
+    static constexpr int degree = T_Preconditioner::degree;
+    static constexpr int inner_precond = T_Preconditioner::precond;
+    static constexpr int inner_tolerance = tolerance;
+    static constexpr int inner_maxit = maxIteration;
+
     template <class BlockGridT, class ExactT, class CommT>
     KrylovSolver(const BlockGridT& grid, const ExactT& exact, CommT&)
         : exact_(&exact), f_(&ProblemTrampoline<ExactT>::f), u_(&ProblemTrampoline<ExactT>::u),
@@ -114,8 +131,22 @@ public:
         pps_config c;
         check(pps_config_default(&c, PPS_PRESET_CPU), "pps_config_default");
         c.krylov = KRYLOV;
-        c.precond = T_Preconditioner::precond;
-        c.cheb_degree = T_Preconditioner::degree > 0 ? T_Preconditioner::degree : 1;
+        if constexpr (KRYLOV == PPS_KRYLOV_CHEBYSHEV) {
+            c.precond = PPS_PREC_CHEBYSHEV;
+            c.cheb_degree = maxIteration;   // chebyshevMax
+        } else {
+            c.precond = T_Preconditioner::precond;
+            c.cheb_degree = T_Preconditioner::degree > 0 ? T_Preconditioner::degree : 1;
+            if constexpr (T_Preconditioner::precond == PPS_PREC_BICGSTAB || T_Preconditioner::precond == PPS_PREC_CG) {
+                static_assert(T_Preconditioner::inner_precond == PPS_PREC_NONE ||
+                                  T_Preconditioner::inner_precond == PPS_PREC_CHEBYSHEV,
+                              "an inner solver is preconditioned by NoneSolver or ChebyshevIteration");
+                c.precond_tol = static_cast<double>(T_Preconditioner::inner_tolerance) * p.toll_scaling;
+                c.precond_maxit = T_Preconditioner::inner_maxit;
+                c.precond_inner = T_Preconditioner::inner_precond;
+                nested_ = true;
+            }
+        }
         c.cheb_eps = p.epsilon;
         c.rescale_min = p.rescale_min;
         c.rescale_max = p.rescale_max;
@@ -161,7 +192,12 @@ public:
     {
         return std::chrono::duration<double>(stats_.seconds_solve);
     }
-    int getNumIterationPreconditionerFinal() const { return stats_.precond_applications; }
+    // numIterationPreconditionerFinal_: the inner solver's iterations, summed
+    // (BiCGstabAlpaka.hpp:214,290), or else the preconditioner applications
+    int getNumIterationPreconditionerFinal() const
+    {
+        return nested_ ? stats_.precond_iterations : stats_.precond_applications;
+    }
     pps_status lastStatus() const { return status_; }
     const pps_stats& stats() const { return stats_; }
     pps_solver* handle() const { return s_; }
@@ -206,6 +242,7 @@ private:
     pps_status status_ = PPS_OK;
     std::array<int, 3> npdata_{};
     std::array<double, 3> ds_{}, origin_{};
+    bool nested_ = false;
 };
 
 // BiCGSTAB<DIM, T_data, tolerance, maxIteration, isMainLoop, communicationON, T_Preconditioner>
@@ -219,6 +256,17 @@ template <int DIM, typename T_data, int tolerance, int maxIteration, bool isMain
           typename T_Preconditioner>
 using BaseCG = KrylovSolver<DIM, T_data, tolerance, maxIteration, isMainLoop, communicationON, T_Preconditioner,
                             PPS_KRYLOV_CG>;
+
+// ChebyshevIteration<DIM, T_data, tolerance, maxIteration, isMainLoop, communicationON,
+// T_Preconditioner>: a preconditioner tag (isMainLoop false), or the Chebyshev
+// iteration as the main solver (isMainLoop true), degree maxIteration.
+template <int DIM, typename T_data, int tolerance, int maxIteration, bool isMainLoop, bool communicationON,
+          typename T_Preconditioner>
+using ChebyshevIteration = typename std::conditional<
+    isMainLoop,
+    KrylovSolver<DIM, T_data, tolerance, maxIteration, isMainLoop, communicationON, T_Preconditioner,
+                 PPS_KRYLOV_CHEBYSHEV>,
+    ChebyshevTag<DIM, T_data, tolerance, maxIteration, isMainLoop, communicationON, T_Preconditioner>>::type;
 
 }  // namespace pps
 

@@ -28,8 +28,8 @@ LIB_PATH = os.path.join(HERE, "libpps.so")
 
 OK, NOT_CONVERGED, BREAKDOWN, NAN_DETECTED, TIMEOUT = 0, 1, 2, 3, 4
 ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_ZERO_RHS, ERR_UNSUPPORTED, ERR_NO_DEVICE = -1, -2, -3, -4, -5, -6
-KRYLOV_BICGSTAB, KRYLOV_CG, KRYLOV_FCG = 0, 1, 2
-PREC_NONE, PREC_CHEBYSHEV = 0, 1
+KRYLOV_BICGSTAB, KRYLOV_CG, KRYLOV_FCG, KRYLOV_CHEBYSHEV = 0, 1, 2, 3
+PREC_NONE, PREC_CHEBYSHEV, PREC_BICGSTAB, PREC_CG = 0, 1, 2, 3
 FORM_PARITY_FP64, FORM_FP64, FORM_MIXED = 0, 1, 2
 FORMS = {"parity": FORM_PARITY_FP64, "fp64": FORM_FP64, "mixed": FORM_MIXED}
 PRESET_CPU, PRESET_ALPAKA = 0, 1
@@ -61,7 +61,8 @@ class PpsConfig(C.Structure):
                 ("rescale_min", C.c_double), ("rescale_max", C.c_double), ("tol", C.c_double),
                 ("maxit", C.c_int), ("form", C.c_int), ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
                 ("max_refinements", C.c_int), ("check_every", C.c_int), ("use_graph", C.c_int),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("precond_tol", C.c_double), ("precond_maxit", C.c_int),
+                ("precond_inner", C.c_int)]
 
 
 class PpsStats(C.Structure):
@@ -70,7 +71,8 @@ class PpsStats(C.Structure):
                 ("seconds_solve", C.c_double), ("seconds_total", C.c_double), ("seconds_h2d", C.c_double),
                 ("seconds_d2h", C.c_double), ("hbm_bytes", C.c_double), ("kernel_launches", C.c_int),
                 ("sweep_seconds", C.c_double), ("sweep_launches", C.c_int), ("sweep_bytes", C.c_double),
-                ("learned_applications", C.c_int), ("fallback_iteration", C.c_int)]
+                ("learned_applications", C.c_int), ("fallback_iteration", C.c_int),
+                ("precond_iterations", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -257,6 +259,32 @@ class NoneSolver:
     """Identity preconditioner (noneSolver.hpp:15-27)."""
 
 
+@dataclass
+class BiCGSTABPreconditioner:
+    """An inner BiCGSTAB solve as the preconditioner: the BiCGSTAB class with
+    isMainLoop false (BiCGSTAB.hpp:55-322, CPU/include/inputParam.hpp:30).  From X = 0
+    it iterates on B / ||B|| until ||r|| < tolerance or max_iteration iterations,
+    itself preconditioned by `preconditioner` (NoneSolver or ChebyshevIteration).
+    Defaults: the CPU preset (tollPreconditionerSolver 1e4 x 1e-10, 150 iterations)."""
+    tolerance: float = 1e4 * 1e-10
+    max_iteration: int = 150
+    preconditioner: object = field(default_factory=NoneSolver)
+
+    kind = PREC_BICGSTAB
+
+
+@dataclass
+class BaseCGPreconditioner:
+    """An inner CG solve as the preconditioner: the BaseCG class with isMainLoop
+    false (baseCG.hpp:44-260, CPU/include/inputParam.hpp:29, there preconditioned by
+    the Chebyshev iteration)."""
+    tolerance: float = 1e4 * 1e-10
+    max_iteration: int = 150
+    preconditioner: object = field(default_factory=ChebyshevIteration)
+
+    kind = PREC_CG
+
+
 def _ptr(a: np.ndarray) -> int:
     if a.dtype != np.float64 or not a.flags.c_contiguous:
         raise TypeError("fields must be C-contiguous float64 arrays")
@@ -276,16 +304,32 @@ class Solver:
         cfg = PpsConfig()
         L.pps_config_default(C.byref(cfg), PRESET_CPU)
         if preconditioner is None:
-            preconditioner = ChebyshevIteration()
+            preconditioner = self.default_preconditioner()
         cfg.krylov = self.krylov
+
+        def chebyshev(p):
+            cfg.cheb_degree = p.degree
+            cfg.cheb_eps = p.epsilon
+            cfg.rescale_min = p.rescale_eig_min
+            cfg.rescale_max = p.rescale_eig_max
+
         if isinstance(preconditioner, NoneSolver):
             cfg.precond = PREC_NONE
+        elif isinstance(preconditioner, (BiCGSTABPreconditioner, BaseCGPreconditioner)):
+            cfg.precond = preconditioner.kind
+            cfg.precond_tol = float(preconditioner.tolerance)
+            cfg.precond_maxit = int(preconditioner.max_iteration)
+            inner = preconditioner.preconditioner
+            if isinstance(inner, ChebyshevIteration):
+                cfg.precond_inner = PREC_CHEBYSHEV
+                chebyshev(inner)
+            elif isinstance(inner, NoneSolver) or inner is None:
+                cfg.precond_inner = PREC_NONE
+            else:
+                raise TypeError("an inner solver is preconditioned by NoneSolver or ChebyshevIteration")
         else:
             cfg.precond = PREC_CHEBYSHEV
-            cfg.cheb_degree = preconditioner.degree
-            cfg.cheb_eps = preconditioner.epsilon
-            cfg.rescale_min = preconditioner.rescale_eig_min
-            cfg.rescale_max = preconditioner.rescale_eig_max
+            chebyshev(preconditioner)
         cfg.tol = float(tolerance)
         cfg.maxit = int(max_iteration)
         cfg.form = FORMS[form] if isinstance(form, str) else int(form)
@@ -303,6 +347,10 @@ class Solver:
         self._h = h
         self._stats = PpsStats()
         self.last_status = OK
+
+    @staticmethod
+    def default_preconditioner():
+        return ChebyshevIteration()
 
     def close(self):
         if getattr(self, "_h", None):
@@ -467,6 +515,21 @@ class FlexibleCG(Solver):
     """Flexible CG: BaseCG's loop with a Polak-Ribiere beta, so the preconditioner may
     change between applications (no reference counterpart; FP64 and MIXED forms)."""
     krylov = KRYLOV_FCG
+
+
+class ChebyshevSolver(Solver):
+    """The Chebyshev iteration as the main solver: ChebyshevIteration with isMainLoop
+    true (chebyshevIteration.hpp:48-140, chebyshevIterationAlpaka.hpp:320-587).  The
+    `preconditioner` argument carries the polynomial's parameters; by default degree
+    24 with the eigenvalue bounds unscaled (rescale 1, epsilon 0), as the reference
+    asks for this use (ALP/include/inputParam.hpp:21).  One application of the
+    polynomial to the adjusted b overwrites x; get_error_compute_operator() is the
+    absolute ||b - A x||."""
+    krylov = KRYLOV_CHEBYSHEV
+
+    @staticmethod
+    def default_preconditioner():
+        return ChebyshevIteration(degree=24, epsilon=0.0, rescale_eig_min=1.0, rescale_eig_max=1.0)
 
 
 class Batch:

@@ -234,6 +234,11 @@ void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double
 // x += scale * e at the unknowns (FP64 += FP32).
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState* st,
                          cudaStream_t s);
+// Start of an inner BiCGSTAB solve from X = 0: r = r0 = p = B at the unknowns, sum B^2.
+template <typename T>
+void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* p, RedCtx rc, cudaStream_t s);
+// out = (float)in over a whole field.
+void cast_field_f32(const double* in, float* out, long long n, cudaStream_t s);
 template <typename T>
 void fill_field(T* p, long long n, T v, cudaStream_t s);
 // Scalar state helpers.

@@ -1544,6 +1544,38 @@ __global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double*
     }
 }
 
+// Start of an inner BiCGSTAB solve from X = 0 (BiCGSTAB.hpp:94-126 with isMainLoop
+// false): the residual of the zero iterate is B, so r = r0 = p = B at the unknowns,
+// and sum B^2 feeds FIN_RES0 (||B|| is the normalisation and the initial residual).
+template <typename T>
+__global__ void __launch_bounds__(256) k_bicg_start(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ r,
+                                                    T* __restrict__ r0, T* __restrict__ p, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<T> a;
+    if (q.active) {
+        long long c = q.c;
+#pragma unroll 4
+        for (int k = q.k0; k < q.k1; k++) {
+            const T v = B[c];
+            r[c] = v;
+            r0[c] = v;
+            p[c] = v;
+            a.add(v, v);
+            c += g.sk;
+        }
+    }
+    double v[1] = {a.value()};
+    reduce_finalize<1>(v, rc);
+}
+
+__global__ void k_cast_f32(const double* __restrict__ in, float* __restrict__ out, long long n)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        out[c] = (float)in[c];
+}
+
 template <typename T>
 __global__ void k_fill(T* p, long long n, T v)
 {
@@ -1757,6 +1789,18 @@ void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* 
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
+void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* p, RedCtx rc, cudaStream_t s)
+{
+    k_bicg_start<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, r, r0, p, rc);
+    PPS_COUNT_LAUNCH();
+}
+void cast_field_f32(const double* in, float* out, long long n, cudaStream_t s)
+{
+    const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+    k_cast_f32<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(in, out, n);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
 void fill_field(T* p, long long n, T v, cudaStream_t s)
 {
     k_fill<T><<<par_blocks(n), 256, 0, s>>>(p, n, v);
@@ -1804,7 +1848,8 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
                                        cudaStream_t);                                                            \
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
                                    const Coef&, RedCtx, cudaStream_t, bool);                                     \
-    template void fill_field<T>(T*, long long, T, cudaStream_t);
+    template void fill_field<T>(T*, long long, T, cudaStream_t);                                                  \
+    template void fast_bicg_start<T>(const Geo&, const Shape&, const T*, T*, T*, T*, RedCtx, cudaStream_t);
 
 PPS_INST(double)
 PPS_INST(float)

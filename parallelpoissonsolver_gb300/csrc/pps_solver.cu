@@ -121,6 +121,17 @@ struct pps_solver {
     // Parity-form Chebyshev buffers rotate like the reference's member pointers.
     double *pY = nullptr, *pZ = nullptr, *pW = nullptr;
 
+    // The preconditioner the solve applies at this moment: cfg.precond, or, inside
+    // the inner solve of PPS_PREC_BICGSTAB / PPS_PREC_CG, cfg.precond_inner.
+    int prec_kind = PPS_PREC_CHEBYSHEV;
+    // PPS_PREC_BICGSTAB / PPS_PREC_CG: the inner solver's work fields (in the form's precision)
+    // and its own Krylov scalars; inner iterations summed over the applications.
+    Fields<double> in64;
+    Fields<float> in32;
+    DevState* d_st_in = nullptr;
+    DevState* h_st_in = nullptr;   // pinned
+    long long prec_iters = 0;
+
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     const void* g_key_x = nullptr;
@@ -211,10 +222,11 @@ long long face_count(const pps_solver* s, int f)
 }
 
 template <typename T>
-void alloc_fields(Fields<T>& F, long long ntot, bool with_e)
+void alloc_fields(Fields<T>& F, long long ntot, bool with_e, bool with_cheb = true)
 {
     T** all[] = {&F.p, &F.r, &F.r0, &F.Mp, &F.AMp, &F.z, &F.Az, &F.Y, &F.Z, &F.W};
     for (T** q : all) {
+        if (!with_cheb && (q == &F.Y || q == &F.Z || q == &F.W)) continue;
         CK(cudaMalloc((void**)q, sizeof(T) * (size_t)ntot));
         CK(cudaMemset(*q, 0, sizeof(T) * (size_t)ntot));
     }
@@ -245,9 +257,12 @@ void free_all(pps_solver* s)
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     free_fields(s->f64);
     free_fields(s->f32);
-    void* ptrs[] = {s->d_x, s->d_b, s->d_bt, s->d_dot, s->d_st, s->d_hist, s->d_partials, s->d_counter};
+    free_fields(s->in64);
+    free_fields(s->in32);
+    void* ptrs[] = {s->d_x, s->d_b, s->d_bt, s->d_dot, s->d_st, s->d_hist, s->d_partials, s->d_counter, s->d_st_in};
     for (void* q : ptrs)
         if (q) cudaFree(q);
+    if (s->h_st_in) cudaFreeHost(s->h_st_in);
     for (int i = 0; i < 6; i++)
         if (s->d_faces[i]) cudaFree(s->d_faces[i]);
     if (s->h_st) cudaFreeHost(s->h_st);
@@ -289,11 +304,46 @@ void par_neumann_helper(pps_solver* s, double* f)
     if (s->has_neumann) neumann_fill<double>(s->geo, f, faces_of(s), 0, 1.0, s->stream);
 }
 
-// ChebyshevIteration::operator() in preconditioner mode (chebyshevIteration.hpp:48-140)
+// While the inner solve of PPS_PREC_BICGSTAB / PPS_PREC_CG runs, the kernels and the
+// host polls use its own Krylov scalars, and the preconditioner applied inside it
+// is the inner solver's (precond_inner).  Restored when the scope ends.
+struct InnerScope {
+    pps_solver* s;
+    DevState* d;
+    DevState* h;
+    int kind;
+    explicit InnerScope(pps_solver* s_) : s(s_), d(s_->d_st), h(s_->h_st), kind(s_->prec_kind)
+    {
+        s->d_st = s->d_st_in;
+        s->h_st = s->h_st_in;
+        s->prec_kind = s->cfg.precond_inner;
+    }
+    ~InnerScope()
+    {
+        s->d_st = d;
+        s->h_st = h;
+        s->prec_kind = kind;
+    }
+};
+
+void par_bicgstab_precond(pps_solver* s, double* B, double* X);
+void par_cg_precond(pps_solver* s, double* B, double* X);
+
+// The preconditioner s->prec_kind names, applied X = M^{-1} B: NoneSolver's copy
+// (noneSolver.hpp:23-26), ChebyshevIteration::operator() in preconditioner mode
+// (chebyshevIteration.hpp:48-140), or the inner BiCGSTAB solve.
 void par_precond(pps_solver* s, double* B, double* X)
 {
     const Geo& g = s->geo;
-    if (s->cfg.precond == PPS_PREC_NONE) {
+    if (s->prec_kind == PPS_PREC_BICGSTAB) {
+        par_bicgstab_precond(s, B, X);
+        return;
+    }
+    if (s->prec_kind == PPS_PREC_CG) {
+        par_cg_precond(s, B, X);
+        return;
+    }
+    if (s->prec_kind == PPS_PREC_NONE) {
         CK(cudaMemcpyAsync(X, B, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, s->stream));
         return;
     }
@@ -318,6 +368,133 @@ double par_true_residual(pps_solver* s, double* x, double* b, double* r, double 
     if (s->has_neumann) neumann_fill<double>(s->geo, x, faces_of(s), 1, normb, s->stream);
     par_residual(s->geo, x, b, r, s->stream);
     return std::sqrt(par_dot(s, r, r));
+}
+
+// The iteration loop of BiCGSTAB::operator() (BiCGSTAB.hpp:131-292) with the
+// preconditioner s->prec_kind names.  On entry F.r, F.p and F.r0 hold the initial
+// residual.  `main` records the history and counts the applications.
+int par_bicgstab_loop(pps_solver* s, Fields<double>& F, double* x, double toll, int maxit, bool main,
+                      double* err_iter)
+{
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    double rho0 = 1, rho1 = 1, alphak = 1, omegak = 1, betak = 1, s1 = 0, s2 = 0;
+    int iter = 0;
+    while (iter < maxit) {
+        par_precond(s, F.p, F.Mp);
+        par_neumann_helper(s, F.Mp);
+        par_stencil(g, F.Mp, F.AMp, st);
+        s2 = par_dot(s, F.r0, F.AMp);
+        alphak = rho0 / s2;
+        par_axpy(g, F.r, F.AMp, alphak, st);
+        par_precond(s, F.r, F.z);
+        par_neumann_helper(s, F.z);
+        if (main) s->stats.precond_applications += 2;
+        par_stencil(g, F.z, F.Az, st);
+        par_dot2(s, F.r, F.Az, F.Az, F.Az, &s1, &s2);
+        omegak = s1 / s2;
+        par_update_x_all(g, x, F.Mp, F.z, alphak, omegak, st);
+        par_axpy(g, F.r, F.Az, omegak, st);
+        par_dot2(s, F.r0, F.r, F.r, F.r, &s1, &s2);
+        *err_iter = std::sqrt(s2);
+        rho1 = s1;
+        betak = rho1 / rho0 * alphak / omegak;
+        rho0 = rho1;
+        par_update_p(g, F.p, F.r, F.AMp, betak, omegak, st);
+        iter++;
+        if (main) s->history.push_back(*err_iter);
+        if (*err_iter < toll) break;
+    }
+    return iter;
+}
+
+// BiCGSTAB::operator() as a preconditioner: isMainLoop false, communicationOFF
+// (BiCGSTAB.hpp:55-322).  X = 0; B is normalised in place by its own norm over the
+// unknowns (normalizeProblemToFieldBNorm<false>, iterativeSolverBase.hpp:171-234,
+// without boundary adjustment); the loop runs to precond_tol on that system with
+// precond_inner as its preconditioner; X and B are scaled back at the end, so B
+// returns as (B / n) * n like the reference's.
+void par_bicgstab_precond(pps_solver* s, double* B, double* X)
+{
+    const Geo& g = s->geo;
+    Fields<double>& W = s->in64;
+    cudaStream_t st = s->stream;
+    const size_t fb = sizeof(double) * (size_t)g.ntot;
+    zero_fields(W, g.ntot, st);                   // BiCGSTAB.hpp:60-66
+    CK(cudaMemsetAsync(X, 0, fb, st));            // :94-97
+    const double normb = std::sqrt(par_dot(s, B, B));
+    par_scale_all(g, X, B, normb, 1, st);
+    par_neumann_helper(s, X);                     // resetNeumanBCs<false,true>: the mirror copy
+    par_residual(g, X, B, W.r, st);
+    const double errC = std::sqrt(par_dot(s, W.r, W.r));
+    if (errC < s->cfg.precond_tol) return;        // :117-121: X and B stay normalised
+    CK(cudaMemcpyAsync(W.p, W.r, fb, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(W.r0, W.r, fb, cudaMemcpyDeviceToDevice, st));
+    double err = 0;
+    {
+        InnerScope in(s);
+        s->prec_iters += par_bicgstab_loop(s, W, X, s->cfg.precond_tol, s->cfg.precond_maxit, false, &err);
+    }
+    par_neumann_helper(s, X);
+    par_scale_all(g, X, B, normb, 0, st);
+}
+
+// The iteration loop of BaseCG::operator() (baseCG.hpp:115-228) with the
+// preconditioner s->prec_kind names.  On entry F.r holds the initial residual, F.z
+// its preconditioned value and F.p = F.z; F.AMp serves as Apk.  orderNeumanBcs == 2,
+// so the loop makes no Neumann resets (baseCG.hpp:123-124, 237-238).
+int par_cg_loop(pps_solver* s, Fields<double>& F, double* x, double toll, int maxit, bool main, double* err_iter)
+{
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    double* zk = F.z;
+    double* Apk = F.AMp;
+    double alphak = 1, betak = 1, pSum1 = 0, pSum2 = 0, pSumRk = 0;
+    int iter = 0;
+    while (iter < maxit) {
+        par_stencil(g, F.p, Apk, st);
+        par_dot2(s, F.r, zk, F.p, Apk, &pSum1, &pSum2);
+        alphak = pSum1 / pSum2;
+        par_update_x(g, x, F.p, alphak, st);
+        par_axpy(g, F.r, Apk, alphak, st);
+        par_precond(s, F.r, zk);
+        if (main) s->stats.precond_applications++;
+        par_dot2(s, F.r, zk, F.r, F.r, &pSum2, &pSumRk);
+        betak = pSum2 / pSum1;
+        *err_iter = std::sqrt(pSumRk);
+        par_update_p_cg(g, F.p, zk, betak, st);
+        iter++;
+        if (main) s->history.push_back(*err_iter);
+        if (*err_iter < toll) break;
+    }
+    return iter;
+}
+
+// BaseCG::operator() as a preconditioner: isMainLoop false, communicationOFF
+// (baseCG.hpp:44-260): as par_bicgstab_precond, except that z = M r and p = z start
+// the loop and X gets no Neumann reset at the end (orderNeumanBcs == 2).
+void par_cg_precond(pps_solver* s, double* B, double* X)
+{
+    const Geo& g = s->geo;
+    Fields<double>& W = s->in64;
+    cudaStream_t st = s->stream;
+    const size_t fb = sizeof(double) * (size_t)g.ntot;
+    zero_fields(W, g.ntot, st);                   // baseCG.hpp:49-52
+    CK(cudaMemsetAsync(X, 0, fb, st));            // :81-84
+    const double normb = std::sqrt(par_dot(s, B, B));
+    par_scale_all(g, X, B, normb, 1, st);
+    par_neumann_helper(s, X);
+    par_residual(g, X, B, W.r, st);
+    const double errC = std::sqrt(par_dot(s, W.r, W.r));
+    if (errC < s->cfg.precond_tol) return;        // :104-108: X and B stay normalised
+    double err = 0;
+    {
+        InnerScope in(s);
+        par_precond(s, W.r, W.z);
+        CK(cudaMemcpyAsync(W.p, W.z, fb, cudaMemcpyDeviceToDevice, st));
+        s->prec_iters += par_cg_loop(s, W, X, s->cfg.precond_tol, s->cfg.precond_maxit, false, &err);
+    }
+    par_scale_all(g, X, B, normb, 0, st);
 }
 
 pps_status solve_parity(pps_solver* s, double* x, double* b)
@@ -346,60 +523,16 @@ pps_status solve_parity(pps_solver* s, double* x, double* b)
 
     CK(cudaMemcpyAsync(F.p, F.r, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(F.r0, F.r, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
-    double rho0 = 1, rho1 = 1, alphak = 1, omegak = 1, betak = 1, s1 = 0, s2 = 0;
     int iter = 0;
-    const bool cg = s->cfg.krylov == PPS_KRYLOV_CG;
-    if (cg) {
+    if (s->cfg.krylov == PPS_KRYLOV_CG) {
         // BaseCG::operator() (baseCG.hpp:109-228)
-        double* zk = F.z;
-        double* Apk = F.AMp;
-        par_precond(s, F.r, zk);
+        par_precond(s, F.r, F.z);
         S.precond_applications++;
-        CK(cudaMemcpyAsync(F.p, zk, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
-        double pSum1 = 0, pSum2 = 0, pSumRk = 0;
-        while (iter < s->cfg.maxit) {
-            par_stencil(g, F.p, Apk, st);
-            par_dot2(s, F.r, zk, F.p, Apk, &pSum1, &pSum2);
-            alphak = pSum1 / pSum2;
-            par_update_x(g, x, F.p, alphak, st);
-            par_axpy(g, F.r, Apk, alphak, st);
-            par_precond(s, F.r, zk);
-            S.precond_applications++;
-            par_dot2(s, F.r, zk, F.r, F.r, &pSum2, &pSumRk);
-            betak = pSum2 / pSum1;
-            S.err_iter = std::sqrt(pSumRk);
-            par_update_p_cg(g, F.p, zk, betak, st);
-            iter++;
-            s->history.push_back(S.err_iter);
-            if (S.err_iter < toll) break;
-        }
+        CK(cudaMemcpyAsync(F.p, F.z, sizeof(double) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+        iter = par_cg_loop(s, F, x, toll, s->cfg.maxit, true, &S.err_iter);
     } else {
         // BiCGSTAB::operator() (BiCGSTAB.hpp:131-292)
-        while (iter < s->cfg.maxit) {
-            par_precond(s, F.p, F.Mp);
-            par_neumann_helper(s, F.Mp);
-            par_stencil(g, F.Mp, F.AMp, st);
-            s2 = par_dot(s, F.r0, F.AMp);
-            alphak = rho0 / s2;
-            par_axpy(g, F.r, F.AMp, alphak, st);
-            par_precond(s, F.r, F.z);
-            par_neumann_helper(s, F.z);
-            S.precond_applications += 2;
-            par_stencil(g, F.z, F.Az, st);
-            par_dot2(s, F.r, F.Az, F.Az, F.Az, &s1, &s2);
-            omegak = s1 / s2;
-            par_update_x_all(g, x, F.Mp, F.z, alphak, omegak, st);
-            par_axpy(g, F.r, F.Az, omegak, st);
-            par_dot2(s, F.r0, F.r, F.r, F.r, &s1, &s2);
-            S.err_iter = std::sqrt(s2);
-            rho1 = s1;
-            betak = rho1 / rho0 * alphak / omegak;
-            rho0 = rho1;
-            par_update_p(g, F.p, F.r, F.AMp, betak, omegak, st);
-            iter++;
-            s->history.push_back(S.err_iter);
-            if (S.err_iter < toll) break;
-        }
+        iter = par_bicgstab_loop(s, F, x, toll, s->cfg.maxit, true, &S.err_iter);
         if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, normb, st);
     }
     S.iterations = iter;
@@ -490,12 +623,21 @@ template <typename T>
 void fast_cheb(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const ChebP& p);
 
 template <typename T>
+void fast_inner_precond(pps_solver* s, T* B, T* X, Launcher& L, bool cg);
+
+// The preconditioner s->prec_kind names: the identity, the Chebyshev polynomial,
+// or the inner BiCGSTAB solve.
+template <typename T>
 void fast_precond(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
 {
     const Geo& g = s->geo;
-    if (s->cfg.precond == PPS_PREC_NONE) {
+    if (s->prec_kind == PPS_PREC_NONE) {
         CK(cudaMemcpyAsync(X, B, sizeof(T) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, s->stream));
         L.bytes += bytes_of<T>(g.ntot, 2);
+        return;
+    }
+    if (s->prec_kind == PPS_PREC_BICGSTAB || s->prec_kind == PPS_PREC_CG) {
+        fast_inner_precond<T>(s, B, X, L, s->prec_kind == PPS_PREC_CG);
         return;
     }
     fast_cheb<T>(s, F, B, X, L, cheb_of(s));
@@ -825,6 +967,65 @@ void fast_bicgstab_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     L.launches += 5;
 }
 
+template <typename T>
+Fields<T>& inner_fields(pps_solver* s);
+template <>
+Fields<double>& inner_fields<double>(pps_solver* s)
+{
+    return s->in64;
+}
+template <>
+Fields<float>& inner_fields<float>(pps_solver* s)
+{
+    return s->in32;
+}
+
+void read_state(pps_solver* s);
+
+template <typename T>
+void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L);
+
+// BiCGSTAB or CG as the preconditioner (BiCGSTAB.hpp:55-322, baseCG.hpp:44-260 with
+// isMainLoop false): X = 0, then iterations on B with their own Krylov scalars, to
+// ||r|| < precond_tol ||B|| or precond_maxit iterations, preconditioned by
+// precond_inner.  The reference normalises B to unit norm first; the iteration is
+// invariant under that scaling, so the fast forms leave B unchanged.  The host
+// polls the inner stop flag every few iterations (an inner solve cannot sit inside
+// a captured graph, so the outer loop runs without one).
+template <typename T>
+void fast_inner_precond(pps_solver* s, T* B, T* X, Launcher& L, bool cg)
+{
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    Fields<T>& W = inner_fields<T>(s);
+    fill_field<T>(X, g.ntot, (T)0, st);
+    L.bytes += bytes_of<T>(g.ntot, 1);
+    if (s->cfg.precond_maxit < 1) return;
+    InnerScope in(s);
+    // FIN_RES0 with tol_relative: the stop target becomes precond_tol * ||B||
+    state_init(s->d_st, s->d_hist, s->cfg.precond_maxit, 0.0, s->cfg.precond_tol, 1, 1, 1.0, 0, st);
+    fast_bicg_start<T>(g, s->shape, B, W.r, W.r0, W.p, red(s, FIN_RES0), st);
+    L.bytes += bytes_of<T>(s->n_unknowns, 4);
+    if (cg) {
+        // z = M r, p = z (baseCG.hpp:110-112)
+        fast_precond<T>(s, W, W.r, W.z, L);
+        CK(cudaMemcpyAsync(W.p, W.z, sizeof(T) * (size_t)g.ntot, cudaMemcpyDeviceToDevice, st));
+    }
+    const int poll = 4;
+    for (;;) {
+        for (int q = 0; q < poll; q++) {
+            if (cg) fast_cg_iteration<T>(s, W, X, L);
+            else fast_bicgstab_iteration<T>(s, W, X, L);
+        }
+        read_state(s);
+        if (s->h_st->done) break;
+    }
+    s->prec_iters += s->h_st->iter;
+    // BiCGSTAB ends with resetNeumanBCs<false,true> on X, the mirror copy; CG with
+    // orderNeumanBcs == 2 does not
+    if (!cg && s->has_neumann) neumann_fill<T>(g, X, faces_of(s), 0, 1.0, st);
+}
+
 // One CG iteration (baseCG.hpp:115-228). The caller applied z = M^{-1} r and p = z.
 template <typename T>
 void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
@@ -919,7 +1120,11 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
     // flexible CG swaps its direction fields every iteration: a captured chunk must
     // hold an even number of iterations to leave them where the capture found them
     if (s->cfg.krylov == PPS_KRYLOV_FCG) chunk += chunk & 1;
-    const bool graph = s->cfg.use_graph != 0 && !L.profile;
+    // the inner BiCGSTAB preconditioner is host-polled: no graph, and every outer
+    // iteration is followed by a poll so that no inner solve runs after the stop
+    const bool inner = s->cfg.precond == PPS_PREC_BICGSTAB || s->cfg.precond == PPS_PREC_CG;
+    if (inner) chunk = 1;
+    const bool graph = s->cfg.use_graph != 0 && !L.profile && !inner;
     std::vector<std::pair<int, double>> errs;   // (iteration, residual norm) seen by the fallback rule
     // inside the iterations the learned cycle's kernels return at once after the stop
     // test (a converged iteration skips its preconditioner)
@@ -1153,6 +1358,84 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
     return rc;
 }
 
+// ChebyshevIteration::operator() as the main solver (chebyshevIteration.hpp:48-140
+// with isMainLoop true; chebyshevIterationAlpaka.hpp:320-587): bt = a copy of b
+// adjusted for the boundary data (its boundary nodes keep b's values, which the
+// stencil of the first step reads), X = -s_{n-2}(bt) at the unknowns (the initial
+// guess is overwritten), then the true residual with normFieldB_ = 1, reported
+// absolute.  PARITY and FP64 apply the polynomial once, as the reference does;
+// MIXED applies it in FP32, first to bt and then, up to max_refinements times, to
+// the FP64 residual, until ||b - A x|| < tol ||b_adj||.
+pps_status solve_cheb_main(pps_solver* s, double* x, const double* b)
+{
+    s->learned_apps = 0;
+    s->fallback_iter = -1;
+    s->net_active = false;
+    const Geo& g = s->geo;
+    cudaStream_t st = s->stream;
+    pps_stats& S = s->stats;
+    const size_t fb = sizeof(double) * (size_t)g.ntot;
+    const int n = s->cfg.cheb_degree;
+    double* bt = s->d_bt;
+    CK(cudaMemcpyAsync(bt, b, fb, cudaMemcpyDeviceToDevice, st));
+    par_adjust_b(g, b, x, faces_of(s), bt, st);
+    s->history.clear();
+    double err = 0;
+    int passes = 1;
+    pps_status rc = PPS_OK;
+    if (s->cfg.form == PPS_FORM_PARITY_FP64) {
+        S.norm_b = std::sqrt(par_dot(s, bt, bt));
+        CK(cudaMemsetAsync(s->pW, 0, fb, st));   // a new object's W (the output at degree 1)
+        par_precond(s, bt, x);
+        err = par_true_residual(s, x, const_cast<double*>(b), s->f64.r, 1.0);
+    } else {
+        S.norm_b = norm_badj(s, x, b);
+        state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, st);
+        Launcher L{s, s->cfg.use_graph == 0};
+        const Coef a = op_coef(g);
+        if (s->cfg.form == PPS_FORM_FP64) {
+            Fields<double>& F = s->f64;
+            double* X = n == 1 ? F.z : x;   // degree 1 fills the whole output field
+            fast_cheb<double>(s, F, bt, X, L, cheb_of(s));
+            if (n == 1) fast_scale_copy<double>(g, s->shape, F.z, x, 1.0, nullptr, st);
+            if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+            fast_residual<double>(g, s->shape, x, b, F.Az, nullptr, nullptr, a, red(s, FIN_STORE), st);
+            read_state(s);
+            err = std::sqrt(s->h_st->sums[0]);
+        } else {
+            Fields<float>& F = s->f32;
+            const double tol_abs = s->cfg.tol * S.norm_b;
+            cast_field_f32(bt, F.p, g.ntot, st);
+            fast_cheb<float>(s, F, F.p, F.e, L, cheb_of(s));
+            fast_scale_copy<double>(g, s->shape, b, x, 0.0, nullptr, st);   // x = 0 at the unknowns
+            for (;;) {
+                fast_add_correction(g, s->shape, x, F.e, s->d_st, st);
+                if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+                fast_residual<float>(g, s->shape, x, b, F.r, nullptr, nullptr, a, red(s, FIN_STORE), st);
+                read_state(s);
+                err = std::sqrt(s->h_st->sums[0]);
+                if (!std::isfinite(err)) {
+                    rc = PPS_NAN_DETECTED;
+                    break;
+                }
+                if (err < tol_abs || passes > s->cfg.max_refinements) break;
+                s->history.push_back(err);
+                fast_cheb<float>(s, F, F.r, F.e, L, cheb_of(s));
+                passes++;
+            }
+            S.refinements = passes - 1;
+        }
+        S.hbm_bytes += L.bytes;
+    }
+    s->history.push_back(err);
+    S.iterations = n * passes;
+    S.precond_applications = passes;
+    S.err_iter = err;
+    S.err_true = err;
+    if (rc != PPS_OK) return rc;
+    return err < s->cfg.tol * S.norm_b ? PPS_OK : PPS_NOT_CONVERGED;
+}
+
 // ---------------------------------------------------------------------------
 // Autotuner: tile shapes of the z-marching kernels, timed on the solver's grid
 // ---------------------------------------------------------------------------
@@ -1268,13 +1551,24 @@ pps_status validate(const pps_grid* g, const pps_config* c)
     if (G > 4.0e9) { set_error("grid too large for the 32-bit plane indexing"); return PPS_ERR_INVALID_ARG; }
     for (int f = 0; f < 6; f++)
         if (g->bcs[f] != 0 && g->bcs[f] != 1) { set_error("bcs must be 0 (Dirichlet) or 1 (Neumann)"); return PPS_ERR_INVALID_ARG; }
-    if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG && c->krylov != PPS_KRYLOV_FCG) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
+    if (c->krylov != PPS_KRYLOV_BICGSTAB && c->krylov != PPS_KRYLOV_CG && c->krylov != PPS_KRYLOV_FCG &&
+        c->krylov != PPS_KRYLOV_CHEBYSHEV) { set_error("unknown krylov"); return PPS_ERR_INVALID_ARG; }
+    if (c->krylov == PPS_KRYLOV_CHEBYSHEV && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
     if (c->krylov == PPS_KRYLOV_FCG && c->form == PPS_FORM_PARITY_FP64) { set_error("flexible CG has no reference counterpart, so no PARITY form"); return PPS_ERR_UNSUPPORTED; }
     if (c->krylov == PPS_KRYLOV_FCG)
         for (int f = 0; f < 6; f++)
             if (g->bcs[f] != 0) { set_error("flexible CG takes Dirichlet grids only"); return PPS_ERR_UNSUPPORTED; }
-    if (c->precond != PPS_PREC_NONE && c->precond != PPS_PREC_CHEBYSHEV) { set_error("unknown precond"); return PPS_ERR_INVALID_ARG; }
-    if (c->precond == PPS_PREC_CHEBYSHEV && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
+    const bool chebmain = c->krylov == PPS_KRYLOV_CHEBYSHEV;
+    const bool nested = !chebmain && (c->precond == PPS_PREC_BICGSTAB || c->precond == PPS_PREC_CG);
+    if (!chebmain && c->precond != PPS_PREC_NONE && c->precond != PPS_PREC_CHEBYSHEV && !nested) { set_error("unknown precond"); return PPS_ERR_INVALID_ARG; }
+    if (nested) {
+        if (!(c->precond_tol > 0.0 && c->precond_tol < 1.0)) { set_error("an inner-solver preconditioner needs 0 < precond_tol < 1"); return PPS_ERR_INVALID_ARG; }
+        if (c->precond_maxit < 0 || c->precond_maxit > 100000000) { set_error("precond_maxit out of range"); return PPS_ERR_INVALID_ARG; }
+        if (c->precond_inner != PPS_PREC_NONE && c->precond_inner != PPS_PREC_CHEBYSHEV) { set_error("precond_inner must be none or Chebyshev"); return PPS_ERR_INVALID_ARG; }
+    }
+    const bool uses_cheb = !chebmain && (c->precond == PPS_PREC_CHEBYSHEV ||
+                                         (nested && c->precond_inner == PPS_PREC_CHEBYSHEV));
+    if (uses_cheb && (c->cheb_degree < 1 || c->cheb_degree > 10000)) { set_error("cheb_degree out of range"); return PPS_ERR_INVALID_ARG; }
     if (c->maxit < 0 || c->maxit > 100000000) { set_error("maxit out of range"); return PPS_ERR_INVALID_ARG; }
     if (!(c->tol >= 0.0)) { set_error("tol must be >= 0"); return PPS_ERR_INVALID_ARG; }
     if (c->form < PPS_FORM_PARITY_FP64 || c->form > PPS_FORM_MIXED) { set_error("unknown form"); return PPS_ERR_INVALID_ARG; }
@@ -1319,9 +1613,12 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
     s->sweep_bytes_acc = 0;
     s->sweep_launch_acc = 0;
     launches_counter_reset();
+    s->prec_kind = s->cfg.krylov == PPS_KRYLOV_CHEBYSHEV ? (int)PPS_PREC_CHEBYSHEV : s->cfg.precond;
+    s->prec_iters = 0;
     CK(cudaEventRecord(s->ev0, s->stream));
     pps_status rc;
-    if (s->cfg.form == PPS_FORM_PARITY_FP64) rc = solve_parity(s, x_dev, b_dev);
+    if (s->cfg.krylov == PPS_KRYLOV_CHEBYSHEV) rc = solve_cheb_main(s, x_dev, b_dev);
+    else if (s->cfg.form == PPS_FORM_PARITY_FP64) rc = solve_parity(s, x_dev, b_dev);
     else if (s->cfg.form == PPS_FORM_FP64) rc = solve_fp64(s, x_dev, b_dev);
     else rc = solve_mixed(s, x_dev, b_dev);
     CK(cudaEventRecord(s->ev1, s->stream));
@@ -1342,6 +1639,7 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
     S.sweep_bytes = s->sweep_bytes_acc;
     S.learned_applications = s->learned_apps;
     S.fallback_iteration = s->fallback_iter;
+    S.precond_iterations = (int)std::min<long long>(s->prec_iters, INT32_MAX);
     return rc;
 }
 
@@ -1366,6 +1664,8 @@ pps_status pps_config_default(pps_config* c, int preset)
         c->rescale_max = 1.0 - 1e-4;
         c->tol = 1.0 * 1e-10;
         c->maxit = 1000;
+        c->precond_tol = (double)100000000 * 1e-10;   // tollMainSolver * 1e8 * tollScalingFactor
+        c->precond_maxit = 500;
     } else if (preset == PPS_PRESET_CPU) {
         // CPU/include/solverSetup.hpp:22-40
         c->cheb_degree = 11;
@@ -1374,6 +1674,8 @@ pps_status pps_config_default(pps_config* c, int preset)
         c->rescale_max = 1.0 - 1e-4;
         c->tol = (double)100 * 1e-10;
         c->maxit = 1700;
+        c->precond_tol = (double)10000 * 1e-10;   // tollPreconditionerSolver * tollScalingFactor
+        c->precond_maxit = 150;                    // iterMaxPreconditioner
     } else {
         return PPS_ERR_INVALID_ARG;
     }
@@ -1384,6 +1686,7 @@ pps_status pps_config_default(pps_config* c, int preset)
     c->check_every = 0;
     c->use_graph = 1;
     c->device = 0;
+    c->precond_inner = PPS_PREC_NONE;
     return PPS_OK;
 }
 
@@ -1462,12 +1765,24 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         } else {
             alloc_fields<double>(s->f64, g.ntot, false);
         }
-        if (cfg->form == PPS_FORM_PARITY_FP64) {
+        if (cfg->form == PPS_FORM_PARITY_FP64 || cfg->krylov == PPS_KRYLOV_CHEBYSHEV) {
             CK(cudaMalloc((void**)&s->d_bt, fb));
             CK(cudaMemset(s->d_bt, 0, fb));
+        }
+        if (cfg->form == PPS_FORM_PARITY_FP64) {
             s->pY = s->f64.Y;
             s->pZ = s->f64.Z;
             s->pW = s->f64.W;
+        }
+        if (cfg->krylov != PPS_KRYLOV_CHEBYSHEV && (cfg->precond == PPS_PREC_BICGSTAB || cfg->precond == PPS_PREC_CG)) {
+            // the inner solver's fields; its Chebyshev buffers only where the fast
+            // forms apply a Chebyshev polynomial inside it (PARITY uses pY, pZ, pW)
+            const bool cheb_in = cfg->precond_inner == PPS_PREC_CHEBYSHEV && cfg->form != PPS_FORM_PARITY_FP64;
+            if (cfg->form == PPS_FORM_MIXED) alloc_fields<float>(s->in32, g.ntot, false, cheb_in);
+            else alloc_fields<double>(s->in64, g.ntot, false, cheb_in);
+            CK(cudaMalloc((void**)&s->d_st_in, sizeof(DevState)));
+            CK(cudaMemset(s->d_st_in, 0, sizeof(DevState)));
+            CK(cudaMallocHost((void**)&s->h_st_in, sizeof(DevState)));
         }
         CK(cudaMalloc((void**)&s->d_dot, 4 * sizeof(double)));
         CK(cudaMalloc((void**)&s->d_st, sizeof(DevState)));
@@ -1655,14 +1970,18 @@ pps_status pps_get_history(const pps_solver* s, double* out, int cap, int* count
 pps_status pps_write_residual_history(const pps_solver* s, const char* path)
 {
     // Format of iterativeSolverBaseAlpaka.hpp:620-638: solver time, iterations,
-    // preconditioner applications, then one residual per line.
+    // preconditioner iterations (an inner solver's, summed; otherwise the number of
+    // applications), then one residual per line.
     if (!s || !path) return PPS_ERR_INVALID_ARG;
     FILE* f = fopen(path, "w");
     if (!f) {
         set_error(std::string("cannot open ") + path);
         return PPS_ERR_INVALID_ARG;
     }
-    fprintf(f, "%.17g\n%d\n%d\n", s->stats.seconds_solve, s->stats.iterations, s->stats.precond_applications);
+    const bool nested = s->cfg.krylov != PPS_KRYLOV_CHEBYSHEV &&
+                        (s->cfg.precond == PPS_PREC_BICGSTAB || s->cfg.precond == PPS_PREC_CG);
+    fprintf(f, "%.17g\n%d\n%d\n", s->stats.seconds_solve, s->stats.iterations,
+            nested ? s->stats.precond_iterations : s->stats.precond_applications);
     for (double v : s->history) fprintf(f, "%.17g\n", v);
     fclose(f);
     return PPS_OK;
@@ -1722,6 +2041,7 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         CK(cudaSetDevice(s->device));
         const Geo& g = s->geo;
         const size_t fb = sizeof(double) * (size_t)g.ntot;
+        s->prec_kind = s->cfg.krylov == PPS_KRYLOV_CHEBYSHEV ? (int)PPS_PREC_CHEBYSHEV : s->cfg.precond;
         if (s->cfg.form == PPS_FORM_PARITY_FP64) {
             CK(cudaMemcpyAsync(s->d_b, B, fb, cudaMemcpyHostToDevice, s->stream));
             CK(cudaMemcpyAsync(s->d_x, X, fb, cudaMemcpyHostToDevice, s->stream));

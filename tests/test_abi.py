@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(pps_lib):
 
 def test_abi_version_and_status_strings(pps_lib):
     L = pps_lib.load()
-    assert L.pps_abi_version() == 1
+    assert L.pps_abi_version() == 2
     for st in (0, 1, 2, 3, 4, -1, -2, -3, -4, -5, -6):
         assert pps_lib.status_string(st) not in ("", "unknown status")
 
@@ -55,6 +55,11 @@ def test_presets_match_reference_constants(pps_lib):
     assert L.pps_config_default(C.byref(cfg), pps_lib.PRESET_ALPAKA) == 0
     # ALP/include/solverSetup.hpp:52,58-59,68-71
     assert (cfg.cheb_degree, cfg.cheb_eps, cfg.rescale_min, cfg.maxit, cfg.tol) == (24, 0.0, 100.0, 1000, 1e-10)
+    # the inner-solver preconditioner: tollPreconditionerSolver = tollMainSolver * 1e8, 500 iterations
+    assert (cfg.precond_tol, cfg.precond_maxit, cfg.precond_inner) == (1e8 * 1e-10, 500, pps_lib.PREC_NONE)
+    assert L.pps_config_default(C.byref(cfg), pps_lib.PRESET_CPU) == 0
+    # CPU solverSetup.hpp:31-33: tollPreconditionerSolver 1e4, iterMaxPreconditioner 150
+    assert (cfg.precond_tol, cfg.precond_maxit) == (1e4 * 1e-10, 150)
     assert L.pps_config_default(C.byref(cfg), 7) == pps_lib.ERR_INVALID_ARG
 
 
@@ -69,6 +74,14 @@ def test_presets_match_reference_constants(pps_lib):
     dict(tol=-1.0),
     dict(form=7),
     dict(form=2, inner_tol=1.5),
+    dict(precond=4),
+    dict(precond=2, precond_tol=1.5),
+    dict(precond=3, precond_tol=0.0),
+    dict(precond=2, precond_inner=2),
+    dict(precond=3, precond_maxit=-1),
+    dict(precond=2, precond_inner=1, cheb_degree=0),
+    dict(krylov=3, cheb_degree=0),
+    dict(krylov=3, cheb_degree=10001),
 ])
 def test_invalid_arguments_are_rejected_before_any_device_work(pps_lib, bad):
     L = pps_lib.load()
@@ -76,7 +89,8 @@ def test_invalid_arguments_are_rejected_before_any_device_work(pps_lib, bad):
                           bcs=bad.get("bcs", (0,) * 6)).c()
     cfg = pps_lib.PpsConfig()
     L.pps_config_default(C.byref(cfg), 0)
-    for k in ("krylov", "precond", "cheb_degree", "maxit", "tol", "form", "inner_tol"):
+    for k in ("krylov", "precond", "cheb_degree", "maxit", "tol", "form", "inner_tol", "precond_tol",
+              "precond_maxit", "precond_inner"):
         if k in bad:
             setattr(cfg, k, bad[k])
     h = C.c_void_p()
@@ -107,4 +121,61 @@ def test_cpp_shim_compiles():
     src = os.path.join(ROOT, "include", "pps_solver.hpp")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-x", "c++", "-I", INCLUDE, src],
                        capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+SHIM_COMPOSITIONS = r"""
+#include <array>
+#include "pps_solver.hpp"
+struct Grid {
+    std::array<int, 3> getNranks() const { return {1, 1, 1}; }
+    std::array<int, 3> getNpglobal() const { return {10, 10, 10}; }
+    std::array<double, 3> getDs() const { return {0.1, 0.1, 0.1}; }
+    std::array<double, 3> getOrigin() const { return {0, 0, 0}; }
+    std::array<int, 6> getBcsType() const { return {0, 0, 0, 0, 0, 0}; }
+};
+struct Exact {
+    double setFieldB(double, double, double) const { return 0; }
+    double trueSolutionFxyz(double, double, double) const { return 0; }
+    double trueSolutionDdir(double, double, double, int) const { return 0; }
+};
+struct Comm {};
+using None = pps::NoneSolver<3, double, 10000, 150>;
+using Cheb = pps::ChebyshevIteration<3, double, 10000, 11, false, false, None>;
+using InnerBiCG = pps::BiCGSTAB<3, double, 10000, 150, false, false, None>;
+using InnerCG = pps::BaseCG<3, double, 10000, 150, false, false, Cheb>;
+using S1 = pps::BiCGSTAB<3, double, 100, 1700, true, true, Cheb>;
+using S2 = pps::BiCGSTAB<3, double, 100, 1700, true, true, InnerBiCG>;
+using S3 = pps::BiCGSTAB<3, double, 100, 1700, true, true, InnerCG>;
+using S4 = pps::ChebyshevIteration<3, double, 10000, 80, true, true, None>;
+using S5 = pps::BaseCG<3, double, 100, 1700, true, true, InnerBiCG>;
+static_assert(InnerBiCG::precond == PPS_PREC_BICGSTAB && InnerCG::precond == PPS_PREC_CG, "");
+static_assert(InnerCG::inner_precond == PPS_PREC_CHEBYSHEV && InnerCG::degree == 11, "");
+template <class S>
+void use(const Grid& g, const Exact& e, Comm& c, double* x, double* b)
+{
+    S s(g, e, c);
+    s.setProblem(x, b);
+    s(x, b);
+    (void)s.getNumIterationFinal();
+    (void)s.getErrorComputeOperator();
+    (void)s.getNumIterationPreconditionerFinal();
+}
+template void use<S1>(const Grid&, const Exact&, Comm&, double*, double*);
+template void use<S2>(const Grid&, const Exact&, Comm&, double*, double*);
+template void use<S3>(const Grid&, const Exact&, Comm&, double*, double*);
+template void use<S4>(const Grid&, const Exact&, Comm&, double*, double*);
+template void use<S5>(const Grid&, const Exact&, Comm&, double*, double*);
+"""
+
+
+def test_cpp_shim_instantiates_every_composition(tmp_path):
+    """The type aliases of inputParam.hpp's compositions (main Chebyshev iteration,
+    BiCGSTAB and CG as preconditioners) instantiate against the shim."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    src = tmp_path / "compositions.cpp"
+    src.write_text(SHIM_COMPOSITIONS)
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", INCLUDE, str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
