@@ -147,6 +147,8 @@ Shape make_shape(const Geo& g, int ty, int target_blocks, int cx = 1);
 void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s);
 void par_residual(const Geo& g, const double* x, const double* b, double* r, cudaStream_t s);
 void par_adjust_b(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s);
+// The same at every data node the reference's face loops reach (boundary nodes too).
+void par_adjust_b_data(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s);
 void par_cheb_s01(const Geo& g, const double* B, double* Y, double* Z, double theta, double t2rd, cudaStream_t s);
 void par_cheb_sweep(const Geo& g, const double* Y, const double* B, const double* Z, double* W, double rc,
                     double two_sigma, double two_over_delta, double ro, cudaStream_t s);

@@ -149,6 +149,25 @@ __global__ void k_par_adjust_b(Geo g, const double* __restrict__ b, const double
     }
 }
 
+// The same adjustment at every data node it reaches, boundary nodes included: the
+// reference adjusts a full copy of b face by face, and the plane next to one face
+// holds boundary nodes of the others (iterativeSolverBase.hpp:429-534).  The
+// Chebyshev main solver reads them through the stencil of its first step.
+__global__ void k_par_adjust_b_data(Geo g, const double* __restrict__ b, const double* __restrict__ x, Faces f,
+                                    double* __restrict__ bt)
+{
+    const long long nx = g.n[0], ny = g.n[1], n = nx * ny * (long long)g.n[2];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % nx);
+        const long long q = t / nx;
+        const int j = 1 + (int)(q % ny);
+        const int k = 1 + (int)(q / ny);
+        const long long c = i + g.sj * j + g.sk * k;
+        bt[c] = badj_exact(g, b, x, f, c, i, j, k);
+    }
+}
+
 // Z = B/theta; Y = 2*rho/delta * (2*B + A(B)/theta)   (chebyshevIteration.hpp:79-90)
 __global__ void k_par_cheb_s01(Geo g, const double* __restrict__ B, double* __restrict__ Y, double* __restrict__ Z,
                                double theta, double t2rd, double h2x, double h2y, double h2z)
@@ -309,6 +328,11 @@ void par_residual(const Geo& g, const double* x, const double* b, double* r, cud
 void par_adjust_b(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s)
 {
     k_par_adjust_b<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, b, x, f, bt);
+    PPS_COUNT_LAUNCH();
+}
+void par_adjust_b_data(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s)
+{
+    k_par_adjust_b_data<<<par_blocks((long long)g.n[0] * g.n[1] * g.n[2]), 256, 0, s>>>(g, b, x, f, bt);
     PPS_COUNT_LAUNCH();
 }
 void par_cheb_s01(const Geo& g, const double* B, double* Y, double* Z, double theta, double t2rd, cudaStream_t s)

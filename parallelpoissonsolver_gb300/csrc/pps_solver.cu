@@ -1360,10 +1360,10 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
 
 // ChebyshevIteration::operator() as the main solver (chebyshevIteration.hpp:48-140
 // with isMainLoop true; chebyshevIterationAlpaka.hpp:320-587): bt = a copy of b
-// adjusted for the boundary data (its boundary nodes keep b's values, which the
-// stencil of the first step reads), X = -s_{n-2}(bt) at the unknowns (the initial
-// guess is overwritten), then the true residual with normFieldB_ = 1, reported
-// absolute.  PARITY and FP64 apply the polynomial once, as the reference does;
+// adjusted for the boundary data (its boundary nodes hold b's values, adjusted where
+// a face's neighbour plane reaches them; the stencil of the first step reads them),
+// X = -s_{n-2}(bt) at the unknowns (the initial guess is overwritten), then the true
+// residual with normFieldB_ = 1, reported absolute.  PARITY and FP64 apply the polynomial once, as the reference does;
 // MIXED applies it in FP32, first to bt and then, up to max_refinements times, to
 // the FP64 residual, until ||b - A x|| < tol ||b_adj||.
 pps_status solve_cheb_main(pps_solver* s, double* x, const double* b)
@@ -1378,7 +1378,7 @@ pps_status solve_cheb_main(pps_solver* s, double* x, const double* b)
     const int n = s->cfg.cheb_degree;
     double* bt = s->d_bt;
     CK(cudaMemcpyAsync(bt, b, fb, cudaMemcpyDeviceToDevice, st));
-    par_adjust_b(g, b, x, faces_of(s), bt, st);
+    par_adjust_b_data(g, b, x, faces_of(s), bt, st);
     s->history.clear();
     double err = 0;
     int passes = 1;
