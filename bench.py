@@ -477,6 +477,135 @@ def run_large(args, dev: int):
     }
 
 
+def composition_cpu_sample(m: int, cfg: dict, outer_its: int, inner_its: int, threads: int):
+    """Bounded sample of the oracle port (bit-identical to the reference CPU solver)
+    for a composition with an inner solver: set-up alone (maxit 0), then one outer
+    iteration with 2 and with 4 inner iterations per application (2 applications
+    per BiCGSTAB iteration), extrapolated to the GPU run's iteration counts."""
+    from oracle import oracle as O
+    g = O.cube(m)
+    x0, b0 = make_inputs(m)
+
+    def t(**kw):
+        c = O.Config(**{**cfg, **kw, "threads": threads})
+        tt = time.perf_counter()
+        O.solve(g, c, x0.copy(), b0.copy())
+        return time.perf_counter() - tt
+
+    t(maxit=1, prec_maxit=1)   # warm the thread pool, page in the fields
+    t0, t2, t4 = t(maxit=0), t(maxit=1, prec_maxit=2), t(maxit=1, prec_maxit=4)
+    t_inner = max(t4 - t2, 0.0) / 4.0
+    t_outer = max(t2 - t0 - 4.0 * t_inner, 0.0)
+    return {"value": t0 + outer_its * t_outer + inner_its * t_inner, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"{m}^3: set-up, then one outer iteration with 2 and 4 inner iterations per application; "
+                      f"{t_inner * 1e3:.1f} ms per inner iteration, {t_outer * 1e3:.1f} ms per outer iteration "
+                      f"outside them, extrapolated to {outer_its} outer / {inner_its} inner iterations"}
+
+
+def chebyshev_cpu_sample(m: int, degree: int, threads: int):
+    """The oracle's Chebyshev main solver at degrees 4 and 12; the difference gives the
+    cost of a sweep, extrapolated to `degree`."""
+    from oracle import oracle as O
+    g = O.cube(m)
+    x0, b0 = make_inputs(m)
+
+    def t(n):
+        c = O.Config(krylov=O.CHEBYSHEV_MAIN, cheb_degree=n, cheb_eps=0.0, rescale_min=1.0, rescale_max=1.0,
+                     threads=threads)
+        tt = time.perf_counter()
+        O.solve(g, c, x0.copy(), b0.copy())
+        return time.perf_counter() - tt
+
+    t(2)
+    t4, t12 = t(4), t(12)
+    sweep = max(t12 - t4, 0.0) / 8.0
+    return {"value": t4 + (degree - 4) * sweep, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"{m}^3 at degrees 4 and 12: {sweep * 1e3:.1f} ms per sweep, extrapolated to degree {degree}"}
+
+
+def run_compositions(args, dev: int, threads: int):
+    """The other compositions of inputParam.hpp on the benchmark's field at
+    --comp-size^3 (k^-2 random field, Dirichlet 0, stop at 1e-10): BiCGSTAB
+    preconditioned by an inner BiCGSTAB solve (CPU/include/inputParam.hpp:30, the CPU
+    preset 1e-6 / 150 iterations) and by an inner CG solve with the Chebyshev
+    polynomial (inputParam.hpp:29), and the Chebyshev iteration as the main solver
+    (ALP/include/inputParam.hpp:37) with its eigenvalue bounds unscaled.  Each: device
+    time of a solve, iterations, the algorithmic HBM bytes of all its kernels over that
+    time against the measured copy bandwidth, and the oracle's CPU time extrapolated
+    from a bounded sample."""
+    import math
+
+    import torch
+
+    import parallelpoissonsolver_gb300 as pps
+
+    m = args.comp_size
+    grid = pps.BlockGrid.cube(m)
+    x_h, b_h = make_inputs(m)
+    b_d = torch.from_numpy(b_h).to(f"cuda:{dev}")
+    x_d = torch.zeros_like(b_d)
+    peak, peak_kind = measured_peaks()
+    # degree of the Chebyshev main solver: the polynomial's error bound
+    # 2 ((sqrt(k) - 1) / (sqrt(k) + 1))^n below 1e-12 for the condition number k
+    lmin = 3 * 4 * math.sin(math.pi / 2 / (m + 1)) ** 2
+    lmax = 3 * 4 * math.sin(m * math.pi / 2 / (m + 1)) ** 2
+    q = (math.sqrt(lmax / lmin) - 1) / (math.sqrt(lmax / lmin) + 1)
+    deg_fp64 = int(math.ceil(math.log(1e-12 / 2) / math.log(q)))
+    deg_mixed = int(math.ceil(math.log(1e-5 / 2) / math.log(q)))
+    cheb_main = pps.ChebyshevIteration(deg_fp64, 0.0, 1.0, 1.0)
+    solvers = {
+        "bicgstab+inner_bicgstab": {f: pps.BiCGSTAB(grid, pps.BiCGSTABPreconditioner(1e4 * 1e-10, 150),
+                                                    tolerance=TOL, max_iteration=5000, form=f, device=dev)
+                                    for f in ("fp64", "mixed")},
+        "bicgstab+inner_cg_chebyshev": {f: pps.BiCGSTAB(grid, pps.BaseCGPreconditioner(1e4 * 1e-10, 150,
+                                                                                       pps.ChebyshevIteration(DEGREE)),
+                                                        tolerance=TOL, max_iteration=5000, form=f, device=dev)
+                                        for f in ("fp64", "mixed")},
+        "chebyshev_main": {
+            "fp64": pps.ChebyshevSolver(grid, cheb_main, tolerance=TOL, form="fp64", use_graph=False, device=dev),
+            "mixed": pps.ChebyshevSolver(grid, pps.ChebyshevIteration(deg_mixed, 0.0, 1.0, 1.0), tolerance=TOL,
+                                         form="mixed", use_graph=False, device=dev)},
+    }
+    out = {"workload": f"{m}^3, Dirichlet 0, k^-2 random field (seed 2), stop at ||r||/||b_adj|| <= {TOL:g}; "
+                       f"Chebyshev main solver on [lambda_min, lambda_max] (rescale 1, epsilon 0) of degree "
+                       f"{deg_fp64} (FP64, one application) or {deg_mixed} (MIXED, per refinement pass)",
+           "peak_gbs": peak, "peak_kind": peak_kind}
+    for name, forms in solvers.items():
+        out[name] = {}
+        for f, s in forms.items():
+            s.autotune()
+            runs = []
+            for _ in range(3):   # the first run is the warm-up
+                x_d.zero_()
+                torch.cuda.synchronize()
+                st = s.solve_device(x_d.data_ptr(), b_d.data_ptr(), raise_on_error=False)
+                runs.append((st, s.stats()))
+            t = statistics.mean(d["seconds_solve"] for _, d in runs[1:])
+            st, d = runs[-1]
+            rel_err = d["err_true"] / d["norm_b"] if name == "chebyshev_main" else d["err_true"]
+            achieved = d["hbm_bytes"] / t / 1e9
+            out[name][f] = {"status": pps.status_string(st), "seconds": t, "iterations": d["iterations"],
+                            "inner_iterations": d["precond_iterations"], "refinements": d["refinements"],
+                            "true_rel_residual": rel_err, "algorithmic_gbs": achieved,
+                            "frac_of_peak": achieved / peak, "kernel_launches": d["kernel_launches"]}
+            if name == "chebyshev_main" and d["sweep_seconds"] > 0:
+                out[name][f]["sweep_gbs"] = d["sweep_bytes"] / d["sweep_seconds"] / 1e9
+            s.close()
+    if not args.no_cpu_baseline:
+        base = dict(tol=TOL, maxit=5000, prec_tol=1e4 * 1e-10, prec_maxit=150)
+        for name, cfg in (("bicgstab+inner_bicgstab", dict(precond=2, prec_inner=0)),
+                          ("bicgstab+inner_cg_chebyshev", dict(precond=3, prec_inner=1, cheb_degree=DEGREE))):
+            r = out[name]["fp64"]
+            cpu = composition_cpu_sample(m, {**base, **cfg}, r["iterations"], r["inner_iterations"], threads)
+            out[name]["cpu_baseline"] = cpu
+            out[name]["fp64_speedup_vs_cpu"] = cpu["value"] / r["seconds"]
+            out[name]["mixed_speedup_vs_cpu"] = cpu["value"] / out[name]["mixed"]["seconds"]
+        cpu = chebyshev_cpu_sample(m, deg_fp64, threads)
+        out["chebyshev_main"]["cpu_baseline"] = cpu
+        out["chebyshev_main"]["fp64_speedup_vs_cpu"] = cpu["value"] / out["chebyshev_main"]["fp64"]["seconds"]
+    return out
+
+
 def run_batched(args, dist: Dist):
     """256 independent Dirichlet problems, edges uniform on {32,48,64,96,128}, each f a
     seeded sum of 1-8 Gaussian blobs; MIXED form to 1e-10 in one batch (one launch per
@@ -588,6 +717,8 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=3e-3)
     ap.add_argument("--learned-inner-tol", type=float, default=1e-5)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-compositions", action="store_true")
+    ap.add_argument("--comp-size", type=int, default=256)
     ap.add_argument("--large", action="store_true", help="also run the 1024^3 charges solve (several minutes)")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=16)
@@ -624,6 +755,8 @@ def main():
     out, iters_fp64 = run_gpu(args, dist)
     if not args.no_batched:
         out["batched"] = run_batched(args, dist)
+    if not args.no_compositions and dist.rank == 0:
+        out["compositions"] = run_compositions(args, dist.local, threads)
     if args.large:
         out["large_1024"] = run_large(args, dist.local)
     if dist.rank == 0:
