@@ -205,7 +205,10 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
 /* Tile shapes of the z-marching kernels (fast forms).  A tile is (32*cx) x ty
  * columns; each thread walks along z; `waves` sets the grid to about
  * waves x 152 SMs x resident blocks.  cheb_* apply to the Chebyshev kernels,
- * other_* to the Krylov update/stencil kernels.  *_us: measured per launch. */
+ * other_* to the Krylov update/stencil kernels.  cheb_cx 4 selects the
+ * x-vectorised FP32 Chebyshev kernels (one float4 per thread, the default where
+ * npglobal[0] + 2 is a multiple of 4; FP64 fields and other rows run cx 1 tiles of
+ * the same size).  *_us: measured per launch. */
 typedef struct {
     int cheb_ty, cheb_cx, cheb_waves;
     int other_ty, other_waves;

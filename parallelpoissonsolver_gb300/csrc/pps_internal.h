@@ -24,7 +24,8 @@ struct Geo {
 // each thread walks kchunk planes along k.
 struct Shape {
     int ty;
-    int cx;           // columns per thread along x (tile width 32*cx); Chebyshev kernels only
+    int cx;           // columns per thread along x (tile width 32*cx); Chebyshev kernels only;
+                      // 4: the x-vectorised FP32 tiles (one float4 per thread, aligned to x = 0)
     int ntx, nty, nchunks, kchunk;
     unsigned nblocks() const { return (unsigned)ntx * (unsigned)nty * (unsigned)nchunks; }
 };

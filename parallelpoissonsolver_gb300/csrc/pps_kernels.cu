@@ -14,6 +14,7 @@
 #include "pps_internal.h"
 
 #include <algorithm>
+#include <type_traits>
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -450,7 +451,9 @@ Shape make_shape(const Geo& g, int ty, int target_blocks, int cx)
     sh.ty = ty;
     sh.cx = cx;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
-    sh.ntx = (ux + 32 * cx - 1) / (32 * cx);
+    // cx = 4: the x-vectorised tiles start at x = 0 (16-byte aligned float4), so they
+    // must reach hi[0] from there
+    sh.ntx = cx == 4 ? (g.hi[0] + 127) / 128 : (ux + 32 * cx - 1) / (32 * cx);
     sh.nty = (uy + ty - 1) / ty;
     const long long tiles = (long long)sh.ntx * sh.nty;
     long long chunks = (target_blocks + tiles - 1) / tiles;
@@ -854,6 +857,110 @@ __global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __
         }
         c0 += sk;
     }
+}
+
+// The FP32 Chebyshev kernels vectorised along x: a thread owns four consecutive x
+// points (one float4), a warp 128, a block 128 x ty columns, tiles aligned to x = 0
+// so that every float4 starts on a 16-byte boundary (the row stride is a multiple
+// of 4 floats).  The x neighbours of a float4 come from the neighbouring lanes by
+// shuffle (lanes 0 and 31 load the one outside the warp); the y and z neighbours
+// are float4 loads, z kept in registers as the thread marches along z.  Points off
+// the unknowns are computed on whatever the field holds there and not stored.  The
+// arithmetic per point is that of k_cheb_s01 / k_cheb_sweep in the same order, so
+// the results are bit-identical; a sweep moves 4x fewer, 4x wider requests.
+struct Col4 {
+    int i0, j, k0, k1;   // first x of the float4, row, planes [k0, k1)
+    long long c;         // field index of (i0, j, k0)
+    bool act;            // the float4 holds an unknown
+};
+
+__device__ __forceinline__ Col4 column4(const Geo& g, const Shape& sh)
+{
+    Col4 q;
+    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
+    q.i0 = bx * 128 + threadIdx.x * 4;
+    q.j = g.lo[1] + by * sh.ty + threadIdx.y;
+    q.k0 = g.lo[2] + blockIdx.y * sh.kchunk;
+    q.k1 = min(q.k0 + sh.kchunk, g.hi[2]);
+    q.act = q.i0 < g.hi[0] && q.i0 + 4 > g.lo[0];
+    q.c = q.i0 + g.sj * q.j + g.sk * q.k0;
+    return q;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b)
+{
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// MODE 0: W = s1 of U (k_cheb_s01); 1: a sweep without Z; 2: a sweep with Z.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cheb_v4(Geo g, Shape sh, const float* __restrict__ U,
+                                                 const float* __restrict__ B, const float* __restrict__ Z,
+                                                 float* __restrict__ W, CT<float> cf, const int* done)
+{
+    EARLY_EXIT(done);
+    const Col4 q = column4(g, sh);
+    if (q.j >= g.hi[1]) return;   // a warp shares its row, so its lanes leave together
+    const bool act = q.act;
+    const int lane = threadIdx.x;
+    const bool m0 = q.i0 >= g.lo[0] && q.i0 < g.hi[0], m1 = q.i0 + 1 >= g.lo[0] && q.i0 + 1 < g.hi[0];
+    const bool m2 = q.i0 + 2 >= g.lo[0] && q.i0 + 2 < g.hi[0], m3 = q.i0 + 3 >= g.lo[0] && q.i0 + 3 < g.hi[0];
+    const bool all4 = m0 && m1 && m2 && m3;
+    const long long sj = g.sj, sk = g.sk;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    long long c = q.c;
+    float4 um = act ? ld4(U + c - sk) : zero, uc = act ? ld4(U + c) : zero;
+#pragma unroll 2
+    for (int k = q.k0; k < q.k1; k++) {
+        const float4 up = act ? ld4(U + c + sk) : zero;
+        const float4 uy = act ? add4(ld4(U + c - sj), ld4(U + c + sj)) : zero;
+        const float4 bv = (MODE >= 1 && act) ? ld4(B + c) : zero;
+        const float4 zv = (MODE == 2 && act) ? ld4(Z + c) : zero;
+        float left = __shfl_up_sync(0xffffffffu, uc.w, 1), right = __shfl_down_sync(0xffffffffu, uc.x, 1);
+        if (lane == 0) left = act ? U[c - 1] : 0.f;
+        if (lane == 31) right = act && q.i0 + 4 < sj ? U[c + 4] : 0.f;
+        float4 w;
+        w.x = fmx(cf.cz, um.x + up.x, fmx(cf.cy, uy.x, fmx(cf.cx, left + uc.y, cf.cc * uc.x)));
+        w.y = fmx(cf.cz, um.y + up.y, fmx(cf.cy, uy.y, fmx(cf.cx, uc.x + uc.z, cf.cc * uc.y)));
+        w.z = fmx(cf.cz, um.z + up.z, fmx(cf.cy, uy.z, fmx(cf.cx, uc.y + uc.w, cf.cc * uc.z)));
+        w.w = fmx(cf.cz, um.w + up.w, fmx(cf.cy, uy.w, fmx(cf.cx, uc.z + right, cf.cc * uc.w)));
+        if (MODE >= 1) {
+            w.x = fmx(cf.cb, bv.x, w.x);
+            w.y = fmx(cf.cb, bv.y, w.y);
+            w.z = fmx(cf.cb, bv.z, w.z);
+            w.w = fmx(cf.cb, bv.w, w.w);
+        }
+        if (MODE == 2) {
+            w.x = fmx(cf.cw, zv.x, w.x);
+            w.y = fmx(cf.cw, zv.y, w.y);
+            w.z = fmx(cf.cw, zv.z, w.z);
+            w.w = fmx(cf.cw, zv.w, w.w);
+        }
+        if (act) {
+            if (all4) {
+                *reinterpret_cast<float4*>(W + c) = w;
+            } else {
+                if (m0) W[c] = w.x;
+                if (m1) W[c + 1] = w.y;
+                if (m2) W[c + 2] = w.z;
+                if (m3) W[c + 3] = w.w;
+            }
+        }
+        um = uc;
+        uc = up;
+        c += sk;
+    }
+}
+
+// The vectorised kernels take FP32 fields whose rows start on 16-byte boundaries.
+template <typename T>
+static bool v4_ok(const Geo& g, const void* a, const void* b, const void* c, const void* d)
+{
+    if (!std::is_same<T, float>::value || g.sj % 4 != 0) return false;
+    for (const void* p : {a, b, c, d})
+        if (p && ((uintptr_t)p & 15u) != 0) return false;
+    return true;
 }
 
 // Several Chebyshev steps in one pass (temporal blocking).  The steps s1..s_NS of
@@ -1277,6 +1384,74 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil(Geo g, Shape sh, const T*
     reduce_finalize<1>(v, rc);
 }
 
+// k_fcg_p_stencil on the x-vectorised FP32 tiles of k_cheb_v4: p = z + beta p_in
+// formed at every tap (from float4 loads, the x neighbours by shuffle), Ap, and
+// sum p.Ap over the unknowns.  The per-point arithmetic is k_fcg_p_stencil's; the
+// sum visits the points in another order.
+__global__ void __launch_bounds__(256) k_fcg_p_stencil_v4(Geo g, Shape sh, const float* __restrict__ z,
+                                                          const float* __restrict__ pin, float* __restrict__ pout,
+                                                          float* __restrict__ Ap, Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col4 q = column4(g, sh);
+    Acc<float> a1;
+    if (q.j < g.hi[1]) {   // a warp shares its row: the shuffles below see all 32 lanes
+        const bool act = q.act;
+        const int lane = threadIdx.x;
+        const bool m0 = q.i0 >= g.lo[0] && q.i0 < g.hi[0], m1 = q.i0 + 1 >= g.lo[0] && q.i0 + 1 < g.hi[0];
+        const bool m2 = q.i0 + 2 >= g.lo[0] && q.i0 + 2 < g.hi[0], m3 = q.i0 + 3 >= g.lo[0] && q.i0 + 3 < g.hi[0];
+        const bool all4 = m0 && m1 && m2 && m3;
+        const float cc = (float)cf.cc, cx = (float)cf.cx, cy = (float)cf.cy, cz = (float)cf.cz;
+        const bool restart = rc.st->beta == 0.0;
+        const float be = (float)rc.st->beta;
+        const long long sj = g.sj, sk = g.sk;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto pv4 = [&](long long c) -> float4 {
+            if (!act) return zero;
+            const float4 zv = ld4(z + c);
+            if (restart) return zv;
+            const float4 pv = ld4(pin + c);
+            return make_float4(fmx(be, pv.x, zv.x), fmx(be, pv.y, zv.y), fmx(be, pv.z, zv.z), fmx(be, pv.w, zv.w));
+        };
+        auto pv1 = [&](long long c) -> float { return restart ? z[c] : fmx(be, pin[c], z[c]); };
+        long long c = q.c;
+        float4 um = pv4(c - sk), uc = pv4(c);
+#pragma unroll 2
+        for (int k = q.k0; k < q.k1; k++) {
+            const float4 up = pv4(c + sk);
+            const float4 uy = add4(pv4(c - sj), pv4(c + sj));
+            float left = __shfl_up_sync(0xffffffffu, uc.w, 1), right = __shfl_down_sync(0xffffffffu, uc.x, 1);
+            if (lane == 0) left = act ? pv1(c - 1) : 0.f;
+            if (lane == 31) right = act && q.i0 + 4 < sj ? pv1(c + 4) : 0.f;
+            float4 a;
+            a.x = fmx(cz, um.x + up.x, fmx(cy, uy.x, fmx(cx, left + uc.y, cc * uc.x)));
+            a.y = fmx(cz, um.y + up.y, fmx(cy, uy.y, fmx(cx, uc.x + uc.z, cc * uc.y)));
+            a.z = fmx(cz, um.z + up.z, fmx(cy, uy.z, fmx(cx, uc.y + uc.w, cc * uc.z)));
+            a.w = fmx(cz, um.w + up.w, fmx(cy, uy.w, fmx(cx, uc.z + right, cc * uc.w)));
+            if (act) {
+                if (all4) {
+                    *reinterpret_cast<float4*>(pout + c) = uc;
+                    *reinterpret_cast<float4*>(Ap + c) = a;
+                } else {
+                    if (m0) { pout[c] = uc.x; Ap[c] = a.x; }
+                    if (m1) { pout[c + 1] = uc.y; Ap[c + 1] = a.y; }
+                    if (m2) { pout[c + 2] = uc.z; Ap[c + 2] = a.z; }
+                    if (m3) { pout[c + 3] = uc.w; Ap[c + 3] = a.w; }
+                }
+                if (m0) a1.add(uc.x, a.x);
+                if (m1) a1.add(uc.y, a.y);
+                if (m2) a1.add(uc.z, a.z);
+                if (m3) a1.add(uc.w, a.w);
+            }
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    double v[1] = {a1.value()};
+    reduce_finalize<1>(v, rc);
+}
+
 // FCG: x += alpha*p; r -= alpha*Ap; sum r.r (the convergence test, before the
 // preconditioner, which a converged iteration then skips)
 template <typename T>
@@ -1635,6 +1810,17 @@ template <typename T>
 void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& cy, const int* done, cudaStream_t s)
 {
     const CT<T> c = cast_coef<T>(cy);
+    if (sh.cx == 4) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (v4_ok<T>(g, B, Y, nullptr, nullptr)) {
+                k_cheb_v4<0><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, nullptr, nullptr, Y, c, done);
+                PPS_COUNT_LAUNCH();
+                return;
+            }
+        }
+        fast_cheb_s01<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), B, Y, cy, done, s);   // scalar tiles
+        return;
+    }
     if (sh.cx == 2) k_cheb_s01<T, 2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
     else k_cheb_s01<T, 1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
     PPS_COUNT_LAUNCH();
@@ -1644,6 +1830,18 @@ void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, cons
                      const int* done, cudaStream_t s)
 {
     const CT<T> c = cast_coef<T>(cf);
+    if (sh.cx == 4) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (v4_ok<T>(g, Y, B, Z, W)) {
+                if (Z) k_cheb_v4<2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+                else k_cheb_v4<1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+                PPS_COUNT_LAUNCH();
+                return;
+            }
+        }
+        fast_cheb_sweep<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), Y, B, Z, W, cf, done, s);   // scalar tiles
+        return;
+    }
     if (Z) {
         if (sh.cx == 2) k_cheb_sweep<T, 2, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
         else k_cheb_sweep<T, 1, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
@@ -1780,6 +1978,17 @@ template <typename T>
 void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
                         RedCtx rc, cudaStream_t s)
 {
+    if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
+        if constexpr (std::is_same<T, float>::value) {
+            if (sh.cx == 4 && v4_ok<T>(g, z, pin, pout, Ap)) {
+                k_fcg_p_stencil_v4<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
+                PPS_COUNT_LAUNCH();
+                return;
+            }
+        }
+        fast_fcg_p_stencil<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), z, pin, pout, Ap, a, rc, s);
+        return;
+    }
     k_fcg_p_stencil<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }

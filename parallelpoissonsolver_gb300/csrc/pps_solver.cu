@@ -1062,7 +1062,8 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     cudaStream_t st = s->stream;
     const long long N = s->n_unknowns;
     const Coef a = op_coef(g);
-    fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
+    // the direction/stencil kernel runs on the Chebyshev tiles (x-vectorised for FP32)
+    fast_fcg_p_stencil<T>(g, s->shape_cheb, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
     std::swap(F.p, F.Az);
     const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
     if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
@@ -1441,7 +1442,7 @@ pps_status solve_cheb_main(pps_solver* s, double* x, const double* b)
 // ---------------------------------------------------------------------------
 
 const int kTys[] = {2, 4, 8};
-const int kCxs[] = {1, 2};
+const int kCxs[] = {1, 2, 4};
 const int kWaves[] = {1, 2, 4, 8};
 
 int resident_blocks(int ty)
@@ -1459,7 +1460,8 @@ unsigned max_candidate_blocks(const Geo& g)
 {
     unsigned m = 0;
     for (int ty : kTys)
-        for (int w : kWaves) m = std::max(m, tuned_shape(g, ty, 1, w).nblocks());
+        for (int cx : kCxs)
+            for (int w : kWaves) m = std::max(m, tuned_shape(g, ty, cx, w).nblocks());
     return m;
 }
 
@@ -1536,7 +1538,7 @@ bool tuning_valid(const pps_tuning* t)
             if (a[i] == v) return true;
         return false;
     };
-    return in(t->cheb_ty, kTys, 3) && in(t->cheb_cx, kCxs, 2) && in(t->cheb_waves, kWaves, 4) &&
+    return in(t->cheb_ty, kTys, 3) && in(t->cheb_cx, kCxs, 3) && in(t->cheb_waves, kWaves, 4) &&
            in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4) && (t->cheb_fused == 0 || t->cheb_fused == 1);
 }
 
@@ -1728,9 +1730,12 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         g.ntot = g.sk * (grid->npglobal[2] + 2);
         s->n_unknowns = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
         s->shape = make_shape(g, 8, 152 * 8 * 4);
-        s->shape_cheb = s->shape;
+        // the Chebyshev kernels default to the x-vectorised FP32 tiles where the row
+        // stride allows them (FP64 fields run the scalar tiles of the same size)
+        const int cx0 = g.sj % 4 == 0 ? 4 : 1;
+        s->shape_cheb = make_shape(g, 8, 152 * 8 * 4, cx0);
         s->tuning.cheb_ty = 8;
-        s->tuning.cheb_cx = 1;
+        s->tuning.cheb_cx = cx0;
         s->tuning.cheb_waves = 4;
         s->tuning.other_ty = 8;
         s->tuning.other_waves = 4;

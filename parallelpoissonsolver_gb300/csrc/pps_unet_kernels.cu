@@ -9,6 +9,8 @@
 // channels, 16x16x16 BF16 fragments with FP32 accumulators.
 #include "pps_unet_internal.h"
 
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <mma.h>
@@ -1038,55 +1040,91 @@ void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 // Trilinear prolongation, coarse (m) -> fine (2m): fine unknown i takes coarse
 // (i-1)/2 exactly when i is odd (0-based), the mean of its two coarse neighbours
 // otherwise (zero beyond the grid); the transpose of k_restrict up to a factor 8.
-__global__ void k_prolong(Dims dc, const float* __restrict__ coarse, float* __restrict__ fine, int add, const int* __restrict__ stop)
+// One thread per fine (x, y) column marches along z: it interpolates each coarse
+// plane of its chunk in (x, y) once (4 loads) and writes the two fine planes that
+// plane covers (2cz: the mean with the plane below, 2cz+1: the plane itself), so a
+// fine point costs about two coarse loads and one (ADD: two) fine accesses.
+template <bool ADD>
+__global__ void __launch_bounds__(256) k_prolong_z(Dims dc, int ntx, int cchunk, const float* __restrict__ coarse,
+                                                   float* __restrict__ fine, const int* __restrict__ stop)
 {
     if (stop && *(volatile const int*)stop) return;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    const int Wf = dc.W * 2, Hf = dc.H * 2;
-    if (x >= Wf) return;
-    const int idx[3] = {x, y, z};
-    int i0[3], i1[3];
-    float w0[3], w1v[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        if (idx[d] & 1) {
-            i0[d] = idx[d] >> 1;
-            i1[d] = i0[d];
-            w0[d] = 1.0f;
-            w1v[d] = 0.0f;
-        } else {
-            i0[d] = (idx[d] >> 1) - 1;
-            i1[d] = idx[d] >> 1;
-            w0[d] = 0.5f;
-            w1v[d] = 0.5f;
-        }
+    const int Wf = 2 * dc.W, Hf = 2 * dc.H;
+    const int x = (int)(blockIdx.x % ntx) * 32 + threadIdx.x;
+    const int y = (int)(blockIdx.x / ntx) * blockDim.y + threadIdx.y;
+    if (x >= Wf || y >= Hf) return;
+    const int cz0 = blockIdx.y * cchunk, cz1 = min(dc.D, cz0 + cchunk);
+    if (cz0 >= cz1) return;
+    int xa, xb, ya, yb;   // coarse indices along x and y
+    float wxa, wxb, wya, wyb;
+    if (x & 1) {
+        xa = xb = x >> 1;
+        wxa = 1.0f;
+        wxb = 0.0f;
+    } else {
+        xa = (x >> 1) - 1;
+        xb = x >> 1;
+        wxa = xa >= 0 ? 0.5f : 0.0f;
+        wxb = 0.5f;
+        if (xa < 0) xa = xb;
     }
-    float s = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                const int zz = a ? i1[2] : i0[2], yy = b ? i1[1] : i0[1], xx = c ? i1[0] : i0[0];
-                const float w = (a ? w1v[2] : w0[2]) * (b ? w1v[1] : w0[1]) * (c ? w1v[0] : w0[0]);
-                if (w == 0.0f || zz < 0 || yy < 0 || xx < 0 || zz >= dc.D || yy >= dc.H || xx >= dc.W) continue;
-                s += w * coarse[((long long)zz * dc.H + yy) * dc.W + xx];
-            }
-    const long long q = ((long long)z * Hf + y) * Wf + x;
-    fine[q] = add ? fine[q] + s : s;
+    if (y & 1) {
+        ya = yb = y >> 1;
+        wya = 1.0f;
+        wyb = 0.0f;
+    } else {
+        ya = (y >> 1) - 1;
+        yb = y >> 1;
+        wya = ya >= 0 ? 0.5f : 0.0f;
+        wyb = 0.5f;
+        if (ya < 0) ya = yb;
+    }
+    const long long plane = (long long)dc.H * dc.W;
+    const long long oaa = (long long)ya * dc.W + xa, oab = (long long)ya * dc.W + xb;
+    const long long oba = (long long)yb * dc.W + xa, obb = (long long)yb * dc.W + xb;
+    auto interp = [&](int cz) -> float {   // bilinear value of coarse plane cz at this column
+        const float* p = coarse + (long long)cz * plane;
+        return wya * (wxa * p[oaa] + wxb * p[oab]) + wyb * (wxa * p[oba] + wxb * p[obb]);
+    };
+    const long long fplane = (long long)Hf * Wf;
+    long long q = (2LL * cz0 * Hf + y) * Wf + x;
+    float vm = cz0 >= 1 ? interp(cz0 - 1) : 0.0f;
+    for (int cz = cz0; cz < cz1; cz++, q += 2 * fplane) {
+        const float v = interp(cz);
+        const float e = 0.5f * (vm + v);
+        if (ADD) {
+            fine[q] += e;
+            fine[q + fplane] += v;
+        } else {
+            fine[q] = e;
+            fine[q + fplane] = v;
+        }
+        vm = v;
+    }
+}
+
+template <bool ADD>
+static void prolong_z(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
+{
+    const int ty = 8;
+    const int ntx = (2 * dc.W + 31) / 32, nty = (2 * dc.H + ty - 1) / ty;
+    const long long tiles = (long long)ntx * nty;
+    long long chunks = (152LL * 8 * 4 + tiles - 1) / tiles;
+    chunks = std::max(1LL, std::min<long long>(chunks, dc.D));
+    const int cchunk = (int)((dc.D + chunks - 1) / chunks);
+    const unsigned nch = (unsigned)((dc.D + cchunk - 1) / cchunk);
+    k_prolong_z<ADD><<<dim3((unsigned)tiles, nch), dim3(32, ty), 0, s>>>(dc, ntx, cchunk, coarse, fine, g_stop);
+    launches_counter_add(1);
 }
 
 void prolong2(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 0, g_stop);
-    launches_counter_add(1);
+    prolong_z<false>(dc, coarse, fine, s);
 }
 
 void prolong2_add(const Dims& dc, const float* coarse, float* fine, cudaStream_t s)
 {
-    k_prolong<<<field_grid(dc.W * 2, dc.H * 2, dc.D * 2, 128), 128, 0, s>>>(dc, coarse, fine, 1, g_stop);
-    launches_counter_add(1);
+    prolong_z<true>(dc, coarse, fine, s);
 }
 
 }  // namespace unet
