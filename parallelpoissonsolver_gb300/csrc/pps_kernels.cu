@@ -1416,7 +1416,7 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil_v4(Geo g, Shape sh, const
         auto pv1 = [&](long long c) -> float { return restart ? z[c] : fmx(be, pin[c], z[c]); };
         long long c = q.c;
         float4 um = pv4(c - sk), uc = pv4(c);
-#pragma unroll 2
+#pragma unroll 1
         for (int k = q.k0; k < q.k1; k++) {
             const float4 up = pv4(c + sk);
             const float4 uy = add4(pv4(c - sj), pv4(c + sj));

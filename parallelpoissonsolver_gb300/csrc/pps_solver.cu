@@ -781,7 +781,7 @@ void learned_coarse_correction(pps_solver* s, const T* r, const T* z, T* X)
         unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
     } else {
         for (int l = k; l > 1; l--) unet::prolong2(dense_dims(s, l), s->dn_e[(size_t)l], s->dn_e[(size_t)l - 1], st);
-        unet::prolong_add_field<T>(g, s->shape, dense_dims(s, 1), s->dn_e[1], X, st);
+        unet::prolong_add_field<T>(g, s->shape_cheb, dense_dims(s, 1), s->dn_e[1], X, st);
     }
     s->learned_apps++;
 }
@@ -894,7 +894,7 @@ void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
             unet::prolong2(dense_dims(s, l + 1), s->dn_e[(size_t)l + 1], s->dn_e[(size_t)l], st);
         }
     }
-    unet::prolong_add_field<T>(g, s->shape, dense_dims(s, 1), s->dn_e[1], X, st);
+    unet::prolong_add_field<T>(g, s->shape_cheb, dense_dims(s, 1), s->dn_e[1], X, st);
     if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
         unet::field_residual<T>(g, s->shape, B, X, F.r0, st);
         fast_cheb<T>(s, F, F.r0, F.Mp, L, pf);

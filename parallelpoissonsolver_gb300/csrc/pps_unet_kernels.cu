@@ -10,6 +10,7 @@
 #include "pps_unet_internal.h"
 
 #include <algorithm>
+#include <type_traits>
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -816,6 +817,112 @@ __global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims
     if (kk < kk1) f[c] += (T)(0.5f * (vm + v0));   // a last even plane
 }
 
+// k_prolong_add_field on x-vectorised FP32 tiles: a thread owns four consecutive x
+// points of the field (one float4, tiles aligned to x = 0 as the solver's
+// vectorised Chebyshev tiles).  The four points need at most three consecutive
+// coarse x columns, X0..X0+2: per coarse plane the thread interpolates those in y
+// (6 loads), then each point in x, and adds the two fine planes the coarse plane
+// covers with float4 read-modify-writes.  The weights are k_prolong_add_field's
+// (interpolated in y first, so the rounding differs from it).
+__global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
+                                                              float* __restrict__ f, const int* __restrict__ stop)
+{
+    if (stop && *(volatile const int*)stop) return;
+    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
+    const int i0 = bx * 128 + threadIdx.x * 4;
+    const int j = g.lo[1] + by * sh.ty + threadIdx.y;
+    const int k0 = g.lo[2] + blockIdx.y * sh.kchunk, k1 = min(k0 + sh.kchunk, g.hi[2]);
+    if (j >= g.hi[1] || i0 >= g.hi[0] || i0 + 4 <= g.lo[0]) return;
+    const bool m0 = i0 >= g.lo[0] && i0 < g.hi[0], m1 = i0 + 1 >= g.lo[0] && i0 + 1 < g.hi[0];
+    const bool m2 = i0 + 2 >= g.lo[0] && i0 + 2 < g.hi[0], m3 = i0 + 3 >= g.lo[0] && i0 + 3 < g.hi[0];
+    const bool all4 = m0 && m1 && m2 && m3;
+    const int ii0 = i0 - g.lo[0];
+    const bool odd0 = (ii0 & 1) != 0;
+    const int X0 = (ii0 - 1) >> 1;   // floor((ii0 - 1) / 2): the lowest coarse column the points use
+    const int jj = j - g.lo[1];
+    int ya, yb;
+    float wya, wyb;
+    if (jj & 1) {
+        ya = yb = jj >> 1;
+        wya = 1.0f;
+        wyb = 0.0f;
+    } else {
+        ya = (jj >> 1) - 1;
+        yb = jj >> 1;
+        wya = ya >= 0 ? 0.5f : 0.0f;
+        wyb = 0.5f;
+        if (ya < 0) ya = yb;
+    }
+    const long long plane = (long long)dc.H * dc.W;
+    const long long ra = (long long)ya * dc.W, rb = (long long)yb * dc.W;
+    auto load3 = [&](int cz, float (&v)[3]) {   // coarse columns X0..X0+2 of plane cz, interpolated in y
+        const float* p = coarse + (long long)cz * plane;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const int X = X0 + q;
+            v[q] = X >= 0 && X < dc.W ? wya * p[ra + X] + wyb * p[rb + X] : 0.0f;
+        }
+    };
+    // x interpolation at the four points: odd fine columns take one coarse column,
+    // even ones the mean of two (fine ii: odd -> (ii-1)/2, even -> ii/2-1, ii/2)
+    auto xi = [&](const float (&v)[3]) -> float4 {
+        if (odd0) return make_float4(v[0], 0.5f * (v[0] + v[1]), v[1], 0.5f * (v[1] + v[2]));
+        return make_float4(0.5f * (v[0] + v[1]), v[1], 0.5f * (v[1] + v[2]), v[2]);
+    };
+    auto add = [&](long long c, float4 v) {
+        if (all4) {
+            float4 q = *reinterpret_cast<const float4*>(f + c);
+            q.x += v.x;
+            q.y += v.y;
+            q.z += v.z;
+            q.w += v.w;
+            *reinterpret_cast<float4*>(f + c) = q;
+        } else {
+            if (m0) f[c] += v.x;
+            if (m1) f[c + 1] += v.y;
+            if (m2) f[c + 2] += v.z;
+            if (m3) f[c + 3] += v.w;
+        }
+    };
+    const long long sk = g.sk;
+    const int kk1 = k1 - g.lo[2];
+    int kk = k0 - g.lo[2];
+    int cz = kk >> 1;
+    float vm[3] = {0.0f, 0.0f, 0.0f}, v0[3];
+    if (cz >= 1) load3(cz - 1, vm);
+    load3(cz, v0);
+    float4 xm = xi(vm), x0 = xi(v0);
+    long long c = i0 + g.sj * (long long)j + sk * (long long)k0;
+    if (kk & 1) {   // odd first plane: coarse plane cz alone
+        add(c, x0);
+        c += sk;
+        kk++;
+        xm = x0;
+        cz++;
+        if (cz < dc.D) {
+            load3(cz, v0);
+            x0 = xi(v0);
+        } else {
+            x0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+    for (; kk + 1 < kk1; kk += 2, c += 2 * sk) {
+        float4 xn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (cz + 1 < dc.D) {
+            float vn[3];
+            load3(cz + 1, vn);
+            xn = xi(vn);
+        }
+        add(c, make_float4(0.5f * (xm.x + x0.x), 0.5f * (xm.y + x0.y), 0.5f * (xm.z + x0.z), 0.5f * (xm.w + x0.w)));
+        add(c + sk, x0);
+        xm = x0;
+        x0 = xn;
+        cz++;
+    }
+    if (kk < kk1)   // a last even plane
+        add(c, make_float4(0.5f * (xm.x + x0.x), 0.5f * (xm.y + x0.y), 0.5f * (xm.z + x0.z), 0.5f * (xm.w + x0.w)));
+}
+
 template <typename T>
 void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s)
 {
@@ -848,6 +955,17 @@ void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& d
 template <typename T>
 void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
 {
+    if (sh.cx == 4) {   // the x-vectorised tiles (FP32 rows on 16-byte boundaries), else one column per thread
+        if constexpr (std::is_same<T, float>::value) {
+            if (g.sj % 4 == 0 && ((uintptr_t)f & 15u) == 0) {
+                k_prolong_add_field_v4<<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
+                launches_counter_add(1);
+                return;
+            }
+        }
+        prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
+        return;
+    }
     k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
     launches_counter_add(1);
 }
