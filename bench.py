@@ -349,8 +349,9 @@ def run_gpu(args, dist: Dist):
         "hbm_gbs_solve": stats[-1]["hbm_bytes"] / stats[-1]["seconds_solve"] / 1e9,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_cheb_sweep<float> (Chebyshev sweep: Y with its 6 neighbours, B, Z in, W out; 16 B "
-                      "per unknown; timed in the mixed BiCGSTAB solves, the smoother kernel of the headline too)",
+            "kernel": "k_cheb_v4<1>, k_cheb_v4<2> (the FP32 Chebyshev sweeps, one float4 per thread: Y with its "
+                      "6 neighbours, B, [Z] in, W out; 12 / 16 B per unknown; timed in the mixed BiCGSTAB solves, "
+                      "the smoother kernels of the headline too)",
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
