@@ -183,8 +183,8 @@ def train_network(args, dev: int, coarsen: int):
     from parallelpoissonsolver_gb300 import learned
 
     t0 = time.perf_counter()
-    train = learned.make_dataset(NET_GRID, range(10000, 10000 + args.train_samples), device=dev, coarsen=coarsen)
-    held = learned.make_dataset(NET_GRID, range(30000, 30000 + 16), device=dev, coarsen=coarsen)
+    train = learned.make_dataset_batch(NET_GRID, 10000, args.train_samples, coarsen, device=dev)
+    held = learned.make_dataset_batch(NET_GRID, 30000, args.held_out_pairs, coarsen, device=dev)
     t_data = time.perf_counter() - t0
     scale = learned.fit_scale(train)
     net = pps.UNet((16, 32, 64), seed=1, device=dev, linear=True)
@@ -195,7 +195,8 @@ def train_network(args, dev: int, coarsen: int):
     errs = learned.evaluate(net, held, scale)
     info = {"grid": f"{NET_GRID}^3", "channels": [16, 32, 64], "activation": "identity (linear U-Net)",
             "precision": "BF16 weights/activations, FP32 accumulation (tensor cores)",
-            "train_pairs": len(train), "steps": args.train_steps, "final_loss": float(np.mean(losses[-100:])),
+            "train_pairs": len(train), "held_out_pairs": len(held), "steps": args.train_steps,
+            "final_loss": float(np.mean(losses[-100:])),
             "held_out_rel_err_median": float(np.median(errs)), "held_out_rel_err_max": float(np.max(errs)),
             "data_s": t_data, "train_s": t_train, "scale": scale, "coarsen": coarsen}
     return net, scale, info
@@ -275,7 +276,7 @@ def run_gpu(args, dist: Dist):
     xp = torch.zeros(b_h.shape, dtype=torch.float64).pin_memory()
     bp = torch.from_numpy(b_h).pin_memory()
     xn, bn = xp.numpy(), bp.numpy()
-    e2e = []
+    e2e, e2e_parts = [], []
     for kk in range(args.steps + 1):
         xn[...] = 0.0
         t = time.perf_counter()
@@ -285,7 +286,10 @@ def run_gpu(args, dist: Dist):
             raise RuntimeError(f"e2e solve failed: {pps.status_string(st)}")
         if kk > 0:
             e2e.append(el)
+            d = head.stats()
+            e2e_parts.append((d["seconds_h2d"], d["seconds_solve"], d["seconds_d2h"]))
     t_e2e = dist.max(sum(e2e) / len(e2e))
+    e2e_split = {k: statistics.median(p[i] for p in e2e_parts) for i, k in enumerate(("h2d_s", "solve_s", "d2h_s"))}
 
     # ---- roofline of the FP32 Chebyshev sweep, event-timed on the solver's stream.
     # The headline solve replays CUDA graphs, which carry no events, so the sweeps are
@@ -335,7 +339,8 @@ def run_gpu(args, dist: Dist):
             "network": net_info,
             "tiles": tuned,
         },
-        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8},
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8,
+                "median_split": e2e_split},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "forms": {
             "mixed+learned (FCG)": summary(stats[-1], t_step),
@@ -722,9 +727,10 @@ def main():
     ap.add_argument("--comp-size", type=int, default=256)
     ap.add_argument("--large", action="store_true", help="also run the 1024^3 charges solve (several minutes)")
     ap.add_argument("--no-learned-128", action="store_true")
-    ap.add_argument("--held-out", type=int, default=16)
-    ap.add_argument("--train-samples", type=int, default=256)
-    ap.add_argument("--train-steps", type=int, default=4000)
+    ap.add_argument("--held-out", type=int, default=64, help="held-out right-hand sides of the 128^3 solves")
+    ap.add_argument("--held-out-pairs", type=int, default=1000, help="held-out pairs the network is scored on")
+    ap.add_argument("--train-samples", type=int, default=20000)
+    ap.add_argument("--train-steps", type=int, default=20000)
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])

@@ -92,6 +92,53 @@ def make_dataset(m: int, seeds, device: int = 0, tol: float = 1e-12, coarsen: in
     return out
 
 
+def make_dataset_batch(m: int, seed: int, count: int, coarsen: int, device=0, chunk: int = 2048):
+    """`count` (b, u) pairs for the coarse level of `coarsen` coarsenings, generated
+    in batches from one seeded torch generator on `device` (a CUDA ordinal, or a torch
+    device): the first half k^-2 random fields (the distribution of random_field), the
+    second half sums of 1-8 Gaussian blobs (that of blobs); u from the exact level
+    solve.  Returns a list of dense float32 tensor pairs like make_dataset."""
+    import torch
+    dev = torch.device("cuda", device) if isinstance(device, int) else torch.device(device)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    h = 1.0 / (m + 1)
+    gap = 2.0 ** (-coarsen)
+    kz = torch.fft.fftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
+    kx = torch.fft.rfftfreq(m, d=1.0 / m, dtype=torch.float64, device=dev)
+    k2 = kz[:, None, None] ** 2 + kz[None, :, None] ** 2 + kx[None, None, :] ** 2
+    amp = torch.where(k2 > 0, k2 ** (-2.0 / 4.0), torch.zeros_like(k2))
+    c = torch.arange(1, m + 1, dtype=torch.float64, device=dev) * h
+    out = []
+    n_field = count // 2
+    done = 0
+    while done < count:
+        nb = min(chunk, count - done)
+        nf = max(0, min(nb, n_field - done))   # random fields in this batch
+        parts = []
+        if nf > 0:
+            noise = torch.randn((nf, m, m, m), generator=gen, dtype=torch.float64, device=dev)
+            f = torch.fft.irfftn(torch.fft.rfftn(noise, dim=(1, 2, 3)) * amp, s=(m, m, m), dim=(1, 2, 3))
+            f = f / torch.sqrt(torch.mean(f * f, dim=(1, 2, 3), keepdim=True))
+            parts.append(-f)
+        ng = nb - nf
+        if ng > 0:
+            nblob = torch.randint(1, 9, (ng, 1), generator=gen, device=dev)
+            active = (torch.arange(8, device=dev)[None, :] < nblob).to(torch.float64)
+            ctr = 0.2 + 0.6 * torch.rand((ng, 8, 3), generator=gen, dtype=torch.float64, device=dev)
+            w = 0.02 + 0.08 * torch.rand((ng, 8), generator=gen, dtype=torch.float64, device=dev)
+            a = torch.randn((ng, 8), generator=gen, dtype=torch.float64, device=dev) * active
+            g = torch.exp(-((c[None, None, None, :] - ctr[..., None]) ** 2) / (2 * w[..., None, None] ** 2))
+            f = torch.einsum("bk,bkz,bky,bkx->bzyx", a, g[:, :, 2], g[:, :, 1], g[:, :, 0])
+            parts.append(-f)
+        b = torch.cat(parts, 0)
+        u = level_solve(b, h, gap)
+        for i in range(nb):
+            out.append((b[i].float().contiguous(), u[i].float().contiguous()))
+        done += nb
+    return out
+
+
 def fit_scale(data) -> float:
     import torch
     r = [float(torch.sqrt(torch.mean(u * u)) / torch.sqrt(torch.mean(b * b))) for b, u in data]

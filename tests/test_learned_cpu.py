@@ -35,3 +35,23 @@ def test_level_solve_is_exact(gap):
     t = learned.level_operator_1d(n, gap) / (h * h)
     au = (np.einsum("ai,ijk->ajk", t, u) + np.einsum("bj,ijk->ibk", t, u) + np.einsum("ck,ijk->ijc", t, u))
     assert np.abs(au - b).max() < 1e-10 * np.abs(b).max()
+
+
+def test_batch_dataset_pairs_solve_the_level_operator():
+    """make_dataset_batch: half unit-RMS random fields, half blob sums, each u the exact
+    solution of the coarse-level operator for its b (checked on the CPU)."""
+    n, k = 8, 2
+    data = learned.make_dataset_batch(n, 7, 12, k, device="cpu", chunk=5)
+    assert len(data) == 12
+    h = 1.0 / (n + 1)
+    t = learned.level_operator_1d(n, 2.0 ** (-k)) / (h * h)
+    for i, (b, u) in enumerate(data):
+        assert b.shape == (n, n, n) and u.shape == (n, n, n) and b.dtype == torch.float32
+        bn, un = b.double().numpy(), u.double().numpy()
+        au = (np.einsum("ai,ijk->ajk", t, un) + np.einsum("bj,ijk->ibk", t, un) + np.einsum("ck,ijk->ijc", t, un))
+        assert np.abs(au - bn).max() < 1e-5 * np.abs(bn).max()
+        if i < 6:
+            assert abs(np.sqrt(np.mean(bn * bn)) - 1.0) < 1e-5   # random field, unit RMS
+    # the same seed gives the same data
+    again = learned.make_dataset_batch(n, 7, 12, k, device="cpu", chunk=5)
+    assert all(torch.equal(a[0], c[0]) for a, c in zip(data, again))
