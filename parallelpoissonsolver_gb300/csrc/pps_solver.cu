@@ -1259,7 +1259,11 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     const bool x_zero = x0_zero && !guess;
     const Coef a = op_coef(g);
     state_init(s->d_st, s->d_hist, s->cfg.maxit, s->cfg.tol * normb, 0.0, 0, 0, 1.0 / normb, s->hist_cap, st);
-    fast_residual<double>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st, x_zero);
+    // BiCGSTAB and CG start from r0 = p = r; flexible CG needs r alone (its first
+    // direction is the preconditioned residual)
+    const bool fcg = s->cfg.krylov == PPS_KRYLOV_FCG;
+    fast_residual<double>(g, s->shape, x, b, F.r, fcg ? nullptr : F.r0, fcg ? nullptr : F.p, a, red(s, FIN_RES0), st,
+                          x_zero);
     L.bytes += bytes_of<double>(s->n_unknowns, 5) + bytes_of<double>(s->n_unknowns, 1) * 2;
     pps_status rc = PPS_OK;
     read_state(s);
@@ -1319,7 +1323,9 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         // inner target max(inner_tol, 0.3*tol_abs/err0)*err0 on the device.
         state_init(s->d_st, s->d_hist, std::max(1, std::min(s->cfg.inner_maxit, remaining)), tol_abs,
                    s->cfg.inner_tol, 1, 1, 1.0 / normb, s->hist_cap, st);
-        fast_residual<float>(g, s->shape, x, b, F.r, F.r0, F.p, a, red(s, FIN_RES0), st, ref == 0 && x_zero);
+        const bool fcg = s->cfg.krylov == PPS_KRYLOV_FCG;   // r alone (see solve_fp64)
+        fast_residual<float>(g, s->shape, x, b, F.r, fcg ? nullptr : F.r0, fcg ? nullptr : F.p, a, red(s, FIN_RES0),
+                             st, ref == 0 && x_zero);
         L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 3);
         read_state(s);
         err_outer = s->h_st->err0;
