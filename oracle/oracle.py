@@ -1,7 +1,7 @@
 """ctypes wrapper of the test oracle (TEST INFRASTRUCTURE).
 
 Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
-module, and only as the checker.  The product path never does.
+module, and only to check results.  The product path never does.
 
 * ``liboracle.so``: the C restatement in ``pps_oracle.c`` (runs everywhere).
 * ``_ref/libppsref.so``: the reference's own CPU solver headers compiled by

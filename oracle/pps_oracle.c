@@ -2,7 +2,7 @@
  * pps_oracle.c -- CPU restatement of the reference solve loop (TEST INFRASTRUCTURE).
  *
  * The oracle: only tests, the smoke check and bench.py's CPU-baseline leg call it,
- * always as the checker.  See pps_oracle.h for the reference files each part follows.
+ * always to check results.  See pps_oracle.h for the reference files each part follows.
  *
  * Every arithmetic expression below keeps the reference's operand order so that,
  * compiled with -ffp-contract=off, each result is bit-identical to the reference's

@@ -2,7 +2,7 @@
  * pps_oracle.h -- CPU restatement of the reference solve loop (TEST INFRASTRUCTURE).
  *
  * This is the oracle: tests, the smoke check and the CPU-baseline leg of bench.py
- * call it as the checker.  The product (libpps) never links or calls it.
+ * call it to check results.  The product (libpps) never links or calls it.
  *
  * It restates, in the reference's exact floating-point expression order, the
  * single-rank path of solverPoissonMPI_CPU:
