@@ -255,8 +255,10 @@ pps_status pps_batch_set(pps_batch* batch, int p, const double* x, const double*
 pps_status pps_batch_get(pps_batch* batch, int p, double* x, pps_stats* stats);
 pps_status pps_batch_field_device(pps_batch* batch, int p, double** x_dev, double** b_dev);
 /* Times the batched sweep for every grid shape in the batch over candidate tiles
- * (columns per thread 1/2, z-chunk 8..128) and keeps the fastest per shape. */
+ * (columns per thread 1/2, z-chunk 8..128, and the x-vectorised float4 tiles where
+ * npglobal[0] + 2 is a multiple of 4) and keeps the fastest per shape. */
 pps_status pps_batch_autotune(pps_batch* batch);
+/* The Chebyshev kernels' tile of problem p: cx 1, 2, or 4 (float4 per thread). */
 pps_status pps_batch_tile(const pps_batch* batch, int p, int* cx, int* kchunk);
 /* Solves every problem to cfg->tol (FP64 true residual).  PPS_NOT_CONVERGED if any
  * problem stopped short. */

@@ -40,9 +40,14 @@ struct Fail {};
 
 const double kPi = 3.141592653589793;
 
+// Tiles of one grid shape: columns per thread and planes per z-chunk of every
+// kernel, and, where the rows allow it, the x-vectorised float4 tiles (v4, with their
+// own z-chunk) that the Chebyshev kernels then run on.
 struct SizeTile {
     int cx = 1;
     int kchunk = 32;
+    bool v4 = false;
+    int kchunk4 = 32;
 };
 
 const int kKchunks[] = {8, 16, 32, 64, 128};
@@ -68,6 +73,10 @@ struct pps_batch {
     BProb* dprob = nullptr;
     unsigned* dblk = nullptr;
     unsigned blk_cap = 0;
+    // the Chebyshev kernels' table (v4 tiles where chosen)
+    BProb* dprob4 = nullptr;
+    unsigned* dblk4 = nullptr;
+    unsigned blk_cap4 = 0;
     double* partials = nullptr;
     unsigned* counters = nullptr;
     BState* dst = nullptr;
@@ -75,6 +84,7 @@ struct pps_batch {
     void* coef = nullptr;
     int cstride = 0;
     BatchDev B;
+    BatchDev B4;
     cudaGraphExec_t gexec = nullptr;
     int g_iters = 0;
     int g_launches = 0;
@@ -90,16 +100,19 @@ long long key_of(const Geo& g)
            (long long)(g.hi[2] - g.lo[2]);
 }
 
-BProb make_prob(const Geo& g, long long off, const SizeTile& t)
+// The problem's tile for the Chebyshev kernels (cheb) or for the others.  v4 tiles
+// start at x = 0 and must reach hi[0]; they need a row stride of whole float4s.
+BProb make_prob(const Geo& g, long long off, const SizeTile& t, bool cheb)
 {
     BProb P;
     P.g = g;
     P.off = off;
-    P.cx = t.cx;
+    const bool v4 = cheb && t.v4 && g.sj % 4 == 0 && off % 4 == 0;
+    P.cx = v4 ? 4 : t.cx;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
-    P.ntx = (ux + 32 * t.cx - 1) / (32 * t.cx);
+    P.ntx = v4 ? (g.hi[0] + 127) / 128 : (ux + 32 * t.cx - 1) / (32 * t.cx);
     P.nty = (uy + 7) / 8;
-    P.kchunk = std::min(t.kchunk, uz);
+    P.kchunk = std::min(v4 ? t.kchunk4 : t.kchunk, uz);
     P.nchunks = (uz + P.kchunk - 1) / P.kchunk;
     P.nblocks = (unsigned)P.ntx * P.nty * P.nchunks;
     P.first_block = 0;
@@ -107,9 +120,14 @@ BProb make_prob(const Geo& g, long long off, const SizeTile& t)
 }
 
 // Builds the problem table and the block -> problem map for the problems in
-// `which` (biggest first, so the longest items start first), uploads them.
-BatchDev build_table(pps_batch* s, const std::vector<int>& which)
+// `which` (biggest first, so the longest items start first), uploads them: the
+// table of every kernel, or (cheb) the Chebyshev kernels' own.
+BatchDev build_table(pps_batch* s, const std::vector<int>& which, bool cheb = false)
 {
+    BProb*& dprob = cheb ? s->dprob4 : s->dprob;
+    unsigned*& dblk = cheb ? s->dblk4 : s->dblk;
+    unsigned& cap = cheb ? s->blk_cap4 : s->blk_cap;
+    const BatchDev& previous = cheb ? s->B4 : s->B;
     std::vector<int> order = which;
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
         const long long na = (long long)(s->geo[a].hi[0] - s->geo[a].lo[0]) * (s->geo[a].hi[1] - s->geo[a].lo[1]) *
@@ -120,32 +138,35 @@ BatchDev build_table(pps_batch* s, const std::vector<int>& which)
     });
     std::vector<BProb> hp((size_t)s->nprob);
     std::vector<unsigned> blk;
-    for (int p = 0; p < s->nprob; p++) hp[(size_t)p] = make_prob(s->geo[(size_t)p], s->off[(size_t)p], s->tiles[key_of(s->geo[(size_t)p])]);
+    for (int p = 0; p < s->nprob; p++)
+        hp[(size_t)p] = make_prob(s->geo[(size_t)p], s->off[(size_t)p], s->tiles[key_of(s->geo[(size_t)p])], cheb);
     for (int p : order) {
         BProb& P = hp[(size_t)p];
         P.first_block = (unsigned)blk.size();
         for (unsigned q = 0; q < P.nblocks; q++) blk.push_back((unsigned)p);
     }
-    if (blk.size() > s->blk_cap) {
+    if (blk.size() > cap) {
         if (s->gexec) {   // a captured graph holds the old table pointers
             cudaGraphExecDestroy(s->gexec);
             s->gexec = nullptr;
         }
-        if (s->dblk) cudaFree(s->dblk);
-        if (s->partials) cudaFree(s->partials);
-        s->blk_cap = (unsigned)blk.size();
-        BK(cudaMalloc((void**)&s->dblk, sizeof(unsigned) * s->blk_cap));
-        BK(cudaMalloc((void**)&s->partials, sizeof(double) * 4 * (size_t)s->blk_cap));
+        if (dblk) cudaFree(dblk);
+        cap = (unsigned)blk.size();
+        BK(cudaMalloc((void**)&dblk, sizeof(unsigned) * cap));
+        if (!cheb) {   // block partials of the reductions (the Chebyshev kernels reduce nothing)
+            if (s->partials) cudaFree(s->partials);
+            BK(cudaMalloc((void**)&s->partials, sizeof(double) * 4 * (size_t)cap));
+        }
     }
-    BK(cudaMemcpyAsync(s->dprob, hp.data(), sizeof(BProb) * hp.size(), cudaMemcpyHostToDevice, s->stream));
-    BK(cudaMemcpyAsync(s->dblk, blk.data(), sizeof(unsigned) * blk.size(), cudaMemcpyHostToDevice, s->stream));
+    BK(cudaMemcpyAsync(dprob, hp.data(), sizeof(BProb) * hp.size(), cudaMemcpyHostToDevice, s->stream));
+    BK(cudaMemcpyAsync(dblk, blk.data(), sizeof(unsigned) * blk.size(), cudaMemcpyHostToDevice, s->stream));
     BK(cudaStreamSynchronize(s->stream));
     BatchDev B;
-    B.prob = s->dprob;
-    B.blk2prob = s->dblk;
+    B.prob = dprob;
+    B.blk2prob = dblk;
     B.nprob = s->nprob;
     B.total_blocks = (unsigned)blk.size();
-    if (s->gexec && B.total_blocks != s->B.total_blocks) {   // the graph was captured for another table
+    if (s->gexec && B.total_blocks != previous.total_blocks) {   // the graph was captured for another table
         cudaGraphExecDestroy(s->gexec);
         s->gexec = nullptr;
     }
@@ -188,10 +209,12 @@ void b_precond(pps_batch* s, const BatchDev& B, const float* Bf, float* X)
     float* Y = s->Y;
     float* Z = s->Z;
     float* W = s->W;
-    b_cheb_s01(B, Bf, Y, s->coef, s->cstride, 0, s->dst, s->stream);
+    const BatchDev& B4 = s->B4;   // the Chebyshev kernels' tiles (B: the others')
+    (void)B;
+    b_cheb_s01(B4, Bf, Y, s->coef, s->cstride, 0, s->dst, s->stream);
     for (int it = 2; it <= n - 2; it++) {
         const bool last = it == n - 2;
-        b_cheb_sweep(B, Y, Bf, it == 2 ? nullptr : Z, last ? X : W, s->coef, s->cstride, it - 1, s->dst, s->stream);
+        b_cheb_sweep(B4, Y, Bf, it == 2 ? nullptr : Z, last ? X : W, s->coef, s->cstride, it - 1, s->dst, s->stream);
         if (!last) {
             float* t = Z;
             Z = Y;
@@ -237,7 +260,7 @@ void free_batch(pps_batch* s)
 {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     void* ptrs[] = {s->x, s->b, s->p, s->r, s->r0, s->Mp, s->AMp, s->z, s->Az, s->Y, s->Z, s->W, s->e,
-                    s->dprob, s->dblk, s->partials, s->counters, s->dst, s->coef};
+                    s->dprob, s->dblk, s->dprob4, s->dblk4, s->partials, s->counters, s->dst, s->coef};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (s->hst) cudaFreeHost(s->hst);
@@ -265,6 +288,7 @@ pps_status run_batch(pps_batch* s)
     std::vector<int> all((size_t)s->nprob);
     std::iota(all.begin(), all.end(), 0);
     s->B = build_table(s, all);
+    s->B4 = build_table(s, all, true);
     const BatchDev& B = s->B;
     std::vector<BState> init((size_t)s->nprob);
     std::memset(init.data(), 0, sizeof(BState) * init.size());
@@ -362,14 +386,27 @@ void tune_shape(pps_batch* s, long long key, const std::vector<int>& which)
     std::vector<BState> init((size_t)s->nprob);
     std::memset(init.data(), 0, sizeof(BState) * init.size());
     BK(cudaMemcpyAsync(s->dst, init.data(), sizeof(BState) * init.size(), cudaMemcpyHostToDevice, s->stream));
-    for (int cx : {1, 2}) {
+    const Geo& g0 = s->geo[(size_t)which[0]];
+    const bool v4_ok = g0.sj % 4 == 0;
+    float best4 = 1e30f;
+    int best_kc4 = 32;
+    // the one-column tiles (cx 1, 2) for every kernel, then the v4 tiles for the
+    // Chebyshev kernels (kept when they beat the best one-column tile on the sweep)
+    for (int cx : {1, 2, 4}) {
+        if (cx == 4 && !v4_ok) break;
         for (int kc : kKchunks) {
-            SizeTile t;
-            t.cx = cx;
-            t.kchunk = kc;
+            SizeTile t = best_t;
+            if (cx == 4) {
+                t.v4 = true;
+                t.kchunk4 = kc;
+            } else {
+                t.cx = cx;
+                t.kchunk = kc;
+                t.v4 = false;
+            }
             s->tiles[key] = t;
-            const BatchDev B = build_table(s, which);
-            s->B = B;
+            const BatchDev B = build_table(s, which, true);
+            s->B4 = B;
             auto launch = [&]() {
                 b_cheb_sweep(B, s->Y, s->r, s->Z, s->W, s->coef, s->cstride, std::min(2, s->cstride - 1), s->dst,
                              s->stream);
@@ -382,12 +419,19 @@ void tune_shape(pps_batch* s, long long key, const std::vector<int>& which)
             BK(cudaEventSynchronize(s->ev1));
             float ms = 0;
             BK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-            if (ms < best) {
+            if (cx == 4) {
+                if (ms < best4) {
+                    best4 = ms;
+                    best_kc4 = kc;
+                }
+            } else if (ms < best) {
                 best = ms;
                 best_t = t;
             }
         }
     }
+    best_t.v4 = best4 < best;
+    best_t.kchunk4 = best_kc4;
     s->tiles[key] = best_t;
 }
 
@@ -485,6 +529,7 @@ pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* 
             BK(cudaMemsetAsync(*q, 0, sizeof(float) * (size_t)pool, s->stream));
         }
         BK(cudaMalloc((void**)&s->dprob, sizeof(BProb) * (size_t)nprob));
+        BK(cudaMalloc((void**)&s->dprob4, sizeof(BProb) * (size_t)nprob));
         BK(cudaMalloc((void**)&s->counters, sizeof(unsigned) * (size_t)nprob));
         BK(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * (size_t)nprob, s->stream));
         BK(cudaMalloc((void**)&s->dst, sizeof(BState) * (size_t)nprob));
@@ -594,8 +639,9 @@ pps_status pps_batch_tile(const pps_batch* s, int p, int* cx, int* kchunk)
     if (!s || p < 0 || p >= s->nprob) return PPS_ERR_INVALID_ARG;
     auto it = s->tiles.find(key_of(s->geo[(size_t)p]));
     if (it == s->tiles.end()) return PPS_ERR_INVALID_ARG;
-    if (cx) *cx = it->second.cx;
-    if (kchunk) *kchunk = it->second.kchunk;
+    const bool v4 = it->second.v4 && s->geo[(size_t)p].sj % 4 == 0;   // the Chebyshev kernels' tile
+    if (cx) *cx = v4 ? 4 : it->second.cx;
+    if (kchunk) *kchunk = v4 ? it->second.kchunk4 : it->second.kchunk;
     return PPS_OK;
 }
 

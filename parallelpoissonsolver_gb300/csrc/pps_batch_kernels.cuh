@@ -29,7 +29,8 @@ __device__ __forceinline__ BCol bcolumn(const BatchDev& B)
     const unsigned tile = local % tiles, chunk = local / tiles;
     const int bx = (int)(tile % (unsigned)P.ntx), by = (int)(tile / (unsigned)P.ntx);
     q.cx = P.cx;
-    q.i = P.g.lo[0] + bx * 32 * P.cx + threadIdx.x;
+    // cx 4: the x-vectorised Chebyshev tiles, a float4 per thread from x = 0
+    q.i = P.cx == 4 ? bx * 128 + threadIdx.x * 4 : P.g.lo[0] + bx * 32 * P.cx + threadIdx.x;
     q.j = P.g.lo[1] + by * (int)blockDim.y + threadIdx.y;
     q.k0 = P.g.lo[2] + (int)chunk * P.kchunk;
     q.k1 = min(q.k0 + P.kchunk, P.g.hi[2]);
@@ -258,6 +259,10 @@ __global__ void __launch_bounds__(256) bk_cheb_s01(BatchDev B, const float* __re
     if (!q.active) return;
     const CT<float> cf = coef[(size_t)q.p * cstride + ci];
     const Geo& g = q.P->g;
+    if (q.cx == 4) {   // the block's rows are whole warps: all lanes reach the shuffles
+        cheb_v4_march<0>(g, q.i, q.k0, q.k1, q.c, Bf, nullptr, nullptr, Y, cf);
+        return;
+    }
     const long long sj = g.sj, sk = g.sk;
     for (int u = 0; u < q.cx; u++) {
         if (q.i + 32 * u >= g.hi[0]) break;
@@ -289,6 +294,10 @@ __global__ void __launch_bounds__(256) bk_cheb_sweep(BatchDev B, const float* __
     if (!q.active) return;
     const CT<float> cf = coef[(size_t)q.p * cstride + ci];
     const Geo& g = q.P->g;
+    if (q.cx == 4) {
+        cheb_v4_march<HAS_Z ? 2 : 1>(g, q.i, q.k0, q.k1, q.c, Y, Bf, Z, W, cf);
+        return;
+    }
     const long long sj = g.sj, sk = g.sk;
     for (int u = 0; u < q.cx; u++) {
         if (q.i + 32 * u >= g.hi[0]) break;

@@ -893,33 +893,33 @@ __device__ __forceinline__ float4 add4(float4 a, float4 b)
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-// MODE 0: W = s1 of U (k_cheb_s01); 1: a sweep without Z; 2: a sweep with Z.
+// One thread's march of k_cheb_v4 along z: the float4 at x = i0 (a multiple of 4)
+// of the row whose plane-k0 index is c, planes [k0, k1).  MODE 0: W = s1 of U
+// (k_cheb_s01); 1: a sweep without Z; 2: a sweep with Z.  Every lane of the warp must
+// call it (the x neighbours come by shuffle); lanes whose float4 holds no unknown
+// compute on zeros and store nothing.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_cheb_v4(Geo g, Shape sh, const float* __restrict__ U,
-                                                 const float* __restrict__ B, const float* __restrict__ Z,
-                                                 float* __restrict__ W, CT<float> cf, const int* done)
+__device__ __forceinline__ void cheb_v4_march(const Geo& g, int i0, int k0, int k1, long long c,
+                                              const float* __restrict__ U, const float* __restrict__ B,
+                                              const float* __restrict__ Z, float* __restrict__ W, const CT<float>& cf)
 {
-    EARLY_EXIT(done);
-    const Col4 q = column4(g, sh);
-    if (q.j >= g.hi[1]) return;   // a warp shares its row, so its lanes leave together
-    const bool act = q.act;
+    const bool act = i0 < g.hi[0] && i0 + 4 > g.lo[0];
     const int lane = threadIdx.x;
-    const bool m0 = q.i0 >= g.lo[0] && q.i0 < g.hi[0], m1 = q.i0 + 1 >= g.lo[0] && q.i0 + 1 < g.hi[0];
-    const bool m2 = q.i0 + 2 >= g.lo[0] && q.i0 + 2 < g.hi[0], m3 = q.i0 + 3 >= g.lo[0] && q.i0 + 3 < g.hi[0];
+    const bool m0 = i0 >= g.lo[0] && i0 < g.hi[0], m1 = i0 + 1 >= g.lo[0] && i0 + 1 < g.hi[0];
+    const bool m2 = i0 + 2 >= g.lo[0] && i0 + 2 < g.hi[0], m3 = i0 + 3 >= g.lo[0] && i0 + 3 < g.hi[0];
     const bool all4 = m0 && m1 && m2 && m3;
     const long long sj = g.sj, sk = g.sk;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    long long c = q.c;
     float4 um = act ? ld4(U + c - sk) : zero, uc = act ? ld4(U + c) : zero;
 #pragma unroll 2
-    for (int k = q.k0; k < q.k1; k++) {
+    for (int k = k0; k < k1; k++) {
         const float4 up = act ? ld4(U + c + sk) : zero;
         const float4 uy = act ? add4(ld4(U + c - sj), ld4(U + c + sj)) : zero;
         const float4 bv = (MODE >= 1 && act) ? ld4(B + c) : zero;
         const float4 zv = (MODE == 2 && act) ? ld4(Z + c) : zero;
         float left = __shfl_up_sync(0xffffffffu, uc.w, 1), right = __shfl_down_sync(0xffffffffu, uc.x, 1);
         if (lane == 0) left = act ? U[c - 1] : 0.f;
-        if (lane == 31) right = act && q.i0 + 4 < sj ? U[c + 4] : 0.f;
+        if (lane == 31) right = act && i0 + 4 < sj ? U[c + 4] : 0.f;
         float4 w;
         w.x = fmx(cf.cz, um.x + up.x, fmx(cf.cy, uy.x, fmx(cf.cx, left + uc.y, cf.cc * uc.x)));
         w.y = fmx(cf.cz, um.y + up.y, fmx(cf.cy, uy.y, fmx(cf.cx, uc.x + uc.z, cf.cc * uc.y)));
@@ -951,6 +951,17 @@ __global__ void __launch_bounds__(256) k_cheb_v4(Geo g, Shape sh, const float* _
         uc = up;
         c += sk;
     }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cheb_v4(Geo g, Shape sh, const float* __restrict__ U,
+                                                 const float* __restrict__ B, const float* __restrict__ Z,
+                                                 float* __restrict__ W, CT<float> cf, const int* done)
+{
+    EARLY_EXIT(done);
+    const Col4 q = column4(g, sh);
+    if (q.j >= g.hi[1]) return;   // a warp shares its row, so its lanes leave together
+    cheb_v4_march<MODE>(g, q.i0, q.k0, q.k1, q.c, U, B, Z, W, cf);
 }
 
 // The vectorised kernels take FP32 fields whose rows start on 16-byte boundaries.

@@ -55,7 +55,7 @@ def test_batch_graph_equals_direct_and_autotune(gpu):
         bt = pps.Batch(grids, use_graph=graph)
         if tune:
             tiles = bt.autotune()
-            assert all(cx in (1, 2) and kc in (8, 16, 32, 64, 128) for cx, kc in tiles)
+            assert all(cx in (1, 2, 4) and kc in (8, 16, 32, 64, 128) for cx, kc in tiles)
         for p, (x, b) in enumerate(fields):
             bt.set(p, x, b)
         assert bt.solve() == pps.OK
