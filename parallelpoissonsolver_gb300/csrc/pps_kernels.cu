@@ -14,6 +14,7 @@
 #include "pps_internal.h"
 
 #include <algorithm>
+#include <initializer_list>
 #include <type_traits>
 
 #include <cuda_runtime.h>
@@ -1594,6 +1595,166 @@ __global__ void __launch_bounds__(256) k_fcg_dot_flat(long long n, const T* __re
     reduce_finalize<3>(v, rc);
 }
 
+// The BiCGSTAB updates in the same flat form (Dirichlet grids: r, r0, Mp, z, Az,
+// AMp and p are zero off the unknowns, so the guard cells of x and p keep their
+// values and add nothing to the sums; the reference itself updates x over every
+// cell, BiCGSTAB.hpp:227-230).
+// x += alpha Mp + omega z; r -= omega Az; sums r0.r, r.r   (BiCGSTAB.hpp:227-257)
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_xr_flat(long long n, T* __restrict__ x, const T* __restrict__ Mp,
+                                                        const T* __restrict__ z, T* __restrict__ r,
+                                                        const T* __restrict__ Az, const T* __restrict__ r0, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    typedef Vec16<T> VT;
+    typedef typename VT::type V;
+    const T a = (T)rc.st->alpha, w = (T)rc.st->omega;
+    Acc<T> a1, a2;
+    const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        V xv = reinterpret_cast<const V*>(x)[i], mv = reinterpret_cast<const V*>(Mp)[i];
+        V zv = reinterpret_cast<const V*>(z)[i], rv = reinterpret_cast<const V*>(r)[i];
+        V av = reinterpret_cast<const V*>(Az)[i], ov = reinterpret_cast<const V*>(r0)[i];
+#pragma unroll
+        for (int e = 0; e < VT::n; e++) {
+            VT::at(xv, e) = fmx(w, VT::at(zv, e), fmx(a, VT::at(mv, e), VT::at(xv, e)));
+            const T rn = fmx(-w, VT::at(av, e), VT::at(rv, e));
+            VT::at(rv, e) = rn;
+            a1.add(VT::at(ov, e), rn);
+            a2.add(rn, rn);
+        }
+        reinterpret_cast<V*>(x)[i] = xv;
+        reinterpret_cast<V*>(r)[i] = rv;
+    }
+    for (long long i = nv * VT::n + t0; i < n; i += stride) {
+        x[i] = fmx(w, z[i], fmx(a, Mp[i], x[i]));
+        const T rn = fmx(-w, Az[i], r[i]);
+        r[i] = rn;
+        a1.add(r0[i], rn);
+        a2.add(rn, rn);
+    }
+    double v[2] = {a1.value(), a2.value()};
+    reduce_finalize<2>(v, rc);
+}
+
+// p = r + beta (p - omega AMp)   (BiCGSTAB.hpp:261-272)
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_p_flat(long long n, T* __restrict__ p, const T* __restrict__ r,
+                                                       const T* __restrict__ AMp, const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    typedef Vec16<T> VT;
+    typedef typename VT::type V;
+    const T be = (T)st->beta, w = (T)st->omega;
+    const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        V pv = reinterpret_cast<const V*>(p)[i], rv = reinterpret_cast<const V*>(r)[i];
+        V av = reinterpret_cast<const V*>(AMp)[i];
+#pragma unroll
+        for (int e = 0; e < VT::n; e++) VT::at(pv, e) = fmx(be, fmx(-w, VT::at(av, e), VT::at(pv, e)), VT::at(rv, e));
+        reinterpret_cast<V*>(p)[i] = pv;
+    }
+    for (long long i = nv * VT::n + t0; i < n; i += stride) p[i] = fmx(be, fmx(-w, AMp[i], p[i]), r[i]);
+}
+
+// r -= alpha v   (BiCGSTAB.hpp:167-178)
+template <typename T>
+__global__ void __launch_bounds__(256) k_axpy_alpha_flat(long long n, T* __restrict__ r, const T* __restrict__ v,
+                                                         const DevState* st)
+{
+    EARLY_EXIT(&st->done);
+    typedef Vec16<T> VT;
+    typedef typename VT::type V;
+    const T a = (T)st->alpha;
+    const long long nv = n / VT::n, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = t0; i < nv; i += stride) {
+        V rv = reinterpret_cast<const V*>(r)[i], vv = reinterpret_cast<const V*>(v)[i];
+#pragma unroll
+        for (int e = 0; e < VT::n; e++) VT::at(rv, e) = fmx(-a, VT::at(vv, e), VT::at(rv, e));
+        reinterpret_cast<V*>(r)[i] = rv;
+    }
+    for (long long i = nv * VT::n + t0; i < n; i += stride) r[i] = fmx(-a, v[i], r[i]);
+}
+
+// The BiCGSTAB stencils on the x-vectorised FP32 tiles: Au = A u and, NS = 1, sum
+// w.Au (k_stencil_dot, w = r0) or, NS = 2, sums w.Au and Au.Au (k_stencil_dot2,
+// w = r); per point the arithmetic of the one-column kernels, the sums in another
+// order.
+template <int NS>
+__global__ void __launch_bounds__(256) k_stencil_dots_v4(Geo g, Shape sh, const float* __restrict__ u,
+                                                         const float* __restrict__ wv, float* __restrict__ Au,
+                                                         Coef cf, RedCtx rc)
+{
+    EARLY_EXIT(&rc.st->done);
+    const Col4 q = column4(g, sh);
+    Acc<float> a1, a2;
+    if (q.j < g.hi[1]) {   // a warp shares its row: the shuffles below see all 32 lanes
+        const bool act = q.act;
+        const int lane = threadIdx.x;
+        const bool m0 = q.i0 >= g.lo[0] && q.i0 < g.hi[0], m1 = q.i0 + 1 >= g.lo[0] && q.i0 + 1 < g.hi[0];
+        const bool m2 = q.i0 + 2 >= g.lo[0] && q.i0 + 2 < g.hi[0], m3 = q.i0 + 3 >= g.lo[0] && q.i0 + 3 < g.hi[0];
+        const bool all4 = m0 && m1 && m2 && m3;
+        const float cc = (float)cf.cc, cx = (float)cf.cx, cy = (float)cf.cy, cz = (float)cf.cz;
+        const long long sj = g.sj, sk = g.sk;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        long long c = q.c;
+        float4 um = act ? ld4(u + c - sk) : zero, uc = act ? ld4(u + c) : zero;
+#pragma unroll 1
+        for (int k = q.k0; k < q.k1; k++) {
+            const float4 up = act ? ld4(u + c + sk) : zero;
+            const float4 uy = act ? add4(ld4(u + c - sj), ld4(u + c + sj)) : zero;
+            float left = __shfl_up_sync(0xffffffffu, uc.w, 1), right = __shfl_down_sync(0xffffffffu, uc.x, 1);
+            if (lane == 0) left = act ? u[c - 1] : 0.f;
+            if (lane == 31) right = act && q.i0 + 4 < sj ? u[c + 4] : 0.f;
+            float4 a;
+            a.x = fmx(cz, um.x + up.x, fmx(cy, uy.x, fmx(cx, left + uc.y, cc * uc.x)));
+            a.y = fmx(cz, um.y + up.y, fmx(cy, uy.y, fmx(cx, uc.x + uc.z, cc * uc.y)));
+            a.z = fmx(cz, um.z + up.z, fmx(cy, uy.z, fmx(cx, uc.y + uc.w, cc * uc.z)));
+            a.w = fmx(cz, um.w + up.w, fmx(cy, uy.w, fmx(cx, uc.z + right, cc * uc.w)));
+            if (act) {
+                const float4 w4 = ld4(wv + c);
+                if (all4) {
+                    *reinterpret_cast<float4*>(Au + c) = a;
+                } else {
+                    if (m0) Au[c] = a.x;
+                    if (m1) Au[c + 1] = a.y;
+                    if (m2) Au[c + 2] = a.z;
+                    if (m3) Au[c + 3] = a.w;
+                }
+                if (m0) {
+                    a1.add(w4.x, a.x);
+                    if (NS == 2) a2.add(a.x, a.x);
+                }
+                if (m1) {
+                    a1.add(w4.y, a.y);
+                    if (NS == 2) a2.add(a.y, a.y);
+                }
+                if (m2) {
+                    a1.add(w4.z, a.z);
+                    if (NS == 2) a2.add(a.z, a.z);
+                }
+                if (m3) {
+                    a1.add(w4.w, a.w);
+                    if (NS == 2) a2.add(a.w, a.w);
+                }
+            }
+            um = uc;
+            uc = up;
+            c += sk;
+        }
+    }
+    if (NS == 1) {
+        double v[1] = {a1.value()};
+        reduce_finalize<1>(v, rc);
+    } else {
+        double v[2] = {a1.value(), a2.value()};
+        reduce_finalize<2>(v, rc);
+    }
+}
+
 // r = b - A x in FP64 (computeErrorOperatorA, iterativeSolverBase.hpp:236-280),
 // stored as TR; optional copies into r0 and p (BiCGSTAB.hpp:125-126); sum r^2.
 // A double as m * 2^(e - 1075) with |m| < 2^53 (subnormals: e = 1, no hidden bit).
@@ -1904,6 +2065,17 @@ template <typename T>
 void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T* Au, const Coef& a, RedCtx rc,
                       cudaStream_t s)
 {
+    if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
+        if constexpr (std::is_same<T, float>::value) {
+            if (sh.cx == 4 && v4_ok<T>(g, u, r0, Au, nullptr)) {
+                k_stencil_dots_v4<1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r0, Au, a, rc);
+                PPS_COUNT_LAUNCH();
+                return;
+            }
+        }
+        fast_stencil_dot<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), u, r0, Au, a, rc, s);
+        return;
+    }
     k_stencil_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r0, Au, a, rc);
     PPS_COUNT_LAUNCH();
 }
@@ -1911,12 +2083,37 @@ template <typename T>
 void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T* Au, const Coef& a, RedCtx rc,
                        cudaStream_t s)
 {
+    if (sh.cx != 1) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (sh.cx == 4 && v4_ok<T>(g, u, r, Au, nullptr)) {
+                k_stencil_dots_v4<2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r, Au, a, rc);
+                PPS_COUNT_LAUNCH();
+                return;
+            }
+        }
+        fast_stencil_dot2<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), u, r, Au, a, rc, s);
+        return;
+    }
     k_stencil_dot2<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r, Au, a, rc);
     PPS_COUNT_LAUNCH();
+}
+// Dirichlet grids with 16-byte aligned fields: the flat vector forms of the updates.
+static bool flat_ok(const Geo& g, std::initializer_list<const void*> ptrs)
+{
+    for (int f = 0; f < 6; f++)
+        if (g.bcs[f] != 0) return false;
+    for (const void* p : ptrs)
+        if (((uintptr_t)p & 15u) != 0) return false;
+    return true;
 }
 template <typename T>
 void fast_axpy_alpha(const Geo& g, const Shape& sh, T* r, const T* v, const DevState* st, cudaStream_t s)
 {
+    if (flat_ok(g, {r, v})) {
+        k_axpy_alpha_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, r, v, st);
+        PPS_COUNT_LAUNCH();
+        return;
+    }
     k_axpy_alpha<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, v, st);
     PPS_COUNT_LAUNCH();
 }
@@ -1924,12 +2121,22 @@ template <typename T>
 void fast_update_xr(const Geo& g, const Shape& sh, T* x, const T* Mp, const T* z, T* r, const T* Az, const T* r0,
                     RedCtx rc, cudaStream_t s)
 {
+    if (flat_ok(g, {x, Mp, z, r, Az, r0})) {
+        k_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, Mp, z, r, Az, r0, rc);
+        PPS_COUNT_LAUNCH();
+        return;
+    }
     k_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, Mp, z, r, Az, r0, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_update_p(const Geo& g, const Shape& sh, T* p, const T* r, const T* AMp, const DevState* st, cudaStream_t s)
 {
+    if (flat_ok(g, {p, r, AMp})) {
+        k_update_p_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, p, r, AMp, st);
+        PPS_COUNT_LAUNCH();
+        return;
+    }
     k_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, r, AMp, st);
     PPS_COUNT_LAUNCH();
 }
