@@ -1079,11 +1079,13 @@ __global__ void __launch_bounds__(256) k_level_pass(Dims d, DLevel L, int kchunk
     if (z < z1) point(1, 0.0f);   // the last plane: upper wall one fine spacing above
 }
 
-static void level_launch(const Dims& d, int& kchunk, dim3& grid)
+static void level_launch(const Dims& d, int& kchunk, dim3& grid, int waves = 4)
 {
-    // 32 x 8 columns per block, z split into chunks for about 8 blocks per SM
+    // 32 x 8 columns per block, z split into chunks for about `waves` waves of 8
+    // blocks per SM (one wave left the 256^3 level at under half the HBM rate; the
+    // first Chebyshev step, whose columns start with ten divisions, keeps one)
     const int tx = (d.W + 31) / 32, ty = (d.H + 7) / 8;
-    long long chunks = (152LL * 8 + (long long)tx * ty - 1) / ((long long)tx * ty);
+    long long chunks = (152LL * 8 * waves + (long long)tx * ty - 1) / ((long long)tx * ty);
     if (chunks < 1) chunks = 1;
     if (chunks > d.D) chunks = d.D;
     kchunk = (int)((d.D + chunks - 1) / chunks);
@@ -1104,7 +1106,7 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
 {
     int kchunk;
     dim3 grid;
-    level_launch(d, kchunk, grid);
+    level_launch(d, kchunk, grid, first ? 1 : 4);
     const dim3 blk(32, 8);
     if (first) {
         if (acc) k_level_pass<true, true, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
