@@ -287,9 +287,10 @@ def run_gpu(args, dist: Dist):
         if kk > 0:
             e2e.append(el)
             d = head.stats()
-            e2e_parts.append((d["seconds_h2d"], d["seconds_solve"], d["seconds_d2h"]))
+            e2e_parts.append((d["seconds_h2d"], d["seconds_solve"], d["seconds_d2h"], d["seconds_total"], el))
     t_e2e = dist.max(sum(e2e) / len(e2e))
-    e2e_split = {k: statistics.median(p[i] for p in e2e_parts) for i, k in enumerate(("h2d_s", "solve_s", "d2h_s"))}
+    e2e_split = {k: statistics.median(p[i] for p in e2e_parts)
+                 for i, k in enumerate(("h2d_s", "solve_s", "d2h_s", "call_s", "python_s"))}
 
     # ---- roofline of the FP32 Chebyshev sweep, event-timed on the solver's stream.
     # The headline solve replays CUDA graphs, which carry no events, so the sweeps are
