@@ -1764,25 +1764,19 @@ struct MI {
 };
 __device__ __forceinline__ MI msplit(double v)
 {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    const int ex = (int)((u >> 52) & 0x7ffu);
-    unsigned long long mag = u & 0xFFFFFFFFFFFFFull;
+    const long long u = __double_as_longlong(v);
+    const int ex = (int)(u >> 52) & 0x7ff;
+    const long long mag = (u & 0xFFFFFFFFFFFFFll) | ((long long)(ex != 0) << 52);
+    const long long sgn = u >> 63;   // 0 or -1
     MI r;
-    if (ex != 0) {
-        mag |= 1ull << 52;
-        r.e = ex;
-    } else {
-        r.e = 1;
-    }
-    r.m = (u >> 63) ? -(long long)mag : (long long)mag;
+    r.m = (mag ^ sgn) - sgn;
+    r.e = ex + (ex == 0);
     return r;
 }
-// m * 2^(e - E) for E >= e, truncated toward zero
+// m * 2^(e - E) for E >= e, rounded toward minus infinity (one arithmetic shift)
 __device__ __forceinline__ long long malign(const MI& a, int E)
 {
-    const int sh = min(E - a.e, 63);
-    const long long mag = (a.m < 0 ? -a.m : a.m) >> sh;
-    return a.m < 0 ? -mag : mag;
+    return a.m >> min(E - a.e, 63);
 }
 
 // Counts the entries of a whole field (guard layers included) whose bit pattern is
@@ -1824,9 +1818,9 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
         // Equal spacings: A x = cx (sum of the six neighbours - 6 x).  The seven values
         // are aligned to the largest one's exponent as 53-bit integers, so the second
         // difference is exact in int64 on the integer pipe; one conversion and one FMA
-        // remain on the FP64 pipe (instead of eight operations).  Truncating the
-        // smaller values' low bits costs at most 2^-53 of the largest, the rounding
-        // the FP64 stencil has anyway.
+        // remain on the FP64 pipe (instead of eight operations).  Dropping the smaller
+        // values' low bits (an arithmetic shift) costs at most 2^-53 of the largest per
+        // value, the rounding the FP64 stencil has anyway.
         const long long sj = g.sj, sk = g.sk;
         long long c = q.c;
         MI um = msplit(x[c - sk]), uc = msplit(x[c]);
@@ -1840,9 +1834,18 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
             } else {
                 const long long D = malign(w, E) + malign(e, E) + malign(sv, E) + malign(nv, E) + malign(um, E) +
                                     malign(up, E) - 6 * malign(uc, E);
-                // A x = cx * D * 2^(E - 1075); below 2^-1022 it is far under b's rounding
-                const double scale = E >= 53 ? __longlong_as_double((long long)(E - 52) << 52) : 0.0;
-                rv = fmx(-(cf.cx * scale), __ll2double_rn(D), b[c]);
+                // A x = cx * D * 2^(E - 1075); below 2^-1022 it is far under b's rounding.
+                // The power of two goes into the exponent bits of D on the integer pipe
+                // (exact: D converts to a normal double and the sum stays normal).
+                const double Dd = __ll2double_rn(D);
+                if (E >= 53 && E <= 2000) {
+                    const double Ds = D != 0 ? __longlong_as_double(__double_as_longlong(Dd) + ((long long)(E - 1075) << 52))
+                                             : 0.0;
+                    rv = fmx(-cf.cx, Ds, b[c]);
+                } else {
+                    const double scale = E >= 53 ? __longlong_as_double((long long)(E - 52) << 52) : 0.0;
+                    rv = fmx(-(cf.cx * scale), Dd, b[c]);
+                }
             }
             const TR rs = (TR)rv;
             r[c] = rs;
