@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <functional>
 #include <chrono>
 #include <cmath>
@@ -1498,6 +1499,7 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
     for (int ty : kTys)
         for (int cx : kCxs)
             for (int w : kWaves) {
+                if (cx == 4 && !std::is_same<T, float>::value) continue;   // FP64 runs one-column tiles
                 const Shape sh = tuned_shape(g, ty, cx, w);
                 const double us = time_launches<T>(s, reps, [&]() {
                     fast_cheb_sweep<T>(g, sh, F.Y, F.r, F.Z, F.W, c, &s->d_st->done, s->stream);

@@ -294,7 +294,9 @@ def test_autotune_keeps_results(gpu, oracle, form, tmp_path):
     s = make_solver(case, form)
     cache = str(tmp_path / "tuning.json")
     t = s.autotune(cache=cache)
-    assert t["cheb_ty"] in (2, 4, 8) and t["cheb_cx"] in (1, 2) and t["cheb_us"] > 0
+    # cx 4: the x-vectorised FP32 tiles (FP64 fields have none to pick)
+    assert t["cheb_ty"] in (2, 4, 8) and t["cheb_cx"] in ((1, 2) if form == "fp64" else (1, 2, 4))
+    assert t["cheb_us"] > 0
     assert s.tuning()["cheb_waves"] == t["cheb_waves"]
     for f, a in enumerate(faces):
         if a is not None:
