@@ -341,7 +341,7 @@ def run_gpu(args, dist: Dist):
             "tiles": tuned,
         },
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8,
-                "median_split": e2e_split},
+                "median_split": e2e_split, "samples_s": [round(v, 5) for v in e2e]},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "forms": {
             "mixed+learned (FCG)": summary(stats[-1], t_step),
