@@ -204,11 +204,14 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X);
 
 /* Tile shapes of the z-marching kernels (fast forms).  A tile is (32*cx) x ty
  * columns; each thread walks along z; `waves` sets the grid to about
- * waves x 152 SMs x resident blocks.  cheb_* apply to the Chebyshev kernels,
- * other_* to the Krylov update/stencil kernels.  cheb_cx 4 selects the
- * x-vectorised FP32 Chebyshev kernels (one float4 per thread, the default where
+ * waves x 152 SMs x resident blocks.  cheb_* apply to the Chebyshev kernels and to
+ * the Krylov stencil kernels that run on the same tiles (flexible CG's direction
+ * update, BiCGSTAB's and CG's stencil + dots, the learned cycle's last
+ * prolongation), other_* to the remaining Krylov update/stencil kernels.  cheb_cx 4
+ * selects the x-vectorised FP32 kernels (one float4 per thread, the default where
  * npglobal[0] + 2 is a multiple of 4; FP64 fields and other rows run cx 1 tiles of
- * the same size).  *_us: measured per launch. */
+ * the same size).  cheb_us: the sweep's time per launch; other_us: the
+ * stencil+dot kernel's. */
 typedef struct {
     int cheb_ty, cheb_cx, cheb_waves;
     int other_ty, other_waves;
@@ -219,9 +222,11 @@ typedef struct {
 } pps_tuning;
 
 /* Autotuner (no reference counterpart; the reference fixes its launch shapes,
- * ALP/include/alpakaHelper.hpp:122-140): times every candidate shape of the sweep
- * and of the stencil+dot kernel on this solver's grid and buffers, applies the
- * fastest and returns it.  Candidates: ty 2/4/8, cx 1/2, waves 1/2/4/8. */
+ * ALP/include/alpakaHelper.hpp:122-140): times every candidate shape on this
+ * solver's grid and buffers, applies the fastest and returns it.  The Chebyshev
+ * tiles are scored by the sweep's time plus that of the method's Krylov stencil
+ * kernel on the same tiles; the other tiles by the stencil+dot kernel.
+ * Candidates: ty 2/4/8, cx 1/2/4 (4: FP32 only), waves 1/2/4/8. */
 pps_status pps_autotune(pps_solver* s, pps_tuning* out);
 pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out);
 /* Applies a stored tuning (e.g. from a table persisted by the caller). */

@@ -234,9 +234,10 @@ void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx r
 // ||b_adj||^2 over the unknowns, b_adj formed on the fly (FP64).
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
                     cudaStream_t s, bool x_zero = false);
-// x += scale * e at the unknowns (FP64 += FP32).
+// x += e at the unknowns (FP64 += FP32).  e_zero_off: e is +-0 off the unknowns,
+// which lets Dirichlet grids run the flat vector form.
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState* st,
-                         cudaStream_t s);
+                         cudaStream_t s, bool e_zero_off = false);
 // Start of an inner BiCGSTAB solve from X = 0: r = r0 = p = B at the unknowns, sum B^2.
 template <typename T>
 void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* p, RedCtx rc, cudaStream_t s);
@@ -244,6 +245,9 @@ void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* 
 void cast_field_f32(const double* in, float* out, long long n, cudaStream_t s);
 template <typename T>
 void fill_field(T* p, long long n, T v, cudaStream_t s);
+// Zero the boundary nodes and guard layers of a padded field.
+template <typename T>
+void zero_off_unknowns(const Geo& g, T* p, cudaStream_t s);
 // Scalar state helpers.
 void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
                 int rho0_from_r, double hist_scale, int hist_cap, cudaStream_t s);

@@ -12,6 +12,7 @@
 //              block to finish sums the partials in block order and advances the
 //              Krylov scalars on the device (no host round trip).
 #include "pps_internal.h"
+#include "pps_reduce.cuh"
 
 #include <algorithm>
 #include <initializer_list>
@@ -22,7 +23,8 @@
 
 namespace pps {
 
-static int g_launches = 0;
+// launches issued by this thread (each solve runs on its calling thread)
+static thread_local int g_launches = 0;
 int launches_counter_reset() { int v = g_launches; g_launches = 0; return v; }
 int launches_counter() { return g_launches; }
 void launches_counter_add(int d) { g_launches += d; }
@@ -465,10 +467,6 @@ Shape make_shape(const Geo& g, int ty, int target_blocks, int cx)
     return sh;
 }
 
-// Fused multiply-add for either storage type.
-__device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
-
 struct Col {
     int i, j, k0, k1;
     long long c;
@@ -492,248 +490,6 @@ __device__ __forceinline__ Col column(const Geo& g, const Shape& sh)
 static inline dim3 grid_of(const Shape& sh) { return dim3((unsigned)(sh.ntx * sh.nty), (unsigned)sh.nchunks, 1); }
 static inline dim3 block_of(const Shape& sh) { return dim3(32, (unsigned)sh.ty, 1); }
 
-// Accumulator of exact products: FP64 FMA for double data; for float data a
-// double-float pair (Dekker/Knuth error-free product and sum in FP32), so the
-// inner products of the mixed form are FP64-accurate without FP64 arithmetic
-// per point (GB300 runs FP64 at 1/64 of the FP32 rate).
-template <typename T>
-struct Acc;
-template <>
-struct Acc<double> {
-    double s = 0.0;
-    __device__ __forceinline__ void add(double a, double b) { s = fmx(a, b, s); }
-    __device__ __forceinline__ double value() const { return s; }
-};
-template <>
-struct Acc<float> {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add(float a, float b)
-    {
-        const float p = __fmul_rn(a, b);
-        const float e = __fmaf_rn(a, b, -p);
-        const float s = __fadd_rn(hi, p);
-        const float bb = __fsub_rn(s, hi);
-        const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-        hi = s;
-        lo = __fadd_rn(lo, __fadd_rn(t, e));
-    }
-    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ void finalize(const RedCtx& rc, const double* tot)
-{
-    DevState* st = rc.st;
-    for (int q = 0; q < 4; q++) st->sums[q] = tot[q];
-    switch (rc.kind) {
-    case FIN_NORMB:
-        st->normb = sqrt(tot[0]);
-        break;
-    case FIN_RES0: {
-        const double e0 = sqrt(tot[0]);
-        st->err0 = e0;
-        st->err = e0;
-        if (rc.hist && st->hist_cap > 0) rc.hist[0] = e0 * st->hist_scale;
-        st->rho0 = st->rho0_from_r ? tot[0] : st->normb * st->normb;
-        st->iter = 0;
-        if (!(e0 == e0) || isinf(e0)) {
-            st->status = 3;
-            st->done = 1;
-        } else if (e0 < st->tol_abs) {
-            st->status = 0;
-            st->done = 1;
-        } else {
-            st->done = 0;
-            st->status = 0;
-            // inner solve of a refinement step: reduce by tol_rel, or less if enough
-            if (st->tol_relative) st->tol_abs = fmax(st->tol_rel, 0.3 * st->tol_abs / e0) * e0;
-        }
-        break;
-    }
-    case FIN_ALPHA: {
-        const double a = st->rho0 / tot[0];
-        st->alpha = a;
-        if (!isfinite(a)) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_OMEGA: {
-        const double w = tot[0] / tot[1];
-        st->omega = w;
-        if (!isfinite(w) || w == 0.0) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_CONV: {
-        const double err = sqrt(tot[1]);
-        const double rho1 = tot[0];
-        st->err = err;
-        st->beta = rho1 / st->rho0 * st->alpha / st->omega;
-        st->rho0 = rho1;
-        st->iter += 1;
-        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
-        if (!isfinite(err)) {
-            st->status = 3;
-            st->done = 1;
-        } else if (err < st->tol_abs) {
-            st->status = 0;
-            st->done = 1;
-        } else if (st->iter >= st->maxit) {
-            st->status = 1;
-            st->done = 1;
-        } else if (!isfinite(st->beta)) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_CG_ALPHA: {
-        st->rho0 = tot[0];                    // r.z
-        st->alpha = tot[0] / tot[1];          // r.z / p.Ap
-        if (!isfinite(st->alpha)) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_CG_CONV: {
-        const double err = sqrt(tot[1]);
-        st->err = err;
-        st->beta = tot[0] / st->rho0;         // r_new.z_new / r.z
-        st->iter += 1;
-        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
-        if (!isfinite(err)) {
-            st->status = 3;
-            st->done = 1;
-        } else if (err < st->tol_abs) {
-            st->status = 0;
-            st->done = 1;
-        } else if (st->iter >= st->maxit) {
-            st->status = 1;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_FCG_ALPHA: {
-        st->alpha = st->rho0 / tot[0];        // z.r / p.Ap
-        if (!isfinite(st->alpha)) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_FCG_SETUP: {
-        st->rho0 = tot[0];                    // z.r
-        st->beta = 0.0;
-        break;
-    }
-    case FIN_FCG_RES: {
-        // flexible CG after x, r: the recursive residual norm and the stop test
-        const double err = sqrt(tot[0]);
-        st->err = err;
-        st->iter += 1;
-        if (rc.hist && st->iter < st->hist_cap) rc.hist[st->iter] = err * st->hist_scale;
-        if (!isfinite(err)) {
-            st->status = 3;
-            st->done = 1;
-        } else if (err < st->tol_abs) {
-            st->status = 0;
-            st->done = 1;
-        } else if (st->iter >= st->maxit) {
-            st->status = 1;
-            st->done = 1;
-        }
-        break;
-    }
-    case FIN_FCG_CONV: {
-        // flexible CG, Polak-Ribiere: beta = z_new.(r_new - r_old) / (z_old.r_old)
-        // with r_new - r_old = -alpha Ap
-        st->beta = -st->alpha * tot[1] / st->rho0;
-        st->rho0 = tot[0];
-        if (!isfinite(st->beta)) {
-            st->status = 2;
-            st->done = 1;
-        }
-        break;
-    }
-    default:
-        break;
-    }
-}
-
-// Block reduction of NS partial sums, then the last block reduces all block
-// partials in block order and runs the finalizer.  Every thread of every block
-// must call this (inactive threads pass zeros).
-template <int NS>
-__device__ __forceinline__ void reduce_finalize(double (&v)[NS], const RedCtx& rc)
-{
-    __shared__ double sm[32][NS];
-    __shared__ int is_last;
-    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-    const int nthr = blockDim.x * blockDim.y;
-    const int lane = tid & 31, warp = tid >> 5, nwarp = (nthr + 31) >> 5;
-    const unsigned nblocks = gridDim.x * gridDim.y;
-    const unsigned bid = blockIdx.x + gridDim.x * blockIdx.y;
-#pragma unroll
-    for (int q = 0; q < NS; q++) {
-        const double w = warp_sum(v[q]);
-        if (lane == 0) sm[warp][q] = w;
-    }
-    __syncthreads();
-    if (tid == 0) {
-#pragma unroll
-        for (int q = 0; q < NS; q++) {
-            double s = 0.0;
-            for (int w = 0; w < nwarp; w++) s += sm[w][q];
-            rc.partials[(size_t)bid * 4 + q] = s;
-        }
-        __threadfence();
-        const unsigned ticket = atomicAdd(rc.counter, 1u);
-        is_last = (ticket == nblocks - 1);
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    double acc[NS];
-#pragma unroll
-    for (int q = 0; q < NS; q++) acc[q] = 0.0;
-    for (unsigned b = tid; b < nblocks; b += nthr) {
-#pragma unroll
-        for (int q = 0; q < NS; q++) acc[q] += __ldcg(&rc.partials[(size_t)b * 4 + q]);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NS; q++) {
-        const double w = warp_sum(acc[q]);
-        if (lane == 0) sm[warp][q] = w;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        double tot[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int q = 0; q < NS; q++) {
-            double s = 0.0;
-            for (int w = 0; w < nwarp; w++) s += sm[w][q];
-            tot[q] = s;
-        }
-        finalize(rc, tot);
-        __threadfence();
-        *rc.counter = 0u;
-    }
-}
-
-#define EARLY_EXIT(done)                                      \
-    if (done != nullptr && *(volatile const int*)(done) != 0) return;
 
 // Chebyshev coefficients cast to the storage type on the host (no FP64 work
 // in the FP32 kernels; GB300 issues FP64 at 1/64 of the FP32 rate).
@@ -1786,8 +1542,17 @@ __global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double
     double cnt = 0.0;
     const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    for (long long i = t0; i < nv; i += stride) {
-        const longlong2 v = reinterpret_cast<const longlong2*>(x)[i];
+    const longlong2* xv = reinterpret_cast<const longlong2*>(x);
+    long long i = t0;
+    for (; i + 3 * stride < nv; i += 4 * stride) {   // four loads in flight per thread
+        longlong2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = xv[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; u++) cnt += ((unsigned long long)v[u].x << 1 != 0ull) + ((unsigned long long)v[u].y << 1 != 0ull);
+    }
+    for (; i < nv; i += stride) {
+        const longlong2 v = xv[i];
         cnt += ((unsigned long long)v.x << 1 != 0ull) + ((unsigned long long)v.y << 1 != 0ull);
     }
     for (long long i = nv * 2 + t0; i < n; i += stride) cnt += ((unsigned long long)__double_as_longlong(x[i]) << 1) != 0ull;
@@ -1806,14 +1571,24 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
     const Col q = column(g, sh);
     Acc<TR> acc;
     if (XZERO && q.active) {   // x = 0 on every point the stencil reads: r = b
+        const long long sk = g.sk;
         long long c = q.c;
-        for (int k = q.k0; k < q.k1; k++, c += g.sk) {
-            const TR rs = (TR)b[c];
-            r[c] = rs;
-            if (r0) r0[c] = rs;
-            if (p) p[c] = rs;
+        int k = q.k0;
+        auto put = [&](long long cc, double bv) {
+            const TR rs = (TR)bv;
+            r[cc] = rs;
+            if (r0) r0[cc] = rs;
+            if (p) p[cc] = rs;
             acc.add(rs, rs);
+        };
+        for (; k + 4 <= q.k1; k += 4, c += 4 * sk) {   // four planes' loads in flight, summed in plane order
+            double bv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) bv[u] = b[c + u * sk];
+#pragma unroll
+            for (int u = 0; u < 4; u++) put(c + u * sk, bv[u]);
         }
+        for (; k < q.k1; k++, c += sk) put(c, b[c]);
     } else if (ISO && q.active) {
         // Equal spacings: A x = cx (sum of the six neighbours - 6 x).  The seven values
         // are aligned to the largest one's exponent as 53-bit integers, so the second
@@ -1894,10 +1669,22 @@ __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double
 {
     const Col q = column(g, sh);
     double s = 0.0;
-    if (q.active) {
+    if (XZERO && q.active) {   // four planes' loads in flight, summed in plane order
+        const long long sk = g.sk;
+        long long c = q.c;
+        int k = q.k0;
+        for (; k + 4 <= q.k1; k += 4, c += 4 * sk) {
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = b[c + u * sk];
+#pragma unroll
+            for (int u = 0; u < 4; u++) s = fmx(v[u], v[u], s);
+        }
+        for (; k < q.k1; k++, c += sk) s = fmx(b[c], b[c], s);
+    } else if (q.active) {
         long long c = q.c;
         for (int k = q.k0; k < q.k1; k++) {
-            const double v = XZERO ? b[c] : badj_exact(g, b, x, f, c, q.i, q.j, k);
+            const double v = badj_exact(g, b, x, f, c, q.i, q.j, k);
             s = fmx(v, v, s);
             c += g.sk;
         }
@@ -1911,11 +1698,53 @@ __global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double*
 {
     const Col q = column(g, sh);
     if (!q.active) return;
+    const long long sk = g.sk;
     long long c = q.c;
-    for (int k = q.k0; k < q.k1; k++) {
-        x[c] += (double)e[c];
-        c += g.sk;
+    int k = q.k0;
+    for (; k + 4 <= q.k1; k += 4, c += 4 * sk) {   // four planes' loads in flight
+        double xv[4];
+        float ev[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            xv[u] = x[c + u * sk];
+            ev[u] = e[c + u * sk];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) x[c + u * sk] = xv[u] + (double)ev[u];
     }
+    for (; k < q.k1; k++, c += sk) x[c] += (double)e[c];
+}
+
+// The same over the whole padded array in 16-byte vectors, for corrections that are
+// +-0 off the unknowns (Dirichlet grids): x changes only where e is non-zero, so
+// the boundary nodes and guards keep their bits.
+__global__ void __launch_bounds__(256) k_add_correction_flat(long long n, double* __restrict__ x,
+                                                             const float* __restrict__ e)
+{
+    const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double2* xv = reinterpret_cast<double2*>(x);
+    const float2* ev = reinterpret_cast<const float2*>(e);
+    long long i = t0;
+    for (; i + stride < nv; i += 2 * stride) {   // two vectors of each in flight per thread
+        double2 a = xv[i], b = xv[i + stride];
+        const float2 ea = ev[i], eb = ev[i + stride];
+        if (ea.x != 0.0f) a.x += (double)ea.x;
+        if (ea.y != 0.0f) a.y += (double)ea.y;
+        if (eb.x != 0.0f) b.x += (double)eb.x;
+        if (eb.y != 0.0f) b.y += (double)eb.y;
+        xv[i] = a;
+        xv[i + stride] = b;
+    }
+    for (; i < nv; i += stride) {
+        double2 a = xv[i];
+        const float2 ea = ev[i];
+        if (ea.x != 0.0f) a.x += (double)ea.x;
+        if (ea.y != 0.0f) a.y += (double)ea.y;
+        xv[i] = a;
+    }
+    for (long long q = nv * 2 + t0; q < n; q += stride)
+        if (e[q] != 0.0f) x[q] += (double)e[q];
 }
 
 // Start of an inner BiCGSTAB solve from X = 0 (BiCGSTAB.hpp:94-126 with isMainLoop
@@ -1955,6 +1784,20 @@ __global__ void k_fill(T* p, long long n, T v)
 {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         p[c] = v;
+}
+
+// Zero every entry of a padded field that is not an unknown (boundary nodes and
+// guard layers), the state the solver's work fields keep between solves.
+template <typename T>
+__global__ void k_zero_off_unknowns(Geo g, T* p)
+{
+    const long long nj = g.sk / g.sj;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.ntot;
+         c += (long long)gridDim.x * blockDim.x) {
+        const long long i = c % g.sj, j = (c / g.sj) % nj, k = c / g.sk;
+        const bool unknown = i >= g.lo[0] && i < g.hi[0] && j >= g.lo[1] && j < g.hi[1] && k >= g.lo[2] && k < g.hi[2];
+        if (!unknown) p[c] = (T)0;
+    }
 }
 
 __global__ void k_state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
@@ -2237,9 +2080,14 @@ void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double
     else k_norm_badj<false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
     PPS_COUNT_LAUNCH();
 }
-void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s)
+void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s,
+                         bool e_zero_off)
 {
-    k_add_correction<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, e);
+    if (e_zero_off && flat_ok(g, {x}) && ((uintptr_t)e & 7u) == 0) {
+        k_add_correction_flat<<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, e);
+    } else {
+        k_add_correction<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, e);
+    }
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -2258,6 +2106,12 @@ template <typename T>
 void fill_field(T* p, long long n, T v, cudaStream_t s)
 {
     k_fill<T><<<par_blocks(n), 256, 0, s>>>(p, n, v);
+    PPS_COUNT_LAUNCH();
+}
+template <typename T>
+void zero_off_unknowns(const Geo& g, T* p, cudaStream_t s)
+{
+    k_zero_off_unknowns<T><<<par_blocks(g.ntot), 256, 0, s>>>(g, p);
     PPS_COUNT_LAUNCH();
 }
 void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
@@ -2303,6 +2157,7 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
     template void fast_residual<T>(const Geo&, const Shape&, const double*, const double*, T*, T*, T*,           \
                                    const Coef&, RedCtx, cudaStream_t, bool);                                     \
     template void fill_field<T>(T*, long long, T, cudaStream_t);                                                  \
+    template void zero_off_unknowns<T>(const Geo&, T*, cudaStream_t);                                             \
     template void fast_bicg_start<T>(const Geo&, const Shape&, const T*, T*, T*, T*, RedCtx, cudaStream_t);
 
 PPS_INST(double)

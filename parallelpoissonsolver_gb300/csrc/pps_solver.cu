@@ -864,9 +864,11 @@ void dense_cheb(pps_solver* s, int l, const float* B, float* X, bool acc)
 //   level l = k-1..1:        z_l += P z_{l+1};  z_l += S_l (r_l - A_l z_l)
 //   level 0:                 X += P z_1;  [X += S_0 (B - A X)]
 // S_l: Chebyshev smoothers on the high-frequency end of each level's spectrum;
-// dn[l] holds r_l, dn_e[l] holds z_l.
+// dn[l] holds r_l, dn_e[l] holds z_l.  With `dots` (flexible CG: X = z, B = r) the
+// last prolongation also sums z.r and z.Ap when it can; returns whether it did.
 template <typename T>
-void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+bool learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const T* Ap = nullptr,
+                    const RedCtx* dots = nullptr)
 {
     const Geo& g = s->geo;
     cudaStream_t st = s->stream;
@@ -877,8 +879,17 @@ void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
     for (int l = 1; l < k; l++) {
         if (s->cyc_coarse > 0) {
             dense_cheb(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], false);
-            dense_residual(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], s->dt[(size_t)l]);
-            unet::restrict2(dense_dims(s, l + 1), s->dt[(size_t)l], s->dn[(size_t)l + 1], st);
+            const unet::Dims dl = dense_dims(s, l);
+            if ((long long)dl.W * dl.H * dl.D <= (1LL << 21)) {
+                // up to 128^3 the fused residual + restriction wins (the levels are
+                // L2-resident and launch-bound); above, its 3 x 3 window's recomputed
+                // points cost more than the stored residual's extra pass
+                unet::level_residual_restrict(dense_dims(s, l + 1), level_op(s, l), s->dn_e[(size_t)l],
+                                              s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
+            } else {
+                dense_residual(s, l, s->dn[(size_t)l], s->dn_e[(size_t)l], s->dt[(size_t)l]);
+                unet::restrict2(dense_dims(s, l + 1), s->dt[(size_t)l], s->dn[(size_t)l + 1], st);
+            }
         } else {
             unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
         }
@@ -895,13 +906,16 @@ void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
             unet::prolong2(dense_dims(s, l + 1), s->dn_e[(size_t)l + 1], s->dn_e[(size_t)l], st);
         }
     }
-    unet::prolong_add_field<T>(g, s->shape_cheb, dense_dims(s, 1), s->dn_e[1], X, st);
-    if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
+    const bool post = (s->net_flags & PPS_LEARNED_POST_SMOOTH) != 0;
+    const bool summed = unet::prolong_add_field<T>(g, s->shape_cheb, dense_dims(s, 1), s->dn_e[1], X, st, B, Ap,
+                                                   post ? nullptr : dots);
+    if (post) {
         unet::field_residual<T>(g, s->shape, B, X, F.r0, st);
         fast_cheb<T>(s, F, F.r0, F.Mp, L, pf);
         unet::field_axpy<T>(g, s->shape, X, F.Mp, st);
     }
     s->learned_apps++;
+    return summed;
 }
 
 // Preconditioner of the flexible-CG loop: the Chebyshev polynomial (or identity),
@@ -909,15 +923,16 @@ void learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
 // the network: the two-grid cycle around the solver's own preconditioner
 //   z = Cheb(r);  z += gain P^k N(R^k (r - A z));  [z += Cheb(r - A z)]
 // or the multigrid V-cycle of learned_vcycle.
+// With `dots` (flexible CG) the V-cycle may finish the z.r, z.Ap reduction itself:
+// the return value says whether it did.
 template <typename T>
-void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
+bool precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const T* Ap = nullptr,
+                 const RedCtx* dots = nullptr)
 {
-    if (s->net && s->net_active && s->cyc_fine > 0 && s->net_coarsen >= 1) {
-        learned_vcycle<T>(s, F, B, X, L);
-        return;
-    }
+    if (s->net && s->net_active && s->cyc_fine > 0 && s->net_coarsen >= 1)
+        return learned_vcycle<T>(s, F, B, X, L, Ap, dots);
     fast_precond<T>(s, F, B, X, L);
-    if (!(s->net && s->net_active)) return;
+    if (!(s->net && s->net_active)) return false;
     learned_coarse_correction<T>(s, B, X, X);
     if (s->net_flags & PPS_LEARNED_POST_SMOOTH) {
         // post-smoothing through the fields flexible CG leaves free (r0, Mp)
@@ -926,6 +941,7 @@ void precond_any(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L)
         fast_precond<T>(s, F, F.r0, F.Mp, L);
         unet::field_axpy<T>(g, s->shape, X, F.Mp, s->stream);
     }
+    return false;
 }
 
 // One application of the preconditioner the flexible-CG iterations use (with the
@@ -1071,9 +1087,14 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
     if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
     else fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
-    precond_any<T>(s, F, F.r, F.z, L);
-    if (flat) fast_fcg_dot_flat<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
-    else fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, red(s, FIN_FCG_CONV), st);
+    const RedCtx conv = red(s, FIN_FCG_CONV);
+    if (precond_any<T>(s, F, F.r, F.z, L, F.AMp, &conv)) {   // the V-cycle summed z.r, z.Ap
+        L.bytes += bytes_of<T>(N, 4 + 6 + 2);
+        L.launches += 2;
+        return;
+    }
+    if (flat) fast_fcg_dot_flat<T>(g, sh, F.r, F.z, F.AMp, conv, st);
+    else fast_fcg_dot<T>(g, sh, F.r, F.z, F.AMp, conv, st);
     L.bytes += bytes_of<T>(N, 4 + 6 + 3);
     L.launches += 3;
 }
@@ -1353,7 +1374,9 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         pull_history(s, it, true);
         S.precond_applications += it * (s->cfg.krylov == PPS_KRYLOV_BICGSTAB ? 2 : 1);
         S.err_iter = s->h_st->err / normb;
-        fast_add_correction(g, s->shape, x, F.e, s->d_st, st);
+        // e started at zero and the updates add multiples of fields that are zero off
+        // the unknowns on Dirichlet grids
+        fast_add_correction(g, s->shape, x, F.e, s->d_st, st, true);
         L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 1);
         if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
         S.refinements++;
@@ -1495,6 +1518,17 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
     const int reps = N > (1LL << 24) ? 5 : 20;
     state_init(s->d_st, s->d_hist, 1, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
     const Coef c = cheb_sweep_coef(op_coef(g), cheb_of(s), 0.5, 0.5, 1.0);
+    const Coef a = op_coef(g);
+    // The Chebyshev tiles also carry the Krylov stencil kernel of the method (flexible
+    // CG's direction update + stencil, BiCGSTAB's and CG's stencil + dots), whose
+    // reads of two fields with their y halo make it the more shape-sensitive one: a
+    // candidate is scored by the sweep's time plus that kernel's.
+    const bool fcg = s->cfg.krylov == PPS_KRYLOV_FCG;
+    if (fcg) {   // a non-zero beta, so the direction kernel reads p as well as z
+        const double beta = 0.5;
+        CK(cudaMemcpyAsync(&s->d_st->beta, &beta, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     double best_us = 1e30;
     for (int ty : kTys)
         for (int cx : kCxs)
@@ -1504,15 +1538,18 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
                 const double us = time_launches<T>(s, reps, [&]() {
                     fast_cheb_sweep<T>(g, sh, F.Y, F.r, F.Z, F.W, c, &s->d_st->done, s->stream);
                 });
-                if (us < best_us) {
-                    best_us = us;
+                const double ks = time_launches<T>(s, reps, [&]() {
+                    if (fcg) fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_STORE), s->stream);
+                    else fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red(s, FIN_STORE), s->stream);
+                });
+                if (us + ks < best_us) {
+                    best_us = us + ks;
                     best->cheb_ty = ty;
                     best->cheb_cx = cx;
                     best->cheb_waves = w;
                     best->cheb_us = us;
                 }
             }
-    const Coef a = op_coef(g);
     best_us = 1e30;
     for (int ty : kTys)
         for (int w : kWaves) {
@@ -1656,9 +1693,6 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
 }
 
 }  // namespace
-
-// Extra graph bookkeeping fields live outside the struct definition above.
-// (declared here to keep the struct readable)
 
 extern "C" {
 
@@ -2067,11 +2101,16 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         }
         state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
         Launcher L{s, false};
+        // B and X pass through the solver's own r and z, whole (boundary nodes and
+        // guards included, as the caller gave them); afterwards those entries are
+        // zeroed again, the state the solves expect of their work fields.
         if (s->cfg.form == PPS_FORM_FP64) {
             CK(cudaMemcpyAsync(s->f64.r, B, fb, cudaMemcpyHostToDevice, s->stream));
             CK(cudaMemcpyAsync(s->f64.z, X, fb, cudaMemcpyHostToDevice, s->stream));
             precond_once<double>(s, s->f64, s->f64.r, s->f64.z, L);
             CK(cudaMemcpyAsync(X, s->f64.z, fb, cudaMemcpyDeviceToHost, s->stream));
+            zero_off_unknowns<double>(g, s->f64.r, s->stream);
+            zero_off_unknowns<double>(g, s->f64.z, s->stream);
             CK(cudaStreamSynchronize(s->stream));
             return PPS_OK;
         }
@@ -2084,6 +2123,8 @@ pps_status pps_apply_preconditioner(pps_solver* s, const double* B, double* X)
         CK(cudaMemcpyAsync(s->f32.z, hx.data(), sizeof(float) * (size_t)g.ntot, cudaMemcpyHostToDevice, s->stream));
         precond_once<float>(s, s->f32, s->f32.r, s->f32.z, L);
         CK(cudaMemcpyAsync(hx.data(), s->f32.z, sizeof(float) * (size_t)g.ntot, cudaMemcpyDeviceToHost, s->stream));
+        zero_off_unknowns<float>(g, s->f32.r, s->stream);
+        zero_off_unknowns<float>(g, s->f32.z, s->stream);
         CK(cudaStreamSynchronize(s->stream));
         for (long long q = 0; q < g.ntot; q++) X[q] = (double)hx[(size_t)q];
         return PPS_OK;

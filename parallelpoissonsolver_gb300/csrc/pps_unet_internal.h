@@ -57,8 +57,13 @@ template <typename T>
 void field_axpy(const Geo& g, const Shape& sh, T* x, const T* y, cudaStream_t s);
 template <typename T>
 void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& dc, float* coarse, cudaStream_t s);
+// f += P coarse at the unknowns.  With `dots` (flexible CG's z = M r finished by this
+// prolongation) the FP32 float4 kernel also runs the z.r, z.Ap reduction `dots`
+// describes over the unknowns and the call returns true; otherwise (FP64, unaligned
+// rows, no `dots`) it returns false and the caller sums them.
 template <typename T>
-void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s);
+bool prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s,
+                       const T* r = nullptr, const T* Ap = nullptr, const RedCtx* dots = nullptr);
 // 2x full-weighting restriction and trilinear prolongation of dense unknown arrays
 // (prolong2_add: fine += P coarse).
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s);
@@ -84,6 +89,9 @@ struct LCoef {
 };
 // W = B - A Y on the level
 void level_residual(const Dims& d, const DLevel& L, const float* Y, const float* B, float* W, cudaStream_t s);
+// R (B - A_l Y): level l's residual restricted to level l+1 (dims dc) in one pass
+void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, const float* B, float* coarse,
+                             cudaStream_t s);
 void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, const float* Z, float* W,
                 const LCoef& c, bool first, bool acc, cudaStream_t s);
 

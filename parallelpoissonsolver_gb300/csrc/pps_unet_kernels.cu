@@ -8,6 +8,7 @@
 // GEMMs on the tensor cores: M = voxels, N = output channels, K = 27 taps x input
 // channels, 16x16x16 BF16 fragments with FP32 accumulators.
 #include "pps_unet_internal.h"
+#include "pps_reduce.cuh"
 
 #include <algorithm>
 #include <type_traits>
@@ -817,22 +818,14 @@ __global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims
     if (kk < kk1) f[c] += (T)(0.5f * (vm + v0));   // a last even plane
 }
 
-// k_prolong_add_field on x-vectorised FP32 tiles: a thread owns four consecutive x
-// points of the field (one float4, tiles aligned to x = 0 as the solver's
-// vectorised Chebyshev tiles).  The four points need at most three consecutive
-// coarse x columns, X0..X0+2: per coarse plane the thread interpolates those in y
-// (6 loads), then each point in x, and adds the two fine planes the coarse plane
-// covers with float4 read-modify-writes.  The weights are k_prolong_add_field's
-// (interpolated in y first, so the rounding differs from it).
-__global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
-                                                              float* __restrict__ f, const int* __restrict__ stop)
+// One thread's column of k_prolong_add_field_v4: fine x points i0..i0+3 (those
+// that are unknowns) of row j, planes k0..k1-1.
+template <bool DOTS>
+__device__ __forceinline__ void prolong_v4_column(const Geo& g, const Dims& dc, const float* __restrict__ coarse,
+                                                  float* __restrict__ f, const float* __restrict__ r,
+                                                  const float* __restrict__ Ap, int i0, int j, int k0, int k1,
+                                                  Acc<float>& zr, Acc<float>& zap)
 {
-    if (stop && *(volatile const int*)stop) return;
-    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
-    const int i0 = bx * 128 + threadIdx.x * 4;
-    const int j = g.lo[1] + by * sh.ty + threadIdx.y;
-    const int k0 = g.lo[2] + blockIdx.y * sh.kchunk, k1 = min(k0 + sh.kchunk, g.hi[2]);
-    if (j >= g.hi[1] || i0 >= g.hi[0] || i0 + 4 <= g.lo[0]) return;
     const bool m0 = i0 >= g.lo[0] && i0 < g.hi[0], m1 = i0 + 1 >= g.lo[0] && i0 + 1 < g.hi[0];
     const bool m2 = i0 + 2 >= g.lo[0] && i0 + 2 < g.hi[0], m3 = i0 + 3 >= g.lo[0] && i0 + 3 < g.hi[0];
     const bool all4 = m0 && m1 && m2 && m3;
@@ -877,11 +870,31 @@ __global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, D
             q.z += v.z;
             q.w += v.w;
             *reinterpret_cast<float4*>(f + c) = q;
+            if (DOTS) {
+                const float4 rv = *reinterpret_cast<const float4*>(r + c);
+                const float4 av = *reinterpret_cast<const float4*>(Ap + c);
+                zr.add(q.x, rv.x);
+                zap.add(q.x, av.x);
+                zr.add(q.y, rv.y);
+                zap.add(q.y, av.y);
+                zr.add(q.z, rv.z);
+                zap.add(q.z, av.z);
+                zr.add(q.w, rv.w);
+                zap.add(q.w, av.w);
+            }
         } else {
-            if (m0) f[c] += v.x;
-            if (m1) f[c + 1] += v.y;
-            if (m2) f[c + 2] += v.z;
-            if (m3) f[c + 3] += v.w;
+            const bool m[4] = {m0, m1, m2, m3};
+            const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                if (m[e]) {
+                    const float q = f[c + e] + vv[e];
+                    f[c + e] = q;
+                    if (DOTS) {
+                        zr.add(q, r[c + e]);
+                        zap.add(q, Ap[c + e]);
+                    }
+                }
         }
     };
     const long long sk = g.sk;
@@ -923,6 +936,36 @@ __global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, D
         add(c, make_float4(0.5f * (xm.x + x0.x), 0.5f * (xm.y + x0.y), 0.5f * (xm.z + x0.z), 0.5f * (xm.w + x0.w)));
 }
 
+
+// k_prolong_add_field on x-vectorised FP32 tiles: a thread owns four consecutive x
+// points of the field (one float4, tiles aligned to x = 0 as the solver's
+// vectorised Chebyshev tiles).  The four points need at most three consecutive
+// coarse x columns, X0..X0+2: per coarse plane the thread interpolates those in y
+// (6 loads), then each point in x, and adds the two fine planes the coarse plane
+// covers with float4 read-modify-writes.  The weights are k_prolong_add_field's
+// (interpolated in y first, so the rounding differs from it).
+// DOTS: f is flexible CG's z = M r, finished here, so the kernel also sums z.r and
+// z.Ap over the unknowns (the FIN_FCG_CONV reduction) while z is in registers.
+template <bool DOTS>
+__global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
+                                                              float* __restrict__ f, const int* __restrict__ stop,
+                                                              const float* __restrict__ r, const float* __restrict__ Ap,
+                                                              RedCtx rc)
+{
+    if (stop && *(volatile const int*)stop) return;
+    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
+    const int i0 = bx * 128 + threadIdx.x * 4;
+    const int j = g.lo[1] + by * sh.ty + threadIdx.y;
+    const int k0 = g.lo[2] + blockIdx.y * sh.kchunk, k1 = min(k0 + sh.kchunk, g.hi[2]);
+    Acc<float> zr, zap;
+    if (!(j >= g.hi[1] || i0 >= g.hi[0] || i0 + 4 <= g.lo[0]))
+        prolong_v4_column<DOTS>(g, dc, coarse, f, r, Ap, i0, j, k0, k1, zr, zap);
+    if (DOTS) {
+        double v[2] = {zr.value(), zap.value()};
+        reduce_finalize<2>(v, rc);
+    }
+}
+
 template <typename T>
 void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s)
 {
@@ -953,21 +996,28 @@ void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& d
     launches_counter_add(1);
 }
 template <typename T>
-void prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s)
+bool prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const float* coarse, T* f, cudaStream_t s,
+                       const T* r, const T* Ap, const RedCtx* dots)
 {
     if (sh.cx == 4) {   // the x-vectorised tiles (FP32 rows on 16-byte boundaries), else one column per thread
         if constexpr (std::is_same<T, float>::value) {
-            if (g.sj % 4 == 0 && ((uintptr_t)f & 15u) == 0) {
-                k_prolong_add_field_v4<<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
+            auto a16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+            if (g.sj % 4 == 0 && a16(f)) {
+                if (dots && r && Ap && a16(r) && a16(Ap))
+                    k_prolong_add_field_v4<true><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop, r, Ap,
+                                                                                 *dots);
+                else
+                    k_prolong_add_field_v4<false><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop,
+                                                                                  nullptr, nullptr, RedCtx{});
                 launches_counter_add(1);
-                return;
+                return dots && r && Ap && a16(r) && a16(Ap);
             }
         }
-        prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
-        return;
+        return prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
     }
     k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
     launches_counter_add(1);
+    return false;
 }
 template void field_residual_dense<float>(const Geo&, const float*, const float*, float*, cudaStream_t);
 template void field_residual_dense<double>(const Geo&, const double*, const double*, float*, cudaStream_t);
@@ -978,8 +1028,10 @@ template void field_axpy<double>(const Geo&, const Shape&, double*, const double
 template void field_residual_restrict<float>(const Geo&, const float*, const float*, const Dims&, float*, cudaStream_t);
 template void field_residual_restrict<double>(const Geo&, const double*, const double*, const Dims&, float*,
                                               cudaStream_t);
-template void prolong_add_field<float>(const Geo&, const Shape&, const Dims&, const float*, float*, cudaStream_t);
-template void prolong_add_field<double>(const Geo&, const Shape&, const Dims&, const float*, double*, cudaStream_t);
+template bool prolong_add_field<float>(const Geo&, const Shape&, const Dims&, const float*, float*, cudaStream_t,
+                                       const float*, const float*, const RedCtx*);
+template bool prolong_add_field<double>(const Geo&, const Shape&, const Dims&, const float*, double*, cudaStream_t,
+                                        const double*, const double*, const RedCtx*);
 
 // ---------------------------------------------------------------------------
 // Coarse levels of the learned multigrid cycle: dense [z][y][x] arrays with the
@@ -1090,6 +1142,117 @@ static void level_launch(const Dims& d, int& kchunk, dim3& grid, int waves = 4)
     if (chunks > d.D) chunks = d.D;
     kchunk = (int)((d.D + chunks - 1) / chunks);
     grid = dim3((unsigned)tx, (unsigned)ty, (unsigned)((d.D + kchunk - 1) / kchunk));
+}
+
+// W = B - A_l Y on level l (k_level_pass's residual, the same arithmetic per point)
+// restricted by full weighting to level l+1 in the same pass, so the level-l
+// residual is never stored (restrict2 of it, summed plane by plane).  A thread owns
+// a coarse (x, y) column and marches a chunk of coarse planes; on each fine plane
+// it forms the residual at the 3 x 3 fine points its coarse point weights, from Y
+// of that window on three planes held in registers plus the ring around it.
+__global__ void __launch_bounds__(128) k_level_residual_restrict(Dims dc, DLevel L, int zc, const float* __restrict__ Y,
+                                                                 const float* __restrict__ B,
+                                                                 float* __restrict__ coarse, const int* __restrict__ stop)
+{
+    if (stop && *(volatile const int*)stop) return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dc.W || y >= dc.H) return;
+    const int z0 = blockIdx.z * zc, z1 = min(dc.D, z0 + zc);
+    if (z0 >= z1) return;
+    const int Wf = 2 * dc.W, Hf = 2 * dc.H, Df = 2 * dc.D;
+    const long long sy = Wf, sz = (long long)Wf * Hf;
+    const bool in_a2 = 2 * x + 2 < Wf, in_b2 = 2 * y + 2 < Hf;   // the window's third fine column / row exists
+    const float wt[3] = {0.25f, 0.5f, 0.25f};
+    float ym[3][3], yc[3][3], yp[3][3];   // Y on fine planes f-1, f, f+1 of the window (0 beyond the grid)
+    const long long base = (long long)(2 * y) * sy + 2 * x;
+
+    auto load_plane = [&](int f, float (&pl)[3][3]) {
+        const bool in = f >= 0 && f < Df;
+        const long long o = (long long)f * sz + base;
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+                pl[b][a] = in && (a < 2 || in_a2) && (b < 2 || in_b2) ? Y[o + b * sy + a] : 0.0f;
+    };
+    // the window's weighted residual sum on fine plane f (yc holds plane f)
+    auto plane_sum = [&](int f) -> float {
+        const bool lz = f == Df - 1;
+        const float wzm = lz ? L.last_m[2] : L.ih2[2], wzp = lz ? 0.0f : L.ih2[2];
+        const long long o = (long long)f * sz + base;
+        float acc = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            if (b == 2 && !in_b2) continue;
+            const int yy = 2 * y + b;
+            const bool ly = yy == Hf - 1;
+            const float wym = yy > 0 ? (ly ? L.last_m[1] : L.ih2[1]) : 0.0f, wyp = ly ? 0.0f : L.ih2[1];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (a == 2 && !in_a2) continue;
+                const int xx = 2 * x + a;
+                const bool lx = xx == Wf - 1;
+                const float wxm = xx > 0 ? (lx ? L.last_m[0] : L.ih2[0]) : 0.0f, wxp = lx ? 0.0f : L.ih2[0];
+                const long long q = o + b * sy + a;
+                const float left = a > 0 ? yc[b][a - 1] : (xx > 0 ? Y[q - 1] : 0.0f);
+                const float right = a < 2 ? yc[b][a + 1] : (xx + 1 < Wf ? Y[q + 1] : 0.0f);
+                const float down = b > 0 ? yc[b - 1][a] : (yy > 0 ? Y[q - sy] : 0.0f);
+                const float up = b < 2 ? yc[b + 1][a] : (yy + 1 < Hf ? Y[q + sy] : 0.0f);
+                float ay = -level_negdiag(L, lx, ly, lz) * yc[b][a];
+                ay = fmaf(wxm, left, ay);
+                ay = fmaf(wxp, right, ay);
+                ay = fmaf(wym, down, ay);
+                ay = fmaf(wyp, up, ay);
+                ay = fmaf(wzm, ym[b][a], ay);
+                ay = fmaf(wzp, yp[b][a], ay);
+                acc += wt[b] * wt[a] * (B[q] - ay);
+            }
+        }
+        return acc;
+    };
+    auto shift = [&](int fnext) {
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                ym[b][a] = yc[b][a];
+                yc[b][a] = yp[b][a];
+            }
+        load_plane(fnext, yp);
+    };
+
+    const int f0 = 2 * z0;
+    load_plane(f0 - 1, ym);
+    load_plane(f0, yc);
+    load_plane(f0 + 1, yp);
+    float prev = plane_sum(f0);
+    long long out = ((long long)z0 * dc.H + y) * dc.W + x;
+    const long long cstride = (long long)dc.H * dc.W;
+    for (int cz = z0; cz < z1; cz++, out += cstride) {
+        shift(2 * cz + 2);   // yc: plane 2cz+1
+        const float mid = plane_sum(2 * cz + 1);
+        float next = 0.0f;
+        if (2 * cz + 2 < Df) {
+            shift(2 * cz + 3);   // yc: plane 2cz+2
+            next = plane_sum(2 * cz + 2);
+        }
+        coarse[out] = wt[0] * prev + wt[1] * mid + wt[2] * next;
+        prev = next;
+    }
+}
+
+void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, const float* B, float* coarse,
+                             cudaStream_t s)
+{
+    // 32 x 4 coarse columns per block; z split into chunks for about two waves of
+    // eight blocks per SM
+    const int tx = (dc.W + 31) / 32, ty = (dc.H + 3) / 4;
+    long long chunks = (152LL * 8 * 2 + (long long)tx * ty - 1) / ((long long)tx * ty);
+    chunks = std::max(1LL, std::min(chunks, (long long)dc.D));
+    const int zc = (int)((dc.D + chunks - 1) / chunks);
+    const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((dc.D + zc - 1) / zc));
+    k_level_residual_restrict<<<grid, dim3(32, 4), 0, s>>>(dc, L, zc, Y, B, coarse, g_stop);
+    launches_counter_add(1);
 }
 
 void level_residual(const Dims& d, const DLevel& L, const float* Y, const float* B, float* W, cudaStream_t s)

@@ -472,3 +472,28 @@ def test_inner_solver_preconditioner_application(gpu, oracle, form):
     AX = oracle.apply_A(ogrid_of(oracle, case), X)
     res = np.linalg.norm((B - AX)[sl]) / np.linalg.norm(B[sl])
     assert res < (1e-6 if form != "mixed" else 1e-4)
+
+
+@pytest.mark.parametrize("krylov", ["bicgstab", "fcg"])
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_preconditioner_call_leaves_no_state(gpu, form, krylov):
+    """pps_apply_preconditioner on B and X with nonzero boundary nodes and guards, then
+    a solve on the same handle: the solve's work fields are clean again, so it matches
+    a fresh handle bit for bit."""
+    rng = np.random.default_rng(21)
+    grid = pps.BlockGrid.cube(24)
+    b = np.zeros(grid.shape)
+    b[grid.unknowns()] = rng.standard_normal(b[grid.unknowns()].shape)
+    cls = pps.BiCGSTAB if krylov == "bicgstab" else pps.FlexibleCG
+    out = []
+    for pre in (False, True):
+        s = cls(grid, pps.ChebyshevIteration(11), tolerance=1e-10, max_iteration=2000, form=form)
+        if pre:
+            s.apply_preconditioner(rng.standard_normal(grid.shape), rng.standard_normal(grid.shape))
+        x = np.zeros_like(b)
+        assert s(x, b.copy()) == pps.OK
+        out.append((x, s.get_num_iteration_final(), s.history()))
+        s.close()
+    assert out[0][1] == out[1][1]
+    assert same_bits(out[0][0], out[1][0])
+    assert same_bits(out[0][2], out[1][2])
