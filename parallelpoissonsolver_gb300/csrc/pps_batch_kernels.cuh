@@ -126,6 +126,7 @@ __device__ __forceinline__ void breduce_finalize(double (&v)[NS], const BatchDev
 // is restored as the first stop test.
 __global__ void bk_refine_init(int nprob, BState* bst, int inner_maxit, double inner_tol)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nprob) return;
     BState& b = bst[p];
@@ -149,6 +150,7 @@ __global__ void bk_refine_init(int nprob, BState* bst, int inner_maxit, double i
 // End of a refinement step: count the inner iterations of every problem that ran.
 __global__ void bk_refine_end(int nprob, BState* bst)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nprob) return;
     BState& b = bst[p];
@@ -162,6 +164,7 @@ __global__ void __launch_bounds__(256) bk_norm_badj(BatchDev B, const double* __
                                                     const double* __restrict__ x, double* partials,
                                                     unsigned* counters, BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     const Geo& g = q.P->g;
     double s = 0.0;
@@ -190,6 +193,7 @@ __global__ void __launch_bounds__(256) bk_residual(BatchDev B, const double* __r
                                                    float* __restrict__ r0, float* __restrict__ p,
                                                    double* partials, unsigned* counters, BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_FINISHED(bst, q);
     const Geo& g = q.P->g;
@@ -225,6 +229,7 @@ __global__ void __launch_bounds__(256) bk_residual(BatchDev B, const double* __r
 
 __global__ void __launch_bounds__(256) bk_zero(BatchDev B, float* __restrict__ e, const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_FINISHED(bst, q);
     if (!q.active) return;
@@ -239,6 +244,7 @@ __global__ void __launch_bounds__(256) bk_zero(BatchDev B, float* __restrict__ e
 __global__ void __launch_bounds__(256) bk_add_correction(BatchDev B, double* __restrict__ x,
                                                          const float* __restrict__ e, const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_FINISHED(bst, q);
     if (!q.active) return;
@@ -254,6 +260,7 @@ __global__ void __launch_bounds__(256) bk_cheb_s01(BatchDev B, const float* __re
                                                    const CT<float>* __restrict__ coef, int cstride, int ci,
                                                    const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     if (!q.active) return;
@@ -289,6 +296,7 @@ __global__ void __launch_bounds__(256) bk_cheb_sweep(BatchDev B, const float* __
                                                      float* __restrict__ W, const CT<float>* __restrict__ coef,
                                                      int cstride, int ci, const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     if (!q.active) return;
@@ -326,6 +334,7 @@ __global__ void __launch_bounds__(256) bk_stencil_dot(BatchDev B, const float* _
                                                       const float* __restrict__ w, float* __restrict__ Au,
                                                       double* partials, unsigned* counters, BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     const Geo& g = q.P->g;
@@ -365,6 +374,7 @@ __global__ void __launch_bounds__(256) bk_stencil_dot(BatchDev B, const float* _
 __global__ void __launch_bounds__(256) bk_axpy_alpha(BatchDev B, float* __restrict__ r, const float* __restrict__ v,
                                                      const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     if (!q.active) return;
@@ -382,6 +392,7 @@ __global__ void __launch_bounds__(256) bk_update_xr(BatchDev B, float* __restric
                                                     const float* __restrict__ Az, const float* __restrict__ r0,
                                                     double* partials, unsigned* counters, BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     Acc<float> a1, a2;
@@ -407,6 +418,7 @@ __global__ void __launch_bounds__(256) bk_update_xr(BatchDev B, float* __restric
 __global__ void __launch_bounds__(256) bk_update_p(BatchDev B, float* __restrict__ p, const float* __restrict__ r,
                                                    const float* __restrict__ AMp, const BState* bst)
 {
+    pdl_enter();
     const BCol q = bcolumn(B);
     BSKIP_INNER(bst, q);
     if (!q.active) return;
@@ -425,70 +437,70 @@ static inline unsigned bgrid(const BatchDev& B) { return B.total_blocks; }
 
 void b_refine_init(const BatchDev& B, BState* bst, int inner_maxit, double inner_tol, cudaStream_t s)
 {
-    bk_refine_init<<<(B.nprob + 127) / 128, 128, 0, s>>>(B.nprob, bst, inner_maxit, inner_tol);
+    launch_pdl(bk_refine_init, (B.nprob + 127) / 128, 128, 0, s, B.nprob, bst, inner_maxit, inner_tol);
     PPS_COUNT_LAUNCH();
 }
 void b_refine_end(const BatchDev& B, BState* bst, cudaStream_t s)
 {
-    bk_refine_end<<<(B.nprob + 127) / 128, 128, 0, s>>>(B.nprob, bst);
+    launch_pdl(bk_refine_end, (B.nprob + 127) / 128, 128, 0, s, B.nprob, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_norm_badj(const BatchDev& B, const double* b, const double* x, double* part, unsigned* cnt, BState* bst,
                  cudaStream_t s)
 {
-    bk_norm_badj<<<bgrid(B), dim3(32, 8), 0, s>>>(B, b, x, part, cnt, bst);
+    launch_pdl(bk_norm_badj, bgrid(B), dim3(32, 8), 0, s, B, b, x, part, cnt, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_residual(const BatchDev& B, const double* x, const double* b, float* r, float* r0, float* p, double* part,
                 unsigned* cnt, BState* bst, cudaStream_t s)
 {
-    bk_residual<<<bgrid(B), dim3(32, 8), 0, s>>>(B, x, b, r, r0, p, part, cnt, bst);
+    launch_pdl(bk_residual, bgrid(B), dim3(32, 8), 0, s, B, x, b, r, r0, p, part, cnt, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_zero(const BatchDev& B, float* e, const BState* bst, cudaStream_t s)
 {
-    bk_zero<<<bgrid(B), dim3(32, 8), 0, s>>>(B, e, bst);
+    launch_pdl(bk_zero, bgrid(B), dim3(32, 8), 0, s, B, e, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_add_correction(const BatchDev& B, double* x, const float* e, const BState* bst, cudaStream_t s)
 {
-    bk_add_correction<<<bgrid(B), dim3(32, 8), 0, s>>>(B, x, e, bst);
+    launch_pdl(bk_add_correction, bgrid(B), dim3(32, 8), 0, s, B, x, e, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_cheb_s01(const BatchDev& B, const float* Bf, float* Y, const void* coef, int cstride, int ci,
                 const BState* bst, cudaStream_t s)
 {
-    bk_cheb_s01<<<bgrid(B), dim3(32, 8), 0, s>>>(B, Bf, Y, (const CT<float>*)coef, cstride, ci, bst);
+    launch_pdl(bk_cheb_s01, bgrid(B), dim3(32, 8), 0, s, B, Bf, Y, (const CT<float>*)coef, cstride, ci, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_cheb_sweep(const BatchDev& B, const float* Y, const float* Bf, const float* Z, float* W, const void* coef,
                   int cstride, int ci, const BState* bst, cudaStream_t s)
 {
-    if (Z) bk_cheb_sweep<true><<<bgrid(B), dim3(32, 8), 0, s>>>(B, Y, Bf, Z, W, (const CT<float>*)coef, cstride, ci, bst);
-    else bk_cheb_sweep<false><<<bgrid(B), dim3(32, 8), 0, s>>>(B, Y, Bf, Z, W, (const CT<float>*)coef, cstride, ci, bst);
+    if (Z) launch_pdl(bk_cheb_sweep<true>, bgrid(B), dim3(32, 8), 0, s, B, Y, Bf, Z, W, (const CT<float>*)coef, cstride, ci, bst);
+    else launch_pdl(bk_cheb_sweep<false>, bgrid(B), dim3(32, 8), 0, s, B, Y, Bf, Z, W, (const CT<float>*)coef, cstride, ci, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_stencil_dot(const BatchDev& B, const float* u, const float* w, float* Au, int nsums, double* part,
                    unsigned* cnt, BState* bst, cudaStream_t s)
 {
-    if (nsums == 1) bk_stencil_dot<1><<<bgrid(B), dim3(32, 8), 0, s>>>(B, u, w, Au, part, cnt, bst);
-    else bk_stencil_dot<2><<<bgrid(B), dim3(32, 8), 0, s>>>(B, u, w, Au, part, cnt, bst);
+    if (nsums == 1) launch_pdl(bk_stencil_dot<1>, bgrid(B), dim3(32, 8), 0, s, B, u, w, Au, part, cnt, bst);
+    else launch_pdl(bk_stencil_dot<2>, bgrid(B), dim3(32, 8), 0, s, B, u, w, Au, part, cnt, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_axpy_alpha(const BatchDev& B, float* r, const float* v, const BState* bst, cudaStream_t s)
 {
-    bk_axpy_alpha<<<bgrid(B), dim3(32, 8), 0, s>>>(B, r, v, bst);
+    launch_pdl(bk_axpy_alpha, bgrid(B), dim3(32, 8), 0, s, B, r, v, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_update_xr(const BatchDev& B, float* x, const float* Mp, const float* z, float* r, const float* Az,
                  const float* r0, double* part, unsigned* cnt, BState* bst, cudaStream_t s)
 {
-    bk_update_xr<<<bgrid(B), dim3(32, 8), 0, s>>>(B, x, Mp, z, r, Az, r0, part, cnt, bst);
+    launch_pdl(bk_update_xr, bgrid(B), dim3(32, 8), 0, s, B, x, Mp, z, r, Az, r0, part, cnt, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_update_p(const BatchDev& B, float* p, const float* r, const float* AMp, const BState* bst, cudaStream_t s)
 {
-    bk_update_p<<<bgrid(B), dim3(32, 8), 0, s>>>(B, p, r, AMp, bst);
+    launch_pdl(bk_update_p, bgrid(B), dim3(32, 8), 0, s, B, p, r, AMp, bst);
     PPS_COUNT_LAUNCH();
 }
 void b_cast_coef(const Coef* in, void* out, size_t n)

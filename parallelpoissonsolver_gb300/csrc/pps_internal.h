@@ -9,6 +9,37 @@ extern "C" void pps_internal_set_error(const char* msg);
 
 namespace pps {
 
+// Programmatic dependent launch.  Kernels go onto the stream with
+// cudaLaunchAttributeProgrammaticStreamSerialization, so the next kernel's blocks
+// can be dispatched while the current one drains instead of after it completed.
+// Every kernel of the library begins with pdl_enter(): it lets the next kernel
+// launch (griddepcontrol.launch_dependents) and then waits until the kernel before
+// it has completed with its memory visible (griddepcontrol.wait), before touching
+// any global memory.  The wait is transitive along the stream, and it returns at
+// once when the kernel was launched without the attribute.
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+#endif
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // Geometry of one single-rank grid in the guard-padded field layout
 // (iterativeSolverBase.hpp:34-35): index = i + sj*j + sk*k with
 // 0 <= i < n0+2 etc.; data nodes are 1..n, unknowns lo..hi-1 (blockGrid.hpp:184-222).

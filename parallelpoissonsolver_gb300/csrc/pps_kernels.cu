@@ -84,6 +84,7 @@ static inline unsigned par_blocks(long long n)
 __global__ void k_par_stencil(Geo g, const double* __restrict__ u, double* __restrict__ out, double h2x,
                               double h2y, double h2z)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -95,6 +96,7 @@ __global__ void k_par_stencil(Geo g, const double* __restrict__ u, double* __res
 __global__ void k_par_residual(Geo g, const double* __restrict__ x, const double* __restrict__ b,
                                double* __restrict__ r, double h2x, double h2y, double h2z)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -141,6 +143,7 @@ __device__ __forceinline__ double badj_exact(const Geo& g, const double* __restr
 __global__ void k_par_adjust_b(Geo g, const double* __restrict__ b, const double* __restrict__ x, Faces f,
                                double* __restrict__ bt)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -160,6 +163,7 @@ __global__ void k_par_adjust_b(Geo g, const double* __restrict__ b, const double
 __global__ void k_par_adjust_b_data(Geo g, const double* __restrict__ b, const double* __restrict__ x, Faces f,
                                     double* __restrict__ bt)
 {
+    pdl_enter();
     const long long nx = g.n[0], ny = g.n[1], n = nx * ny * (long long)g.n[2];
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
@@ -176,6 +180,7 @@ __global__ void k_par_adjust_b_data(Geo g, const double* __restrict__ b, const d
 __global__ void k_par_cheb_s01(Geo g, const double* __restrict__ B, double* __restrict__ Y, double* __restrict__ Z,
                                double theta, double t2rd, double h2x, double h2y, double h2z)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -191,6 +196,7 @@ __global__ void k_par_cheb_sweep(Geo g, const double* __restrict__ Y, const doub
                                  const double* __restrict__ Z, double* __restrict__ W, double rc, double two_sigma,
                                  double two_over_delta, double ro, double h2x, double h2y, double h2z)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -204,6 +210,7 @@ __global__ void k_par_cheb_sweep(Geo g, const double* __restrict__ Y, const doub
 
 __global__ void k_par_neg(Geo g, const double* __restrict__ W, double* __restrict__ X)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -214,6 +221,7 @@ __global__ void k_par_neg(Geo g, const double* __restrict__ W, double* __restric
 
 __global__ void k_par_axpy(Geo g, double* __restrict__ r, const double* __restrict__ v, double a)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -226,12 +234,14 @@ __global__ void k_par_axpy(Geo g, double* __restrict__ r, const double* __restri
 __global__ void k_par_update_x_all(long long n, double* __restrict__ x, const double* __restrict__ Mp,
                                    const double* __restrict__ z, double a, double w)
 {
+    pdl_enter();
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         x[c] = __dadd_rn(__dadd_rn(x[c], __dmul_rn(a, Mp[c])), __dmul_rn(w, z[c]));
 }
 
 __global__ void k_par_update_x(Geo g, double* __restrict__ x, const double* __restrict__ p, double a)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -244,6 +254,7 @@ __global__ void k_par_update_x(Geo g, double* __restrict__ x, const double* __re
 __global__ void k_par_update_p(Geo g, double* __restrict__ p, const double* __restrict__ r,
                                const double* __restrict__ AMp, double beta, double omega)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -255,6 +266,7 @@ __global__ void k_par_update_p(Geo g, double* __restrict__ p, const double* __re
 // p = z + beta*p   (baseCG.hpp:204)
 __global__ void k_par_update_p_cg(Geo g, double* __restrict__ p, const double* __restrict__ z, double beta)
 {
+    pdl_enter();
     const Lin L = unknown_box(g);
     PAR_LOOP(g, L)
     {
@@ -265,6 +277,7 @@ __global__ void k_par_update_p_cg(Geo g, double* __restrict__ p, const double* _
 
 __global__ void k_par_scale_all(long long n, double* __restrict__ x, double* __restrict__ b, double v, int divide)
 {
+    pdl_enter();
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
         if (divide) {
             x[c] = __ddiv_rn(x[c], v);
@@ -286,6 +299,7 @@ __global__ void __launch_bounds__(SEQ_THREADS) k_seq_dot2(Geo g, const double* _
                                                           const double* __restrict__ b1, const double* __restrict__ a2,
                                                           const double* __restrict__ b2, double* __restrict__ out)
 {
+    pdl_enter();
     __shared__ double p1[SEQ_CHUNK];
     __shared__ double p2[SEQ_CHUNK];
     const Lin L = unknown_box(g);
@@ -319,79 +333,79 @@ __global__ void __launch_bounds__(SEQ_THREADS) k_seq_dot2(Geo g, const double* _
 
 void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s)
 {
-    k_par_stencil<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, u, out, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
+    launch_pdl(k_par_stencil, par_blocks(unknown_box(g).n), 256, 0, s, g, u, out, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
                                                                  g.ds[2] * g.ds[2]);
     PPS_COUNT_LAUNCH();
 }
 void par_residual(const Geo& g, const double* x, const double* b, double* r, cudaStream_t s)
 {
-    k_par_residual<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, x, b, r, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
+    launch_pdl(k_par_residual, par_blocks(unknown_box(g).n), 256, 0, s, g, x, b, r, g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
                                                                   g.ds[2] * g.ds[2]);
     PPS_COUNT_LAUNCH();
 }
 void par_adjust_b(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s)
 {
-    k_par_adjust_b<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, b, x, f, bt);
+    launch_pdl(k_par_adjust_b, par_blocks(unknown_box(g).n), 256, 0, s, g, b, x, f, bt);
     PPS_COUNT_LAUNCH();
 }
 void par_adjust_b_data(const Geo& g, const double* b, const double* x, Faces f, double* bt, cudaStream_t s)
 {
-    k_par_adjust_b_data<<<par_blocks((long long)g.n[0] * g.n[1] * g.n[2]), 256, 0, s>>>(g, b, x, f, bt);
+    launch_pdl(k_par_adjust_b_data, par_blocks((long long)g.n[0] * g.n[1] * g.n[2]), 256, 0, s, g, b, x, f, bt);
     PPS_COUNT_LAUNCH();
 }
 void par_cheb_s01(const Geo& g, const double* B, double* Y, double* Z, double theta, double t2rd, cudaStream_t s)
 {
-    k_par_cheb_s01<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, B, Y, Z, theta, t2rd, g.ds[0] * g.ds[0],
+    launch_pdl(k_par_cheb_s01, par_blocks(unknown_box(g).n), 256, 0, s, g, B, Y, Z, theta, t2rd, g.ds[0] * g.ds[0],
                                                                   g.ds[1] * g.ds[1], g.ds[2] * g.ds[2]);
     PPS_COUNT_LAUNCH();
 }
 void par_cheb_sweep(const Geo& g, const double* Y, const double* B, const double* Z, double* W, double rc,
                     double two_sigma, double two_over_delta, double ro, cudaStream_t s)
 {
-    k_par_cheb_sweep<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, Y, B, Z, W, rc, two_sigma, two_over_delta, ro,
+    launch_pdl(k_par_cheb_sweep, par_blocks(unknown_box(g).n), 256, 0, s, g, Y, B, Z, W, rc, two_sigma, two_over_delta, ro,
                                                                     g.ds[0] * g.ds[0], g.ds[1] * g.ds[1],
                                                                     g.ds[2] * g.ds[2]);
     PPS_COUNT_LAUNCH();
 }
 void par_neg(const Geo& g, const double* W, double* X, cudaStream_t s)
 {
-    k_par_neg<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, W, X);
+    launch_pdl(k_par_neg, par_blocks(unknown_box(g).n), 256, 0, s, g, W, X);
     PPS_COUNT_LAUNCH();
 }
 void par_axpy(const Geo& g, double* r, const double* v, double a, cudaStream_t s)
 {
-    k_par_axpy<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, r, v, a);
+    launch_pdl(k_par_axpy, par_blocks(unknown_box(g).n), 256, 0, s, g, r, v, a);
     PPS_COUNT_LAUNCH();
 }
 void par_update_x_all(const Geo& g, double* x, const double* Mp, const double* z, double a, double w, cudaStream_t s)
 {
-    k_par_update_x_all<<<par_blocks(g.ntot), 256, 0, s>>>(g.ntot, x, Mp, z, a, w);
+    launch_pdl(k_par_update_x_all, par_blocks(g.ntot), 256, 0, s, g.ntot, x, Mp, z, a, w);
     PPS_COUNT_LAUNCH();
 }
 void par_update_x(const Geo& g, double* x, const double* p, double a, cudaStream_t s)
 {
-    k_par_update_x<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, x, p, a);
+    launch_pdl(k_par_update_x, par_blocks(unknown_box(g).n), 256, 0, s, g, x, p, a);
     PPS_COUNT_LAUNCH();
 }
 void par_update_p(const Geo& g, double* p, const double* r, const double* AMp, double beta, double omega, cudaStream_t s)
 {
-    k_par_update_p<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, p, r, AMp, beta, omega);
+    launch_pdl(k_par_update_p, par_blocks(unknown_box(g).n), 256, 0, s, g, p, r, AMp, beta, omega);
     PPS_COUNT_LAUNCH();
 }
 void par_update_p_cg(const Geo& g, double* p, const double* z, double beta, cudaStream_t s)
 {
-    k_par_update_p_cg<<<par_blocks(unknown_box(g).n), 256, 0, s>>>(g, p, z, beta);
+    launch_pdl(k_par_update_p_cg, par_blocks(unknown_box(g).n), 256, 0, s, g, p, z, beta);
     PPS_COUNT_LAUNCH();
 }
 void par_scale_all(const Geo& g, double* x, double* b, double v, int divide, cudaStream_t s)
 {
-    k_par_scale_all<<<par_blocks(g.ntot), 256, 0, s>>>(g.ntot, x, b, v, divide);
+    launch_pdl(k_par_scale_all, par_blocks(g.ntot), 256, 0, s, g.ntot, x, b, v, divide);
     PPS_COUNT_LAUNCH();
 }
 void seq_dot2(const Geo& g, const double* a1, const double* b1, const double* a2, const double* b2, double* out,
               cudaStream_t s)
 {
-    k_seq_dot2<<<1, SEQ_THREADS, 0, s>>>(g, a1, b1, a2, b2, out);
+    launch_pdl(k_seq_dot2, 1, SEQ_THREADS, 0, s, g, a1, b1, a2, b2, out);
     PPS_COUNT_LAUNCH();
 }
 
@@ -402,6 +416,7 @@ void seq_dot2(const Geo& g, const double* a1, const double* b1, const double* a2
 template <typename T>
 __global__ void k_neumann_fill(Geo g, T* __restrict__ field, Faces f, int face, int field_mode, double normb)
 {
+    pdl_enter();
     const int dir = face / 2, side = face % 2;
     const int a0 = dir == 0 ? 1 : 0;          // first remaining axis
     const int a1 = dir == 2 ? 1 : 2;          // second remaining axis
@@ -437,7 +452,7 @@ void neumann_fill(const Geo& g, T* field, Faces f, int field_mode, double normb,
         const long long total = (long long)g.n[dir == 0 ? 1 : 0] * g.n[dir == 2 ? 1 : 2];
         unsigned blocks = (unsigned)((total + 255) / 256);
         if (blocks > 1024) blocks = 1024;
-        k_neumann_fill<T><<<blocks, 256, 0, s>>>(g, field, f, face, field_mode, normb);
+        launch_pdl(k_neumann_fill<T>, blocks, 256, 0, s, g, field, f, face, field_mode, normb);
         PPS_COUNT_LAUNCH();
     }
 }
@@ -536,6 +551,7 @@ template <typename T, int CX>
 __global__ void __launch_bounds__(256) k_cheb_s01(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ Y,
                                                   CT<T> cf, const int* done)
 {
+    pdl_enter();
     EARLY_EXIT(done);
     const Col q = column_cx(g, sh, CX);
     if (!q.active) return;
@@ -579,6 +595,7 @@ __global__ void __launch_bounds__(256) k_cheb_sweep(Geo g, Shape sh, const T* __
                                                     const T* __restrict__ B, const T* __restrict__ Z,
                                                     T* __restrict__ W, CT<T> cf, const int* done)
 {
+    pdl_enter();
     EARLY_EXIT(done);
     const Col q = column_cx(g, sh, CX);
     if (!q.active) return;
@@ -715,6 +732,7 @@ __global__ void __launch_bounds__(256) k_cheb_v4(Geo g, Shape sh, const float* _
                                                  const float* __restrict__ B, const float* __restrict__ Z,
                                                  float* __restrict__ W, CT<float> cf, const int* done)
 {
+    pdl_enter();
     EARLY_EXIT(done);
     const Col4 q = column4(g, sh);
     if (q.j >= g.hi[1]) return;   // a warp shares its row, so its lanes leave together
@@ -767,6 +785,7 @@ template <typename T, int NS>
 __global__ void __launch_bounds__(256) k_cheb_fused(Geo g, int ntx, int kchunk, const T* __restrict__ B,
                                                     T* __restrict__ X, ChebStages<T> cs, const int* done)
 {
+    pdl_enter();
     EARLY_EXIT(done);
     typedef FuseDims<NS> FD;
     constexpr int NT = 256;
@@ -882,6 +901,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_scale_copy(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ X, T a,
                                                     const int* done)
 {
+    pdl_enter();
     EARLY_EXIT(done);
     const Col q = column(g, sh);
     if (!q.active) return;
@@ -898,6 +918,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_stencil_dot(Geo g, Shape sh, const T* __restrict__ u,
                                                      const T* __restrict__ r0, T* __restrict__ Au, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> acc;
@@ -931,6 +952,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_stencil_dot2(Geo g, Shape sh, const T* __restrict__ u,
                                                       const T* __restrict__ r, T* __restrict__ Au, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1, a2;
@@ -965,6 +987,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_axpy_alpha(Geo g, Shape sh, T* __restrict__ r, const T* __restrict__ v,
                                                     const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     const Col q = column(g, sh);
     if (!q.active) return;
@@ -983,6 +1006,7 @@ __global__ void __launch_bounds__(256) k_update_xr(Geo g, Shape sh, T* __restric
                                                    const T* __restrict__ z, T* __restrict__ r,
                                                    const T* __restrict__ Az, const T* __restrict__ r0, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1, a2;
@@ -1008,6 +1032,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_update_p(Geo g, Shape sh, T* __restrict__ p, const T* __restrict__ r,
                                                   const T* __restrict__ AMp, const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     const Col q = column(g, sh);
     if (!q.active) return;
@@ -1026,6 +1051,7 @@ __global__ void __launch_bounds__(256) k_cg_stencil_dot(Geo g, Shape sh, const T
                                                         const T* __restrict__ r, const T* __restrict__ z,
                                                         T* __restrict__ Ap, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1, a2;
@@ -1060,6 +1086,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_cg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
                                                       T* __restrict__ r, const T* __restrict__ Ap, const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     const Col q = column(g, sh);
     if (!q.active) return;
@@ -1078,6 +1105,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_cg_dot_rz(Geo g, Shape sh, const T* __restrict__ r, const T* __restrict__ z,
                                                    RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1, a2;
@@ -1100,6 +1128,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_cg_update_p(Geo g, Shape sh, T* __restrict__ p, const T* __restrict__ z,
                                                      const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     const Col q = column(g, sh);
     if (!q.active) return;
@@ -1120,6 +1149,7 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil(Geo g, Shape sh, const T*
                                                        const T* __restrict__ pin, T* __restrict__ pout,
                                                        T* __restrict__ Ap, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1;
@@ -1160,6 +1190,7 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil_v4(Geo g, Shape sh, const
                                                           const float* __restrict__ pin, float* __restrict__ pout,
                                                           float* __restrict__ Ap, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col4 q = column4(g, sh);
     Acc<float> a1;
@@ -1226,6 +1257,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_update_xr(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ p,
                                                        T* __restrict__ r, const T* __restrict__ Ap, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> rr;
@@ -1251,6 +1283,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_dot(Geo g, Shape sh, const T* __restrict__ r, const T* __restrict__ z,
                                                  const T* __restrict__ Ap, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a1, a2, a3;
@@ -1292,6 +1325,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_update_xr_flat(long long n, T* __restrict__ x, const T* __restrict__ p,
                                                             T* __restrict__ r, const T* __restrict__ Ap, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
@@ -1325,6 +1359,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_fcg_dot_flat(long long n, const T* __restrict__ r, const T* __restrict__ z,
                                                       const T* __restrict__ Ap, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
@@ -1361,6 +1396,7 @@ __global__ void __launch_bounds__(256) k_update_xr_flat(long long n, T* __restri
                                                         const T* __restrict__ z, T* __restrict__ r,
                                                         const T* __restrict__ Az, const T* __restrict__ r0, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
@@ -1399,6 +1435,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_update_p_flat(long long n, T* __restrict__ p, const T* __restrict__ r,
                                                        const T* __restrict__ AMp, const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
@@ -1420,6 +1457,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_axpy_alpha_flat(long long n, T* __restrict__ r, const T* __restrict__ v,
                                                          const DevState* st)
 {
+    pdl_enter();
     EARLY_EXIT(&st->done);
     typedef Vec16<T> VT;
     typedef typename VT::type V;
@@ -1444,6 +1482,7 @@ __global__ void __launch_bounds__(256) k_stencil_dots_v4(Geo g, Shape sh, const 
                                                          const float* __restrict__ wv, float* __restrict__ Au,
                                                          Coef cf, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col4 q = column4(g, sh);
     Acc<float> a1, a2;
@@ -1539,6 +1578,7 @@ __device__ __forceinline__ long long malign(const MI& a, int E)
 // not +-0, in 16-byte vectors.
 __global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double* __restrict__ x, RedCtx rc)
 {
+    pdl_enter();
     double cnt = 0.0;
     const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1568,6 +1608,7 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
                                                   const double* __restrict__ b, TR* __restrict__ r,
                                                   TR* __restrict__ r0, TR* __restrict__ p, Coef cf, RedCtx rc)
 {
+    pdl_enter();
     const Col q = column(g, sh);
     Acc<TR> acc;
     if (XZERO && q.active) {   // x = 0 on every point the stencil reads: r = b
@@ -1667,6 +1708,7 @@ template <bool XZERO>
 __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double* __restrict__ b,
                                                    const double* __restrict__ x, Faces f, RedCtx rc)
 {
+    pdl_enter();
     const Col q = column(g, sh);
     double s = 0.0;
     if (XZERO && q.active) {   // four planes' loads in flight, summed in plane order
@@ -1696,6 +1738,7 @@ __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double
 __global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double* __restrict__ x,
                                                         const float* __restrict__ e)
 {
+    pdl_enter();
     const Col q = column(g, sh);
     if (!q.active) return;
     const long long sk = g.sk;
@@ -1721,6 +1764,7 @@ __global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double*
 __global__ void __launch_bounds__(256) k_add_correction_flat(long long n, double* __restrict__ x,
                                                              const float* __restrict__ e)
 {
+    pdl_enter();
     const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double2* xv = reinterpret_cast<double2*>(x);
@@ -1754,6 +1798,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_bicg_start(Geo g, Shape sh, const T* __restrict__ B, T* __restrict__ r,
                                                     T* __restrict__ r0, T* __restrict__ p, RedCtx rc)
 {
+    pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col q = column(g, sh);
     Acc<T> a;
@@ -1775,6 +1820,7 @@ __global__ void __launch_bounds__(256) k_bicg_start(Geo g, Shape sh, const T* __
 
 __global__ void k_cast_f32(const double* __restrict__ in, float* __restrict__ out, long long n)
 {
+    pdl_enter();
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         out[c] = (float)in[c];
 }
@@ -1782,6 +1828,7 @@ __global__ void k_cast_f32(const double* __restrict__ in, float* __restrict__ ou
 template <typename T>
 __global__ void k_fill(T* p, long long n, T v)
 {
+    pdl_enter();
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         p[c] = v;
 }
@@ -1791,6 +1838,7 @@ __global__ void k_fill(T* p, long long n, T v)
 template <typename T>
 __global__ void k_zero_off_unknowns(Geo g, T* p)
 {
+    pdl_enter();
     const long long nj = g.sk / g.sj;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.ntot;
          c += (long long)gridDim.x * blockDim.x) {
@@ -1803,6 +1851,7 @@ __global__ void k_zero_off_unknowns(Geo g, T* p)
 __global__ void k_state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
                              int rho0_from_r, double hist_scale, int hist_cap)
 {
+    pdl_enter();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         st->rho0 = 1.0;
         st->alpha = st->omega = st->beta = 1.0;
@@ -1831,7 +1880,7 @@ void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& 
     if (sh.cx == 4) {
         if constexpr (std::is_same<T, float>::value) {
             if (v4_ok<T>(g, B, Y, nullptr, nullptr)) {
-                k_cheb_v4<0><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, nullptr, nullptr, Y, c, done);
+                launch_pdl(k_cheb_v4<0>, grid_of(sh), block_of(sh), 0, s, g, sh, B, nullptr, nullptr, Y, c, done);
                 PPS_COUNT_LAUNCH();
                 return;
             }
@@ -1839,8 +1888,8 @@ void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& 
         fast_cheb_s01<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), B, Y, cy, done, s);   // scalar tiles
         return;
     }
-    if (sh.cx == 2) k_cheb_s01<T, 2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
-    else k_cheb_s01<T, 1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, Y, c, done);
+    if (sh.cx == 2) launch_pdl(k_cheb_s01<T, 2>, grid_of(sh), block_of(sh), 0, s, g, sh, B, Y, c, done);
+    else launch_pdl(k_cheb_s01<T, 1>, grid_of(sh), block_of(sh), 0, s, g, sh, B, Y, c, done);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1851,8 +1900,8 @@ void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, cons
     if (sh.cx == 4) {
         if constexpr (std::is_same<T, float>::value) {
             if (v4_ok<T>(g, Y, B, Z, W)) {
-                if (Z) k_cheb_v4<2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
-                else k_cheb_v4<1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+                if (Z) launch_pdl(k_cheb_v4<2>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
+                else launch_pdl(k_cheb_v4<1>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
                 PPS_COUNT_LAUNCH();
                 return;
             }
@@ -1861,11 +1910,11 @@ void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, cons
         return;
     }
     if (Z) {
-        if (sh.cx == 2) k_cheb_sweep<T, 2, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
-        else k_cheb_sweep<T, 1, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+        if (sh.cx == 2) launch_pdl(k_cheb_sweep<T, 2, true>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
+        else launch_pdl(k_cheb_sweep<T, 1, true>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
     } else {
-        if (sh.cx == 2) k_cheb_sweep<T, 2, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
-        else k_cheb_sweep<T, 1, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, Y, B, Z, W, c, done);
+        if (sh.cx == 2) launch_pdl(k_cheb_sweep<T, 2, false>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
+        else launch_pdl(k_cheb_sweep<T, 1, false>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
     }
     PPS_COUNT_LAUNCH();
 }
@@ -1896,15 +1945,15 @@ void fast_cheb_fused(const Geo& g, int nsteps, const T* B, T* X, const Coef* c, 
         attr_set |= 1ull << dev;
     }
     if (nsteps == 2)
-        k_cheb_fused<T, 2><<<grid, block, sizeof(T) * FuseDims<2>::total(), s>>>(g, ntx, kchunk, B, X, cs, done);
+        launch_pdl(k_cheb_fused<T, 2>, grid, block, sizeof(T) * FuseDims<2>::total(), s, g, ntx, kchunk, B, X, cs, done);
     else
-        k_cheb_fused<T, 3><<<grid, block, sizeof(T) * FuseDims<3>::total(), s>>>(g, ntx, kchunk, B, X, cs, done);
+        launch_pdl(k_cheb_fused<T, 3>, grid, block, sizeof(T) * FuseDims<3>::total(), s, g, ntx, kchunk, B, X, cs, done);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_scale_copy(const Geo& g, const Shape& sh, const T* B, T* X, double a, const int* done, cudaStream_t s)
 {
-    k_scale_copy<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, X, (T)a, done);
+    launch_pdl(k_scale_copy<T>, grid_of(sh), block_of(sh), 0, s, g, sh, B, X, (T)a, done);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1914,7 +1963,7 @@ void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T*
     if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, u, r0, Au, nullptr)) {
-                k_stencil_dots_v4<1><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r0, Au, a, rc);
+                launch_pdl(k_stencil_dots_v4<1>, grid_of(sh), block_of(sh), 0, s, g, sh, u, r0, Au, a, rc);
                 PPS_COUNT_LAUNCH();
                 return;
             }
@@ -1922,7 +1971,7 @@ void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T*
         fast_stencil_dot<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), u, r0, Au, a, rc, s);
         return;
     }
-    k_stencil_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r0, Au, a, rc);
+    launch_pdl(k_stencil_dot<T>, grid_of(sh), block_of(sh), 0, s, g, sh, u, r0, Au, a, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1932,7 +1981,7 @@ void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T*
     if (sh.cx != 1) {
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, u, r, Au, nullptr)) {
-                k_stencil_dots_v4<2><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r, Au, a, rc);
+                launch_pdl(k_stencil_dots_v4<2>, grid_of(sh), block_of(sh), 0, s, g, sh, u, r, Au, a, rc);
                 PPS_COUNT_LAUNCH();
                 return;
             }
@@ -1940,7 +1989,7 @@ void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T*
         fast_stencil_dot2<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), u, r, Au, a, rc, s);
         return;
     }
-    k_stencil_dot2<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, u, r, Au, a, rc);
+    launch_pdl(k_stencil_dot2<T>, grid_of(sh), block_of(sh), 0, s, g, sh, u, r, Au, a, rc);
     PPS_COUNT_LAUNCH();
 }
 // Dirichlet grids with 16-byte aligned fields: the flat vector forms of the updates.
@@ -1956,11 +2005,11 @@ template <typename T>
 void fast_axpy_alpha(const Geo& g, const Shape& sh, T* r, const T* v, const DevState* st, cudaStream_t s)
 {
     if (flat_ok(g, {r, v})) {
-        k_axpy_alpha_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, r, v, st);
+        launch_pdl(k_axpy_alpha_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, r, v, st);
         PPS_COUNT_LAUNCH();
         return;
     }
-    k_axpy_alpha<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, v, st);
+    launch_pdl(k_axpy_alpha<T>, grid_of(sh), block_of(sh), 0, s, g, sh, r, v, st);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -1968,74 +2017,74 @@ void fast_update_xr(const Geo& g, const Shape& sh, T* x, const T* Mp, const T* z
                     RedCtx rc, cudaStream_t s)
 {
     if (flat_ok(g, {x, Mp, z, r, Az, r0})) {
-        k_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, Mp, z, r, Az, r0, rc);
+        launch_pdl(k_update_xr_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, Mp, z, r, Az, r0, rc);
         PPS_COUNT_LAUNCH();
         return;
     }
-    k_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, Mp, z, r, Az, r0, rc);
+    launch_pdl(k_update_xr<T>, grid_of(sh), block_of(sh), 0, s, g, sh, x, Mp, z, r, Az, r0, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_update_p(const Geo& g, const Shape& sh, T* p, const T* r, const T* AMp, const DevState* st, cudaStream_t s)
 {
     if (flat_ok(g, {p, r, AMp})) {
-        k_update_p_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, p, r, AMp, st);
+        launch_pdl(k_update_p_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, p, r, AMp, st);
         PPS_COUNT_LAUNCH();
         return;
     }
-    k_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, r, AMp, st);
+    launch_pdl(k_update_p<T>, grid_of(sh), block_of(sh), 0, s, g, sh, p, r, AMp, st);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_cg_stencil_dot(const Geo& g, const Shape& sh, const T* p, const T* r, const T* z, T* Ap, const Coef& a,
                          RedCtx rc, cudaStream_t s)
 {
-    k_cg_stencil_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, r, z, Ap, a, rc);
+    launch_pdl(k_cg_stencil_dot<T>, grid_of(sh), block_of(sh), 0, s, g, sh, p, r, z, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_cg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, const DevState* st,
                        cudaStream_t s)
 {
-    k_cg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, st);
+    launch_pdl(k_cg_update_xr<T>, grid_of(sh), block_of(sh), 0, s, g, sh, x, p, r, Ap, st);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_cg_dot_rz(const Geo& g, const Shape& sh, const T* r, const T* z, RedCtx rc, cudaStream_t s)
 {
-    k_cg_dot_rz<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, rc);
+    launch_pdl(k_cg_dot_rz<T>, grid_of(sh), block_of(sh), 0, s, g, sh, r, z, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_cg_update_p(const Geo& g, const Shape& sh, T* p, const T* z, const DevState* st, cudaStream_t s)
 {
-    k_cg_update_p<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, p, z, st);
+    launch_pdl(k_cg_update_p<T>, grid_of(sh), block_of(sh), 0, s, g, sh, p, z, st);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_fcg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
                         cudaStream_t s)
 {
-    k_fcg_update_xr<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, p, r, Ap, rc);
+    launch_pdl(k_fcg_update_xr<T>, grid_of(sh), block_of(sh), 0, s, g, sh, x, p, r, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s)
 {
-    k_fcg_dot<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, r, z, Ap, rc);
+    launch_pdl(k_fcg_dot<T>, grid_of(sh), block_of(sh), 0, s, g, sh, r, z, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_fcg_update_xr_flat(const Geo& g, const Shape& sh, T* x, const T* p, T* r, const T* Ap, RedCtx rc,
                              cudaStream_t s)
 {
-    k_fcg_update_xr_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, p, r, Ap, rc);
+    launch_pdl(k_fcg_update_xr_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, p, r, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s)
 {
-    k_fcg_dot_flat<T><<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, r, z, Ap, rc);
+    launch_pdl(k_fcg_dot_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, r, z, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
@@ -2045,7 +2094,7 @@ void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin,
     if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, z, pin, pout, Ap)) {
-                k_fcg_p_stencil_v4<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
+                launch_pdl(k_fcg_p_stencil_v4, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
                 PPS_COUNT_LAUNCH();
                 return;
             }
@@ -2053,12 +2102,12 @@ void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin,
         fast_fcg_p_stencil<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), z, pin, pout, Ap, a, rc, s);
         return;
     }
-    k_fcg_p_stencil<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, z, pin, pout, Ap, a, rc);
+    launch_pdl(k_fcg_p_stencil<T>, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx rc, cudaStream_t s)
 {
-    k_count_nonzero<<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, rc);
+    launch_pdl(k_count_nonzero, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, rc);
     PPS_COUNT_LAUNCH();
 }
 template <typename TR>
@@ -2066,58 +2115,58 @@ void fast_residual(const Geo& g, const Shape& sh, const double* x, const double*
                    const Coef& a, RedCtx rc, cudaStream_t s, bool x_zero)
 {
     if (x_zero)
-        k_residual<TR, true, true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, true, true>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
     else if (a.cx == a.cy && a.cx == a.cz)
-        k_residual<TR, true, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, true, false>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
     else
-        k_residual<TR, false, false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, false, false>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
                     cudaStream_t s, bool x_zero)
 {
-    if (x_zero) k_norm_badj<true><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
-    else k_norm_badj<false><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, b, x, f, rc);
+    if (x_zero) launch_pdl(k_norm_badj<true>, grid_of(sh), block_of(sh), 0, s, g, sh, b, x, f, rc);
+    else launch_pdl(k_norm_badj<false>, grid_of(sh), block_of(sh), 0, s, g, sh, b, x, f, rc);
     PPS_COUNT_LAUNCH();
 }
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s,
                          bool e_zero_off)
 {
     if (e_zero_off && flat_ok(g, {x}) && ((uintptr_t)e & 7u) == 0) {
-        k_add_correction_flat<<<sh.nblocks(), 32 * sh.ty, 0, s>>>(g.ntot, x, e);
+        launch_pdl(k_add_correction_flat, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, e);
     } else {
-        k_add_correction<<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, x, e);
+        launch_pdl(k_add_correction, grid_of(sh), block_of(sh), 0, s, g, sh, x, e);
     }
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* p, RedCtx rc, cudaStream_t s)
 {
-    k_bicg_start<T><<<grid_of(sh), block_of(sh), 0, s>>>(g, sh, B, r, r0, p, rc);
+    launch_pdl(k_bicg_start<T>, grid_of(sh), block_of(sh), 0, s, g, sh, B, r, r0, p, rc);
     PPS_COUNT_LAUNCH();
 }
 void cast_field_f32(const double* in, float* out, long long n, cudaStream_t s)
 {
     const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
-    k_cast_f32<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(in, out, n);
+    launch_pdl(k_cast_f32, (unsigned)std::max<long long>(blocks, 1), 256, 0, s, in, out, n);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void fill_field(T* p, long long n, T v, cudaStream_t s)
 {
-    k_fill<T><<<par_blocks(n), 256, 0, s>>>(p, n, v);
+    launch_pdl(k_fill<T>, par_blocks(n), 256, 0, s, p, n, v);
     PPS_COUNT_LAUNCH();
 }
 template <typename T>
 void zero_off_unknowns(const Geo& g, T* p, cudaStream_t s)
 {
-    k_zero_off_unknowns<T><<<par_blocks(g.ntot), 256, 0, s>>>(g, p);
+    launch_pdl(k_zero_off_unknowns<T>, par_blocks(g.ntot), 256, 0, s, g, p);
     PPS_COUNT_LAUNCH();
 }
 void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
                 int rho0_from_r, double hist_scale, int hist_cap, cudaStream_t s)
 {
-    k_state_init<<<1, 32, 0, s>>>(st, hist, maxit, tol_abs, tol_rel, tol_relative, rho0_from_r, hist_scale, hist_cap);
+    launch_pdl(k_state_init, 1, 32, 0, s, st, hist, maxit, tol_abs, tol_rel, tol_relative, rho0_from_r, hist_scale, hist_cap);
     PPS_COUNT_LAUNCH();
 }
 

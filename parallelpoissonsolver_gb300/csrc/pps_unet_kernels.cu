@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
                                               const bf16* __restrict__ Wt, const float* __restrict__ bias,
                                               void* __restrict__ Yv, int ldy, int cy0, int Cout, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     __shared__ __align__(32) bf16 sA[4][CONV_V * 16];
     __shared__ __align__(32) float sC[4][16 * 16];
@@ -103,11 +104,11 @@ void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W
 {
     const dim3 grid((unsigned)(((long long)d.D * d.H * d.W + CONV_V - 1) / CONV_V), (unsigned)(Cout / 16));
     if (out_f32) {
-        if (relu) k_conv<true, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else k_conv<false, true><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        if (relu) launch_pdl(k_conv<true, true>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else launch_pdl(k_conv<false, true>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
     } else {
-        if (relu) k_conv<true, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else k_conv<false, false><<<grid, 128, 0, s>>>(d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        if (relu) launch_pdl(k_conv<true, false>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else launch_pdl(k_conv<false, false>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
     }
     launches_counter_add(1);
 }
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(Dims d, const bf16* __restri
                                                     const bf16* __restrict__ G, int ldg, int cg0, int Cout,
                                                     float* __restrict__ dW)
 {
+    pdl_enter();
     __shared__ __align__(32) bf16 sX[TILE_V * 96];    // 64 voxels x Cin   (col-major A: ci x v)
     __shared__ __align__(32) bf16 sG[TILE_V * 96];    // 64 voxels x Cout  (row-major B: v x co)
     __shared__ __align__(32) float sC[96 * 96 / 4];   // staging of one warp's fragments
@@ -202,13 +204,14 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(Dims d, const bf16* __restri
 void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* G, int ldg, int cg0, int Cout,
                 float* dW, cudaStream_t s)
 {
-    k_conv_wgrad<<<(unsigned)(27 * d.D), 128, 0, s>>>(d, X, ldx, cx0, Cin, G, ldg, cg0, Cout, dW);
+    launch_pdl(k_conv_wgrad, (unsigned)(27 * d.D), 128, 0, s, d, X, ldx, cx0, Cin, G, ldg, cg0, Cout, dW);
     launches_counter_add(1);
 }
 
 // db[co] += sum_v G[v][co]
 __global__ void k_bias_grad(long long nv, const bf16* __restrict__ G, int ldg, int cg0, int Cout, float* __restrict__ db)
 {
+    pdl_enter();
     __shared__ float s[96];
     for (int c = threadIdx.x; c < Cout; c += blockDim.x) s[c] = 0.0f;
     __syncthreads();
@@ -226,7 +229,7 @@ void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* d
 {
     long long blocks = (nv * Cout + 255) / 256;
     if (blocks > 1024) blocks = 1024;
-    k_bias_grad<<<(unsigned)blocks, 256, 0, s>>>(nv, G, ldg, cg0, Cout, db);
+    launch_pdl(k_bias_grad, (unsigned)blocks, 256, 0, s, nv, G, ldg, cg0, Cout, db);
     launches_counter_add(1);
 }
 
@@ -234,6 +237,7 @@ void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* d
 __global__ void k_relu_bwd(long long nv, bf16* __restrict__ G, int ldg, int cg0, const bf16* __restrict__ Y, int ldy,
                            int cy0, int C)
 {
+    pdl_enter();
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv * C; q += (long long)gridDim.x * blockDim.x) {
         const long long v = q / C;
         const int c = (int)(q % C);
@@ -251,13 +255,14 @@ static unsigned eblocks(long long n)
 
 void relu_bwd(long long nv, bf16* G, int ldg, int cg0, const bf16* Y, int ldy, int cy0, int C, cudaStream_t s)
 {
-    k_relu_bwd<<<eblocks(nv * C), 256, 0, s>>>(nv, G, ldg, cg0, Y, ldy, cy0, C);
+    launch_pdl(k_relu_bwd, eblocks(nv * C), 256, 0, s, nv, G, ldg, cg0, Y, ldy, cy0, C);
     launches_counter_add(1);
 }
 
 // 2x average pooling: out (D/2,H/2,W/2) dense C channels <- in slot of ldi
 __global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0, bf16* __restrict__ out, int C, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const long long n = (long long)dout.D * dout.H * dout.W * C;
     const int Hi = dout.H * 2, Wi = dout.W * 2;
@@ -276,13 +281,14 @@ __global__ void k_pool2(Dims dout, const bf16* __restrict__ in, int ldi, int ci0
 
 void pool2(const Dims& dout, const bf16* in, int ldi, int ci0, bf16* out, int C, cudaStream_t s)
 {
-    k_pool2<<<eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s>>>(dout, in, ldi, ci0, out, C, g_stop);
+    launch_pdl(k_pool2, eblocks((long long)dout.D * dout.H * dout.W * C), 256, 0, s, dout, in, ldi, ci0, out, C, g_stop);
     launches_counter_add(1);
 }
 
 // pooling backward: gin slot (fine) += g_out/8 at each of the 8 children
 __global__ void k_pool2_bwd(Dims dout, const bf16* __restrict__ gout, bf16* __restrict__ gin, int ldi, int ci0, int C)
 {
+    pdl_enter();
     const int Hi = dout.H * 2, Wi = dout.W * 2;
     const long long n = (long long)dout.D * 8 * dout.H * dout.W * C;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -297,13 +303,14 @@ __global__ void k_pool2_bwd(Dims dout, const bf16* __restrict__ gout, bf16* __re
 
 void pool2_bwd(const Dims& dout, const bf16* gout, bf16* gin, int ldi, int ci0, int C, cudaStream_t s)
 {
-    k_pool2_bwd<<<eblocks((long long)dout.D * 8 * dout.H * dout.W * C), 256, 0, s>>>(dout, gout, gin, ldi, ci0, C);
+    launch_pdl(k_pool2_bwd, eblocks((long long)dout.D * 8 * dout.H * dout.W * C), 256, 0, s, dout, gout, gin, ldi, ci0, C);
     launches_counter_add(1);
 }
 
 // nearest 2x upsampling: out slot (fine) <- in dense (coarse)
 __global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __restrict__ out, int ldo, int co0, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const long long n = (long long)dfine.D * dfine.H * dfine.W * C;
     const int Hc = dfine.H / 2, Wc = dfine.W / 2;
@@ -317,13 +324,14 @@ __global__ void k_up2(Dims dfine, const bf16* __restrict__ in, int C, bf16* __re
 
 void up2(const Dims& dfine, const bf16* in, int C, bf16* out, int ldo, int co0, cudaStream_t s)
 {
-    k_up2<<<eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s>>>(dfine, in, C, out, ldo, co0, g_stop);
+    launch_pdl(k_up2, eblocks((long long)dfine.D * dfine.H * dfine.W * C), 256, 0, s, dfine, in, C, out, ldo, co0, g_stop);
     launches_counter_add(1);
 }
 
 // upsampling backward: gin (coarse dense) = sum of the 8 children of gout's slot
 __global__ void k_up2_bwd(Dims dcoarse, const bf16* __restrict__ gout, int ldo, int co0, bf16* __restrict__ gin, int C)
 {
+    pdl_enter();
     const long long n = (long long)dcoarse.D * dcoarse.H * dcoarse.W * C;
     const int Hf = dcoarse.H * 2, Wf = dcoarse.W * 2;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -342,13 +350,14 @@ __global__ void k_up2_bwd(Dims dcoarse, const bf16* __restrict__ gout, int ldo, 
 
 void up2_bwd(const Dims& dcoarse, const bf16* gout, int ldo, int co0, bf16* gin, int C, cudaStream_t s)
 {
-    k_up2_bwd<<<eblocks((long long)dcoarse.D * dcoarse.H * dcoarse.W * C), 256, 0, s>>>(dcoarse, gout, ldo, co0, gin, C);
+    launch_pdl(k_up2_bwd, eblocks((long long)dcoarse.D * dcoarse.H * dcoarse.W * C), 256, 0, s, dcoarse, gout, ldo, co0, gin, C);
     launches_counter_add(1);
 }
 
 // Wf[tap'][co][ci] = W[26-tap][ci][co]: the weights of the backward-data convolution.
 __global__ void k_flip(const bf16* __restrict__ W, bf16* __restrict__ Wf, int Cin, int Cout)
 {
+    pdl_enter();
     const int n = 27 * Cin * Cout;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const int co = q % Cout, ci = (q / Cout) % Cin, tap = q / (Cout * Cin);
@@ -358,7 +367,7 @@ __global__ void k_flip(const bf16* __restrict__ W, bf16* __restrict__ Wf, int Ci
 
 void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s)
 {
-    k_flip<<<(27 * Cin * Cout + 255) / 256, 256, 0, s>>>(W, Wf, Cin, Cout);
+    launch_pdl(k_flip, (27 * Cin * Cout + 255) / 256, 256, 0, s, W, Wf, Cin, Cout);
     launches_counter_add(1);
 }
 
@@ -367,6 +376,7 @@ void flip(const bf16* W, bf16* Wf, int Cin, int Cout, cudaStream_t s)
 __global__ void k_mse(long long nv, const float* __restrict__ out, int ldo, const float* __restrict__ t,
                       bf16* __restrict__ G, int ldg, double* loss)
 {
+    pdl_enter();
     double s = 0.0;
     const float inv = (float)(1.0 / (double)nv);
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
@@ -382,7 +392,7 @@ __global__ void k_mse(long long nv, const float* __restrict__ out, int ldo, cons
 
 void mse(long long nv, const float* out, int ldo, const float* t, bf16* G, int ldg, double* loss, cudaStream_t s)
 {
-    k_mse<<<eblocks(nv), 256, 0, s>>>(nv, out, ldo, t, G, ldg, loss);
+    launch_pdl(k_mse, eblocks(nv), 256, 0, s, nv, out, ldo, t, G, ldg, loss);
     launches_counter_add(1);
 }
 
@@ -393,6 +403,7 @@ __global__ void k_adam(long long n, float* __restrict__ p, const float* __restri
                        float* __restrict__ v, bf16* __restrict__ pb, float lr, float b1, float b2, float eps, float c1,
                        float c2, const float* g_rms, float max_norm)
 {
+    pdl_enter();
     float clip = 1.0f;
     if (g_rms) {
         const float norm = *g_rms * sqrtf((float)n);
@@ -415,19 +426,20 @@ void adam(long long n, float* p, const float* g, float* m, float* v, bf16* pb, f
           int step, const float* g_rms, float max_norm, cudaStream_t s)
 {
     const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-    k_adam<<<eblocks(n), 256, 0, s>>>(n, p, g, m, v, pb, lr, b1, b2, eps, c1, c2, g_rms, max_norm);
+    launch_pdl(k_adam, eblocks(n), 256, 0, s, n, p, g, m, v, pb, lr, b1, b2, eps, c1, c2, g_rms, max_norm);
     launches_counter_add(1);
 }
 
 __global__ void k_f32_to_bf16(long long n, const float* __restrict__ a, bf16* __restrict__ b)
 {
+    pdl_enter();
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
         b[q] = __float2bfloat16(a[q]);
 }
 
 void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s)
 {
-    k_f32_to_bf16<<<eblocks(n), 256, 0, s>>>(n, a, b);
+    launch_pdl(k_f32_to_bf16, eblocks(n), 256, 0, s, n, a, b);
     launches_counter_add(1);
 }
 
@@ -435,6 +447,7 @@ void f32_to_bf16(long long n, const float* a, bf16* b, cudaStream_t s)
 // (rms == nullptr: scale 1); the other channels zero.
 __global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const float* rms, bf16* __restrict__ act, int ld, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const float sc = rms ? (*rms > 0.0f ? 1.0f / *rms : 0.0f) : 1.0f;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
@@ -445,7 +458,7 @@ __global__ void k_dense_to_act(long long nv, const float* __restrict__ in, const
 
 void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, int ld, cudaStream_t s)
 {
-    k_dense_to_act<<<eblocks(nv), 256, 0, s>>>(nv, in, rms, act, ld, g_stop);
+    launch_pdl(k_dense_to_act, eblocks(nv), 256, 0, s, nv, in, rms, act, ld, g_stop);
     launches_counter_add(1);
 }
 
@@ -453,6 +466,7 @@ void dense_to_act(long long nv, const float* in, const float* rms, bf16* act, in
 __global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int ld, const float* rms, float gain,
                                float* __restrict__ dense, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const float sc = (rms ? *rms : 1.0f) * gain;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x)
@@ -461,13 +475,14 @@ __global__ void k_out_to_dense(long long nv, const float* __restrict__ out, int 
 
 void out_to_dense(long long nv, const float* out, int ld, const float* rms, float gain, float* dense, cudaStream_t s)
 {
-    k_out_to_dense<<<eblocks(nv), 256, 0, s>>>(nv, out, ld, rms, gain, dense, g_stop);
+    launch_pdl(k_out_to_dense, eblocks(nv), 256, 0, s, nv, out, ld, rms, gain, dense, g_stop);
     launches_counter_add(1);
 }
 
 // rms of a dense FP32 array into *rms (single block, deterministic)
 __global__ void k_rms(long long n, const float* __restrict__ a, float* rms, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     __shared__ double sm[32];
     double s = 0.0;
@@ -485,7 +500,7 @@ __global__ void k_rms(long long n, const float* __restrict__ a, float* rms, cons
 
 void rms(long long n, const float* a, float* out, cudaStream_t s)
 {
-    k_rms<<<1, 1024, 0, s>>>(n, a, out, g_stop);
+    launch_pdl(k_rms, 1, 1024, 0, s, n, a, out, g_stop);
     launches_counter_add(1);
 }
 
@@ -509,6 +524,7 @@ __device__ __forceinline__ long long field_at(const Geo& g, int i, int j, int k)
 template <typename T>
 __global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restrict__ dense, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
@@ -520,6 +536,7 @@ __global__ void k_field_to_dense(Geo g, const T* __restrict__ f, float* __restri
 template <typename T>
 __global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __restrict__ f, float scale, int add, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
@@ -532,7 +549,7 @@ __global__ void k_dense_to_field(Geo g, const float* __restrict__ dense, T* __re
 template <typename T>
 void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
 {
-    k_field_to_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+    launch_pdl(k_field_to_dense<T>, field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s,
         g, f, dense, g_stop);
     launches_counter_add(1);
 }
@@ -540,7 +557,7 @@ void field_to_dense(const Geo& g, const T* f, float* dense, cudaStream_t s)
 template <typename T>
 void dense_to_field(const Geo& g, const float* dense, T* f, float scale, int add, cudaStream_t s)
 {
-    k_dense_to_field<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+    launch_pdl(k_dense_to_field<T>, field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s,
         g, dense, f, scale, add, g_stop);
     launches_counter_add(1);
 }
@@ -588,6 +605,7 @@ template <typename T>
 __global__ void k_field_residual_dense(Geo g, const T* __restrict__ r, const T* __restrict__ z, StencilW<T> w,
                                        float* __restrict__ dense, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1];
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
@@ -625,6 +643,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_field_residual(Geo g, Shape sh, const T* __restrict__ r,
                                                         const T* __restrict__ z, StencilW<T> w, T* __restrict__ out, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
@@ -647,6 +666,7 @@ __global__ void __launch_bounds__(256) k_field_residual(Geo g, Shape sh, const T
 template <typename T>
 __global__ void __launch_bounds__(256) k_field_axpy(Geo g, Shape sh, T* __restrict__ x, const T* __restrict__ y, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
@@ -666,6 +686,7 @@ __global__ void __launch_bounds__(128) k_field_residual_restrict(Geo g, const T*
                                                                  const T* __restrict__ z, StencilW<T> w, Dims dc,
                                                                  int zc, float* __restrict__ coarse, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dc.W || y >= dc.H) return;
@@ -755,6 +776,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_prolong_add_field(Geo g, Shape sh, Dims dc, const float* __restrict__ coarse,
                                                            T* __restrict__ f, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const ZCol q = zcolumn(g, sh);
     if (!q.active) return;
@@ -952,6 +974,7 @@ __global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, D
                                                               const float* __restrict__ r, const float* __restrict__ Ap,
                                                               RedCtx rc)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
     const int i0 = bx * 128 + threadIdx.x * 4;
@@ -969,20 +992,20 @@ __global__ void __launch_bounds__(256) k_prolong_add_field_v4(Geo g, Shape sh, D
 template <typename T>
 void field_residual_dense(const Geo& g, const T* r, const T* z, float* dense, cudaStream_t s)
 {
-    k_field_residual_dense<T><<<field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s>>>(
+    launch_pdl(k_field_residual_dense<T>, field_grid(g.hi[0] - g.lo[0], g.hi[1] - g.lo[1], g.hi[2] - g.lo[2], 128), 128, 0, s,
         g, r, z, stencil_w<T>(g), dense, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
 void field_residual(const Geo& g, const Shape& sh, const T* r, const T* z, T* out, cudaStream_t s)
 {
-    k_field_residual<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, r, z, stencil_w<T>(g), out, g_stop);
+    launch_pdl(k_field_residual<T>, zgrid(sh), zblock(sh), 0, s, g, sh, r, z, stencil_w<T>(g), out, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
 void field_axpy(const Geo& g, const Shape& sh, T* x, const T* y, cudaStream_t s)
 {
-    k_field_axpy<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, x, y, g_stop);
+    launch_pdl(k_field_axpy<T>, zgrid(sh), zblock(sh), 0, s, g, sh, x, y, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
@@ -991,8 +1014,8 @@ void field_residual_restrict(const Geo& g, const T* r, const T* z, const Dims& d
     const int zc = 8;
     const dim3 block(32, 4);
     const dim3 grid((unsigned)((dc.W + 31) / 32), (unsigned)((dc.H + 3) / 4), (unsigned)((dc.D + zc - 1) / zc));
-    if (z) k_field_residual_restrict<T, true><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
-    else k_field_residual_restrict<T, false><<<grid, block, 0, s>>>(g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
+    if (z) launch_pdl(k_field_residual_restrict<T, true>, grid, block, 0, s, g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
+    else launch_pdl(k_field_residual_restrict<T, false>, grid, block, 0, s, g, r, z, stencil_w<T>(g), dc, zc, coarse, g_stop);
     launches_counter_add(1);
 }
 template <typename T>
@@ -1004,10 +1027,10 @@ bool prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const floa
             auto a16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
             if (g.sj % 4 == 0 && a16(f)) {
                 if (dots && r && Ap && a16(r) && a16(Ap))
-                    k_prolong_add_field_v4<true><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop, r, Ap,
+                    launch_pdl(k_prolong_add_field_v4<true>, zgrid(sh), zblock(sh), 0, s, g, sh, dc, coarse, f, g_stop, r, Ap,
                                                                                  *dots);
                 else
-                    k_prolong_add_field_v4<false><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop,
+                    launch_pdl(k_prolong_add_field_v4<false>, zgrid(sh), zblock(sh), 0, s, g, sh, dc, coarse, f, g_stop,
                                                                                   nullptr, nullptr, RedCtx{});
                 launches_counter_add(1);
                 return dots && r && Ap && a16(r) && a16(Ap);
@@ -1015,7 +1038,7 @@ bool prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const floa
         }
         return prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
     }
-    k_prolong_add_field<T><<<zgrid(sh), zblock(sh), 0, s>>>(g, sh, dc, coarse, f, g_stop);
+    launch_pdl(k_prolong_add_field<T>, zgrid(sh), zblock(sh), 0, s, g, sh, dc, coarse, f, g_stop);
     launches_counter_add(1);
     return false;
 }
@@ -1057,6 +1080,7 @@ __global__ void __launch_bounds__(256) k_level_pass(Dims d, DLevel L, int kchunk
                                                     const float* __restrict__ B, const float* __restrict__ Z,
                                                     float* __restrict__ W, LCoef c, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= d.W || y >= d.H) return;
@@ -1154,6 +1178,7 @@ __global__ void __launch_bounds__(128) k_level_residual_restrict(Dims dc, DLevel
                                                                  const float* __restrict__ B,
                                                                  float* __restrict__ coarse, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dc.W || y >= dc.H) return;
@@ -1251,7 +1276,7 @@ void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, co
     chunks = std::max(1LL, std::min(chunks, (long long)dc.D));
     const int zc = (int)((dc.D + chunks - 1) / chunks);
     const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((dc.D + zc - 1) / zc));
-    k_level_residual_restrict<<<grid, dim3(32, 4), 0, s>>>(dc, L, zc, Y, B, coarse, g_stop);
+    launch_pdl(k_level_residual_restrict, grid, dim3(32, 4), 0, s, dc, L, zc, Y, B, coarse, g_stop);
     launches_counter_add(1);
 }
 
@@ -1260,7 +1285,7 @@ void level_residual(const Dims& d, const DLevel& L, const float* Y, const float*
     int kchunk;
     dim3 grid;
     level_launch(d, kchunk, grid);
-    k_level_pass<false, false, false, false><<<grid, dim3(32, 8), 0, s>>>(d, L, kchunk, Y, B, nullptr, W, LCoef{}, g_stop);
+    launch_pdl(k_level_pass<false, false, false, false>, grid, dim3(32, 8), 0, s, d, L, kchunk, Y, B, nullptr, W, LCoef{}, g_stop);
     launches_counter_add(1);
 }
 
@@ -1272,14 +1297,14 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
     level_launch(d, kchunk, grid, first ? 1 : 4);
     const dim3 blk(32, 8);
     if (first) {
-        if (acc) k_level_pass<true, true, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
-        else k_level_pass<true, true, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        if (acc) launch_pdl(k_level_pass<true, true, false, true>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else launch_pdl(k_level_pass<true, true, false, false>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
     } else if (Z) {
-        if (acc) k_level_pass<true, false, true, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
-        else k_level_pass<true, false, true, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        if (acc) launch_pdl(k_level_pass<true, false, true, true>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else launch_pdl(k_level_pass<true, false, true, false>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
     } else {
-        if (acc) k_level_pass<true, false, false, true><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
-        else k_level_pass<true, false, false, false><<<grid, blk, 0, s>>>(d, L, kchunk, Y, B, Z, W, c, g_stop);
+        if (acc) launch_pdl(k_level_pass<true, false, false, true>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
+        else launch_pdl(k_level_pass<true, false, false, false>, grid, blk, 0, s, d, L, kchunk, Y, B, Z, W, c, g_stop);
     }
     launches_counter_add(1);
 }
@@ -1289,6 +1314,7 @@ void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, 
 // per axis; fine values beyond the grid are the Dirichlet zero.
 __global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __restrict__ coarse, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= dc.W) return;
@@ -1316,7 +1342,7 @@ __global__ void k_restrict(Dims dc, const float* __restrict__ fine, float* __res
 
 void restrict2(const Dims& dc, const float* fine, float* coarse, cudaStream_t s)
 {
-    k_restrict<<<field_grid(dc.W, dc.H, dc.D, 128), 128, 0, s>>>(dc, fine, coarse, g_stop);
+    launch_pdl(k_restrict, field_grid(dc.W, dc.H, dc.D, 128), 128, 0, s, dc, fine, coarse, g_stop);
     launches_counter_add(1);
 }
 
@@ -1331,6 +1357,7 @@ template <bool ADD>
 __global__ void __launch_bounds__(256) k_prolong_z(Dims dc, int ntx, int cchunk, const float* __restrict__ coarse,
                                                    float* __restrict__ fine, const int* __restrict__ stop)
 {
+    pdl_enter();
     if (stop && *(volatile const int*)stop) return;
     const int Wf = 2 * dc.W, Hf = 2 * dc.H;
     const int x = (int)(blockIdx.x % ntx) * 32 + threadIdx.x;
@@ -1396,7 +1423,7 @@ static void prolong_z(const Dims& dc, const float* coarse, float* fine, cudaStre
     chunks = std::max(1LL, std::min<long long>(chunks, dc.D));
     const int cchunk = (int)((dc.D + chunks - 1) / chunks);
     const unsigned nch = (unsigned)((dc.D + cchunk - 1) / cchunk);
-    k_prolong_z<ADD><<<dim3((unsigned)tiles, nch), dim3(32, ty), 0, s>>>(dc, ntx, cchunk, coarse, fine, g_stop);
+    launch_pdl(k_prolong_z<ADD>, dim3((unsigned)tiles, nch), dim3(32, ty), 0, s, dc, ntx, cchunk, coarse, fine, g_stop);
     launches_counter_add(1);
 }
 
