@@ -1,6 +1,7 @@
 """One capped solve of the benchmark workload, sized for profiling.
 
     python -m parallelpoissonsolver_gb300.profile_case --size 320 --form mixed --maxit 2
+    python -m parallelpoissonsolver_gb300.profile_case --size 320 --krylov fcg --maxit 3
     python -m parallelpoissonsolver_gb300.profile_case --save-net net.npz          # train the U-Net, save
     python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --maxit 8
     python -m parallelpoissonsolver_gb300.profile_case --size 512 --learned net.npz --cycle 5,4,8 --maxit 20000 \
@@ -38,6 +39,8 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=3e-3)
     ap.add_argument("--post-smooth", action="store_true", help="Chebyshev post-smoothing on the solver's grid")
     ap.add_argument("--refinements", type=int, default=1)
+    ap.add_argument("--krylov", default="bicgstab", choices=("bicgstab", "fcg"),
+                    help="Krylov loop without --learned (fcg: flexible CG with the Chebyshev preconditioner)")
     a = ap.parse_args()
     if a.save_net:
         from parallelpoissonsolver_gb300 import learned
@@ -74,8 +77,9 @@ def main():
             fd, cd, ratio = a.cycle.split(",")
             s.set_learned_cycle(int(fd), int(cd), float(ratio))
     else:
-        s = pps.BiCGSTAB(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
-                         form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)
+        cls = pps.FlexibleCG if a.krylov == "fcg" else pps.BiCGSTAB
+        s = cls(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
+                form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)
     for _ in range(a.repeat):
         x = grid.new_field()
         st = s(x, b.copy(), raise_on_error=True)
