@@ -540,7 +540,7 @@ pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* 
         std::vector<unsigned char> dev(hc.size() * b_coef_size());
         b_cast_coef(hc.data(), dev.data(), hc.size());
         BK(cudaMalloc(&s->coef, dev.size()));
-        BK(cudaMemcpy(s->coef, dev.data(), dev.size(), cudaMemcpyHostToDevice));
+        BK(cudaMemcpyAsync(s->coef, dev.data(), dev.size(), cudaMemcpyHostToDevice, s->stream));
         BK(cudaStreamSynchronize(s->stream));
         return PPS_OK;
     });

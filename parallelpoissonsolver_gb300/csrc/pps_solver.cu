@@ -1855,7 +1855,9 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
             s->sweep_ev.resize((size_t)std::min(pairs, 20000) * 2);
             for (auto& e : s->sweep_ev) CK(cudaEventCreate(&e));
         }
-        CK(cudaStreamSynchronize(s->stream));
+        // the zero fills above ran on the legacy stream, which the handle's non-blocking
+        // stream does not wait for: finish them before the handle is used
+        CK(cudaDeviceSynchronize());
         std::memset(&s->stats, 0, sizeof(s->stats));
         return PPS_OK;
     });
@@ -1952,7 +1954,9 @@ pps_status pps_set_neumann(pps_solver* s, int face, const double* values)
     }
     return guarded([&]() -> pps_status {
         CK(cudaSetDevice(s->device));
-        CK(cudaMemcpy(s->d_faces[face], values, sizeof(double) * (size_t)face_count(s, face), cudaMemcpyHostToDevice));
+        CK(cudaMemcpyAsync(s->d_faces[face], values, sizeof(double) * (size_t)face_count(s, face),
+                           cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
         return PPS_OK;
     });
 }

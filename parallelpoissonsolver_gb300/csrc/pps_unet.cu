@@ -98,11 +98,13 @@ void free_acts(Acts& A)
     A = Acts();
 }
 
-bf16* balloc(long long n)
+// Zeroed on `s`, the stream whose kernels use the buffer next (the legacy stream's
+// fills are not ordered with the library's non-blocking streams).
+bf16* balloc(long long n, cudaStream_t s)
 {
     bf16* p = nullptr;
     UK(cudaMalloc((void**)&p, sizeof(bf16) * (size_t)n));
-    UK(cudaMemset(p, 0, sizeof(bf16) * (size_t)n));
+    UK(cudaMemsetAsync(p, 0, sizeof(bf16) * (size_t)n, s));
     return p;
 }
 
@@ -116,34 +118,34 @@ void ensure_acts(pps_unet* u, int nx, int ny, int nz, bool grads)
     A.s3 = Dims{nz / 4, ny / 4, nx / 4};
     const long long v1 = (long long)nx * ny * nz, v2 = v1 / 8, v3 = v2 / 8;
     const int c1 = u->c1, c2 = u->c2, c3 = u->c3;
-    A.x0 = balloc(v1 * 16);
-    A.e1a = balloc(v1 * c1);
-    A.cat1 = balloc(v1 * (c2 + c1));
-    A.d1a = balloc(v1 * c1);
-    A.d1 = balloc(v1 * c1);
-    A.p1 = balloc(v2 * c1);
-    A.e2a = balloc(v2 * c2);
-    A.cat2 = balloc(v2 * (c3 + c2));
-    A.d2a = balloc(v2 * c2);
-    A.d2 = balloc(v2 * c2);
-    A.p2 = balloc(v3 * c2);
-    A.e3a = balloc(v3 * c3);
-    A.e3 = balloc(v3 * c3);
+    A.x0 = balloc(v1 * 16, u->stream);
+    A.e1a = balloc(v1 * c1, u->stream);
+    A.cat1 = balloc(v1 * (c2 + c1), u->stream);
+    A.d1a = balloc(v1 * c1, u->stream);
+    A.d1 = balloc(v1 * c1, u->stream);
+    A.p1 = balloc(v2 * c1, u->stream);
+    A.e2a = balloc(v2 * c2, u->stream);
+    A.cat2 = balloc(v2 * (c3 + c2), u->stream);
+    A.d2a = balloc(v2 * c2, u->stream);
+    A.d2 = balloc(v2 * c2, u->stream);
+    A.p2 = balloc(v3 * c2, u->stream);
+    A.e3a = balloc(v3 * c3, u->stream);
+    A.e3 = balloc(v3 * c3, u->stream);
     UK(cudaMalloc((void**)&A.out, sizeof(float) * (size_t)v1 * 16));
     if (grads) {
-        A.g_out = balloc(v1 * 16);
-        A.g_d1 = balloc(v1 * c1);
-        A.g_d1a = balloc(v1 * c1);
-        A.g_cat1 = balloc(v1 * (c2 + c1));
-        A.g_d2 = balloc(v2 * c2);
-        A.g_d2a = balloc(v2 * c2);
-        A.g_cat2 = balloc(v2 * (c3 + c2));
-        A.g_e3 = balloc(v3 * c3);
-        A.g_e3a = balloc(v3 * c3);
-        A.g_p2 = balloc(v3 * c2);
-        A.g_e2a = balloc(v2 * c2);
-        A.g_p1 = balloc(v2 * c1);
-        A.g_e1a = balloc(v1 * c1);
+        A.g_out = balloc(v1 * 16, u->stream);
+        A.g_d1 = balloc(v1 * c1, u->stream);
+        A.g_d1a = balloc(v1 * c1, u->stream);
+        A.g_cat1 = balloc(v1 * (c2 + c1), u->stream);
+        A.g_d2 = balloc(v2 * c2, u->stream);
+        A.g_d2a = balloc(v2 * c2, u->stream);
+        A.g_cat2 = balloc(v2 * (c3 + c2), u->stream);
+        A.g_e3 = balloc(v3 * c3, u->stream);
+        A.g_e3a = balloc(v3 * c3, u->stream);
+        A.g_p2 = balloc(v3 * c2, u->stream);
+        A.g_e2a = balloc(v2 * c2, u->stream);
+        A.g_p1 = balloc(v2 * c1, u->stream);
+        A.g_e1a = balloc(v1 * c1, u->stream);
         A.grads = true;
     }
 }
@@ -315,7 +317,7 @@ pps_status pps_unet_create(int c1, int c2, int c3, unsigned long long seed, int 
         float** f[] = {&u->P, &u->G, &u->M, &u->V};
         for (float** q : f) {
             UK(cudaMalloc((void**)q, sizeof(float) * u->npad));
-            UK(cudaMemset(*q, 0, sizeof(float) * u->npad));
+            UK(cudaMemsetAsync(*q, 0, sizeof(float) * u->npad, u->stream));
         }
         UK(cudaMalloc((void**)&u->PB, sizeof(bf16) * u->npad));
         UK(cudaMalloc((void**)&u->WF, sizeof(bf16) * 27 * 96 * 96));
@@ -331,7 +333,7 @@ pps_status pps_unet_create(int c1, int c2, int c3, unsigned long long seed, int 
                     for (int co = 0; co < l.cout; co++)
                         h[l.w + ((size_t)t * l.cin_p + ci) * l.cout_p + co] = nd(rng) * (l.relu ? 1.0f : 0.1f);
         }
-        UK(cudaMemcpy(u->P, h.data(), sizeof(float) * u->npad, cudaMemcpyHostToDevice));
+        UK(cudaMemcpyAsync(u->P, h.data(), sizeof(float) * u->npad, cudaMemcpyHostToDevice, u->stream));
         f32_to_bf16((long long)u->npad, u->P, u->PB, u->stream);
         UK(cudaStreamSynchronize(u->stream));
         return PPS_OK;
@@ -385,7 +387,8 @@ pps_status pps_unet_get_params(const pps_unet* u, float* out)
     return uguard([&]() -> pps_status {
         UK(cudaSetDevice(u->device));
         std::vector<float> h(u->npad);
-        UK(cudaMemcpy(h.data(), u->P, sizeof(float) * u->npad, cudaMemcpyDeviceToHost));
+        UK(cudaMemcpyAsync(h.data(), u->P, sizeof(float) * u->npad, cudaMemcpyDeviceToHost, u->stream));
+        UK(cudaStreamSynchronize(u->stream));
         pack(u, h, out);
         return PPS_OK;
     });
@@ -404,9 +407,9 @@ pps_status pps_unet_set_params(pps_unet* u, const float* in)
                         h[l.w + ((size_t)t * l.cin_p + ci) * l.cout_p + co] = in[l.rw + ((size_t)t * l.cin + ci) * l.cout + co];
             for (int co = 0; co < l.cout; co++) h[l.b + co] = in[l.rb + co];
         }
-        UK(cudaMemcpy(u->P, h.data(), sizeof(float) * u->npad, cudaMemcpyHostToDevice));
-        UK(cudaMemset(u->M, 0, sizeof(float) * u->npad));
-        UK(cudaMemset(u->V, 0, sizeof(float) * u->npad));
+        UK(cudaMemcpyAsync(u->P, h.data(), sizeof(float) * u->npad, cudaMemcpyHostToDevice, u->stream));
+        UK(cudaMemsetAsync(u->M, 0, sizeof(float) * u->npad, u->stream));
+        UK(cudaMemsetAsync(u->V, 0, sizeof(float) * u->npad, u->stream));
         u->step = 0;
         f32_to_bf16((long long)u->npad, u->P, u->PB, u->stream);
         UK(cudaStreamSynchronize(u->stream));
@@ -458,7 +461,8 @@ pps_status pps_unet_gradients(pps_unet* u, int nx, int ny, int nz, const float* 
         pps_status rc = loss_and_grads(u, nx, ny, nz, in_dev, target_dev, loss);
         if (rc != PPS_OK) return rc;
         std::vector<float> h(u->npad);
-        UK(cudaMemcpy(h.data(), u->G, sizeof(float) * u->npad, cudaMemcpyDeviceToHost));
+        UK(cudaMemcpyAsync(h.data(), u->G, sizeof(float) * u->npad, cudaMemcpyDeviceToHost, u->stream));
+        UK(cudaStreamSynchronize(u->stream));
         pack(u, h, grads);
         return PPS_OK;
     });
