@@ -182,7 +182,9 @@ pps_status pps_set_neumann(pps_solver* s, int face, const double* values);
  * The MIXED form applies the polynomial in FP32 to the FP64 residual up to
  * max_refinements + 1 times, stopping at tol (iterations: degree x passes). */
 pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats);
-/* The same with device pointers (fields already resident in HBM). */
+/* The same with device pointers (fields already resident in HBM).  The solver's
+ * stream is non-blocking: work that writes x_dev or b_dev on another stream must be
+ * complete before the call (the call returns with the solve finished). */
 pps_status pps_solve_device(pps_solver* s, double* x_dev, double* b_dev, pps_stats* stats);
 
 /* Getters (iterativeSolverBase.hpp:410-425; iterativeSolverBaseAlpaka.hpp:599-640). */
@@ -284,7 +286,9 @@ int pps_unet_param_count(const pps_unet* net);
 pps_status pps_unet_set_activation(pps_unet* net, int linear);
 pps_status pps_unet_get_params(const pps_unet* net, float* out);
 pps_status pps_unet_set_params(pps_unet* net, const float* in);
-/* normalize = 1: the input is scaled to unit RMS and the output scaled back. */
+/* normalize = 1: the input is scaled to unit RMS and the output scaled back.
+ * The network's calls run on its own non-blocking stream and return with their work
+ * finished; device inputs written on another stream must be complete before the call. */
 pps_status pps_unet_forward(pps_unet* net, int nx, int ny, int nz, const float* in_dev, float* out_dev,
                             int normalize);
 /* MSE loss of the (unnormalised) output against target, and its gradient (host array

@@ -154,6 +154,7 @@ def train(net: "pps.UNet", data, scale: float, steps: int, lr: float = 2e-3, see
         rb = torch.sqrt(torch.mean(b * b))
         prepared.append(((b / rb).contiguous(), (u / (rb * scale)).contiguous()))
     shape = tuple(data[0][0].shape)
+    torch.cuda.synchronize()   # the network's stream does not wait for torch's
     losses = []
     t0 = time.perf_counter()
     for k in range(steps):
@@ -171,6 +172,7 @@ def evaluate(net: "pps.UNet", data, scale: float):
     """Relative L2 error of scale * rms(b) * N(b/rms(b)) against u for each sample."""
     import torch
     errs = []
+    torch.cuda.synchronize()   # the network's stream does not wait for torch's
     for b, u in data:
         out = torch.empty_like(b)
         net.forward(tuple(b.shape), b.data_ptr(), out.data_ptr(), normalize=True)
