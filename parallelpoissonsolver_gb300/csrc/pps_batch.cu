@@ -272,8 +272,10 @@ void free_batch(pps_batch* s)
 template <typename Fn>
 pps_status bguard(Fn&& fn)
 {
+    const unsigned long long f0 = launch_failures();
     try {
-        return fn();
+        const pps_status rc = fn();
+        return rc >= 0 && launch_failures() != f0 ? PPS_ERR_CUDA : rc;
     } catch (const Fail&) {
         return PPS_ERR_CUDA;
     } catch (const std::bad_alloc&) {

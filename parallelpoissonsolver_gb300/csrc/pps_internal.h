@@ -24,6 +24,12 @@ __device__ __forceinline__ void pdl_enter()
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 #endif
+// Kernel launches that failed on this thread.  A failed launch leaves no sticky CUDA
+// error for a later synchronisation to report, so the entry points compare this count
+// before and after their work and return PPS_ERR_CUDA when it grew.
+unsigned long long launch_failures();
+void note_launch_failure(cudaError_t e);
+
 template <typename... KArgs, typename... Args>
 inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args)
 {
@@ -37,7 +43,8 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+    if (e != cudaSuccess) note_launch_failure(e);
 }
 
 // Geometry of one single-rank grid in the guard-padded field layout

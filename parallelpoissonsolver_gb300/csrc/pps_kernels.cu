@@ -20,6 +20,7 @@
 
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdio.h>
 
 namespace pps {
 
@@ -28,6 +29,16 @@ static thread_local int g_launches = 0;
 int launches_counter_reset() { int v = g_launches; g_launches = 0; return v; }
 int launches_counter() { return g_launches; }
 void launches_counter_add(int d) { g_launches += d; }
+static thread_local unsigned long long g_launch_failures = 0;
+unsigned long long launch_failures() { return g_launch_failures; }
+void note_launch_failure(cudaError_t e)
+{
+    ++g_launch_failures;
+    const char* what = cudaGetErrorString(e);
+    char msg[160];
+    snprintf(msg, sizeof(msg), "kernel launch failed: %s", what ? what : "unknown error");
+    pps_internal_set_error(msg);
+}
 #define PPS_COUNT_LAUNCH() (++g_launches)
 
 // ---------------------------------------------------------------------------

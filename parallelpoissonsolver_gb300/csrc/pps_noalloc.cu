@@ -107,6 +107,7 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
     double* partials = (double*)(base + kPartialsOffset);
     // The array keeps the previous call's contents: reset the scalar block (done = 0)
     // and the completion counter, which the kernel needs at zero.
+    const unsigned long long failures = launch_failures();
     state_init(st, nullptr, 0, 0.0, 0.0, 0, 0, 1.0, 0, s);
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
@@ -129,6 +130,7 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
     fast_stencil_dot<double>(g, sh, u_dev, u_dev, out_dev, a, rc, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    if (launch_failures() != failures) return PPS_ERR_CUDA;   // the message is set already
     e = cudaMemcpyAsync(energy_dev, &st->sums[0], sizeof(double), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
     return PPS_OK;

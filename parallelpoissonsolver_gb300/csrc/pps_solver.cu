@@ -1641,8 +1641,10 @@ void coords(const pps_solver* s, int i, int j, int k, double* x, double* y, doub
 template <typename Fn>
 pps_status guarded(Fn&& fn)
 {
+    const unsigned long long f0 = launch_failures();
     try {
-        return fn();
+        const pps_status rc = fn();
+        return rc >= 0 && launch_failures() != f0 ? PPS_ERR_CUDA : rc;
     } catch (const CudaFail&) {
         return PPS_ERR_CUDA;
     } catch (const std::bad_alloc&) {

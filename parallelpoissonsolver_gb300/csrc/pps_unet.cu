@@ -243,8 +243,10 @@ pps_status check_dims(int nx, int ny, int nz)
 template <typename Fn>
 pps_status uguard(Fn&& fn)
 {
+    const unsigned long long f0 = pps::launch_failures();
     try {
-        return fn();
+        const pps_status rc = fn();
+        return rc >= 0 && pps::launch_failures() != f0 ? PPS_ERR_CUDA : rc;
     } catch (const UFail&) {
         return PPS_ERR_CUDA;
     } catch (const std::bad_alloc&) {
