@@ -158,6 +158,9 @@ def lib():
         L.ora_solve.argtypes = [C.POINTER(OraGrid), C.POINTER(OraConfig), dp, dp, C.c_void_p, C.c_void_p,
                                 C.POINTER(OraStats)]
         L.ora_solve.restype = C.c_int
+        L.ora_solve_stamped.argtypes = [C.POINTER(OraGrid), C.POINTER(OraConfig), dp, dp, C.c_void_p,
+                                        C.c_void_p, C.POINTER(OraStats), C.c_void_p]
+        L.ora_solve_stamped.restype = C.c_int
         L.ora_eigen_bounds.argtypes = [C.POINTER(OraGrid), C.POINTER(C.c_double)]
         L.ora_cheb_params.argtypes = [C.POINTER(OraGrid), C.POINTER(OraConfig), C.POINTER(C.c_double)]
         L.ora_apply_A.argtypes = [C.POINTER(OraGrid), dp, dp]
@@ -237,6 +240,24 @@ def solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, neumann=None) -
         raise ValueError("oracle rejected the configuration")
     return Result(st.iterations, st.err_iter, st.err_true, st.norm_b, st.seconds_loop, st.seconds_total,
                   hist[: st.iterations + 1].copy(), st.prec_iterations)
+
+
+def solve_stamped(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray):
+    """solve() for BiCGSTAB, also returning wall-clock stamps: [call start, end of
+    iteration 1, ..., end of the last iteration, call end] (seconds, monotonic)."""
+    assert cfg.krylov == BICGSTAB
+    assert x.shape == grid.shape and b.shape == grid.shape
+    hist = np.full(cfg.maxit + 1, -1.0)
+    stamps = np.zeros(cfg.maxit + 2)
+    st = OraStats()
+    rc = lib().ora_solve_stamped(C.byref(grid.c()), C.byref(cfg.c()), x, b, None, hist.ctypes.data, C.byref(st),
+                                 stamps.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle rejected the configuration")
+    n = st.iterations
+    res = Result(n, st.err_iter, st.err_true, st.norm_b, st.seconds_loop, st.seconds_total, hist[: n + 1].copy(),
+                 st.prec_iterations)
+    return res, stamps[: n + 2].copy()
 
 
 def ref_solve(grid: Grid, cfg: Config, x: np.ndarray, b: np.ndarray, problem: int = 0, neumann=None) -> Result:

@@ -31,6 +31,7 @@ typedef struct {
     double ds[3], origin[3];
     int bcs[6];
     int nthreads;
+    double* stamps;          /* main loop: wall clock at the end of each iteration */
 } grid_t;
 
 static int make_grid(const ora_grid* g, int threads, grid_t* G)
@@ -55,6 +56,7 @@ static int make_grid(const ora_grid* g, int threads, grid_t* G)
         G->hi[d] = G->dhi[d] - (g->bcs[2 * d + 1] == 0 ? 1 : 0);
     }
     G->nthreads = threads > 0 ? threads : 1;
+    G->stamps = NULL;
     return 0;
 }
 
@@ -388,6 +390,7 @@ static int bicgstab_loop(const grid_t* G, prec_t* P, bicg_t* W, double* x, doubl
         }
         iter++;
         if (hist) hist[iter] = *err_iter;
+        if (hist && G->stamps) G->stamps[iter] = now_s();
         if (*err_iter < toll) break;
     }
     return iter;
@@ -608,12 +611,13 @@ static void prec_free(prec_t* P)
     if (P->kind == ORA_PREC_BICGSTAB || P->kind == ORA_PREC_CG) bicg_free(&P->W);
 }
 
-int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
-              const double* const* neumann, double* history, ora_stats* st)
+static int solve_impl(const ora_grid* g, const ora_config* c, double* x, double* b,
+                      const double* const* neumann, double* history, ora_stats* st, double* stamps)
 {
     grid_t G;
     if (!g || !c || !x || !b || !st) return -1;
     if (make_grid(g, c->threads, &G) != 0) return -1;
+    G.stamps = stamps;
     if (c->maxit < 0 || c->cheb_degree < 1) return -1;
     if (c->krylov != ORA_BICGSTAB && c->krylov != ORA_CG && c->krylov != ORA_CHEBYSHEV_MAIN) return -1;
     if (c->precond < ORA_PREC_NONE || c->precond > ORA_PREC_CG) return -1;
@@ -649,6 +653,22 @@ int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
     if (nested) prec_free(&Pin);
     prec_free(&P);
     st->seconds_total = now_s() - t0;
+    return rc;
+}
+
+int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
+              const double* const* neumann, double* history, ora_stats* st)
+{
+    return solve_impl(g, c, x, b, neumann, history, st, NULL);
+}
+
+int ora_solve_stamped(const ora_grid* g, const ora_config* c, double* x, double* b,
+                      const double* const* neumann, double* history, ora_stats* st, double* stamps)
+{
+    if (!stamps || !history || c == NULL || c->krylov != ORA_BICGSTAB) return -1;
+    stamps[0] = now_s();
+    const int rc = solve_impl(g, c, x, b, neumann, history, st, stamps);
+    if (rc == 0) stamps[st->iterations + 1] = now_s();
     return rc;
 }
 

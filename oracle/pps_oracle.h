@@ -84,6 +84,14 @@ typedef struct {
 int ora_solve(const ora_grid* g, const ora_config* c, double* x, double* b,
               const double* const* neumann, double* history, ora_stats* st);
 
+/* ora_solve for the BiCGSTAB main solver, also writing wall-clock stamps (seconds
+ * on CLOCK_MONOTONIC): stamps[0] when the call starts, stamps[i] when iteration i
+ * ends (1 <= i <= iterations), stamps[iterations + 1] when the call returns.
+ * stamps needs maxit+2 doubles; history is required.  The benchmark's reference
+ * arm times one complete solve in chunks with them. */
+int ora_solve_stamped(const ora_grid* g, const ora_config* c, double* x, double* b,
+                      const double* const* neumann, double* history, ora_stats* st, double* stamps);
+
 /* Building blocks, exposed for kernel-level parity tests. */
 void ora_eigen_bounds(const ora_grid* g, double out[2]);                 /* eigenValuesGlobal_ */
 void ora_cheb_params(const ora_grid* g, const ora_config* c, double out[3]); /* theta, delta, sigma */

@@ -1,6 +1,7 @@
-"""bench.py --impl reference on CPU: the reference arm's JSON line (the oracle's C
-restatement timed on the host cores), on a small grid so that it runs in seconds, and
-its behaviour under two ranks (rank 0 alone prints, the other exits 0 quietly)."""
+"""bench.py --impl reference on CPU: the reference arm's JSON line (one complete solve
+by the oracle's C restatement on the host cores, timed in K chunks of consecutive
+iterations), on a small grid so that it runs in seconds, and its behaviour under two
+ranks (rank 0 alone prints, the other exits 0 quietly)."""
 import json
 import os
 import socket
@@ -8,7 +9,7 @@ import subprocess
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CMD = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "24", "--steps", "1",
+CMD = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "24", "--steps", "3",
        "--warmup", "0", "--cpu-threads", "2"]
 
 
@@ -26,7 +27,12 @@ def test_reference_arm_prints_the_contract_line():
               "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["higher_is_better"] is False
-    assert d["value"] > 0 and abs(d["ms_per_step"] - 1e3 * d["value"]) < 1e-6 * d["ms_per_step"]
+    # the K steps are chunks of one complete solve: together they are its measured time
+    assert d["steps"] == 3 and d["value"] > 0
+    assert abs(d["ms_per_step"] * d["steps"] - 1e3 * d["value"]) < 1e-6 * 1e3 * d["value"]
+    cfg = d["config"]
+    assert len(cfg["chunk_seconds"]) == 3 and abs(sum(cfg["chunk_seconds"]) - d["value"]) < 1e-2
+    assert cfg["iterations"] > 3 and cfg["err_iter"] < 1e-10
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == 2
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
