@@ -340,22 +340,25 @@ pps_status pps_restrict2(int nx, int ny, int nz, const float* fine_dev, float* c
 pps_status pps_prolong2(int nx, int ny, int nz, const float* coarse_dev, float* fine_dev);
 
 /* Operator apply that allocates nothing.  No counterpart in the reference: it is for
- * callers that cannot call cudaMalloc -- code recorded into a CUDA graph (no
- * allocation while a stream is captured), loops that forbid allocation after
- * start-up, or plugins whose host framework owns all device memory -- and so
- * cannot create a pps_solver.
+ * callers that cannot call cudaMalloc -- loops that forbid allocation after
+ * start-up, plugins whose host framework owns all device memory, applications
+ * whose device-memory budget is fixed when they start -- and so cannot create a
+ * pps_solver.
  *
  * On device pointers of the field layout: out_dev = A u at the unknowns (the FP64
  * form's kernel; every other entry of out_dev is left as it was) and
- * *energy_dev = sum of u*(A u) over the unknowns.  Work is queued on `stream`
- * (a cudaStream_t; NULL = the legacy default stream); the call does not wait.
+ * *energy_dev = sum of u*(A u) over the unknowns.  u_dev, out_dev and energy_dev
+ * must not overlap (an in-place call is rejected with PPS_ERR_INVALID_ARG).  Work
+ * is queued on `stream` (a cudaStream_t; NULL = the legacy default stream); the
+ * call does not wait.
  *
  * Its reduction scratch is a file-scope __device__ array of
  * 512 + 32*PPS_NOALLOC_MAX_BLOCKS bytes (about 512 KiB) that every GPU which loads
  * the library holds until the process exits.  Grids whose launch needs more than
  * PPS_NOALLOC_MAX_BLOCKS thread blocks are rejected with PPS_ERR_INVALID_ARG.
  * The first call on each device looks up the array's device address with that
- * device current; make that first call before any stream capture.  All calls
+ * device current and keeps it; make that first call before any stream capture,
+ * and do not use the entry point across a cudaDeviceReset.  All calls
  * share the one array, so calls that overlap on the GPU (other streams, other
  * threads) race: serialise them. */
 #define PPS_NOALLOC_MAX_BLOCKS 16384

@@ -23,7 +23,21 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libppsref.so")
-REF_INCLUDE = "/root/reference/solverPoissonMPI_CPU/include"
+
+
+def _ref_include() -> str:
+    """Where the reference's solverPoissonMPI_CPU/include lies: $REF_INCLUDE, else
+    the default of the recipe that compiles it (oracle/Makefile)."""
+    if os.environ.get("REF_INCLUDE"):
+        return os.environ["REF_INCLUDE"]
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF_INCLUDE ?="):
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+REF_INCLUDE = _ref_include()
 
 BICGSTAB, CG, CHEBYSHEV_MAIN = 0, 1, 2
 PREC_NONE, PREC_CHEBYSHEV, PREC_BICGSTAB, PREC_CG = 0, 1, 2, 3
@@ -139,7 +153,7 @@ def build(ref: bool | None = None, quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "all"], check=True, stdout=out)
     if ref is None:
-        ref = os.path.isdir(REF_INCLUDE)
+        ref = bool(REF_INCLUDE) and os.path.isdir(REF_INCLUDE)
     if ref:
         subprocess.run(["make", "-C", HERE, "ref", f"REF_INCLUDE={REF_INCLUDE}"], check=True, stdout=out)
 

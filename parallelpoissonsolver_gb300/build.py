@@ -1,7 +1,9 @@
 """In-tree build of libpps.so (nvcc, sm_103a only).
 
-The two translation units compile in parallel and link into
-``parallelpoissonsolver_gb300/libpps.so`` beside this file.
+The six translation units of csrc/ (kernels, solver, allocation-free entry point,
+batched solves, U-Net kernels and U-Net host code) compile in parallel, one
+-gencode for sm_103a, and link into ``parallelpoissonsolver_gb300/libpps.so``
+beside this file.
 """
 from __future__ import annotations
 

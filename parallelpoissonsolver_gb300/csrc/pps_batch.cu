@@ -323,15 +323,20 @@ pps_status run_batch(pps_batch* s)
             if (!s->gexec || s->g_iters != chunk) {
                 if (s->gexec) cudaGraphExecDestroy(s->gexec);
                 s->gexec = nullptr;
-                cudaGraph_t gr;
+                cudaGraph_t gr = nullptr;
                 const int c0 = launches_counter();
-                BK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                for (int q = 0; q < chunk; q++) b_iteration(s, B);
-                BK(cudaStreamEndCapture(st, &gr));
+                {
+                    BK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    CaptureGuard cap(st);   // an error below ends the capture
+                    for (int q = 0; q < chunk; q++) b_iteration(s, B);
+                    BK(cap.end(&gr));
+                }
                 s->g_launches = launches_counter() - c0;
                 launches_counter_add(-s->g_launches);
-                BK(cudaGraphInstantiate(&s->gexec, gr, 0));
+                const cudaError_t ie = cudaGraphInstantiate(&s->gexec, gr, 0);
                 cudaGraphDestroy(gr);
+                if (ie != cudaSuccess) s->gexec = nullptr;
+                BK(ie);
                 s->g_iters = chunk;
             }
         }

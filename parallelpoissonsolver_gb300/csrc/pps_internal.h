@@ -47,6 +47,29 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     if (e != cudaSuccess) note_launch_failure(e);
 }
 
+// Ends a stream capture that an error left open, dropping the partial graph, so the
+// stream does not stay in capture mode and fail every later call on it.  end()
+// closes the capture normally.
+struct CaptureGuard {
+    cudaStream_t stream;
+    bool open = true;
+    explicit CaptureGuard(cudaStream_t s) : stream(s) {}
+    CaptureGuard(const CaptureGuard&) = delete;
+    CaptureGuard& operator=(const CaptureGuard&) = delete;
+    cudaError_t end(cudaGraph_t* g)
+    {
+        open = false;
+        return cudaStreamEndCapture(stream, g);
+    }
+    ~CaptureGuard()
+    {
+        if (!open) return;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream, &g);
+        if (g) cudaGraphDestroy(g);
+    }
+};
+
 // Geometry of one single-rank grid in the guard-padded field layout
 // (iterativeSolverBase.hpp:34-35): index = i + sj*j + sk*k with
 // 0 <= i < n0+2 etc.; data nodes are 1..n, unknowns lo..hi-1 (blockGrid.hpp:184-222).
@@ -113,6 +136,16 @@ struct RedCtx {
     DevState* st;
     double* hist;
     int kind;
+    // Canonical sums (FP64 form): when cells is set, a kernel launched on the
+    // canonical shape (canon_shape) stores one partial per cell -- 32 consecutive
+    // columns of one row over one canonical z chunk, summed by the thread along z in
+    // plane order and over the warp's lanes by a fixed shuffle tree -- at
+    // cells[q * cell_n + cell], cell = (chunk * cell_ny + row) * cell_ntx + tile;
+    // k_canon_finalize then sums the cells in a fixed tree.  The result depends on
+    // the grid alone, not on the tile shape the autotuner picked or the SM count.
+    double* cells = nullptr;
+    int cell_ntx = 0, cell_ny = 0;
+    long long cell_n = 0;
 };
 
 // Chebyshev coefficients of one sweep in pre-folded form (the alpaka kernels fold
@@ -181,6 +214,12 @@ size_t b_coef_size();
 
 // ---- launch wrappers (pps_kernels.cu) ----
 Shape make_shape(const Geo& g, int ty, int target_blocks, int cx = 1);
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// cached per device): launch grids are sized in waves of it.
+int sm_count();
+// Canonical shape of canonical sums (RedCtx::cells) and the number of cells per sum.
+Shape canon_shape(const Geo& g, int ty);
+long long canon_cells(const Geo& g);
 
 // Parity (bit-exact FP64) kernels.
 void par_stencil(const Geo& g, const double* u, double* out, cudaStream_t s);

@@ -87,7 +87,7 @@ __device__ __forceinline__ double opA_exact(const double* __restrict__ d, long l
 static inline unsigned par_blocks(long long n)
 {
     long long b = (n + 255) / 256;
-    if (b > 152LL * 64) b = 152LL * 64;
+    if (b > sm_count() * 64LL) b = sm_count() * 64LL;
     if (b < 1) b = 1;
     return (unsigned)b;
 }
@@ -474,6 +474,19 @@ template void neumann_fill<float>(const Geo&, float*, Faces, int, double, cudaSt
 // Fast kernels
 // ---------------------------------------------------------------------------
 
+int sm_count()
+{
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    int n = __atomic_load_n(&cached[dev], __ATOMIC_RELAXED);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+        __atomic_store_n(&cached[dev], n, __ATOMIC_RELAXED);
+    }
+    return n;
+}
+
 Shape make_shape(const Geo& g, int ty, int target_blocks, int cx)
 {
     Shape sh;
@@ -491,6 +504,112 @@ Shape make_shape(const Geo& g, int ty, int target_blocks, int cx)
     sh.kchunk = (int)((uz + chunks - 1) / chunks);
     sh.nchunks = (uz + sh.kchunk - 1) / sh.kchunk;
     return sh;
+}
+
+// Canonical launch shape of the FP64 form's reduction kernels: one-column tiles of
+// 32 x ty and a z chunk fixed by the grid alone, so that the cells of canonical sums
+// (RedCtx::cells) are the same whatever ty the autotuner picked.  ty does not enter
+// the cells: each warp stores its own.
+Shape canon_shape(const Geo& g, int ty)
+{
+    Shape sh;
+    sh.ty = ty;
+    sh.cx = 1;
+    const int ux = g.hi[0] - g.lo[0], uy = g.hi[1] - g.lo[1], uz = g.hi[2] - g.lo[2];
+    sh.ntx = (ux + 31) / 32;
+    sh.nty = (uy + ty - 1) / ty;
+    sh.kchunk = std::min(64, std::max(4, (uz + 15) / 16));
+    sh.nchunks = (uz + sh.kchunk - 1) / sh.kchunk;
+    return sh;
+}
+
+long long canon_cells(const Geo& g)
+{
+    const Shape sh = canon_shape(g, 8);
+    return (long long)sh.ntx * (g.hi[1] - g.lo[1]) * sh.nchunks;
+}
+
+// The context and shape of one canonical launch.
+static void canon_launch(const Geo& g, Shape& sh, RedCtx& rc)
+{
+    sh = canon_shape(g, sh.ty);
+    rc.cell_ntx = sh.ntx;
+    rc.cell_ny = g.hi[1] - g.lo[1];
+    rc.cell_n = (long long)sh.ntx * rc.cell_ny * sh.nchunks;
+}
+
+// Sum of the cells of a canonical launch in a fixed tree, then the finalizer.
+// Block b of CANON_BLOCKS sums cells [b*per, (b+1)*per) (thread t the ones at t +
+// 256 m, in order; then the warps' shuffle trees and the eight warps in order); the
+// last block to finish sums the CANON_BLOCKS partials the same way.  Launched with
+// CANON_BLOCKS x 256 threads after the kernel that stored the cells; `done` is that
+// kernel's early-exit flag (null if it always runs).
+static constexpr int CANON_BLOCKS = 128;
+template <int NS>
+__global__ void __launch_bounds__(256) k_canon_finalize(RedCtx rc, const int* done)
+{
+    pdl_enter();
+    EARLY_EXIT(done);
+    __shared__ double sm[8][NS];
+    __shared__ int is_last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long n = rc.cell_n;
+    const long long per = (n + CANON_BLOCKS - 1) / CANON_BLOCKS;
+    const long long c0 = (long long)blockIdx.x * per, c1 = min(n, c0 + per);
+    double acc[NS];
+#pragma unroll
+    for (int q = 0; q < NS; q++) acc[q] = 0.0;
+    for (long long c = c0 + tid; c < c1; c += 256) {
+#pragma unroll
+        for (int q = 0; q < NS; q++) acc[q] += rc.cells[q * n + c];
+    }
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+        const double w = warp_sum(acc[q]);
+        if (lane == 0) sm[warp][q] = w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NS; q++) {
+            double t = 0.0;
+            for (int w = 0; w < 8; w++) t += sm[w][q];
+            rc.partials[(size_t)blockIdx.x * 4 + q] = t;
+        }
+        __threadfence();
+        is_last = atomicAdd(rc.counter, 1u) == CANON_BLOCKS - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+#pragma unroll
+    for (int q = 0; q < NS; q++) acc[q] = tid < CANON_BLOCKS ? __ldcg(&rc.partials[(size_t)tid * 4 + q]) : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+        const double w = warp_sum(acc[q]);
+        if (lane == 0) sm[warp][q] = w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double tot[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < NS; q++) {
+            double t = 0.0;
+            for (int w = 0; w < 8; w++) t += sm[w][q];
+            tot[q] = t;
+        }
+        finalize(rc, tot);
+        __threadfence();
+        *rc.counter = 0u;
+    }
+}
+
+template <int NS>
+static void canon_finalize(const RedCtx& rc, const int* done, cudaStream_t s)
+{
+    launch_pdl(k_canon_finalize<NS>, CANON_BLOCKS, 256, 0, s, rc, done);
+    PPS_COUNT_LAUNCH();
 }
 
 struct Col {
@@ -955,7 +1074,7 @@ __global__ void __launch_bounds__(256) k_stencil_dot(Geo g, Shape sh, const T* _
         }
     }
     double v[1] = {acc.value()};
-    reduce_finalize<1>(v, rc);
+    reduce_emit<1>(v, rc, sh);
 }
 
 // Au = A(u); sum r*Au, sum Au*Au   (BiCGSTAB.hpp:189-225, BiCGstab2Kernel)
@@ -990,7 +1109,7 @@ __global__ void __launch_bounds__(256) k_stencil_dot2(Geo g, Shape sh, const T* 
         }
     }
     double v[2] = {a1.value(), a2.value()};
-    reduce_finalize<2>(v, rc);
+    reduce_emit<2>(v, rc, sh);
 }
 
 // r -= alpha*v   (BiCGSTAB.hpp:167-178)
@@ -1035,7 +1154,7 @@ __global__ void __launch_bounds__(256) k_update_xr(Geo g, Shape sh, T* __restric
         }
     }
     double v[2] = {a1.value(), a2.value()};
-    reduce_finalize<2>(v, rc);
+    reduce_emit<2>(v, rc, sh);
 }
 
 // p = r + beta*(p - omega*AMp)   (BiCGSTAB.hpp:261-272)
@@ -1089,7 +1208,7 @@ __global__ void __launch_bounds__(256) k_cg_stencil_dot(Geo g, Shape sh, const T
         }
     }
     double v[2] = {a1.value(), a2.value()};
-    reduce_finalize<2>(v, rc);
+    reduce_emit<2>(v, rc, sh);
 }
 
 // CG: x += alpha*p; r -= alpha*Ap   (baseCG.hpp:154-165)
@@ -1131,7 +1250,7 @@ __global__ void __launch_bounds__(256) k_cg_dot_rz(Geo g, Shape sh, const T* __r
         }
     }
     double v[2] = {a1.value(), a2.value()};
-    reduce_finalize<2>(v, rc);
+    reduce_emit<2>(v, rc, sh);
 }
 
 // CG: p = z + beta*p   (baseCG.hpp:197-207)
@@ -1669,9 +1788,13 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
                     const double Ds = D != 0 ? __longlong_as_double(__double_as_longlong(Dd) + ((long long)(E - 1075) << 52))
                                              : 0.0;
                     rv = fmx(-cf.cx, Ds, b[c]);
+                } else if (E > 2000) {
+                    // magnitudes near the top of the range: cx * D first, then the power of
+                    // two 2^(E-1075) (a normal double), so nothing overflows while A x is
+                    // finite, and D = 0 gives b exactly
+                    rv = fmx(-(cf.cx * Dd), __longlong_as_double((long long)(E - 52) << 52), b[c]);
                 } else {
-                    const double scale = E >= 53 ? __longlong_as_double((long long)(E - 52) << 52) : 0.0;
-                    rv = fmx(-(cf.cx * scale), Dd, b[c]);
+                    rv = b[c];   // every value below 2^-1022: A x is far under b's rounding
                 }
             }
             const TR rs = (TR)rv;
@@ -1710,7 +1833,7 @@ __global__ void __launch_bounds__(256) k_residual(Geo g, Shape sh, const double*
         }
     }
     double v[1] = {acc.value()};
-    reduce_finalize<1>(v, rc);
+    reduce_emit<1>(v, rc, sh);
 }
 
 // sum b_adj^2 over the unknowns (normalizeProblemToFieldBNorm, iterativeSolverBase.hpp:171-234);
@@ -1743,7 +1866,7 @@ __global__ void __launch_bounds__(256) k_norm_badj(Geo g, Shape sh, const double
         }
     }
     double v[1] = {s};
-    reduce_finalize<1>(v, rc);
+    reduce_emit<1>(v, rc, sh);
 }
 
 __global__ void __launch_bounds__(256) k_add_correction(Geo g, Shape sh, double* __restrict__ x,
@@ -1826,7 +1949,7 @@ __global__ void __launch_bounds__(256) k_bicg_start(Geo g, Shape sh, const T* __
         }
     }
     double v[1] = {a.value()};
-    reduce_finalize<1>(v, rc);
+    reduce_emit<1>(v, rc, sh);
 }
 
 __global__ void k_cast_f32(const double* __restrict__ in, float* __restrict__ out, long long n)
@@ -1939,7 +2062,7 @@ void fast_cheb_fused(const Geo& g, int nsteps, const T* B, T* X, const Coef* c, 
     const long long tiles = (long long)ntx * nty;
     // z chunks: about 8 blocks per SM, each chunk at most 128 planes (the wavefront
     // re-reads 2*nsteps planes per chunk)
-    long long chunks = std::max((152LL * 8 + tiles - 1) / tiles, (long long)((uz + 127) / 128));
+    long long chunks = std::max((sm_count() * 8LL + tiles - 1) / tiles, (long long)((uz + 127) / 128));
     chunks = std::max(1LL, std::min(chunks, (long long)uz));
     const int kchunk = (int)((uz + chunks - 1) / chunks);
     const dim3 grid((unsigned)tiles, (unsigned)((uz + kchunk - 1) / kchunk));
@@ -1971,6 +2094,14 @@ template <typename T>
 void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T* Au, const Coef& a, RedCtx rc,
                       cudaStream_t s)
 {
+    if (rc.cells) {   // canonical sums: one-column kernel on the canonical shape
+        Shape c = sh;
+        canon_launch(g, c, rc);
+        launch_pdl(k_stencil_dot<T>, grid_of(c), block_of(c), 0, s, g, c, u, r0, Au, a, rc);
+        PPS_COUNT_LAUNCH();
+        canon_finalize<1>(rc, &rc.st->done, s);
+        return;
+    }
     if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, u, r0, Au, nullptr)) {
@@ -1989,6 +2120,14 @@ template <typename T>
 void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T* Au, const Coef& a, RedCtx rc,
                        cudaStream_t s)
 {
+    if (rc.cells) {
+        Shape c = sh;
+        canon_launch(g, c, rc);
+        launch_pdl(k_stencil_dot2<T>, grid_of(c), block_of(c), 0, s, g, c, u, r, Au, a, rc);
+        PPS_COUNT_LAUNCH();
+        canon_finalize<2>(rc, &rc.st->done, s);
+        return;
+    }
     if (sh.cx != 1) {
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, u, r, Au, nullptr)) {
@@ -2027,6 +2166,14 @@ template <typename T>
 void fast_update_xr(const Geo& g, const Shape& sh, T* x, const T* Mp, const T* z, T* r, const T* Az, const T* r0,
                     RedCtx rc, cudaStream_t s)
 {
+    if (rc.cells) {
+        Shape c = sh;
+        canon_launch(g, c, rc);
+        launch_pdl(k_update_xr<T>, grid_of(c), block_of(c), 0, s, g, c, x, Mp, z, r, Az, r0, rc);
+        PPS_COUNT_LAUNCH();
+        canon_finalize<2>(rc, &rc.st->done, s);
+        return;
+    }
     if (flat_ok(g, {x, Mp, z, r, Az, r0})) {
         launch_pdl(k_update_xr_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, Mp, z, r, Az, r0, rc);
         PPS_COUNT_LAUNCH();
@@ -2050,6 +2197,14 @@ template <typename T>
 void fast_cg_stencil_dot(const Geo& g, const Shape& sh, const T* p, const T* r, const T* z, T* Ap, const Coef& a,
                          RedCtx rc, cudaStream_t s)
 {
+    if (rc.cells) {
+        Shape c = sh;
+        canon_launch(g, c, rc);
+        launch_pdl(k_cg_stencil_dot<T>, grid_of(c), block_of(c), 0, s, g, c, p, r, z, Ap, a, rc);
+        PPS_COUNT_LAUNCH();
+        canon_finalize<2>(rc, &rc.st->done, s);
+        return;
+    }
     launch_pdl(k_cg_stencil_dot<T>, grid_of(sh), block_of(sh), 0, s, g, sh, p, r, z, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
@@ -2063,6 +2218,14 @@ void fast_cg_update_xr(const Geo& g, const Shape& sh, T* x, const T* p, T* r, co
 template <typename T>
 void fast_cg_dot_rz(const Geo& g, const Shape& sh, const T* r, const T* z, RedCtx rc, cudaStream_t s)
 {
+    if (rc.cells) {
+        Shape c = sh;
+        canon_launch(g, c, rc);
+        launch_pdl(k_cg_dot_rz<T>, grid_of(c), block_of(c), 0, s, g, c, r, z, rc);
+        PPS_COUNT_LAUNCH();
+        canon_finalize<2>(rc, &rc.st->done, s);
+        return;
+    }
     launch_pdl(k_cg_dot_rz<T>, grid_of(sh), block_of(sh), 0, s, g, sh, r, z, rc);
     PPS_COUNT_LAUNCH();
 }
@@ -2125,20 +2288,26 @@ template <typename TR>
 void fast_residual(const Geo& g, const Shape& sh, const double* x, const double* b, TR* r, TR* r0, TR* p,
                    const Coef& a, RedCtx rc, cudaStream_t s, bool x_zero)
 {
+    Shape c = sh;
+    if (rc.cells) canon_launch(g, c, rc);
     if (x_zero)
-        launch_pdl(k_residual<TR, true, true>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, true, true>, grid_of(c), block_of(c), 0, s, g, c, x, b, r, r0, p, a, rc);
     else if (a.cx == a.cy && a.cx == a.cz)
-        launch_pdl(k_residual<TR, true, false>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, true, false>, grid_of(c), block_of(c), 0, s, g, c, x, b, r, r0, p, a, rc);
     else
-        launch_pdl(k_residual<TR, false, false>, grid_of(sh), block_of(sh), 0, s, g, sh, x, b, r, r0, p, a, rc);
+        launch_pdl(k_residual<TR, false, false>, grid_of(c), block_of(c), 0, s, g, c, x, b, r, r0, p, a, rc);
     PPS_COUNT_LAUNCH();
+    if (rc.cells) canon_finalize<1>(rc, nullptr, s);
 }
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
                     cudaStream_t s, bool x_zero)
 {
-    if (x_zero) launch_pdl(k_norm_badj<true>, grid_of(sh), block_of(sh), 0, s, g, sh, b, x, f, rc);
-    else launch_pdl(k_norm_badj<false>, grid_of(sh), block_of(sh), 0, s, g, sh, b, x, f, rc);
+    Shape c = sh;
+    if (rc.cells) canon_launch(g, c, rc);
+    if (x_zero) launch_pdl(k_norm_badj<true>, grid_of(c), block_of(c), 0, s, g, c, b, x, f, rc);
+    else launch_pdl(k_norm_badj<false>, grid_of(c), block_of(c), 0, s, g, c, b, x, f, rc);
     PPS_COUNT_LAUNCH();
+    if (rc.cells) canon_finalize<1>(rc, nullptr, s);
 }
 void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* e, const DevState*, cudaStream_t s,
                          bool e_zero_off)
@@ -2153,12 +2322,15 @@ void fast_add_correction(const Geo& g, const Shape& sh, double* x, const float* 
 template <typename T>
 void fast_bicg_start(const Geo& g, const Shape& sh, const T* B, T* r, T* r0, T* p, RedCtx rc, cudaStream_t s)
 {
-    launch_pdl(k_bicg_start<T>, grid_of(sh), block_of(sh), 0, s, g, sh, B, r, r0, p, rc);
+    Shape c = sh;
+    if (rc.cells) canon_launch(g, c, rc);
+    launch_pdl(k_bicg_start<T>, grid_of(c), block_of(c), 0, s, g, c, B, r, r0, p, rc);
     PPS_COUNT_LAUNCH();
+    if (rc.cells) canon_finalize<1>(rc, &rc.st->done, s);
 }
 void cast_field_f32(const double* in, float* out, long long n, cudaStream_t s)
 {
-    const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+    const long long blocks = std::min<long long>((n + 255) / 256, sm_count() * 16LL);
     launch_pdl(k_cast_f32, (unsigned)std::max<long long>(blocks, 1), 256, 0, s, in, out, n);
     PPS_COUNT_LAUNCH();
 }

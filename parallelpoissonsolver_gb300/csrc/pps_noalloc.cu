@@ -1,12 +1,16 @@
 // pps_apply_operator_noalloc: the FP64 operator apply + energy reduction for
 // callers that cannot allocate device memory.
 //
-// Who needs it: code that must not call cudaMalloc -- a host application that
-// records the solve step into a CUDA graph (allocation is not allowed while a
-// stream is being captured), a real-time loop that forbids allocation after
-// start-up, or a plugin running inside a framework that owns all device memory
-// through its own pool.  Those callers own their input and output buffers but
-// cannot create a pps_solver, whose constructor allocates the work fields.
+// Who needs it: code that must not call cudaMalloc -- a real-time loop that
+// forbids allocation after start-up, a plugin running inside a framework that owns
+// all device memory through its own pool, or an application whose device-memory
+// budget is fixed when it starts.  Those callers own their input and output
+// buffers but cannot create a pps_solver, whose constructor allocates the work
+// fields.
+//
+// The scratch array's device address is looked up on a device's first call and
+// kept for the life of the process; cudaDeviceReset on that device invalidates it,
+// so the entry point must not be used across a device reset.
 //
 // The kernel is k_stencil_dot<double> (the FP64 form's stencil + dot kernel).
 // Its reduction scratch -- the scalar block, the block-completion counter and
@@ -20,6 +24,7 @@
 
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -69,6 +74,9 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
 {
     if (!grid || !u_dev || !out_dev || !energy_dev)
         return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: null argument");
+    // Each thread reads u around its points while others write out, so an in-place
+    // call (or any overlap, or energy inside either field) would read overwritten
+    // values: rejected below, once the field size is known.
     Geo g;
     for (int d = 0; d < 3; d++) {
         if (grid->npglobal[d] < 3) return fail(PPS_ERR_INVALID_ARG, "npglobal must be >= 3 on every axis");
@@ -87,7 +95,14 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
     g.sj = grid->npglobal[0] + 2;
     g.sk = g.sj * (grid->npglobal[1] + 2);
     g.ntot = g.sk * (grid->npglobal[2] + 2);
-    const Shape sh = make_shape(g, 8, 152 * 8 * 4);
+    {
+        const uintptr_t nb = (uintptr_t)g.ntot * sizeof(double);
+        const uintptr_t u0 = (uintptr_t)u_dev, o0 = (uintptr_t)out_dev, e0 = (uintptr_t)energy_dev;
+        auto overlap = [](uintptr_t a, uintptr_t na, uintptr_t b, uintptr_t nb2) { return a < b + nb2 && b < a + na; };
+        if (overlap(u0, nb, o0, nb) || overlap(e0, sizeof(double), u0, nb) || overlap(e0, sizeof(double), o0, nb))
+            return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: u, out and energy must not overlap");
+    }
+    const Shape sh = make_shape(g, 8, sm_count() * 8 * 4);
     if (sh.nblocks() > (unsigned)PPS_NOALLOC_MAX_BLOCKS)
         return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: the grid needs " +
                                              std::to_string(sh.nblocks()) + " blocks of partial sums; the "

@@ -254,6 +254,28 @@ __device__ __forceinline__ void reduce_finalize(double (&v)[NS], const RedCtx& r
     }
 }
 
+// The end of a z-marching kernel on the one-column tiles: the deterministic block
+// reduction above, or, with canonical sums, one partial per warp stored as its cell
+// (every lane calls it; rows past the last unknown own no cell).
+template <int NS>
+__device__ __forceinline__ void reduce_emit(double (&v)[NS], const RedCtx& rc, const Shape& sh)
+{
+    if (rc.cells == nullptr) {
+        reduce_finalize<NS>(v, rc);
+        return;
+    }
+    const int bx = blockIdx.x % sh.ntx;
+    const int row = (blockIdx.x / sh.ntx) * sh.ty + threadIdx.y;
+    double w[NS];
+#pragma unroll
+    for (int q = 0; q < NS; q++) w[q] = warp_sum(v[q]);
+    if (row < rc.cell_ny && threadIdx.x == 0) {
+        const long long cell = ((long long)blockIdx.y * rc.cell_ny + row) * rc.cell_ntx + bx;
+#pragma unroll
+        for (int q = 0; q < NS; q++) rc.cells[q * rc.cell_n + cell] = w[q];
+    }
+}
+
 #define EARLY_EXIT(done)                                      \
     if (done != nullptr && *(volatile const int*)(done) != 0) return;
 

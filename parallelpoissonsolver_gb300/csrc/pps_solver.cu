@@ -111,6 +111,7 @@ struct pps_solver {
     double* d_partials = nullptr;
     unsigned* d_counter = nullptr;
     double* h_dot = nullptr;   // pinned
+    double* d_cells = nullptr; // FP64 form: cells of canonical sums (3 per cell)
 
     double* d_faces[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool has_neumann = false;
@@ -193,6 +194,18 @@ RedCtx red(pps_solver* s, int kind)
     return rc;
 }
 
+// The sums of the reference methods (BiCGSTAB, CG, their start and the true
+// residual) in the FP64 form are canonical: one partial per fixed cell of the grid,
+// summed in a fixed tree, so the iterates, the iteration count and the residual
+// history depend on the grid and the data alone -- not on the tiles pps_autotune
+// picks nor on the GPU's SM count.  The other forms keep the block reduction.
+RedCtx red_c(pps_solver* s, int kind)
+{
+    RedCtx rc = red(s, kind);
+    rc.cells = s->d_cells;
+    return rc;
+}
+
 // A(u) = cc*u + c_d*(pairs) with c_d = 1/h_d^2  (matrixFreeOperatorA.hpp:34-38)
 Coef op_coef_ds(const double ds[3])
 {
@@ -260,7 +273,8 @@ void free_all(pps_solver* s)
     free_fields(s->f32);
     free_fields(s->in64);
     free_fields(s->in32);
-    void* ptrs[] = {s->d_x, s->d_b, s->d_bt, s->d_dot, s->d_st, s->d_hist, s->d_partials, s->d_counter, s->d_st_in};
+    void* ptrs[] = {s->d_x, s->d_b, s->d_bt, s->d_dot, s->d_st, s->d_hist, s->d_partials, s->d_counter, s->d_st_in,
+                    s->d_cells};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (s->h_st_in) cudaFreeHost(s->h_st_in);
@@ -975,15 +989,15 @@ void fast_bicgstab_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     if (s->has_neumann) neumann_fill<T>(g, F.Mp, faces_of(s), 0, 1.0, st);
     // the stencils run on the Chebyshev tiles (x-vectorised for FP32); the updates
     // are flat 16-byte vector passes on Dirichlet grids
-    fast_stencil_dot<T>(g, s->shape_cheb, F.Mp, F.r0, F.AMp, a, red(s, FIN_ALPHA), st);
+    fast_stencil_dot<T>(g, s->shape_cheb, F.Mp, F.r0, F.AMp, a, red_c(s, FIN_ALPHA), st);
     fast_axpy_alpha<T>(g, sh, F.r, F.AMp, s->d_st, st);
     fast_precond<T>(s, F, F.r, F.z, L);
     if (s->has_neumann) neumann_fill<T>(g, F.z, faces_of(s), 0, 1.0, st);
-    fast_stencil_dot2<T>(g, s->shape_cheb, F.z, F.r, F.Az, a, red(s, FIN_OMEGA), st);
-    fast_update_xr<T>(g, sh, xacc, F.Mp, F.z, F.r, F.Az, F.r0, red(s, FIN_CONV), st);
+    fast_stencil_dot2<T>(g, s->shape_cheb, F.z, F.r, F.Az, a, red_c(s, FIN_OMEGA), st);
+    fast_update_xr<T>(g, sh, xacc, F.Mp, F.z, F.r, F.Az, F.r0, red_c(s, FIN_CONV), st);
     fast_update_p<T>(g, sh, F.p, F.r, F.AMp, s->d_st, st);
     L.bytes += bytes_of<T>(N, 3 + 3 + 3 + 8 + 4);
-    L.launches += 5;
+    L.launches += s->d_cells ? 8 : 5;
 }
 
 template <typename T>
@@ -1023,7 +1037,7 @@ void fast_inner_precond(pps_solver* s, T* B, T* X, Launcher& L, bool cg)
     InnerScope in(s);
     // FIN_RES0 with tol_relative: the stop target becomes precond_tol * ||B||
     state_init(s->d_st, s->d_hist, s->cfg.precond_maxit, 0.0, s->cfg.precond_tol, 1, 1, 1.0, 0, st);
-    fast_bicg_start<T>(g, s->shape, B, W.r, W.r0, W.p, red(s, FIN_RES0), st);
+    fast_bicg_start<T>(g, s->shape, B, W.r, W.r0, W.p, red_c(s, FIN_RES0), st);
     L.bytes += bytes_of<T>(s->n_unknowns, 4);
     if (cg) {
         // z = M r, p = z (baseCG.hpp:110-112)
@@ -1054,13 +1068,13 @@ void fast_cg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     cudaStream_t st = s->stream;
     const long long N = s->n_unknowns;
     const Coef a = op_coef(g);
-    fast_cg_stencil_dot<T>(g, sh, F.p, F.r, F.z, F.AMp, a, red(s, FIN_CG_ALPHA), st);
+    fast_cg_stencil_dot<T>(g, sh, F.p, F.r, F.z, F.AMp, a, red_c(s, FIN_CG_ALPHA), st);
     fast_cg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, s->d_st, st);
     fast_precond<T>(s, F, F.r, F.z, L);
-    fast_cg_dot_rz<T>(g, sh, F.r, F.z, red(s, FIN_CG_CONV), st);
+    fast_cg_dot_rz<T>(g, sh, F.r, F.z, red_c(s, FIN_CG_CONV), st);
     fast_cg_update_p<T>(g, sh, F.p, F.z, s->d_st, st);
     L.bytes += bytes_of<T>(N, 4 + 6 + 2 + 3);
-    L.launches += 4;
+    L.launches += s->d_cells ? 6 : 4;
 }
 
 bool aligned16(const void* p)
@@ -1166,19 +1180,24 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
                     cudaGraphExecDestroy(s->gexec);
                     s->gexec = nullptr;
                 }
-                cudaGraph_t gr;
+                cudaGraph_t gr = nullptr;
                 Launcher LG{s, false};
                 const double sb = s->sweep_bytes_acc;
                 const int sl = s->sweep_launch_acc;
                 const int la = s->learned_apps;
                 const int c0 = launches_counter();
-                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-                for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, LG);
-                CK(cudaStreamEndCapture(s->stream, &gr));
+                {
+                    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                    CaptureGuard cap(s->stream);   // an error below ends the capture
+                    for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, LG);
+                    CK(cap.end(&gr));
+                }
                 LG.launches = launches_counter() - c0;
                 launches_counter_add(-LG.launches);
-                CK(cudaGraphInstantiate(&s->gexec, gr, 0));
+                const cudaError_t ie = cudaGraphInstantiate(&s->gexec, gr, 0);
                 cudaGraphDestroy(gr);
+                if (ie != cudaSuccess) s->gexec = nullptr;
+                CK(ie);
                 s->g_key_x = xacc;
                 s->g_form = form;
                 s->g_iters = chunk;
@@ -1255,7 +1274,7 @@ bool field_is_zero(pps_solver* s, const double* x)
 double norm_badj(pps_solver* s, const double* x, const double* b, bool x_zero = false)
 {
     state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
-    fast_norm_badj(s->geo, s->shape, b, x, faces_of(s), red(s, FIN_NORMB), s->stream, x_zero);
+    fast_norm_badj(s->geo, s->shape, b, x, faces_of(s), red_c(s, FIN_NORMB), s->stream, x_zero);
     read_state(s);
     return s->h_st->normb;
 }
@@ -1286,8 +1305,8 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     // BiCGSTAB and CG start from r0 = p = r; flexible CG needs r alone (its first
     // direction is the preconditioned residual)
     const bool fcg = s->cfg.krylov == PPS_KRYLOV_FCG;
-    fast_residual<double>(g, s->shape, x, b, F.r, fcg ? nullptr : F.r0, fcg ? nullptr : F.p, a, red(s, FIN_RES0), st,
-                          x_zero);
+    fast_residual<double>(g, s->shape, x, b, F.r, fcg ? nullptr : F.r0, fcg ? nullptr : F.p, a,
+                          fcg ? red(s, FIN_RES0) : red_c(s, FIN_RES0), st, x_zero);
     L.bytes += bytes_of<double>(s->n_unknowns, 5) + bytes_of<double>(s->n_unknowns, 1) * 2;
     pps_status rc = PPS_OK;
     read_state(s);
@@ -1309,7 +1328,7 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
     S.precond_applications += S.iterations * (s->cfg.krylov == PPS_KRYLOV_BICGSTAB ? 2 : 1);
     // final true residual (computeErrorOperatorA after the loop, BiCGSTAB.hpp:305-308)
     if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
-    fast_residual<double>(g, s->shape, x, b, F.Az, nullptr, nullptr, a, red(s, FIN_STORE), st);
+    fast_residual<double>(g, s->shape, x, b, F.Az, nullptr, nullptr, a, red_c(s, FIN_STORE), st);
     read_state(s);
     S.err_true = std::sqrt(s->h_st->sums[0]) / normb;
     S.hbm_bytes += L.bytes;
@@ -1485,7 +1504,7 @@ int resident_blocks(int ty)
 
 Shape tuned_shape(const Geo& g, int ty, int cx, int waves)
 {
-    return make_shape(g, ty, waves * 152 * resident_blocks(ty), cx);
+    return make_shape(g, ty, waves * sm_count() * resident_blocks(ty), cx);
 }
 
 unsigned max_candidate_blocks(const Geo& g)
@@ -1540,7 +1559,7 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
                 });
                 const double ks = time_launches<T>(s, reps, [&]() {
                     if (fcg) fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_STORE), s->stream);
-                    else fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red(s, FIN_STORE), s->stream);
+                    else fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red_c(s, FIN_STORE), s->stream);
                 });
                 if (us + ks < best_us) {
                     best_us = us + ks;
@@ -1556,7 +1575,7 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
             const Shape sh = tuned_shape(g, ty, 1, w);
             const double us = time_launches<T>(s, reps, [&]() {
                 state_init(s->d_st, s->d_hist, 1, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
-                fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red(s, FIN_STORE), s->stream);
+                fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red_c(s, FIN_STORE), s->stream);
             });
             if (us < best_us) {
                 best_us = us;
@@ -1775,11 +1794,11 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         g.sk = g.sj * (grid->npglobal[1] + 2);
         g.ntot = g.sk * (grid->npglobal[2] + 2);
         s->n_unknowns = (long long)(g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
-        s->shape = make_shape(g, 8, 152 * 8 * 4);
+        s->shape = make_shape(g, 8, sm_count() * 8 * 4);
         // the Chebyshev kernels default to the x-vectorised FP32 tiles where the row
         // stride allows them (FP64 fields run the scalar tiles of the same size)
         const int cx0 = g.sj % 4 == 0 ? 4 : 1;
-        s->shape_cheb = make_shape(g, 8, 152 * 8 * 4, cx0);
+        s->shape_cheb = make_shape(g, 8, sm_count() * 8 * 4, cx0);
         s->tuning.cheb_ty = 8;
         s->tuning.cheb_cx = cx0;
         s->tuning.cheb_waves = 4;
@@ -1842,8 +1861,10 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         CK(cudaMallocHost((void**)&s->h_dot, 4 * sizeof(double)));
         s->hist_cap = cfg->maxit + 2;
         CK(cudaMalloc((void**)&s->d_hist, sizeof(double) * (size_t)s->hist_cap));
-        const unsigned nb = std::max(max_candidate_blocks(g), 1u);
+        const unsigned nb = std::max(max_candidate_blocks(g), 128u);   // 128: the canonical sums' blocks
         CK(cudaMalloc((void**)&s->d_partials, sizeof(double) * 4 * (size_t)nb));
+        if (cfg->form == PPS_FORM_FP64)
+            CK(cudaMalloc((void**)&s->d_cells, sizeof(double) * 3 * (size_t)canon_cells(g)));
         CK(cudaMalloc((void**)&s->d_counter, sizeof(unsigned)));
         CK(cudaMemset(s->d_counter, 0, sizeof(unsigned)));
         for (int f = 0; f < 6; f++) {

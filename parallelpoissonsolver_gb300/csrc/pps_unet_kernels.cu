@@ -248,7 +248,7 @@ __global__ void k_relu_bwd(long long nv, bf16* __restrict__ G, int ldg, int cg0,
 static unsigned eblocks(long long n)
 {
     long long b = (n + 255) / 256;
-    if (b > 152LL * 32) b = 152LL * 32;
+    if (b > sm_count() * 32LL) b = sm_count() * 32LL;
     if (b < 1) b = 1;
     return (unsigned)b;
 }
@@ -1161,7 +1161,7 @@ static void level_launch(const Dims& d, int& kchunk, dim3& grid, int waves = 4)
     // blocks per SM (one wave left the 256^3 level at under half the HBM rate; the
     // first Chebyshev step, whose columns start with ten divisions, keeps one)
     const int tx = (d.W + 31) / 32, ty = (d.H + 7) / 8;
-    long long chunks = (152LL * 8 * waves + (long long)tx * ty - 1) / ((long long)tx * ty);
+    long long chunks = (sm_count() * 8LL * waves + (long long)tx * ty - 1) / ((long long)tx * ty);
     if (chunks < 1) chunks = 1;
     if (chunks > d.D) chunks = d.D;
     kchunk = (int)((d.D + chunks - 1) / chunks);
@@ -1272,7 +1272,7 @@ void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, co
     // 32 x 4 coarse columns per block; z split into chunks for about two waves of
     // eight blocks per SM
     const int tx = (dc.W + 31) / 32, ty = (dc.H + 3) / 4;
-    long long chunks = (152LL * 8 * 2 + (long long)tx * ty - 1) / ((long long)tx * ty);
+    long long chunks = (sm_count() * 8LL * 2 + (long long)tx * ty - 1) / ((long long)tx * ty);
     chunks = std::max(1LL, std::min(chunks, (long long)dc.D));
     const int zc = (int)((dc.D + chunks - 1) / chunks);
     const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((dc.D + zc - 1) / zc));
@@ -1419,7 +1419,7 @@ static void prolong_z(const Dims& dc, const float* coarse, float* fine, cudaStre
     const int ty = 8;
     const int ntx = (2 * dc.W + 31) / 32, nty = (2 * dc.H + ty - 1) / ty;
     const long long tiles = (long long)ntx * nty;
-    long long chunks = (152LL * 8 * 4 + tiles - 1) / tiles;
+    long long chunks = (sm_count() * 8LL * 4 + tiles - 1) / tiles;
     chunks = std::max(1LL, std::min<long long>(chunks, dc.D));
     const int cchunk = (int)((dc.D + chunks - 1) / chunks);
     const unsigned nch = (unsigned)((dc.D + cchunk - 1) / cchunk);
