@@ -269,6 +269,10 @@ def run_gpu(args, dist: Dist):
     t_step = dist.max(sum(dev_times) / len(dev_times))
     head_x = x_d.clone()
 
+    # ---- what the network earns: the same V-cycle with its coarsest-level solver
+    # swapped (no fallback, so each cycle's own convergence shows) ----
+    coarse = coarse_solver_comparison(args, grid, prec, net, k, gain, dev, solve)
+
     # ---- the reference method in mixed precision, and in plain FP64 ----
     mixed_stats = [solve(mixed) for _ in range(max(1, args.plain_steps))]
     t_mixed = sum(s["seconds_solve"] for s in mixed_stats) / len(mixed_stats)
@@ -377,6 +381,7 @@ def run_gpu(args, dist: Dist):
         },
         "clocks": clocks.summary(),
         "wall_s_timed_region": wall,
+        "coarse_solvers": coarse,
     }
     if not args.no_learned_128:
         out["learned_128"] = run_learned_128(args, dev)
@@ -384,6 +389,33 @@ def run_gpu(args, dist: Dist):
     mixed.close()
     plain.close()
     return out, plain_stats[-1]["iterations"]
+
+
+def coarse_solver_comparison(args, grid, prec, net, k: int, gain: float, dev: int, solve):
+    """The headline's flexible CG + V-cycle with the coarsest level (16^3)
+    solved four ways: the trained network, no correction, the coarse levels' Jacobi-
+    scaled Chebyshev smoother, and the level operator's exact inverse (tensor-product
+    eigen-solve).  Same workload, tolerance, inner tolerance and graph replay as the
+    headline, with the fallback switched off.  Per variant: iterations, refinements,
+    device time per solve (median of 3 after one warm-up) and the true residual."""
+    import parallelpoissonsolver_gb300 as pps
+    kinds = [("network", pps.COARSE_NETWORK), ("zero", pps.COARSE_ZERO), ("smooth", pps.COARSE_SMOOTH),
+             ("exact", pps.COARSE_EXACT)]
+    s = pps.FlexibleCG(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=True,
+                       inner_tol=args.learned_inner_tol, device=dev)
+    s.set_learned(net, k, gain, pps.LEARNED_PRECONDITIONER | pps.LEARNED_NO_FALLBACK)
+    s.set_learned_cycle(*VCYCLE)
+    s.autotune()
+    out = {"coarse_grid": f"{NET_GRID}^3", "fallback": "off", "timing": "median of 3 solves after 1 warm-up"}
+    for name, kind in kinds:
+        s.set_coarse_solver(kind)
+        solve(s)
+        runs = [solve(s) for _ in range(3)]
+        r = runs[-1]
+        out[name] = {"seconds": statistics.median(x["seconds_solve"] for x in runs), "iterations": r["iterations"],
+                     "refinements": r["refinements"], "err_true": r["err_true"]}
+    s.close()
+    return out
 
 
 def run_learned_128(args, dev: int):

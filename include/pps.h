@@ -194,6 +194,12 @@ pps_status pps_get_stats(const pps_solver* s, pps_stats* stats);
 pps_status pps_get_history(const pps_solver* s, double* out, int cap, int* count);
 /* residualHistory.txt writer (iterativeSolverBaseAlpaka.hpp:620-638). */
 pps_status pps_write_residual_history(const pps_solver* s, const char* path);
+/* solution.dat writer (the alpaka driver's MPI-IO dump, ALP/src/main.cpp:135-146):
+ * the rank's whole guard-padded field x ((n0+2)(n1+2)(n2+2) doubles, memory order)
+ * at byte offset rank * G * 8 of `path`, which is created if missing and not
+ * truncated otherwise.  x may be host or device memory; a device field is copied
+ * on `stream` (a cudaStream_t, NULL = legacy default), after the work queued there. */
+pps_status pps_write_solution(const pps_grid* grid, const double* x, int rank, const char* path, void* stream);
 
 /* Building blocks, on host arrays of the field layout.
  * out = A u at the unknowns (MatrixFreeOperatorA::operator(), FP64). */
@@ -331,6 +337,20 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
  * smoothing there).  fine_degree = 0 (the default) keeps the two-grid cycle around
  * the solver's own Chebyshev preconditioner. */
 pps_status pps_set_learned_cycle(pps_solver* s, int fine_degree, int coarse_degree, double ratio);
+
+/* Coarsest-level solver of the learned multigrid V-cycle (pps_set_learned_cycle).
+ * No counterpart in the reference: it measures what the network earns in the cycle
+ * by putting plain alternatives in its place, with everything else unchanged:
+ *   PPS_COARSE_NETWORK  the attached U-Net (the default);
+ *   PPS_COARSE_ZERO     no correction on the coarsest level;
+ *   PPS_COARSE_SMOOTH   the coarse levels' Jacobi-scaled Chebyshev smoother
+ *                       (coarse_degree >= 2 of pps_set_learned_cycle);
+ *   PPS_COARSE_EXACT    the level operator's exact inverse by a tensor-product
+ *                       eigen-solve (at most 32 unknowns per axis on that level).
+ * The network stays attached (it holds the cycle's level count and settings);
+ * pps_set_learned resets the choice to PPS_COARSE_NETWORK. */
+enum { PPS_COARSE_NETWORK = 0, PPS_COARSE_ZERO = 1, PPS_COARSE_SMOOTH = 2, PPS_COARSE_EXACT = 3 };
+pps_status pps_set_coarse_solver(pps_solver* s, int kind);
 
 /* 2x grid transfers of dense unknown arrays (coarse extents nx, ny, nz; the fine
  * grid has twice as many unknowns per axis, coarse unknown i on fine unknown 2i+1):

@@ -35,6 +35,8 @@ FORMS = {"parity": FORM_PARITY_FP64, "fp64": FORM_FP64, "mixed": FORM_MIXED}
 PRESET_CPU, PRESET_ALPAKA = 0, 1
 PROBLEM_REFERENCE_DEFAULT, PROBLEM_SINE = 0, 1
 LEARNED_INITIAL_GUESS, LEARNED_PRECONDITIONER, LEARNED_NO_FALLBACK, LEARNED_POST_SMOOTH = 1, 2, 4, 8
+# coarsest-level solvers of the learned V-cycle (pps_set_coarse_solver)
+COARSE_NETWORK, COARSE_ZERO, COARSE_SMOOTH, COARSE_EXACT = 0, 1, 2, 3
 
 # Every symbol include/pps.h declares.
 EXPORTED = [
@@ -47,7 +49,8 @@ EXPORTED = [
     "pps_batch_autotune", "pps_batch_tile", "pps_batch_solve",
     "pps_unet_create", "pps_unet_destroy", "pps_unet_param_count", "pps_unet_get_params", "pps_unet_set_params",
     "pps_unet_forward", "pps_unet_gradients", "pps_unet_train_step", "pps_restrict2", "pps_prolong2",
-    "pps_set_learned", "pps_unet_set_activation", "pps_set_learned_cycle",
+    "pps_set_learned", "pps_unet_set_activation", "pps_set_learned_cycle", "pps_set_coarse_solver",
+    "pps_write_solution",
 ]
 
 
@@ -168,6 +171,8 @@ def load(build_if_missing: bool = False):
     L.pps_restrict2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_set_learned.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
     L.pps_set_learned_cycle.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+    L.pps_set_coarse_solver.argtypes = [vp, C.c_int]
+    L.pps_write_solution.argtypes = [C.POINTER(PpsGrid), vp, C.c_int, C.c_char_p, vp]
     L.pps_unet_set_activation.argtypes = [vp, C.c_int]
     L.pps_prolong2.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
     L.pps_status_string.restype = C.c_char_p
@@ -446,6 +451,15 @@ class Solver:
         if st != OK:
             raise PpsError(st, "pps_set_learned_cycle")
 
+    def set_coarse_solver(self, kind: int):
+        """Coarsest-level solver of the learned V-cycle (pps_set_coarse_solver):
+        COARSE_NETWORK (the attached U-Net), COARSE_ZERO (no correction there),
+        COARSE_SMOOTH (the coarse smoother) or COARSE_EXACT (tensor-product
+        eigen-solve), to measure what the network earns."""
+        st = load().pps_set_coarse_solver(self._h, int(kind))
+        if st != OK:
+            raise PpsError(st, "pps_set_coarse_solver")
+
     def tuning_key(self) -> str:
         n = self.grid.npglobal
         return f"{n[0]}x{n[1]}x{n[2]}:form{self.config.form}"
@@ -712,6 +726,20 @@ def apply_operator_noalloc(grid: BlockGrid, u_ptr: int, out_ptr: int, energy_ptr
     energy = sum u*(A u), with no device allocation (see include/pps.h)."""
     return int(load().pps_apply_operator_noalloc(C.byref(grid.c()), C.c_void_p(u_ptr), C.c_void_p(out_ptr),
                                                  C.c_void_p(energy_ptr), C.c_void_p(stream or None)))
+
+
+def write_solution(grid: BlockGrid, x, path: str, rank: int = 0, stream: int = 0):
+    """solution.dat (pps_write_solution): the rank's guard-padded field at byte offset
+    rank * G * 8 of `path`.  x: a float64 numpy field, or a device pointer (int)."""
+    if isinstance(x, np.ndarray):
+        if x.shape != grid.shape or x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise ValueError("x must be a C-contiguous float64 field of the grid's shape")
+        ptr = x.ctypes.data
+    else:
+        ptr = int(x)
+    st = load().pps_write_solution(C.byref(grid.c()), ptr, int(rank), path.encode(), stream or None)
+    if st != OK:
+        raise PpsError(st, "pps_write_solution")
 
 
 def check_solution(grid: BlockGrid, x: np.ndarray, exact: np.ndarray):

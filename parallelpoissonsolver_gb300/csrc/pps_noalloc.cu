@@ -95,6 +95,11 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
     g.sj = grid->npglobal[0] + 2;
     g.sk = g.sj * (grid->npglobal[1] + 2);
     g.ntot = g.sk * (grid->npglobal[2] + 2);
+    const Shape sh = make_shape(g, 8, sm_count() * 8 * 4);
+    if (sh.nblocks() > (unsigned)PPS_NOALLOC_MAX_BLOCKS)
+        return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: the grid needs " +
+                                             std::to_string(sh.nblocks()) + " blocks of partial sums; the "
+                                             "static scratch holds " + std::to_string(PPS_NOALLOC_MAX_BLOCKS));
     {
         const uintptr_t nb = (uintptr_t)g.ntot * sizeof(double);
         const uintptr_t u0 = (uintptr_t)u_dev, o0 = (uintptr_t)out_dev, e0 = (uintptr_t)energy_dev;
@@ -102,11 +107,6 @@ extern "C" pps_status pps_apply_operator_noalloc(const pps_grid* grid, const dou
         if (overlap(u0, nb, o0, nb) || overlap(e0, sizeof(double), u0, nb) || overlap(e0, sizeof(double), o0, nb))
             return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: u, out and energy must not overlap");
     }
-    const Shape sh = make_shape(g, 8, sm_count() * 8 * 4);
-    if (sh.nblocks() > (unsigned)PPS_NOALLOC_MAX_BLOCKS)
-        return fail(PPS_ERR_INVALID_ARG, "pps_apply_operator_noalloc: the grid needs " +
-                                             std::to_string(sh.nblocks()) + " blocks of partial sums; the "
-                                             "static scratch holds " + std::to_string(PPS_NOALLOC_MAX_BLOCKS));
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)

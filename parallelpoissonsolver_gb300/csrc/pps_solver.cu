@@ -25,6 +25,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <sys/types.h>
 #include <vector>
 
 using namespace pps;
@@ -164,6 +165,10 @@ struct pps_solver {
     double cyc_ratio = 8.0;
     std::vector<float*> dt;
     float *cY = nullptr, *cZ = nullptr, *cW = nullptr;
+    // coarsest-level solver of the cycle (pps_set_coarse_solver); d_exact: the
+    // eigen-solve's matrices for PPS_COARSE_EXACT
+    int coarse_kind = PPS_COARSE_NETWORK;
+    float* d_exact = nullptr;
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
@@ -285,7 +290,7 @@ void free_all(pps_solver* s)
     for (float* q : s->dn) cudaFree(q);
     for (float* q : s->dn_e) cudaFree(q);
     for (float* q : s->dt) cudaFree(q);
-    for (float* q : {s->cY, s->cZ, s->cW}) cudaFree(q);
+    for (float* q : {s->cY, s->cZ, s->cW, s->d_exact}) cudaFree(q);
     for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -772,6 +777,30 @@ unet::Dims dense_dims(const pps_solver* s, int level)
     return unet::Dims{(g.hi[2] - g.lo[2]) / f, (g.hi[1] - g.lo[1]) / f, (g.hi[0] - g.lo[0]) / f};
 }
 
+unet::DLevel level_op(const pps_solver* s, int l);
+void dense_cheb(pps_solver* s, int l, const float* B, float* X, bool acc);
+
+// The coarsest level's correction z_k from its residual r_k: the network (gain
+// N(r_k)), or the alternative pps_set_coarse_solver chose.
+void coarse_solve(pps_solver* s, int k, const float* r, float* z)
+{
+    const unet::Dims dc = dense_dims(s, k);
+    switch (s->coarse_kind) {
+    case PPS_COARSE_ZERO:
+        unet::level_zero(dc, z, s->stream);
+        break;
+    case PPS_COARSE_SMOOTH:
+        dense_cheb(s, k, r, z, false);
+        break;
+    case PPS_COARSE_EXACT:
+        unet::level_exact(dc, s->d_exact, r, z, s->stream);
+        break;
+    default:
+        if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, r, z, s->net_gain, s->stream) != PPS_OK)
+            throw CudaFail{cudaErrorUnknown};
+    }
+}
+
 // X += gain P^k N(R^k (r - A z)) at the unknowns (R^k r when z is null).  For
 // coarsen k >= 1 the first restriction reads the solver fields and the last
 // prolongation adds into X, so no fine-grid dense array exists; levels 1..k are
@@ -789,9 +818,7 @@ void learned_coarse_correction(pps_solver* s, const T* r, const T* z, T* X)
         unet::field_residual_restrict<T>(g, r, z, dense_dims(s, 1), s->dn[1], st);
         for (int l = 1; l < k; l++) unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
     }
-    const unet::Dims dc = dense_dims(s, k);
-    if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, s->dn[(size_t)k], s->dn_e[(size_t)k], s->net_gain, st) != PPS_OK)
-        throw CudaFail{cudaErrorUnknown};
+    coarse_solve(s, k, s->dn[(size_t)k], s->dn_e[(size_t)k]);
     if (k == 0) {
         unet::dense_to_field<T>(g, s->dn_e[0], X, 1.0f, 1, st);
     } else {
@@ -908,9 +935,7 @@ bool learned_vcycle(pps_solver* s, Fields<T>& F, T* B, T* X, Launcher& L, const 
             unet::restrict2(dense_dims(s, l + 1), s->dn[(size_t)l], s->dn[(size_t)l + 1], st);
         }
     }
-    const unet::Dims dc = dense_dims(s, k);
-    if (pps_internal_unet_apply(s->net, dc.W, dc.H, dc.D, s->dn[(size_t)k], s->dn_e[(size_t)k], s->net_gain, st) != PPS_OK)
-        throw CudaFail{cudaErrorUnknown};
+    coarse_solve(s, k, s->dn[(size_t)k], s->dn_e[(size_t)k]);
     for (int l = k - 1; l >= 1; l--) {
         if (s->cyc_coarse > 0) {
             unet::prolong2_add(dense_dims(s, l + 1), s->dn_e[(size_t)l + 1], s->dn_e[(size_t)l], st);
@@ -2063,6 +2088,70 @@ pps_status pps_write_residual_history(const pps_solver* s, const char* path)
     return PPS_OK;
 }
 
+pps_status pps_write_solution(const pps_grid* grid, const double* x, int rank, const char* path, void* stream)
+{
+    // solution.dat of the alpaka driver (ALP/src/main.cpp:135-146): the rank's whole
+    // guard-padded field, raw doubles in memory order, at byte offset rank * G * 8 of
+    // the file, which is created if missing and otherwise not truncated
+    // (MPI_MODE_CREATE | MPI_MODE_WRONLY), so the ranks' blocks can share one file.
+    if (!grid || !x || !path || rank < 0) return PPS_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; d++)
+        if (grid->npglobal[d] < 1) {
+            set_error("npglobal must be >= 1");
+            return PPS_ERR_INVALID_ARG;
+        }
+    const long long G = (long long)(grid->npglobal[0] + 2) * (grid->npglobal[1] + 2) * (grid->npglobal[2] + 2);
+    cudaPointerAttributes at{};
+    const bool on_device = cudaPointerGetAttributes(&at, x) == cudaSuccess && at.type == cudaMemoryTypeDevice;
+    cudaGetLastError();   // a host pointer unknown to CUDA is not an error here
+    FILE* f = fopen(path, "r+b");
+    if (!f) f = fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("cannot open ") + path);
+        return PPS_ERR_INVALID_ARG;
+    }
+    pps_status rc = PPS_OK;
+    if (fseeko(f, (off_t)rank * (off_t)G * (off_t)sizeof(double), SEEK_SET) != 0) {
+        set_error(std::string("cannot seek in ") + path);
+        rc = PPS_ERR_INVALID_ARG;
+    } else if (!on_device) {
+        if (fwrite(x, sizeof(double), (size_t)G, f) != (size_t)G) {
+            set_error(std::string("short write to ") + path);
+            rc = PPS_ERR_INVALID_ARG;
+        }
+    } else {
+        // device field: staged through pinned chunks, copied on the caller's stream so
+        // they follow the work that produced x
+        rc = guarded([&]() -> pps_status {
+            CK(cudaSetDevice(at.device));
+            cudaStream_t st = (cudaStream_t)stream;
+            const long long chunk = std::min<long long>(G, 8LL << 20);
+            double* stage = nullptr;
+            CK(cudaMallocHost((void**)&stage, sizeof(double) * (size_t)chunk));
+            pps_status r = PPS_OK;
+            for (long long off = 0; off < G && r == PPS_OK; off += chunk) {
+                const long long n = std::min(chunk, G - off);
+                cudaError_t e = cudaMemcpyAsync(stage, x + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) {
+                    set_error(std::string("copying the solution: ") + cudaGetErrorString(e));
+                    r = PPS_ERR_CUDA;
+                } else if (fwrite(stage, sizeof(double), (size_t)n, f) != (size_t)n) {
+                    set_error(std::string("short write to ") + path);
+                    r = PPS_ERR_INVALID_ARG;
+                }
+            }
+            cudaFreeHost(stage);
+            return r;
+        });
+    }
+    if (fclose(f) != 0 && rc == PPS_OK) {
+        set_error(std::string("cannot close ") + path);
+        rc = PPS_ERR_INVALID_ARG;
+    }
+    return rc;
+}
+
 pps_status pps_apply_operator(pps_solver* s, const double* u, double* out)
 {
     if (!s || !u || !out) return PPS_ERR_INVALID_ARG;
@@ -2189,11 +2278,12 @@ pps_status pps_set_learned(pps_solver* s, pps_unet* net, int coarsen, double gai
         for (float* q : s->dn) cudaFree(q);
         for (float* q : s->dn_e) cudaFree(q);
         for (float* q : s->dt) cudaFree(q);
-        for (float* q : {s->cY, s->cZ, s->cW}) cudaFree(q);
+        for (float* q : {s->cY, s->cZ, s->cW, s->d_exact}) cudaFree(q);
         s->dn.clear();
         s->dn_e.clear();
         s->dt.clear();
-        s->cY = s->cZ = s->cW = nullptr;
+        s->cY = s->cZ = s->cW = s->d_exact = nullptr;
+        s->coarse_kind = PPS_COARSE_NETWORK;
         s->net = nullptr;
         if (!net) return PPS_OK;   // detach
         if (s->cfg.form == PPS_FORM_PARITY_FP64) {
@@ -2273,6 +2363,45 @@ pps_status pps_set_learned_cycle(pps_solver* s, int fine_degree, int coarse_degr
         s->gexec = nullptr;
     }
     return PPS_OK;
+}
+
+pps_status pps_set_coarse_solver(pps_solver* s, int kind)
+{
+    if (!s) return PPS_ERR_INVALID_ARG;
+    return guarded([&]() -> pps_status {
+        if (kind < PPS_COARSE_NETWORK || kind > PPS_COARSE_EXACT) {
+            set_error("coarse solver: PPS_COARSE_NETWORK, _ZERO, _SMOOTH or _EXACT");
+            return PPS_ERR_INVALID_ARG;
+        }
+        if (kind != PPS_COARSE_NETWORK && !s->net) {
+            set_error("attach the network (pps_set_learned) before choosing its coarse-level alternative");
+            return PPS_ERR_INVALID_ARG;
+        }
+        if (kind == PPS_COARSE_SMOOTH && s->cyc_coarse < 2) {
+            set_error("PPS_COARSE_SMOOTH needs coarse_degree >= 2 (pps_set_learned_cycle)");
+            return PPS_ERR_INVALID_ARG;
+        }
+        CK(cudaSetDevice(s->device));
+        if (kind == PPS_COARSE_EXACT && !s->d_exact) {
+            const int k = s->net_coarsen;
+            std::vector<float> mats;
+            if (!unet::level_exact_data(dense_dims(s, k), level_op(s, k), mats)) {
+                set_error("PPS_COARSE_EXACT takes at most 32 unknowns per axis on the coarsest level");
+                return PPS_ERR_INVALID_ARG;
+            }
+            CK(unet::level_exact_prepare());
+            CK(cudaMalloc((void**)&s->d_exact, sizeof(float) * mats.size()));
+            CK(cudaMemcpyAsync(s->d_exact, mats.data(), sizeof(float) * mats.size(), cudaMemcpyHostToDevice,
+                               s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+        }
+        s->coarse_kind = kind;
+        if (s->gexec) {   // a captured iteration holds the old coarse solver
+            cudaGraphExecDestroy(s->gexec);
+            s->gexec = nullptr;
+        }
+        return PPS_OK;
+    });
 }
 
 pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out)

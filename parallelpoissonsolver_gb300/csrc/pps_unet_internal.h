@@ -4,6 +4,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/pps.h"
 #include "pps_internal.h"
 
@@ -94,6 +96,19 @@ void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, co
                              cudaStream_t s);
 void level_cheb(const Dims& d, const DLevel& L, const float* Y, const float* B, const float* Z, float* W,
                 const LCoef& c, bool first, bool acc, cudaStream_t s);
+// Exact solve z = A_l^-1 r on a coarse level of at most LEVEL_EXACT_MAX unknowns per
+// axis.  mats holds, per axis x, y, z of extents n_a, the 1-D level operator's
+// eigenvector matrix V_a (n_a x n_a, row-major), its inverse and its eigenvalues:
+// [Vx^-1, Vy^-1, Vz^-1, Vx, Vy, Vz, lam_x, lam_y, lam_z] (level_exact_data builds it).
+constexpr int LEVEL_EXACT_MAX = 32;
+void level_exact(const Dims& d, const float* mats, const float* r, float* z, cudaStream_t s);
+// Host: mats of level_exact for level operator L on dims d (double eigen-solve,
+// stored as float).  Returns false when an axis is longer than LEVEL_EXACT_MAX.
+bool level_exact_data(const Dims& d, const DLevel& L, std::vector<float>& mats);
+// Lets k_level_exact use the shared memory of a 32^3 level (current device).
+cudaError_t level_exact_prepare();
+// z = 0 on a dense level (the zero coarse correction)
+void level_zero(const Dims& d, float* z, cudaStream_t s);
 
 }  // namespace unet
 }  // namespace pps

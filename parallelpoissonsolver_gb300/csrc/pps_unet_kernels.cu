@@ -11,6 +11,7 @@
 #include "pps_reduce.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 #include <cuda_bf16.h>
@@ -1277,6 +1278,179 @@ void level_residual_restrict(const Dims& dc, const DLevel& L, const float* Y, co
     const int zc = (int)((dc.D + chunks - 1) / chunks);
     const dim3 grid((unsigned)tx, (unsigned)ty, (unsigned)((dc.D + zc - 1) / zc));
     launch_pdl(k_level_residual_restrict, grid, dim3(32, 4), 0, s, dc, L, zc, Y, B, coarse, g_stop);
+    launches_counter_add(1);
+}
+
+// Exact coarse-level solve.  Each axis's 1-D level operator A_a (tridiagonal, the
+// wall gap in its last row) is diagonalisable, A_a = V_a diag(lam_a) V_a^-1, so the
+// level operator A = A_x + A_y + A_z (each acting along its axis) has the inverse
+// (V_z V_y V_x) diag(1 / (lam_x + lam_y + lam_z)) (V_z^-1 V_y^-1 V_x^-1).  One block
+// holds the level in shared memory; each pass transforms every line along one axis,
+// a thread per line (the line is read into registers first, so the pass is in place).
+__device__ void exact_pass(float* cube, const float* M, int n_a, int stride, int W, int H, int D, int axis)
+{
+    float v[LEVEL_EXACT_MAX];
+    const int lines = W * H * D / n_a;
+    for (int t = threadIdx.x; t < lines; t += blockDim.x) {
+        int base;
+        if (axis == 0) base = t * W;                                     // lines along x: (y, z)
+        else if (axis == 1) base = (t % W) + (t / W) * W * H;             // along y: (x, z)
+        else base = t;                                                   // along z: (x, y)
+        for (int m = 0; m < n_a; m++) v[m] = cube[base + m * stride];
+        for (int i = 0; i < n_a; i++) {
+            float acc = 0.f;
+            for (int m = 0; m < n_a; m++) acc = fmaf(M[i * n_a + m], v[m], acc);
+            cube[base + i * stride] = acc;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(512) k_level_exact(Dims d, const float* __restrict__ mats,
+                                                     const float* __restrict__ r, float* __restrict__ z,
+                                                     const int* done)
+{
+    pdl_enter();
+    EARLY_EXIT(done);
+    extern __shared__ float sm[];
+    const int W = d.W, H = d.H, D = d.D, n = W * H * D;
+    const int nm = 2 * (W * W + H * H + D * D) + W + H + D;
+    float* cube = sm;
+    float* M = sm + n;
+    for (int i = threadIdx.x; i < nm; i += blockDim.x) M[i] = mats[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) cube[i] = r[i];
+    __syncthreads();
+    const float* Vix = M;
+    const float* Viy = Vix + W * W;
+    const float* Viz = Viy + H * H;
+    const float* Vx = Viz + D * D;
+    const float* Vy = Vx + W * W;
+    const float* Vz = Vy + H * H;
+    const float* lx = Vz + D * D;
+    const float* ly = lx + W;
+    const float* lz = ly + H;
+    exact_pass(cube, Vix, W, 1, W, H, D, 0);
+    __syncthreads();
+    exact_pass(cube, Viy, H, W, W, H, D, 1);
+    __syncthreads();
+    exact_pass(cube, Viz, D, W * H, W, H, D, 2);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int x = i % W, y = (i / W) % H, zz = i / (W * H);
+        cube[i] = cube[i] / (lx[x] + ly[y] + lz[zz]);
+    }
+    __syncthreads();
+    exact_pass(cube, Vx, W, 1, W, H, D, 0);
+    __syncthreads();
+    exact_pass(cube, Vy, H, W, W, H, D, 1);
+    __syncthreads();
+    exact_pass(cube, Vz, D, W * H, W, H, D, 2);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) z[i] = cube[i];
+}
+
+void level_exact(const Dims& d, const float* mats, const float* r, float* z, cudaStream_t s)
+{
+    const size_t smem = sizeof(float) * ((size_t)d.W * d.H * d.D + 2 * (d.W * d.W + d.H * d.H + d.D * d.D) + d.W +
+                                         d.H + d.D);
+    launch_pdl(k_level_exact, 1, 512, smem, s, d, mats, r, z, g_stop);
+    launches_counter_add(1);
+}
+
+// Symmetric eigen-solve by cyclic Jacobi rotations (n <= 32, double): S = Q diag(w) Q^T.
+static void jacobi_eigen(int n, std::vector<double>& S, std::vector<double>& Q, std::vector<double>& w)
+{
+    Q.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++) Q[(size_t)i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0.0, diag = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) (i == j ? diag : off) += S[(size_t)i * n + j] * S[(size_t)i * n + j];
+        if (off <= 1e-30 * diag) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int q = p + 1; q < n; q++) {
+                const double apq = S[(size_t)p * n + q];
+                if (apq == 0.0) continue;
+                const double app = S[(size_t)p * n + p], aqq = S[(size_t)q * n + q];
+                const double theta = (aqq - app) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < n; k++) {   // S <- J^T S J, rows then columns
+                    const double skp = S[(size_t)k * n + p], skq = S[(size_t)k * n + q];
+                    S[(size_t)k * n + p] = c * skp - sn * skq;
+                    S[(size_t)k * n + q] = sn * skp + c * skq;
+                }
+                for (int k = 0; k < n; k++) {
+                    const double spk = S[(size_t)p * n + k], sqk = S[(size_t)q * n + k];
+                    S[(size_t)p * n + k] = c * spk - sn * sqk;
+                    S[(size_t)q * n + k] = sn * spk + c * sqk;
+                }
+                for (int k = 0; k < n; k++) {   // Q <- Q J
+                    const double qkp = Q[(size_t)k * n + p], qkq = Q[(size_t)k * n + q];
+                    Q[(size_t)k * n + p] = c * qkp - sn * qkq;
+                    Q[(size_t)k * n + q] = sn * qkp + c * qkq;
+                }
+            }
+    }
+    w.resize(n);
+    for (int i = 0; i < n; i++) w[i] = S[(size_t)i * n + i];
+}
+
+cudaError_t level_exact_prepare()
+{
+    // the largest level (32^3) needs 150 KiB of shared memory
+    return cudaFuncSetAttribute(k_level_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+bool level_exact_data(const Dims& d, const DLevel& L, std::vector<float>& mats)
+{
+    const int ext[3] = {d.W, d.H, d.D};
+    for (int a = 0; a < 3; a++)
+        if (ext[a] < 1 || ext[a] > LEVEL_EXACT_MAX) return false;
+    std::vector<float> vinv, v, lam;
+    for (int a = 0; a < 3; a++) {
+        const int n = ext[a];
+        // the 1-D operator: diagonal -2/H^2 (last: -2/(H h)), upper 1/H^2, lower 1/H^2
+        // (last row: 2/(H (H+h))).  With d_0 = 1, d_{i+1} = d_i sqrt(lower_i / upper_i)
+        // it is D S D^-1 with S symmetric (off-diagonals sqrt(upper * lower)).
+        std::vector<double> diag(n), up(n > 1 ? n - 1 : 0), lo(n > 1 ? n - 1 : 0);
+        for (int i = 0; i < n; i++) diag[i] = -2.0 * L.ih2[a];
+        diag[n - 1] = L.last_c[a];
+        for (int i = 0; i + 1 < n; i++) {
+            up[i] = L.ih2[a];
+            lo[i] = (i + 1 == n - 1) ? L.last_m[a] : L.ih2[a];
+        }
+        std::vector<double> dsc(n, 1.0);
+        for (int i = 0; i + 1 < n; i++) dsc[i + 1] = dsc[i] * std::sqrt(lo[i] / up[i]);
+        std::vector<double> S((size_t)n * n, 0.0), Q, w;
+        for (int i = 0; i < n; i++) S[(size_t)i * n + i] = diag[i];
+        for (int i = 0; i + 1 < n; i++) S[(size_t)i * n + i + 1] = S[(size_t)(i + 1) * n + i] = std::sqrt(up[i] * lo[i]);
+        jacobi_eigen(n, S, Q, w);
+        // V = D Q, V^-1 = Q^T D^-1
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) vinv.push_back((float)(Q[(size_t)j * n + i] / dsc[j]));
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) v.push_back((float)(dsc[i] * Q[(size_t)i * n + j]));
+        for (int i = 0; i < n; i++) lam.push_back((float)w[i]);
+    }
+    mats.clear();
+    mats.insert(mats.end(), vinv.begin(), vinv.end());
+    mats.insert(mats.end(), v.begin(), v.end());
+    mats.insert(mats.end(), lam.begin(), lam.end());
+    return true;
+}
+
+__global__ void k_level_zero(long long n, float* __restrict__ z, const int* done)
+{
+    pdl_enter();
+    EARLY_EXIT(done);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        z[i] = 0.f;
+}
+
+void level_zero(const Dims& d, float* z, cudaStream_t s)
+{
+    const long long n = (long long)d.W * d.H * d.D;
+    launch_pdl(k_level_zero, eblocks(n), 256, 0, s, n, z, g_stop);
     launches_counter_add(1);
 }
 

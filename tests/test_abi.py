@@ -179,3 +179,21 @@ def test_cpp_shim_instantiates_every_composition(tmp_path):
     src.write_text(SHIM_COMPOSITIONS)
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", INCLUDE, str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_write_solution_host_field(pps_lib, tmp_path):
+    """solution.dat (ALP/src/main.cpp:135-146): each rank's guard-padded field, raw
+    doubles, at offset rank * G * 8; the file is not truncated, so ranks share it.
+    Host fields need no GPU."""
+    grid = pps_lib.BlockGrid(npglobal=(5, 4, 3), ds=(0.1, 0.1, 0.1))
+    rng = __import__("numpy").random.default_rng(0)
+    x0, x1 = rng.standard_normal(grid.shape), rng.standard_normal(grid.shape)
+    path = str(tmp_path / "solution.dat")
+    pps_lib.write_solution(grid, x1, path, rank=1)
+    pps_lib.write_solution(grid, x0, path, rank=0)      # rank 0 after rank 1: no truncation
+    data = __import__("numpy").fromfile(path, dtype="<f8")
+    G = x0.size
+    assert data.size == 2 * G
+    assert (data[:G] == x0.ravel()).all() and (data[G:] == x1.ravel()).all()
+    with pytest.raises(ValueError):
+        pps_lib.write_solution(grid, x0[:-1], path)

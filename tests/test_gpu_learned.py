@@ -218,13 +218,17 @@ def _jacobi_cheb(b, H, h, ratio, n):
     return -s
 
 
-@pytest.mark.parametrize("form,m,fd,cd", [("fp64", 128, 3, 4), ("fp64", 64, 4, 0), ("mixed", 128, 3, 4)])
-def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
+@pytest.mark.parametrize("form,m,fd,cd,coarse", [("fp64", 128, 3, 4, "network"), ("fp64", 64, 4, 0, "network"),
+                                                  ("mixed", 128, 3, 4, "network"), ("fp64", 128, 3, 4, "exact"),
+                                                  ("mixed", 128, 3, 4, "exact"), ("fp64", 128, 3, 4, "zero"),
+                                                  ("fp64", 128, 3, 4, "smooth")])
+def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd, coarse):
     """The multigrid form of the learned cycle, rebuilt level by level in numpy:
     Chebyshev smoothing on [lmax/ratio, lmax] of the solver's grid, Jacobi-scaled
     Chebyshev on the coarse levels (spacing 2^l h, upper wall h above the last
-    unknown), residual restriction, the network on the coarsest level, prolongation,
-    post-smoothing."""
+    unknown), residual restriction, the coarsest level's solver (the network, or the
+    alternatives of pps_set_coarse_solver: the exact level inverse, no correction,
+    the coarse smoother), prolongation, post-smoothing."""
     net = pps.UNet((16, 32, 64), seed=4, linear=True)
     k = int(round(math.log2(m / 32)))
     gain, ratio = 0.6, 8.0
@@ -233,6 +237,9 @@ def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
     s = pps.FlexibleCG(grid, pps.ChebyshevIteration(11), form=form)
     s.set_learned(net, k, gain, pps.LEARNED_PRECONDITIONER | pps.LEARNED_POST_SMOOTH)
     s.set_learned_cycle(fd, cd, ratio)
+    kinds = {"network": pps.COARSE_NETWORK, "exact": pps.COARSE_EXACT, "zero": pps.COARSE_ZERO,
+             "smooth": pps.COARSE_SMOOTH}
+    s.set_coarse_solver(kinds[coarse])
     got = s.apply_preconditioner(b.copy())
 
     inner = (slice(2, m + 2),) * 3
@@ -246,6 +253,12 @@ def test_learned_vcycle_matches_its_composition(gpu, form, m, fd, cd):
         return _along_axes([2.0 * _restrict_1d(2 * c.shape[0]).T] * 3, c)
 
     def network(r):
+        if coarse == "exact":   # A_k^-1 r: spacing 2^k h, upper wall h above the last unknown
+            return learned.level_solve(torch.from_numpy(r), h * 2 ** k, 2.0 ** -k).numpy()
+        if coarse == "zero":
+            return np.zeros_like(r)
+        if coarse == "smooth":
+            return _jacobi_cheb(r, h * 2 ** k, h, ratio, cd)
         cin = torch.from_numpy(np.ascontiguousarray(r, np.float32)).cuda()
         cout = torch.empty_like(cin)
         net.forward(r.shape, cin.data_ptr(), cout.data_ptr(), normalize=True)
