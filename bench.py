@@ -15,7 +15,10 @@ and write is shared with the machine's other jobs, and a contended copy can run 
 a fraction of its usual rate; the mean and every sample are listed beside it).  The
 reference method (BiCGSTAB + Chebyshev) is timed beside it in mixed
 precision and in plain FP64.  Every field is 0.5-1.1 GB, far larger than the 129 MB L2, so no L2 flush
-is needed between steps.
+is needed between steps.  Outside the timed region the line also carries: the
+headline's V-cycle with its coarsest level solved without the network (what the
+network earns), the compositions at 256^3, the batched solves, the learned
+preconditioner at 128^3, and the 1024^3 charges solve (mixed+learned and plain FP64).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--size M] [--impl reference]
   python bench.py --profile-case ...     (one capped solve for an ncu capture, no bench line)
@@ -470,9 +473,10 @@ def run_learned_128(args, dev: int):
 
 
 def run_large(args, dev: int):
-    """Config 5 (opt-in, --large): one 1024^3 Dirichlet solve of 64 Gaussian charges on a
-    k^-3 background, the mixed + learned V-cycle (network on the 16^3 level, six
-    coarsenings) against the plain FP64 BiCGSTAB + Chebyshev path, both to 1e-10."""
+    """Config 5 (default on; --no-large skips it): one 1024^3 Dirichlet solve of 64
+    Gaussian charges on a k^-3 background, the mixed + learned V-cycle (network on the
+    16^3 level, six coarsenings; two timed solves after a warm-up) against the plain
+    FP64 BiCGSTAB + Chebyshev path (one solve), both to 1e-10."""
     import math
 
     import torch
@@ -890,7 +894,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-compositions", action="store_true")
     ap.add_argument("--comp-size", type=int, default=256)
-    ap.add_argument("--large", action="store_true", help="also run the 1024^3 charges solve (several minutes)")
+    ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 charges solve (config 5, ~3 min)")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=64, help="held-out right-hand sides of the 128^3 solves")
     ap.add_argument("--held-out-pairs", type=int, default=1000, help="held-out pairs the network is scored on")
@@ -916,7 +920,7 @@ def main():
         out["batched"] = run_batched(args, dist)
     if not args.no_compositions and dist.rank == 0:
         out["compositions"] = run_compositions(args, dist.local, threads)
-    if args.large:
+    if not args.no_large and dist.rank == 0:
         out["large_1024"] = run_large(args, dist.local)
     if dist.rank == 0:
         if not args.no_cpu_baseline:
