@@ -605,6 +605,10 @@ __global__ void __launch_bounds__(256) k_canon_finalize(RedCtx rc, const int* do
     }
 }
 
+// Equal weights on the three axes (equal spacings): the FP64 kernels then sum the six
+// neighbours on the integer pipe.
+static inline bool iso_coef(const Coef& c) { return c.cx == c.cy && c.cx == c.cz; }
+
 template <int NS>
 static void canon_finalize(const RedCtx& rc, const int* done, cudaStream_t s)
 {
@@ -1704,6 +1708,122 @@ __device__ __forceinline__ long long malign(const MI& a, int E)
     return a.m >> min(E - a.e, 63);
 }
 
+// FP64 kernels on equal spacings (cx = cy = cz): GB300 issues FP64 at 1/64 of the
+// FP32 rate, so the plain FP64 stencil (three pair sums and four multiply-adds) is
+// bound by the FP64 pipe, not by HBM.  With one weight for the six neighbours their
+// sum moves to the integer pipe: each value as m * 2^(e-1075) (msplit), aligned to
+// the largest exponent E by an arithmetic shift, summed exactly in int64
+// (|sum| < 6 * 2^53), converted once, and scaled by 2^(E-1075) in the exponent bits.
+// The shifts drop at most one unit of 2^(E-1075) per value, the rounding FP64
+// additions of the same values have anyway.  Returns false when a value is Inf/NaN
+// (E = 2047) or the scaling would leave the normal range (E < 53 or E > 2000); the
+// caller then adds in FP64.
+__device__ __forceinline__ bool nsum6(const MI& a, const MI& b, const MI& c, const MI& d, const MI& e, const MI& f,
+                                      double& out)
+{
+    const int E = max(max(max(a.e, b.e), max(c.e, d.e)), max(e.e, f.e));
+    if (E < 53 || E > 2000) return false;
+    const long long S = malign(a, E) + malign(b, E) + malign(c, E) + malign(d, E) + malign(e, E) + malign(f, E);
+    if (S == 0) {
+        out = 0.0;
+        return true;
+    }
+    out = __longlong_as_double(__double_as_longlong(__ll2double_rn(S)) + ((long long)(E - 1075) << 52));
+    return true;
+}
+
+// The Chebyshev steps of the FP64 form on equal spacings (one column per thread, z
+// kept in registers with its integer split):
+//   MODE 0: W = cc U + cx (sum of U's six neighbours)               (s1, U = B)
+//   MODE 1: W = cc U + cx (six-neighbour sum) + cb B                 (first sweep)
+//   MODE 2: W = cc U + cx (six-neighbour sum) + cb B + cw Z          (later sweeps)
+// with the coefficients of k_cheb_s01 / k_cheb_sweep: 3, 4 or 5 FP64 operations per
+// unknown instead of 8 or 9.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cheb_iso64(Geo g, Shape sh, const double* __restrict__ U,
+                                                    const double* __restrict__ B, const double* __restrict__ Z,
+                                                    double* __restrict__ W, CT<double> cf, const int* done)
+{
+    pdl_enter();
+    EARLY_EXIT(done);
+    const Col q = column(g, sh);
+    if (!q.active) return;
+    const long long sj = g.sj, sk = g.sk;
+    long long c = q.c;
+    double um = U[c - sk], uc = U[c];
+    MI mm = msplit(um), mc = msplit(uc);
+#pragma unroll 2
+    for (int k = q.k0; k < q.k1; k++) {
+        const double up = U[c + sk];
+        const double xw = U[c - 1], xe = U[c + 1], ys = U[c - sj], yn = U[c + sj];
+        const MI mp = msplit(up);
+        double s6, w;
+        if (nsum6(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
+            w = fmx(cf.cx, s6, cf.cc * uc);
+        } else {
+            w = cf.cc * uc;
+            w = fmx(cf.cx, xw + xe, w);
+            w = fmx(cf.cy, ys + yn, w);
+            w = fmx(cf.cz, um + up, w);
+        }
+        if (MODE >= 1) w = fmx(cf.cb, B[c], w);
+        if (MODE == 2) w = fmx(cf.cw, Z[c], w);
+        W[c] = w;
+        um = uc;
+        uc = up;
+        mm = mc;
+        mc = mp;
+        c += sk;
+    }
+}
+
+// Au = A u with the six-neighbour sum on the integer pipe (equal spacings), and
+// NS = 1: sum w.Au (k_stencil_dot, w = r0); NS = 2: sums w.Au, Au.Au (k_stencil_dot2,
+// w = r).  Three FP64 operations per unknown for A u instead of seven.
+template <int NS>
+__global__ void __launch_bounds__(256) k_stencil_dots_iso64(Geo g, Shape sh, const double* __restrict__ u,
+                                                            const double* __restrict__ w, double* __restrict__ Au,
+                                                            Coef cf, RedCtx rc)
+{
+    pdl_enter();
+    EARLY_EXIT(&rc.st->done);
+    const Col q = column(g, sh);
+    Acc<double> a1, a2;
+    if (q.active) {
+        const long long sj = g.sj, sk = g.sk;
+        long long c = q.c;
+        double um = u[c - sk], uc = u[c];
+        MI mm = msplit(um), mc = msplit(uc);
+#pragma unroll 2
+        for (int k = q.k0; k < q.k1; k++) {
+            const double up = u[c + sk];
+            const double xw = u[c - 1], xe = u[c + 1], ys = u[c - sj], yn = u[c + sj];
+            const MI mp = msplit(up);
+            double s6, a;
+            if (nsum6(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
+                a = fmx(cf.cx, s6, cf.cc * uc);
+            } else {
+                a = cf.cc * uc;
+                a = fmx(cf.cx, xw + xe, a);
+                a = fmx(cf.cy, ys + yn, a);
+                a = fmx(cf.cz, um + up, a);
+            }
+            Au[c] = a;
+            a1.add(w[c], a);
+            if (NS == 2) a2.add(a, a);
+            um = uc;
+            uc = up;
+            mm = mc;
+            mc = mp;
+            c += sk;
+        }
+    }
+    double v[NS];
+    v[0] = a1.value();
+    if (NS == 2) v[NS - 1] = a2.value();
+    reduce_emit<NS>(v, rc, sh);
+}
+
 // Counts the entries of a whole field (guard layers included) whose bit pattern is
 // not +-0, in 16-byte vectors.
 __global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double* __restrict__ x, RedCtx rc)
@@ -2022,6 +2142,14 @@ void fast_cheb_s01(const Geo& g, const Shape& sh, const T* B, T* Y, const Coef& 
         fast_cheb_s01<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), B, Y, cy, done, s);   // scalar tiles
         return;
     }
+    if constexpr (std::is_same<T, double>::value) {
+        if (iso_coef(cy)) {   // equal spacings: the neighbour sum on the integer pipe
+            const Shape c1 = sh.cx == 1 ? sh : make_shape(g, sh.ty, (int)sh.nblocks(), 1);
+            launch_pdl(k_cheb_iso64<0>, grid_of(c1), block_of(c1), 0, s, g, c1, B, nullptr, nullptr, Y, c, done);
+            PPS_COUNT_LAUNCH();
+            return;
+        }
+    }
     if (sh.cx == 2) launch_pdl(k_cheb_s01<T, 2>, grid_of(sh), block_of(sh), 0, s, g, sh, B, Y, c, done);
     else launch_pdl(k_cheb_s01<T, 1>, grid_of(sh), block_of(sh), 0, s, g, sh, B, Y, c, done);
     PPS_COUNT_LAUNCH();
@@ -2042,6 +2170,15 @@ void fast_cheb_sweep(const Geo& g, const Shape& sh, const T* Y, const T* B, cons
         }
         fast_cheb_sweep<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), Y, B, Z, W, cf, done, s);   // scalar tiles
         return;
+    }
+    if constexpr (std::is_same<T, double>::value) {
+        if (iso_coef(cf)) {   // equal spacings: the neighbour sum on the integer pipe
+            const Shape c1 = sh.cx == 1 ? sh : make_shape(g, sh.ty, (int)sh.nblocks(), 1);
+            if (Z) launch_pdl(k_cheb_iso64<2>, grid_of(c1), block_of(c1), 0, s, g, c1, Y, B, Z, W, c, done);
+            else launch_pdl(k_cheb_iso64<1>, grid_of(c1), block_of(c1), 0, s, g, c1, Y, B, Z, W, c, done);
+            PPS_COUNT_LAUNCH();
+            return;
+        }
     }
     if (Z) {
         if (sh.cx == 2) launch_pdl(k_cheb_sweep<T, 2, true>, grid_of(sh), block_of(sh), 0, s, g, sh, Y, B, Z, W, c, done);
@@ -2094,6 +2231,16 @@ template <typename T>
 void fast_stencil_dot(const Geo& g, const Shape& sh, const T* u, const T* r0, T* Au, const Coef& a, RedCtx rc,
                       cudaStream_t s)
 {
+    if constexpr (std::is_same<T, double>::value) {
+        if (iso_coef(a)) {   // equal spacings: the neighbour sum on the integer pipe
+            Shape c = sh.cx == 1 ? sh : make_shape(g, sh.ty, (int)sh.nblocks(), 1);
+            if (rc.cells) canon_launch(g, c, rc);
+            launch_pdl(k_stencil_dots_iso64<1>, grid_of(c), block_of(c), 0, s, g, c, u, r0, Au, a, rc);
+            PPS_COUNT_LAUNCH();
+            if (rc.cells) canon_finalize<1>(rc, &rc.st->done, s);
+            return;
+        }
+    }
     if (rc.cells) {   // canonical sums: one-column kernel on the canonical shape
         Shape c = sh;
         canon_launch(g, c, rc);
@@ -2120,6 +2267,16 @@ template <typename T>
 void fast_stencil_dot2(const Geo& g, const Shape& sh, const T* u, const T* r, T* Au, const Coef& a, RedCtx rc,
                        cudaStream_t s)
 {
+    if constexpr (std::is_same<T, double>::value) {
+        if (iso_coef(a)) {   // equal spacings: the neighbour sum on the integer pipe
+            Shape c = sh.cx == 1 ? sh : make_shape(g, sh.ty, (int)sh.nblocks(), 1);
+            if (rc.cells) canon_launch(g, c, rc);
+            launch_pdl(k_stencil_dots_iso64<2>, grid_of(c), block_of(c), 0, s, g, c, u, r, Au, a, rc);
+            PPS_COUNT_LAUNCH();
+            if (rc.cells) canon_finalize<2>(rc, &rc.st->done, s);
+            return;
+        }
+    }
     if (rc.cells) {
         Shape c = sh;
         canon_launch(g, c, rc);

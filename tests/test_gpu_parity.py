@@ -215,6 +215,36 @@ def test_operator_kernel(gpu, oracle, form):
         assert np.max(np.abs(got[sl] - want[sl])) <= 1e-12 * np.max(np.abs(want[sl]))
 
 
+@pytest.mark.parametrize("scale", ["unit", "wide"])
+def test_operator_kernel_equal_spacings(gpu, oracle, scale):
+    """FP64 form on equal spacings: the six-neighbour sum runs on the integer pipe
+    (exponent-aligned int64).  Checked against the oracle's FP64 stencil on unit
+    values and on values spread over 600 decades (huge, tiny, subnormal, zero), where
+    the aligned sum takes its fallbacks."""
+    rng = np.random.default_rng(11)
+    case = dict(np=(14, 11, 9), ds=(0.05, 0.05, 0.05), origin=(0.0, 0.0, 0.0), bcs=(0, 1, 1, 0, 0, 0),
+                cfg=BY_NAME["dirichlet_random_m10"]["cfg"])
+    g = grid_of(case)
+    u = rng.standard_normal(g.shape)
+    if scale == "wide":
+        u *= 10.0 ** rng.integers(-300, 300, g.shape)
+        u.ravel()[rng.integers(0, u.size, 40)] = 0.0
+        u.ravel()[rng.integers(0, u.size, 40)] = 5e-320
+    s = make_solver(case, "fp64")
+    got = s.apply_operator(u)
+    want = oracle.apply_A(ogrid_of(oracle, case), u)
+    sl = g.unknowns()
+    # each point against the scale of its own seven values (a stencil over huge and
+    # tiny neighbours is exact only to the rounding of the largest one)
+    ref = np.zeros_like(u)
+    ref[sl] = np.abs(u[sl])
+    for ax in (0, 1, 2):
+        ref[sl] = np.maximum(ref[sl], np.abs(np.roll(u, 1, axis=ax)[sl]))
+        ref[sl] = np.maximum(ref[sl], np.abs(np.roll(u, -1, axis=ax)[sl]))
+    bound = 1e-14 * (6.0 / 0.05 ** 2) * ref[sl] + 1e-300
+    assert np.all(np.abs(got[sl] - want[sl]) <= bound)
+
+
 @pytest.mark.parametrize("form,degree", [("parity", 11), ("parity", 3), ("fp64", 11), ("fp64", 2), ("fp64", 4),
                                          ("fp64", 24), ("mixed", 11)])
 def test_preconditioner_kernel(gpu, oracle, form, degree):
