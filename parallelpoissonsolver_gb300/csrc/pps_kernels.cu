@@ -1715,9 +1715,35 @@ __device__ __forceinline__ long long malign(const MI& a, int E)
 // the largest exponent E by an arithmetic shift, summed exactly in int64
 // (|sum| < 6 * 2^53), converted once, and scaled by 2^(E-1075) in the exponent bits.
 // The shifts drop at most one unit of 2^(E-1075) per value, the rounding FP64
-// additions of the same values have anyway.  Returns false when a value is Inf/NaN
+// additions of the same values have anyway.  INT_CONVERT: the conversion too runs
+// on the integer pipe (scaled_i2d), for kernels whose FP64 pipe is the bound.
+// Returns false when a value is Inf/NaN
 // (E = 2047) or the scaling would leave the normal range (E < 53 or E > 2000); the
 // caller then adds in FP64.
+// S * 2^(E-1075) as a double for 0 < |S| < 2^56 and 53 <= E <= 2000, on the integer
+// pipe (the int64 -> FP64 conversion instruction issues on the FP64 pipe): the
+// leading one of |S| moves to bit 52, the bits below are rounded half away from
+// zero (|S| >= 2^53 only), and the exponent field is written directly (p + E - 52
+// lies in [1, 2004], so the result is normal).
+__device__ __forceinline__ double scaled_i2d(long long S, int E)
+{
+    const unsigned long long sg = (unsigned long long)S & 0x8000000000000000ull;
+    const unsigned long long a = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
+    int p = 63 - __clzll((long long)a);
+    unsigned long long mant;
+    if (p > 52) {
+        mant = ((a >> (p - 53)) + 1ull) >> 1;
+        if (mant >> 53) {
+            mant >>= 1;
+            p++;
+        }
+    } else {
+        mant = a << (52 - p);
+    }
+    return __longlong_as_double((long long)(sg | ((unsigned long long)(p + E - 52) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+template <bool INT_CONVERT>
 __device__ __forceinline__ bool nsum6(const MI& a, const MI& b, const MI& c, const MI& d, const MI& e, const MI& f,
                                       double& out)
 {
@@ -1728,7 +1754,8 @@ __device__ __forceinline__ bool nsum6(const MI& a, const MI& b, const MI& c, con
         out = 0.0;
         return true;
     }
-    out = __longlong_as_double(__double_as_longlong(__ll2double_rn(S)) + ((long long)(E - 1075) << 52));
+    if (INT_CONVERT) out = scaled_i2d(S, E);
+    else out = __longlong_as_double(__double_as_longlong(__ll2double_rn(S)) + ((long long)(E - 1075) << 52));
     return true;
 }
 
@@ -1758,7 +1785,7 @@ __global__ void __launch_bounds__(256) k_cheb_iso64(Geo g, Shape sh, const doubl
         const double xw = U[c - 1], xe = U[c + 1], ys = U[c - sj], yn = U[c + sj];
         const MI mp = msplit(up);
         double s6, w;
-        if (nsum6(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
+        if (nsum6<true>(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
             w = fmx(cf.cx, s6, cf.cc * uc);
         } else {
             w = cf.cc * uc;
@@ -1781,7 +1808,7 @@ __global__ void __launch_bounds__(256) k_cheb_iso64(Geo g, Shape sh, const doubl
 // NS = 1: sum w.Au (k_stencil_dot, w = r0); NS = 2: sums w.Au, Au.Au (k_stencil_dot2,
 // w = r).  Three FP64 operations per unknown for A u instead of seven.
 template <int NS>
-__global__ void __launch_bounds__(256) k_stencil_dots_iso64(Geo g, Shape sh, const double* __restrict__ u,
+__global__ void __launch_bounds__(256, 4) k_stencil_dots_iso64(Geo g, Shape sh, const double* __restrict__ u,
                                                             const double* __restrict__ w, double* __restrict__ Au,
                                                             Coef cf, RedCtx rc)
 {
@@ -1800,7 +1827,7 @@ __global__ void __launch_bounds__(256) k_stencil_dots_iso64(Geo g, Shape sh, con
             const double xw = u[c - 1], xe = u[c + 1], ys = u[c - sj], yn = u[c + sj];
             const MI mp = msplit(up);
             double s6, a;
-            if (nsum6(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
+            if (nsum6<true>(msplit(xw), msplit(xe), msplit(ys), msplit(yn), mm, mp, s6)) {
                 a = fmx(cf.cx, s6, cf.cc * uc);
             } else {
                 a = cf.cc * uc;
