@@ -657,11 +657,23 @@ def run_compositions(args, dev: int, threads: int):
     return out
 
 
+def batch_coarsenings(m: int) -> int:
+    """Coarsenings of the persistent batch's V-cycle for edge m: halve while above 16."""
+    k = 0
+    while m > 16 and m % 2 == 0:
+        m //= 2
+        k += 1
+    return k
+
+
 def run_batched(args, dist: Dist):
     """256 independent Dirichlet problems, edges uniform on {32,48,64,96,128}, each f a
-    seeded sum of 1-8 Gaussian blobs; MIXED form to 1e-10 in one batch (one launch per
-    phase, graph-replayed inner iterations, autotuned tiles per grid size), against the
-    same problems solved one after another by the single-grid solver."""
+    seeded sum of 1-8 Gaussian blobs, MIXED form to 1e-10.  The value: the persistent
+    batch -- flexible CG with a multigrid V-cycle per problem (exact coarsest solve),
+    the whole batch ONE cooperative launch replayed as a CUDA graph.  Beside it: the
+    same method run problem after problem by the single-grid solver, and the
+    per-phase batch of the reference method (BiCGSTAB + Chebyshev, one launch per
+    phase over all problems, autotuned tiles per grid size)."""
     import torch
 
     import parallelpoissonsolver_gb300 as pps
@@ -669,64 +681,84 @@ def run_batched(args, dist: Dist):
 
     edges = workloads.edges_config3(args.batch_problems, seed=3)
     grids = [pps.BlockGrid.cube(m) for m in edges]
-    bt = pps.Batch(grids, pps.ChebyshevIteration(DEGREE), tolerance=TOL, inner_maxit=5000, device=dist.local)
-    rhs = []
-    for i, m in enumerate(edges):
-        b = workloads.blobs(m, 3 + i)
-        rhs.append(b)
-        bt.set(i, np.zeros_like(b), b)
-    tiles = bt.autotune()
+    rhs = [workloads.blobs(m, 3 + i) for i, m in enumerate(edges)]
 
-    times = []
-    stats = None
-    for k in range(1 + args.batch_steps):
+    def timed(bt, steps):
+        times, stats = [], None
+        for k in range(1 + steps):
+            for i, b in enumerate(rhs):
+                bt.set(i, np.zeros_like(b), b)
+            torch.cuda.synchronize()
+            st = bt.solve()
+            if st != pps.OK:
+                raise RuntimeError(f"batched solve: {pps.status_string(st)} {pps.last_error()}")
+            stats = bt.stats()
+            if k > 0:
+                times.append(stats["seconds_solve"])
+        return sum(times) / len(times), stats
+
+    bt = pps.Batch(grids, tolerance=TOL, inner_tol=args.learned_inner_tol, device=dist.local, method="vcycle")
+    t_batch, stats = timed(bt, args.batch_steps)
+    errs = [bt.get(i)[1]["err_true"] for i in range(len(edges))]
+
+    # the same method problem after problem: flexible CG + V-cycle with the exact coarsest solve
+    net = pps.UNet((16, 32, 64), seed=1, linear=True, device=dist.local)   # holds the cycle's settings only
+    solvers = {}
+    for m in sorted(set(edges)):
+        s = pps.FlexibleCG(pps.BlockGrid.cube(m), pps.ChebyshevIteration(DEGREE), tolerance=TOL,
+                           max_iteration=20000, form="mixed", inner_tol=args.learned_inner_tol, device=dist.local)
+        s.set_learned(net, batch_coarsenings(m), 1.0, pps.LEARNED_PRECONDITIONER | pps.LEARNED_NO_FALLBACK)
+        s.set_learned_cycle(*VCYCLE)
+        s.set_coarse_solver(pps.COARSE_EXACT)
+        s.autotune()
+        solvers[m] = s
+
+    def sequential():
         for i, b in enumerate(rhs):
             bt.set(i, np.zeros_like(b), b)
         torch.cuda.synchronize()
-        st = bt.solve()
-        if st != pps.OK:
-            raise RuntimeError(f"batched solve: {pps.status_string(st)}")
-        stats = bt.stats()
-        if k > 0:
-            times.append(stats["seconds_solve"])
-    t_batch = sum(times) / len(times)
+        t0 = time.perf_counter()
+        its = 0
+        for i, m in enumerate(edges):
+            xd, bd = bt.field_device(i)
+            st = solvers[m].solve_device(xd, bd)
+            if st != pps.OK:
+                raise RuntimeError(f"single solve {i}: {pps.status_string(st)}")
+            its = max(its, solvers[m].get_num_iteration_final())
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, its
 
-    # the same problems one at a time, in place on the batch's device fields
-    solvers = {}
-    for m in sorted(set(edges)):
-        s = pps.BiCGSTAB(pps.BlockGrid.cube(m), pps.ChebyshevIteration(DEGREE), tolerance=TOL, max_iteration=20000,
-                         form="mixed", device=dist.local)
-        s.autotune()
-        solvers[m] = s
-    for i, b in enumerate(rhs):
-        bt.set(i, np.zeros_like(b), b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    seq_iters = 0
-    for i, m in enumerate(edges):
-        xd, bd = bt.field_device(i)
-        st = solvers[m].solve_device(xd, bd)
-        if st != pps.OK:
-            raise RuntimeError(f"single solve {i}: {pps.status_string(st)}")
-        seq_iters = max(seq_iters, solvers[m].get_num_iteration_final())
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
+    sequential()   # warm-up (graphs captured)
+    t_seq, seq_iters = sequential()
     for s in solvers.values():
         s.close()
-    by_size = {}
-    for (cx, kc), m in zip(tiles, edges):
-        by_size[str(m)] = {"cx": cx, "kchunk": kc}
-    out = {
+    net.close()
+    bt.close()
+
+    # the reference method as a per-phase batch (one measured solve after a warm-up)
+    ref = pps.Batch(grids, pps.ChebyshevIteration(DEGREE), tolerance=TOL, inner_maxit=5000, device=dist.local)
+    for i, b in enumerate(rhs):
+        ref.set(i, np.zeros_like(b), b)
+    ref.autotune()
+    t_ref, ref_stats = timed(ref, 1)
+    ref.close()
+    return {
         "workload": f"{len(edges)} Dirichlet problems, edges uniform on {{32,48,64,96,128}} (seed 3), f = sum of "
-                    f"1-8 Gaussian blobs (seeds 3+p); MIXED BiCGSTAB + Chebyshev({DEGREE}) to {TOL:g}",
-        "value": t_batch, "unit": "s", "steps": len(times),
+                    f"1-8 Gaussian blobs (seeds 3+p); MIXED to {TOL:g}",
+        "method": "flexible CG + multigrid V-cycle per problem (Chebyshev(5) fine smoothing, Jacobi-Chebyshev(4) "
+                  "on the coarse levels, exact coarsest solve at <= 16^3), FP64 refinement; ONE persistent "
+                  "cooperative launch replayed as a CUDA graph",
+        "value": t_batch, "unit": "s", "steps": args.batch_steps,
         "unknowns": stats["unknowns"], "converged": stats["converged"], "max_err_true": stats["max_err_true"],
         "max_inner_iterations": stats["max_iterations"], "max_refinements": stats["max_refinements"],
         "kernel_launches": stats["kernel_launches"], "graph_replays": stats["graph_replays"],
-        "sequential_single_grid_s": t_seq, "speedup_vs_sequential": t_seq / t_batch, "tiles_by_edge": by_size,
+        "median_err_true": float(np.median(errs)),
+        "sequential_same_method_s": t_seq, "sequential_max_iterations": seq_iters,
+        "speedup_vs_sequential": t_seq / t_batch,
+        "per_phase_bicgstab_batch_s": t_ref, "per_phase_bicgstab_kernel_launches": ref_stats["kernel_launches"],
+        "per_phase_bicgstab_max_inner_iterations": ref_stats["max_iterations"],
+        "speedup_vs_per_phase_bicgstab": t_ref / t_batch,
     }
-    bt.close()
-    return out
 
 
 def cpu_sample(m: int, iterations_needed: int | None, threads: int):

@@ -241,10 +241,17 @@ pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out);
 pps_status pps_set_tuning(pps_solver* s, const pps_tuning* t);
 
 /* ---- Batches: many independent Dirichlet grids solved together ----
- * No reference counterpart (the reference solves one grid per run).  Every problem
- * runs the reference's BiCGSTAB + Chebyshev solve on its own grid, in the MIXED
- * form; each loop phase is one launch over all problems, the inner iteration is
- * replayed as a CUDA graph, and per-problem tile shapes come from the autotuner.
+ * No reference counterpart (the reference solves one grid per run).  Two methods,
+ * both in the MIXED form (FP32 inner iterations, FP64 true residual and refinement):
+ *   krylov PPS_KRYLOV_FCG: flexible CG with a multigrid V-cycle per problem (cubes
+ *     with equal spacings, edge m = c * 2^k, k >= 1, c <= 32), the whole solve ONE
+ *     persistent cooperative launch replayed as a CUDA graph: a fixed program of
+ *     phases per round spread over every block as (problem, tile) items, phases
+ *     separated by a grid barrier whose wait is bounded (pps_batch_set_wait_limit);
+ *     a wait that runs out ends the solve with PPS_TIMEOUT;
+ *   krylov PPS_KRYLOV_BICGSTAB: the reference's BiCGSTAB + Chebyshev per problem,
+ *     one launch per loop phase over all problems, the inner iteration replayed as
+ *     a CUDA graph, per-problem tile shapes from the autotuner.
  * Fields live in device pools owned by the batch (pps_batch_set/get copy them,
  * pps_batch_field_device exposes them). */
 typedef struct pps_batch pps_batch;
@@ -261,7 +268,8 @@ typedef struct {
     double unknowns;            /* sum of the problems' unknowns                           */
 } pps_batch_stats;
 
-/* cfg: form PPS_FORM_MIXED, krylov BiCGSTAB, Chebyshev degree >= 4; grids all-Dirichlet. */
+/* cfg: form PPS_FORM_MIXED; krylov PPS_KRYLOV_FCG (persistent V-cycle) or BiCGSTAB with
+ * Chebyshev degree >= 4; grids all-Dirichlet. */
 pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* cfg, pps_batch** out);
 pps_status pps_batch_destroy(pps_batch* batch);
 pps_status pps_batch_set(pps_batch* batch, int p, const double* x, const double* b);
@@ -276,6 +284,10 @@ pps_status pps_batch_tile(const pps_batch* batch, int p, int* cx, int* kchunk);
 /* Solves every problem to cfg->tol (FP64 true residual).  PPS_NOT_CONVERGED if any
  * problem stopped short. */
 pps_status pps_batch_solve(pps_batch* batch, pps_batch_stats* stats);
+/* Persistent batches (krylov PPS_KRYLOV_FCG): how long a block may wait at a grid
+ * barrier for the others before the solve stops with PPS_TIMEOUT (default 5 s; a
+ * healthy barrier completes in microseconds). */
+pps_status pps_batch_set_wait_limit(pps_batch* batch, double seconds);
 
 /* ---- Learned preconditioner: a 3-D convolutional U-Net ----
  * No reference counterpart.  3 levels with c1/c2/c3 channels (16/32/64), 3x3x3

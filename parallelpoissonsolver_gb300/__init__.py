@@ -50,7 +50,7 @@ EXPORTED = [
     "pps_unet_create", "pps_unet_destroy", "pps_unet_param_count", "pps_unet_get_params", "pps_unet_set_params",
     "pps_unet_forward", "pps_unet_gradients", "pps_unet_train_step", "pps_restrict2", "pps_prolong2",
     "pps_set_learned", "pps_unet_set_activation", "pps_set_learned_cycle", "pps_set_coarse_solver",
-    "pps_write_solution",
+    "pps_write_solution", "pps_batch_set_wait_limit",
 ]
 
 
@@ -158,6 +158,7 @@ def load(build_if_missing: bool = False):
     L.pps_batch_get.argtypes = [vp, C.c_int, vp, C.POINTER(PpsStats)]
     L.pps_batch_field_device.argtypes = [vp, C.c_int, C.POINTER(vp), C.POINTER(vp)]
     L.pps_batch_autotune.argtypes = [vp]
+    L.pps_batch_set_wait_limit.argtypes = [vp, C.c_double]
     L.pps_batch_tile.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.pps_batch_solve.argtypes = [vp, C.POINTER(PpsBatchStats)]
     L.pps_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.c_int, C.POINTER(vp)]
@@ -547,13 +548,16 @@ class ChebyshevSolver(Solver):
 
 
 class Batch:
-    """Many independent Dirichlet grids solved together (pps_batch_*): the MIXED form
-    of BiCGSTAB + Chebyshev per problem, one launch per phase over all problems,
-    the inner iteration replayed as a CUDA graph."""
+    """Many independent Dirichlet grids solved together (pps_batch_*), MIXED form.
+    method "vcycle": flexible CG with a multigrid V-cycle per problem, the whole solve
+    one persistent launch replayed as a CUDA graph (cubes, edge c * 2^k, c <= 32);
+    method "bicgstab": the reference's BiCGSTAB + Chebyshev per problem, one launch
+    per phase over all problems, the inner iteration replayed as a CUDA graph."""
 
     def __init__(self, grids: Sequence[BlockGrid], preconditioner: Optional[ChebyshevIteration] = None,
                  tolerance: float = 1e-10, inner_tol: float = 3e-3, inner_maxit: int = 5000,
-                 max_refinements: int = 12, check_every: int = 8, use_graph: bool = True, device: int = 0):
+                 max_refinements: int = 12, check_every: int = 8, use_graph: bool = True, device: int = 0,
+                 method: str = "bicgstab"):
         L = load()
         self.grids = list(grids)
         prec = preconditioner or ChebyshevIteration()
@@ -565,6 +569,11 @@ class Batch:
         cfg.tol, cfg.inner_tol, cfg.inner_maxit = float(tolerance), float(inner_tol), int(inner_maxit)
         cfg.max_refinements, cfg.check_every = int(max_refinements), int(check_every)
         cfg.use_graph, cfg.device = (1 if use_graph else 0), int(device)
+        if method not in ("bicgstab", "vcycle"):
+            raise ValueError("method: 'bicgstab' or 'vcycle'")
+        self.method = method
+        if method == "vcycle":
+            cfg.krylov = KRYLOV_FCG
         arr = (PpsGrid * len(self.grids))(*[g.c() for g in self.grids])
         h = C.c_void_p()
         st = L.pps_batch_create(len(self.grids), arr, C.byref(cfg), C.byref(h))
@@ -612,6 +621,13 @@ class Batch:
             load().pps_batch_tile(self._h, p, C.byref(cx), C.byref(kc))
             out.append((cx.value, kc.value))
         return out
+
+    def set_wait_limit(self, seconds: float):
+        """Persistent batches: the longest a grid-barrier wait may take before the
+        solve stops with TIMEOUT (pps_batch_set_wait_limit)."""
+        st = load().pps_batch_set_wait_limit(self._h, float(seconds))
+        if st != OK:
+            raise PpsError(st, "pps_batch_set_wait_limit")
 
     def solve(self, raise_on_error: bool = True) -> int:
         st = load().pps_batch_solve(self._h, C.byref(self._stats))

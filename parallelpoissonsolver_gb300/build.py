@@ -1,7 +1,8 @@
 """In-tree build of libpps.so (nvcc, sm_103a only).
 
-The six translation units of csrc/ (kernels, solver, allocation-free entry point,
-batched solves, U-Net kernels and U-Net host code) compile in parallel, one
+The seven translation units of csrc/ (kernels, solver, allocation-free entry point,
+batched solves per phase and in one persistent launch, U-Net kernels and U-Net host
+code) compile in parallel, one
 -gencode for sm_103a, and link into ``parallelpoissonsolver_gb300/libpps.so``
 beside this file.
 """
@@ -16,8 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpps.so")
-SOURCES = ["pps_kernels.cu", "pps_solver.cu", "pps_noalloc.cu", "pps_batch.cu", "pps_unet_kernels.cu",
-           "pps_unet.cu"]
+SOURCES = ["pps_kernels.cu", "pps_solver.cu", "pps_noalloc.cu", "pps_batch.cu", "pps_bvcycle.cu",
+           "pps_unet_kernels.cu", "pps_unet.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               # host code rounds every product and sum separately (aarch64 g++ would fuse them)

@@ -89,6 +89,7 @@ struct pps_batch {
     int g_iters = 0;
     int g_launches = 0;
     pps_batch_stats stats;
+    BvcPlan* vc = nullptr;   // krylov FCG: the persistent V-cycle solve
 };
 
 namespace {
@@ -258,6 +259,7 @@ bool any_unfinished(const pps_batch* s)
 
 void free_batch(pps_batch* s)
 {
+    if (s->vc) bvc_destroy(s->vc);
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     void* ptrs[] = {s->x, s->b, s->p, s->r, s->r0, s->Mp, s->AMp, s->z, s->Az, s->Y, s->Z, s->W, s->e,
                     s->dprob, s->dblk, s->dprob4, s->dblk4, s->partials, s->counters, s->dst, s->coef};
@@ -450,9 +452,11 @@ pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* 
 {
     if (!out || !grids || !cfg || nprob < 1) return PPS_ERR_INVALID_ARG;
     *out = nullptr;
-    if (cfg->form != PPS_FORM_MIXED || cfg->krylov != PPS_KRYLOV_BICGSTAB || cfg->precond != PPS_PREC_CHEBYSHEV ||
-        cfg->cheb_degree < 4) {
-        pps_internal_set_error("batches run the MIXED form of BiCGSTAB + Chebyshev (degree >= 4)");
+    const bool vcycle = cfg->krylov == PPS_KRYLOV_FCG;
+    if (cfg->form != PPS_FORM_MIXED ||
+        (!vcycle && (cfg->krylov != PPS_KRYLOV_BICGSTAB || cfg->precond != PPS_PREC_CHEBYSHEV || cfg->cheb_degree < 4))) {
+        pps_internal_set_error("batches run the MIXED form: flexible CG with the multigrid V-cycle in one persistent "
+                               "launch, or BiCGSTAB + Chebyshev (degree >= 4)");
         return PPS_ERR_UNSUPPORTED;
     }
     if (!(cfg->tol > 0.0) || !(cfg->inner_tol > 0.0 && cfg->inner_tol < 1.0) || cfg->inner_maxit < 1 ||
@@ -541,6 +545,16 @@ pps_status pps_batch_create(int nprob, const pps_grid* grids, const pps_config* 
         BK(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * (size_t)nprob, s->stream));
         BK(cudaMalloc((void**)&s->dst, sizeof(BState) * (size_t)nprob));
         BK(cudaMallocHost((void**)&s->hst, sizeof(BState) * (size_t)nprob));
+        if (vcycle) {   // flexible CG + V-cycle in one persistent launch (pps_bvcycle.cu)
+            const BvcPools pools{s->x, s->b, s->r, s->z, s->p, s->r0, s->AMp, s->e, s->Y, s->Z, s->W};
+            std::string err;
+            if (!bvc_create(&s->vc, nprob, s->geo.data(), s->off.data(), pools, cfg->tol, cfg->inner_tol,
+                            cfg->inner_maxit, cfg->max_refinements, s->stream, err)) {
+                pps_internal_set_error(err.c_str());
+                return err.find("cuda") != std::string::npos ? PPS_ERR_CUDA : PPS_ERR_UNSUPPORTED;
+            }
+            return PPS_OK;
+        }
         s->cstride = cfg->cheb_degree - 2;
         std::vector<Coef> hc((size_t)nprob * s->cstride);
         for (int p = 0; p < nprob; p++) coefs_of(s, p, &hc[(size_t)p * s->cstride]);
@@ -601,7 +615,11 @@ pps_status pps_batch_get(pps_batch* s, int p, double* x, pps_stats* st)
             BK(cudaMemcpyAsync(x, s->x + s->off[(size_t)p], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream));
             BK(cudaStreamSynchronize(s->stream));
         }
-        if (st) {
+        if (st && s->vc) {
+            std::memset(st, 0, sizeof(*st));
+            bvc_result(s->vc, p, st);
+            st->seconds_solve = s->stats.seconds_solve;
+        } else if (st) {
             std::memset(st, 0, sizeof(*st));
             const BState& q = s->hst[p];
             st->iterations = q.total_iters;
@@ -619,15 +637,33 @@ pps_status pps_batch_solve(pps_batch* s, pps_batch_stats* stats)
     if (!s) return PPS_ERR_INVALID_ARG;
     pps_status rc = bguard([&]() -> pps_status {
         BK(cudaSetDevice(s->device));
+        if (s->vc) {
+            std::string err;
+            const pps_status r = bvc_solve(s->vc, s->stream, s->ev0, s->ev1, &s->stats, err);
+            if (!err.empty()) pps_internal_set_error(err.c_str());
+            return r;
+        }
         return run_batch(s);
     });
     if (stats) *stats = s->stats;
     return rc;
 }
 
+pps_status pps_batch_set_wait_limit(pps_batch* s, double seconds)
+{
+    if (!s || !(seconds > 0.0) || !std::isfinite(seconds)) return PPS_ERR_INVALID_ARG;
+    if (!s->vc) {
+        pps_internal_set_error("only the persistent (flexible CG) batch waits on a grid barrier");
+        return PPS_ERR_UNSUPPORTED;
+    }
+    bvc_set_wait_limit(s->vc, seconds);
+    return PPS_OK;
+}
+
 pps_status pps_batch_autotune(pps_batch* s)
 {
     if (!s) return PPS_ERR_INVALID_ARG;
+    if (s->vc) return PPS_OK;   // the persistent solve's work items have a fixed shape
     return bguard([&]() -> pps_status {
         BK(cudaSetDevice(s->device));
         std::map<long long, std::vector<int>> groups;

@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/pps.h"
+
 // Records the message pps_last_error() returns on this thread.
 extern "C" void pps_internal_set_error(const char* msg);
 
@@ -69,6 +73,26 @@ struct CaptureGuard {
         if (g) cudaGraphDestroy(g);
     }
 };
+
+// Cooperative launch (every block resident at once, so blocks may wait on one another
+// through a grid barrier); no programmatic dependent launch: the kernel starts after
+// the one before it has completed.
+template <typename... KArgs, typename... Args>
+inline void launch_coop(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+    if (e != cudaSuccess) note_launch_failure(e);
+}
 
 // Geometry of one single-rank grid in the guard-padded field layout
 // (iterativeSolverBase.hpp:34-35): index = i + sj*j + sk*k with
@@ -332,5 +356,22 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
 int launches_counter_reset();
 int launches_counter();
 void launches_counter_add(int d);
+
+// Batched solves in one persistent launch (flexible CG + multigrid V-cycle per problem,
+// FP64 refinement; csrc/pps_bvcycle.cu).  The pools are the batch's level-0 fields
+// (guard-padded, per-problem offsets); the plan owns its coarse levels.
+struct BvcPlan;
+struct BvcPools {
+    double* x;
+    const double* b;
+    float *r, *z, *pa, *pb, *ap, *e, *y1, *y2, *t0;
+};
+bool bvc_create(BvcPlan** out, int nprob, const Geo* geo, const long long* off, const BvcPools& pools, double tol,
+                double inner_tol, int inner_maxit, int max_refinements, cudaStream_t s, std::string& err);
+void bvc_destroy(BvcPlan* plan);
+void bvc_set_wait_limit(BvcPlan* plan, double seconds);
+pps_status bvc_solve(BvcPlan* plan, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, pps_batch_stats* stats,
+                     std::string& err);
+void bvc_result(const BvcPlan* plan, int q, pps_stats* st);
 
 }  // namespace pps

@@ -1039,6 +1039,8 @@ bool prolong_add_field(const Geo& g, const Shape& sh, const Dims& dc, const floa
         }
         return prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
     }
+    if (sh.cx != 1)   // two-column Chebyshev tiles: the kernel below covers 32 columns per tile
+        return prolong_add_field<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), dc, coarse, f, s);
     launch_pdl(k_prolong_add_field<T>, zgrid(sh), zblock(sh), 0, s, g, sh, dc, coarse, f, g_stop);
     launches_counter_add(1);
     return false;
