@@ -864,7 +864,21 @@ def profile_case(argv):
     ap.add_argument("--refinements", type=int, default=1)
     ap.add_argument("--krylov", default="bicgstab", choices=("bicgstab", "fcg"),
                     help="Krylov loop without --learned (fcg: flexible CG with the Chebyshev preconditioner)")
+    ap.add_argument("--batch-problems", type=int, default=0,
+                    help="instead: one persistent V-cycle batch of this many problems of the batched workload")
     a = ap.parse_args(argv)
+    if a.batch_problems > 0:
+        edges = workloads.edges_config3(a.batch_problems, seed=3)
+        bt = pps.Batch([pps.BlockGrid.cube(m) for m in edges], tolerance=1e-10, inner_tol=1e-5, method="vcycle")
+        for i, m in enumerate(edges):
+            b = workloads.blobs(m, 3 + i)
+            bt.set(i, np.zeros_like(b), b)
+        st = bt.solve()
+        d = bt.stats()
+        print(f"status {pps.status_string(st)}: {d['converged']}/{len(edges)} converged, "
+              f"{d['seconds_solve'] * 1e3:.2f} ms, max inner iterations {d['max_iterations']}")
+        bt.close()
+        return
     if a.save_net:
         from parallelpoissonsolver_gb300 import learned
         train = learned.make_dataset(a.net_grid, range(10000, 10256), coarsen=a.coarsen)
