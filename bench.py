@@ -57,6 +57,7 @@ DEGREE = 11
 # The CPU leg multiplies its timed per-iteration cost by it.
 REFERENCE_ITERATIONS = {512: 166}
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "cheb_sweep_fp32_traffic.txt")
+PROFILE_TRAFFIC_FCG = os.path.join(ROOT, "profiles", "fcg_kernels_traffic.txt")
 
 
 def dist_env():
@@ -162,11 +163,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_ratio():
-    """dram bytes / algorithmic bytes of one FP32 sweep launch, from the committed ncu summary."""
-    if not os.path.exists(PROFILE_TRAFFIC):
+def traffic_ratio(path=PROFILE_TRAFFIC):
+    """dram bytes / algorithmic bytes of the kernel a committed ncu summary covers
+    (default: one FP32 sweep launch)."""
+    if not os.path.exists(path):
         return None
-    for line in open(PROFILE_TRAFFIC):
+    for line in open(path):
         if line.startswith("traffic_over_algorithmic:"):
             return float(line.split(":")[1])
     return None
@@ -305,9 +307,24 @@ def run_gpu(args, dist: Dist):
     e2e_split = {k: statistics.median(p[i] for p in e2e_parts)
                  for i, k in enumerate(("h2d_s", "solve_s", "d2h_s", "call_s", "python_s"))}
 
-    # ---- roofline of the FP32 Chebyshev sweep, event-timed on the solver's stream.
-    # The headline solve replays CUDA graphs, which carry no events, so the sweeps are
-    # timed in the mixed BiCGSTAB solves (the same kernel, degree 11: all 16 B sweeps) ----
+    # ---- roofline of the headline's dominant kernels: flexible CG's direction + stencil
+    # (k_fcg_p_stencil_v4) and x, r update (k_fcg_update_xr_flat), the two largest of its
+    # solve.  The headline replays CUDA graphs, which carry no events, so the same solver
+    # settings run once more uncaptured with the two kernels bracketed by events ----
+    probe = pps.FlexibleCG(grid, prec, tolerance=TOL, max_iteration=20000, form="mixed", use_graph=False,
+                           inner_tol=args.learned_inner_tol, device=dev)
+    probe.set_learned(net, k, gain, flags)
+    probe.set_learned_cycle(*VCYCLE)
+    probe.set_tuning(head.tuning())
+    solve(probe)
+    kstats = [solve(probe) for _ in range(2)]
+    probe.close()
+    kry_s = sum(s["krylov_seconds"] for s in kstats)
+    kry_b = sum(s["krylov_bytes"] for s in kstats)
+    kry_n = sum(s["krylov_launches"] for s in kstats)
+
+    # ---- roofline of the FP32 Chebyshev sweep (the reference method's dominant kernel),
+    # event-timed in the mixed BiCGSTAB solves (degree 11: all 16 B sweeps) ----
     sweep_s = sum(s["sweep_seconds"] for s in mixed_stats)
     sweep_n = sum(s["sweep_launches"] for s in mixed_stats)
     sweep_b = sum(s["sweep_bytes"] for s in mixed_stats)
@@ -369,6 +386,22 @@ def run_gpu(args, dist: Dist):
         "vs_plain_fp64_rel_l2": rel_diff,
         "hbm_gbs_solve": stats[-1]["hbm_bytes"] / stats[-1]["seconds_solve"] / 1e9,
         "roofline": {
+            "bound": "hbm",
+            "kernel": "k_fcg_p_stencil_v4 + k_fcg_update_xr_flat (the headline solve's two largest kernels: "
+                      "flexible CG's direction + stencil, 16 B per unknown, and x, r update, 24 B per unknown; "
+                      "event-timed in uncaptured solves with the headline's settings)",
+            "achieved": (kry_b / kry_s) / 1e9 if kry_s > 0 else None,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": ((kry_b / kry_s) / 1e9 / peak) if kry_s > 0 else None,
+            "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
+            "traffic": (traffic_ratio(PROFILE_TRAFFIC_FCG) * kry_b / kry_n * 2)
+                       if (traffic_ratio(PROFILE_TRAFFIC_FCG) and kry_n) else None,
+            "traffic_unit": "bytes per launch pair (direction + update)",
+            "algorithmic_bytes_per_launch_pair": kry_b / kry_n * 2 if kry_n else None,
+            "launches_timed": kry_n,
+        },
+        "roofline_sweep": {
             "bound": "hbm",
             "kernel": "k_cheb_v4<1>, k_cheb_v4<2> (the FP32 Chebyshev sweeps, one float4 per thread: Y with its "
                       "6 neighbours, B, [Z] in, W out; 12 / 16 B per unknown; timed in the mixed BiCGSTAB solves, "

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define PPS_ABI_VERSION 2
+#define PPS_ABI_VERSION 3
 
 typedef enum {
     PPS_OK = 0,
@@ -139,6 +139,10 @@ typedef struct {
     int precond_iterations;     /* inner solver: its iterations summed over the
                                    applications (numIterationPreconditionerFinal_,
                                    BiCGstabAlpaka.hpp:214,290)                              */
+    double krylov_seconds;      /* flexible CG: device time of its direction + stencil and
+                                   x, r update kernels (event-timed, use_graph 0 only)      */
+    int krylov_launches;        /* those kernels launched                                   */
+    double krylov_bytes;        /* their algorithmic bytes                                  */
 } pps_stats;
 
 typedef struct pps_solver pps_solver;

@@ -172,6 +172,10 @@ struct pps_solver {
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
+    std::vector<cudaEvent_t> krylov_ev;  // pairs, profiling of flexible CG's direction + update kernels
+    int krylov_ev_used = 0;
+    double krylov_bytes_acc = 0;
+    int krylov_launch_acc = 0;
     int sweep_ev_used = 0;
     double bytes_acc = 0;
     int launches_acc = 0;
@@ -292,6 +296,7 @@ void free_all(pps_solver* s)
     for (float* q : s->dt) cudaFree(q);
     for (float* q : {s->cY, s->cZ, s->cW, s->d_exact}) cudaFree(q);
     for (cudaEvent_t e : s->sweep_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->krylov_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -1121,11 +1126,19 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     const long long N = s->n_unknowns;
     const Coef a = op_coef(g);
     // the direction/stencil kernel runs on the Chebyshev tiles (x-vectorised for FP32)
+    const bool prof = L.profile && s->krylov_ev_used + 2 <= (int)s->krylov_ev.size();
+    if (prof) CK(cudaEventRecord(s->krylov_ev[s->krylov_ev_used], st));
     fast_fcg_p_stencil<T>(g, s->shape_cheb, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
     std::swap(F.p, F.Az);
     const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
     if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
     else fast_fcg_update_xr<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
+    if (prof) {   // z, p_in read, p_out, Ap written; x, r read and written, p, Ap read
+        CK(cudaEventRecord(s->krylov_ev[s->krylov_ev_used + 1], st));
+        s->krylov_ev_used += 2;
+        s->krylov_bytes_acc += bytes_of<T>(N, 4 + 6);
+        s->krylov_launch_acc += 2;
+    }
     const RedCtx conv = red(s, FIN_FCG_CONV);
     if (precond_any<T>(s, F, F.r, F.z, L, F.AMp, &conv)) {   // the V-cycle summed z.r, z.Ap
         L.bytes += bytes_of<T>(N, 4 + 6 + 2);
@@ -1707,6 +1720,9 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
     s->sweep_ev_used = 0;
     s->sweep_bytes_acc = 0;
     s->sweep_launch_acc = 0;
+    s->krylov_ev_used = 0;
+    s->krylov_bytes_acc = 0;
+    s->krylov_launch_acc = 0;
     launches_counter_reset();
     s->prec_kind = s->cfg.krylov == PPS_KRYLOV_CHEBYSHEV ? (int)PPS_PREC_CHEBYSHEV : s->cfg.precond;
     s->prec_iters = 0;
@@ -1732,6 +1748,15 @@ pps_status solve_core(pps_solver* s, double* x_dev, double* b_dev)
     S.sweep_seconds = sw;
     S.sweep_launches = s->sweep_launch_acc;
     S.sweep_bytes = s->sweep_bytes_acc;
+    double kt = 0;
+    for (int q = 0; q + 1 < s->krylov_ev_used; q += 2) {
+        float m = 0;
+        CK(cudaEventElapsedTime(&m, s->krylov_ev[q], s->krylov_ev[q + 1]));
+        kt += m * 1e-3;
+    }
+    S.krylov_seconds = kt;
+    S.krylov_launches = s->krylov_launch_acc;
+    S.krylov_bytes = s->krylov_bytes_acc;
     S.learned_applications = s->learned_apps;
     S.fallback_iteration = s->fallback_iter;
     S.precond_iterations = (int)std::min<long long>(s->prec_iters, INT32_MAX);
@@ -1902,6 +1927,8 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
             const int pairs = 2 * (cfg->maxit + 2) + 64;
             s->sweep_ev.resize((size_t)std::min(pairs, 20000) * 2);
             for (auto& e : s->sweep_ev) CK(cudaEventCreate(&e));
+            s->krylov_ev.resize((size_t)std::min(cfg->maxit + 2, 2000) * 2);
+            for (auto& e : s->krylov_ev) CK(cudaEventCreate(&e));
         }
         // the zero fills above ran on the legacy stream, which the handle's non-blocking
         // stream does not wait for: finish them before the handle is used

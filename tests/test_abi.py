@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(pps_lib):
 
 def test_abi_version_and_status_strings(pps_lib):
     L = pps_lib.load()
-    assert L.pps_abi_version() == 2
+    assert L.pps_abi_version() == 3
     for st in (0, 1, 2, 3, 4, -1, -2, -3, -4, -5, -6):
         assert pps_lib.status_string(st) not in ("", "unknown status")
 
