@@ -1619,9 +1619,7 @@ __global__ void __launch_bounds__(256) k_stencil_dots_v4(Geo g, Shape sh, const 
     pdl_enter();
     EARLY_EXIT(&rc.st->done);
     const Col4 q = column4(g, sh);
-    // one accumulator chain per float4 component: four independent dependency chains
-    // instead of one (the double-float adds are long and serial)
-    Acc<float> a1[4], a2[4];
+    Acc<float> a1, a2;
     if (q.j < g.hi[1]) {   // a warp shares its row: the shuffles below see all 32 lanes
         const bool act = q.act;
         const int lane = threadIdx.x;
@@ -1656,20 +1654,20 @@ __global__ void __launch_bounds__(256) k_stencil_dots_v4(Geo g, Shape sh, const 
                     if (m3) Au[c + 3] = a.w;
                 }
                 if (m0) {
-                    a1[0].add(w4.x, a.x);
-                    if (NS == 2) a2[0].add(a.x, a.x);
+                    a1.add(w4.x, a.x);
+                    if (NS == 2) a2.add(a.x, a.x);
                 }
                 if (m1) {
-                    a1[1].add(w4.y, a.y);
-                    if (NS == 2) a2[1].add(a.y, a.y);
+                    a1.add(w4.y, a.y);
+                    if (NS == 2) a2.add(a.y, a.y);
                 }
                 if (m2) {
-                    a1[2].add(w4.z, a.z);
-                    if (NS == 2) a2[2].add(a.z, a.z);
+                    a1.add(w4.z, a.z);
+                    if (NS == 2) a2.add(a.z, a.z);
                 }
                 if (m3) {
-                    a1[3].add(w4.w, a.w);
-                    if (NS == 2) a2[3].add(a.w, a.w);
+                    a1.add(w4.w, a.w);
+                    if (NS == 2) a2.add(a.w, a.w);
                 }
             }
             um = uc;
@@ -1677,17 +1675,11 @@ __global__ void __launch_bounds__(256) k_stencil_dots_v4(Geo g, Shape sh, const 
             c += sk;
         }
     }
-    a1[0].merge(a1[1]);
-    a1[2].merge(a1[3]);
-    a1[0].merge(a1[2]);
     if (NS == 1) {
-        double v[1] = {a1[0].value()};
+        double v[1] = {a1.value()};
         reduce_finalize<1>(v, rc);
     } else {
-        a2[0].merge(a2[1]);
-        a2[2].merge(a2[3]);
-        a2[0].merge(a2[2]);
-        double v[2] = {a1[0].value(), a2[0].value()};
+        double v[2] = {a1.value(), a2.value()};
         reduce_finalize<2>(v, rc);
     }
 }

@@ -40,16 +40,6 @@ struct Acc<float> {
         lo = __fadd_rn(lo, __fadd_rn(t, e));
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-    // adds another accumulator (error-free sum of the heads, tails added) in FP32, so
-    // several chains cost one FP64 conversion at the end
-    __device__ __forceinline__ void merge(const Acc<float>& o)
-    {
-        const float s = __fadd_rn(hi, o.hi);
-        const float bb = __fsub_rn(s, hi);
-        const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(o.hi, bb));
-        hi = s;
-        lo = __fadd_rn(lo, __fadd_rn(o.lo, t));
-    }
 };
 
 __device__ __forceinline__ double warp_sum(double v)
