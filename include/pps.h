@@ -236,8 +236,10 @@ typedef struct {
 /* Autotuner (no reference counterpart; the reference fixes its launch shapes,
  * ALP/include/alpakaHelper.hpp:122-140): times every candidate shape on this
  * solver's grid and buffers, applies the fastest and returns it.  The Chebyshev
- * tiles are scored by the sweep's time plus that of the method's Krylov stencil
- * kernel on the same tiles; the other tiles by the stencil+dot kernel.
+ * tiles are scored by the sweep's time, weighted by the Chebyshev launches per
+ * Krylov stencil launch of an iteration (cheb_degree - 2, or the learned cycle's
+ * fine degree - 2), plus that of the method's Krylov stencil kernel on the same
+ * tiles; the other tiles by the stencil+dot kernel.
  * Candidates: ty 2/4/8, cx 1/2/4 (4: FP32 only), waves 1/2/4/8. */
 pps_status pps_autotune(pps_solver* s, pps_tuning* out);
 pps_status pps_get_tuning(const pps_solver* s, pps_tuning* out);

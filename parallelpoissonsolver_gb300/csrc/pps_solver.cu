@@ -1579,13 +1579,21 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
     // The Chebyshev tiles also carry the Krylov stencil kernel of the method (flexible
     // CG's direction update + stencil, BiCGSTAB's and CG's stencil + dots), whose
     // reads of two fields with their y halo make it the more shape-sensitive one: a
-    // candidate is scored by the sweep's time plus that kernel's.
+    // candidate is scored by the sweep's time, weighted by the Chebyshev launches per
+    // stencil launch of an iteration, plus that kernel's.
     const bool fcg = s->cfg.krylov == PPS_KRYLOV_FCG;
     if (fcg) {   // a non-zero beta, so the direction kernel reads p as well as z
         const double beta = 0.5;
         CK(cudaMemcpyAsync(&s->d_st->beta, &beta, sizeof(double), cudaMemcpyHostToDevice, s->stream));
         CK(cudaStreamSynchronize(s->stream));
     }
+    // Chebyshev launches per launch of the Krylov stencil kernel in one iteration: the
+    // reference method's two applications of degree n (s1 and n - 3 sweeps each) per two
+    // stencil kernels; flexible CG's smoother (the V-cycle's fine degree, or the
+    // polynomial) per direction kernel
+    const int n = s->cfg.cheb_degree;
+    double weight = std::max(1, n - 2);
+    if (fcg && s->cyc_fine > 0) weight = std::max(1, s->cyc_fine - 2);
     double best_us = 1e30;
     for (int ty : kTys)
         for (int cx : kCxs)
@@ -1599,8 +1607,8 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
                     if (fcg) fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_STORE), s->stream);
                     else fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red_c(s, FIN_STORE), s->stream);
                 });
-                if (us + ks < best_us) {
-                    best_us = us + ks;
+                if (weight * us + ks < best_us) {
+                    best_us = weight * us + ks;
                     best->cheb_ty = ty;
                     best->cheb_cx = cx;
                     best->cheb_waves = w;
