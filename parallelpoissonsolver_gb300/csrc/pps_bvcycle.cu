@@ -387,7 +387,6 @@ __device__ void ph_a_fcg(const Dev& D, const Item& it, Acc<float>& acc)
     const float* pin = S.par ? D.pb : D.pa;
     float* pout = S.par ? D.pa : D.pb;
     const float be = (float)S.beta, ih2 = (float)P.ih2;
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         float pc, ps;
@@ -409,7 +408,6 @@ __device__ void ph_a_refine(const Dev& D, const Item& it)
 {
     const Prob& P = D.prob[it.q];
     if (!it.on) return;
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         const float ev = D.e[c];
@@ -425,7 +423,6 @@ __device__ void ph_b_fcg(const Dev& D, const Item& it, Acc<float>& acc)
     if (!it.on) return;
     const float* p = S.par ? D.pb : D.pa;   // the direction phase A wrote (its parity flipped since)
     const float al = (float)S.alpha;
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         D.e[c] = fmaf(al, p[c], D.e[c]);
@@ -442,7 +439,6 @@ __device__ void ph_b_refine(const Dev& D, const Item& it, double& acc)
     if (!it.on) return;
     const long long sj = P.m + 4, sk = sj * sj;
     const double* x = D.x;
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         const double s6 = ((x[c - 1] + x[c + 1]) + (x[c - sj] + x[c + sj])) + (x[c - sk] + x[c + sk]);
@@ -462,7 +458,6 @@ __device__ void ph_cheb0(const Dev& D, const Item& it, int t)
     const float* Y = t == 0 ? D.r : (t == 1 ? D.y1 : D.y2);
     float* W = t == 0 ? D.y1 : (t == 1 ? D.y2 : D.z);
     const float cc = P.fcc[t], cn = P.fcn[t], cb = P.fcb[t], cz = P.fcz[t];
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         float w = fmaf(cn, nsum(Y, c, sj, sk), cc * Y[c]);
@@ -479,7 +474,6 @@ __device__ void ph_r0(const Dev& D, const Item& it)
     if (!it.on) return;
     const long long sj = P.m + 4, sk = sj * sj;
     const float ih2 = (float)P.ih2;
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         D.t0[c] = D.r[c] - (nsum(D.z, c, sj, sk) - 6.f * D.z[c]) * ih2;
@@ -636,7 +630,6 @@ __device__ void ph_p0(const Dev& D, const Item& it, Acc<float>& a1, Acc<float>& 
     const Prob& P = D.prob[it.q];
     if (!it.on) return;
     const int nc = P.n[1];
-#pragma unroll 4
     for (int k = it.k0; k < it.k1; k++) {
         const long long c = idx0(P, it.i, it.j, k);
         const float zv = D.z[c] + prolong_at(D.cz, P.coff[1], nc, it.i, it.j, k);
