@@ -906,10 +906,14 @@ def profile_case(argv):
         for i, m in enumerate(edges):
             b = workloads.blobs(m, 3 + i)
             bt.set(i, np.zeros_like(b), b)
-        st = bt.solve()
-        d = bt.stats()
-        print(f"status {pps.status_string(st)}: {d['converged']}/{len(edges)} converged, "
-              f"{d['seconds_solve'] * 1e3:.2f} ms, max inner iterations {d['max_iterations']}")
+        for _ in range(a.repeat):
+            for i, m in enumerate(edges):
+                b = workloads.blobs(m, 3 + i)
+                bt.set(i, np.zeros_like(b), b)
+            st = bt.solve()
+            d = bt.stats()
+            print(f"status {pps.status_string(st)}: {d['converged']}/{len(edges)} converged, "
+                  f"{d['seconds_solve'] * 1e3:.2f} ms, max inner iterations {d['max_iterations']}")
         bt.close()
         return
     if a.save_net:

@@ -790,7 +790,7 @@ __device__ void run_phase(const Dev& D, const Phase& ph, float* sm)
 // The persistent solve: the norm phase, then rounds of the phase program until every
 // problem has finished (or max_rounds), a grid barrier after every phase.  All blocks
 // read `unfinished` after the same barrier, so they leave the loop together.
-__global__ void __launch_bounds__(NT) k_bvc_solve(Dev D)
+__global__ void __launch_bounds__(NT, 6) k_bvc_solve(Dev D)
 {
     pdl_enter();
     extern __shared__ float sm_ex[];
