@@ -10,7 +10,9 @@ form, mixed+learned: FP64 iterative refinement around FP32 flexible CG whose
 preconditioner is Chebyshev smoothing plus a U-Net coarse-grid correction (the
 network trained here, outside the timed region, by the library's own kernels).
 `e2e` is the same solve through pps_solve() on pinned host buffers, copies
-included: its value is the median over the steps (the host memory the copies read
+included (b uploads first; x's upload and its copy out overlap the solve, and the
+returned x is checked bit for bit against the device-resident solve's): its value
+is the median over the steps (the host memory the copies read
 and write is shared with the machine's other jobs, and a contended copy can run at
 a fraction of its usual rate; the mean and every sample are listed beside it).  The
 reference method (BiCGSTAB + Chebyshev) is timed beside it in mixed
@@ -302,6 +304,8 @@ def run_gpu(args, dist: Dist):
             e2e.append(el)
             d = head.stats()
             e2e_parts.append((d["seconds_h2d"], d["seconds_solve"], d["seconds_d2h"], d["seconds_total"], el))
+    e2e_overlap = head.stats()["copy_overlap"]
+    e2e_same_x = bool(np.array_equal(xn.view(np.uint64), head_x.cpu().numpy().view(np.uint64)))
     t_e2e = dist.max(statistics.median(e2e))
     t_e2e_mean = dist.max(sum(e2e) / len(e2e))
     e2e_split = {k: statistics.median(p[i] for p in e2e_parts)
@@ -373,6 +377,7 @@ def run_gpu(args, dist: Dist):
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * G * 8, "d2h_bytes_per_step": G * 8,
                 "statistic": "median over the steps", "mean_s": t_e2e_mean,
                 "median_split": e2e_split, "samples_s": [round(v, 5) for v in e2e],
+                "copy_overlap": e2e_overlap, "x_bitwise_equal_to_device_solve": e2e_same_x,
                 "samples_ms_h2d_solve_d2h_call": [[round(1e3 * v, 2) for v in p[:4]] for p in e2e_parts]},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "forms": {

@@ -143,6 +143,12 @@ typedef struct {
                                    x, r update kernels (event-timed, use_graph 0 only)      */
     int krylov_launches;        /* those kernels launched                                   */
     double krylov_bytes;        /* their algorithmic bytes                                  */
+    int copy_overlap;           /* pps_solve, MIXED form on pinned arrays: bit 0, b was
+                                   uploaded first and the solve started on it while x
+                                   uploaded; bit 1, x held a non-zero entry and the solve
+                                   restarted on it; bit 2, x's copy out overlapped the
+                                   final residual check.  seconds_h2d is then b's upload,
+                                   seconds_d2h what remained of x's copy out              */
 } pps_stats;
 
 typedef struct pps_solver pps_solver;
@@ -184,7 +190,12 @@ pps_status pps_set_neumann(pps_solver* s, int face, const double* values);
  * absolute ||b - A x|| (the reference does not normalise in this use), history one
  * entry holding it; PPS_OK when it is below tol * norm_b, else PPS_NOT_CONVERGED.
  * The MIXED form applies the polynomial in FP32 to the FP64 residual up to
- * max_refinements + 1 times, stopping at tol (iterations: degree x passes). */
+ * max_refinements + 1 times, stopping at tol (iterations: degree x passes).
+ * On page-locked arrays the MIXED Krylov solves (Dirichlet faces) upload b first
+ * and start on it as if x were zero while x uploads on a second stream; a non-zero
+ * x restarts the solve on it, so the result is the same either way.  x is copied out
+ * after each refinement, the last copy overlapping the final residual check
+ * (pps_stats.copy_overlap); on an error x may hold an intermediate iterate. */
 pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats);
 /* The same with device pointers (fields already resident in HBM).  The solver's
  * stream is non-blocking: work that writes x_dev or b_dev on another stream must be

@@ -76,7 +76,7 @@ class PpsStats(C.Structure):
                 ("sweep_seconds", C.c_double), ("sweep_launches", C.c_int), ("sweep_bytes", C.c_double),
                 ("learned_applications", C.c_int), ("fallback_iteration", C.c_int),
                 ("precond_iterations", C.c_int), ("krylov_seconds", C.c_double), ("krylov_launches", C.c_int),
-                ("krylov_bytes", C.c_double)]
+                ("krylov_bytes", C.c_double), ("copy_overlap", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -332,6 +332,11 @@ void fast_residual(const Geo& g, const Shape& sh, const double* x, const double*
                    const Coef& a, RedCtx rc, cudaStream_t s, bool x_zero = false);
 // Number of entries of a whole FP64 field that are not +-0 (into sums[0]).
 void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx rc, cudaStream_t s);
+// *flag = 1 when an entry of the n doubles at x (16-byte aligned) is not +-0
+void flag_nonzero(long long n, const double* x, int* flag, cudaStream_t s);
+// *h_mapped = *d, h_mapped a page-locked host DevState whose device address equals its
+// host address, stored by a kernel (no copy engine)
+void state_out(const DevState* d, DevState* h_mapped, cudaStream_t s);
 // ||b_adj||^2 over the unknowns, b_adj formed on the fly (FP64).
 void fast_norm_badj(const Geo& g, const Shape& sh, const double* b, const double* x, Faces f, RedCtx rc,
                     cudaStream_t s, bool x_zero = false);

@@ -1877,6 +1877,32 @@ __global__ void __launch_bounds__(256) k_count_nonzero(long long n, const double
     reduce_finalize<1>(v, rc);
 }
 
+// Sets *flag to 1 when some entry of a whole field (guard layers included) is not
+// +-0.  It runs on a second stream while the solve works on b, so it takes no
+// reduction state of the solver: one block-wide OR and a plain store of 1.
+__global__ void __launch_bounds__(256) k_flag_nonzero(long long n, const double* __restrict__ x, int* __restrict__ flag)
+{
+    pdl_enter();
+    const long long nv = n / 2, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const longlong2* xv = reinterpret_cast<const longlong2*>(x);
+    unsigned long long bits = 0;
+    long long i = t0;
+    for (; i + 3 * stride < nv; i += 4 * stride) {   // four loads in flight per thread
+        longlong2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = xv[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; u++) bits |= ((unsigned long long)v[u].x << 1) | ((unsigned long long)v[u].y << 1);
+    }
+    for (; i < nv; i += stride) {
+        const longlong2 v = xv[i];
+        bits |= ((unsigned long long)v.x << 1) | ((unsigned long long)v.y << 1);
+    }
+    for (long long j = nv * 2 + t0; j < n; j += stride) bits |= (unsigned long long)__double_as_longlong(x[j]) << 1;
+    if (__syncthreads_or(bits != 0ull) && threadIdx.x == 0) *flag = 1;
+}
+
 // ISO: equal spacings on the three axes, so the six neighbours share one weight
 // (GB300 runs FP64 at 1/64 of the FP32 rate, and this kernel is bound by it).  The
 // sum of squares of the stored value accumulates in double-float for TR = float.
@@ -2463,6 +2489,11 @@ void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin,
     launch_pdl(k_fcg_p_stencil<T>, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
     PPS_COUNT_LAUNCH();
 }
+void flag_nonzero(long long n, const double* x, int* flag, cudaStream_t s)
+{
+    launch_pdl(k_flag_nonzero, sm_count() * 4, 256, 0, s, n, x, flag);
+    PPS_COUNT_LAUNCH();
+}
 void fast_count_nonzero(const Geo& g, const Shape& sh, const double* x, RedCtx rc, cudaStream_t s)
 {
     launch_pdl(k_count_nonzero, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, x, rc);
@@ -2530,6 +2561,25 @@ void zero_off_unknowns(const Geo& g, T* p, cudaStream_t s)
     launch_pdl(k_zero_off_unknowns<T>, par_blocks(g.ntot), 256, 0, s, g, p);
     PPS_COUNT_LAUNCH();
 }
+// The Krylov scalars to their page-locked host copy, stored by one warp through the
+// mapping of that memory: a host poll that needs no copy engine, so it never queues
+// behind a bulk copy of a field that another stream has in flight.
+__global__ void __launch_bounds__(32) k_state_out(const DevState* __restrict__ d, DevState* __restrict__ h)
+{
+    pdl_enter();
+    constexpr int n = (int)(sizeof(DevState) / sizeof(unsigned long long));
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(d);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(h);
+    for (int i = threadIdx.x; i < n; i += 32) dst[i] = src[i];
+}
+
+void state_out(const DevState* d, DevState* h_mapped, cudaStream_t s)
+{
+    static_assert(sizeof(DevState) % sizeof(unsigned long long) == 0, "DevState is copied in 8-byte words");
+    launch_pdl(k_state_out, 1, 32, 0, s, d, h_mapped);
+    PPS_COUNT_LAUNCH();
+}
+
 void state_init(DevState* st, double* hist, int maxit, double tol_abs, double tol_rel, int tol_relative,
                 int rho0_from_r, double hist_scale, int hist_cap, cudaStream_t s)
 {

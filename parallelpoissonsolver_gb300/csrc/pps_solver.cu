@@ -107,6 +107,7 @@ struct pps_solver {
     Fields<float> f32;
     DevState* d_st = nullptr;
     DevState* h_st = nullptr;  // pinned
+    bool state_mapped = false; // h_st and h_st_in are device-addressable at their host addresses
     double* d_hist = nullptr;
     int hist_cap = 0;
     double* d_partials = nullptr;
@@ -171,6 +172,21 @@ struct pps_solver {
     float* d_exact = nullptr;
 
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // pps_solve on pinned host arrays, MIXED form: b is uploaded first and the solve
+    // starts on it as if x were zero, while x uploads on copy_stream and
+    // k_flag_nonzero tests it (ev_x: x resident, *h_xnz valid).  spec_x: that test is
+    // still unread; the solve reads or writes x only after it (a non-zero x restarts
+    // the solve on it).  out_host: after each update of x, copy_stream copies it to
+    // this host array (ev_out: done); out_current: the last such copy holds the final x.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_h0 = nullptr, ev_b = nullptr, ev_x = nullptr, ev_upd = nullptr, ev_out = nullptr;
+    int* d_xnz = nullptr;
+    int* h_xnz = nullptr;   // pinned
+    bool spec_x = false;
+    bool spec_restarted = false;
+    double* out_host = nullptr;
+    bool out_issued = false;
+    bool out_current = false;
     std::vector<cudaEvent_t> sweep_ev;   // pairs, profiling of sweeps
     std::vector<cudaEvent_t> krylov_ev;  // pairs, profiling of flexible CG's direction + update kernels
     int krylov_ev_used = 0;
@@ -299,6 +315,11 @@ void free_all(pps_solver* s)
     for (cudaEvent_t e : s->krylov_ev) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    for (cudaEvent_t e : {s->ev_h0, s->ev_b, s->ev_x, s->ev_upd, s->ev_out})
+        if (e) cudaEventDestroy(e);
+    if (s->d_xnz) cudaFree(s->d_xnz);
+    if (s->h_xnz) cudaFreeHost(s->h_xnz);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -1171,8 +1192,51 @@ void fast_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
 
 void read_state(pps_solver* s)
 {
-    CK(cudaMemcpyAsync(s->h_st, s->d_st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+    if (s->state_mapped) state_out(s->d_st, s->h_st, s->stream);
+    else CK(cudaMemcpyAsync(s->h_st, s->d_st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+}
+
+// Status of a solve restarted on the uploaded x (internal; never returned to callers)
+constexpr pps_status kRestartOnX = (pps_status)1000;
+
+// Ends a speculative start (pps_solve): when x's upload and test are done (or, with
+// wait, once they are), the solver's stream is ordered after them and the result is
+// read: true when x held a non-zero entry, so the work done on x = 0 is void.  False
+// while they are still running (no wait) or when no start was speculative.
+bool x_was_nonzero(pps_solver* s, bool wait)
+{
+    if (!s->spec_x) return false;
+    if (wait) {
+        CK(cudaEventSynchronize(s->ev_x));
+    } else {
+        const cudaError_t e = cudaEventQuery(s->ev_x);
+        if (e == cudaErrorNotReady) return false;
+        CK(e);
+    }
+    CK(cudaStreamWaitEvent(s->stream, s->ev_x, 0));
+    s->spec_x = false;
+    return *s->h_xnz != 0;
+}
+
+// After an update of x on the solver's stream: copy x to the caller's pinned array on
+// copy_stream, overlapping whatever the solve does next (a final residual check)
+void copy_out(pps_solver* s, const double* x)
+{
+    if (!s->out_host) return;
+    CK(cudaEventRecord(s->ev_upd, s->stream));
+    CK(cudaStreamWaitEvent(s->copy_stream, s->ev_upd, 0));
+    CK(cudaMemcpyAsync(s->out_host, x, sizeof(double) * (size_t)s->geo.ntot, cudaMemcpyDeviceToHost, s->copy_stream));
+    CK(cudaEventRecord(s->ev_out, s->copy_stream));
+    s->out_issued = true;
+    s->out_current = true;
+}
+
+// Before the solver's stream writes x again: the copy out of its previous value ends first
+void before_x_update(pps_solver* s)
+{
+    if (s->out_issued) CK(cudaStreamWaitEvent(s->stream, s->ev_out, 0));
+    s->out_current = false;
 }
 
 int auto_check_every(const pps_solver* s, int elem_size)
@@ -1259,6 +1323,7 @@ pps_status run_iterations(pps_solver* s, Fields<T>& F, T* xacc, int form, Launch
             for (int q = 0; q < chunk; q++) fast_iteration<T>(s, F, xacc, L);
         }
         read_state(s);
+        if (x_was_nonzero(s, false)) return kRestartOnX;
         if (s->h_st->done) break;
         if (learned) {
             // fall back to the plain preconditioner when the per-iteration reduction,
@@ -1374,23 +1439,32 @@ pps_status solve_fp64(pps_solver* s, double* x, const double* b)
 }
 
 // MIXED form: FP64 iterative refinement around an FP32 inner solve.
-pps_status solve_mixed(pps_solver* s, double* x, const double* b)
+// One pass of the MIXED solve.  Under a speculative start (spec_x) it runs on x = 0
+// and, where it would next read or write x (or return), first reads the test of the
+// uploaded x: a non-zero x returns kRestartOnX with x untouched.
+pps_status solve_mixed_pass(pps_solver* s, double* x, const double* b)
 {
     const Geo& g = s->geo;
     Fields<float>& F = s->f32;
     cudaStream_t st = s->stream;
     pps_stats& S = s->stats;
     Launcher L{s, s->cfg.use_graph == 0};
-    if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
-    const bool x0_zero = !s->has_neumann && field_is_zero(s, x);
+    if (s->has_neumann) {
+        before_x_update(s);
+        neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+    }
+    const bool x0_zero = s->spec_x || (!s->has_neumann && field_is_zero(s, x));
     const double normb = norm_badj(s, x, b, x0_zero);
     S.norm_b = normb;
-    if (!(normb > 0.0)) return PPS_ERR_ZERO_RHS;
+    if (!(normb > 0.0)) return x_was_nonzero(s, true) ? kRestartOnX : PPS_ERR_ZERO_RHS;
     s->net_active = s->net && (s->net_flags & PPS_LEARNED_PRECONDITIONER) && s->cfg.krylov == PPS_KRYLOV_FCG;
     s->learned_apps = 0;
     s->fallback_iter = -1;
     const bool guess = s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS);
-    if (guess) learned_initial_guess(s, x, b);
+    if (guess) {
+        before_x_update(s);
+        learned_initial_guess(s, x, b);
+    }
     const bool x_zero = x0_zero && !guess;
     const Coef a = op_coef(g);
     const double tol_abs = s->cfg.tol * normb;
@@ -1413,10 +1487,14 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         if (s->history.empty()) s->history.push_back(err_outer / normb);
         else s->history.back() = err_outer / normb;   // true residual replaces the recursive estimate
         if (err_outer < tol_abs) {
+            if (x_was_nonzero(s, true)) return kRestartOnX;
             rc = PPS_OK;
             break;
         }
-        if (ref == s->cfg.max_refinements || remaining <= 0) break;
+        if (ref == s->cfg.max_refinements || remaining <= 0) {
+            if (x_was_nonzero(s, true)) return kRestartOnX;
+            break;
+        }
         fill_field<float>(F.e, g.ntot, 0.0f, st);
         if (s->cfg.krylov == PPS_KRYLOV_CG) {
             precond_any<float>(s, F, F.r, F.z, L);
@@ -1426,6 +1504,7 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
             fcg_setup<float>(s, F, L);
         }
         pps_status irc = run_iterations<float>(s, F, F.e, PPS_FORM_MIXED, L);
+        if (irc == kRestartOnX || x_was_nonzero(s, true)) return kRestartOnX;
         const int it = s->h_st->iter;
         total_iter += it;
         pull_history(s, it, true);
@@ -1433,9 +1512,11 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
         S.err_iter = s->h_st->err / normb;
         // e started at zero and the updates add multiples of fields that are zero off
         // the unknowns on Dirichlet grids
+        before_x_update(s);
         fast_add_correction(g, s->shape, x, F.e, s->d_st, st, true);
         L.bytes += bytes_of<double>(s->n_unknowns, 2) + bytes_of<float>(s->n_unknowns, 1);
         if (s->has_neumann) neumann_fill<double>(g, x, faces_of(s), 1, 1.0, st);
+        copy_out(s, x);   // overlaps the residual check that follows
         S.refinements++;
         if (irc == PPS_NAN_DETECTED) {
             rc = irc;
@@ -1446,6 +1527,17 @@ pps_status solve_mixed(pps_solver* s, double* x, const double* b)
     S.err_true = err_outer / normb;
     S.hbm_bytes += L.bytes;
     return rc;
+}
+
+pps_status solve_mixed(pps_solver* s, double* x, const double* b)
+{
+    const pps_status rc = solve_mixed_pass(s, x, b);
+    if (rc != kRestartOnX) return rc;
+    // the uploaded x held a non-zero entry: the pass on x = 0 is void, solve from x
+    s->spec_restarted = true;
+    s->stats.precond_applications = 0;
+    s->stats.refinements = 0;
+    return solve_mixed_pass(s, x, b);
 }
 
 // ChebyshevIteration::operator() as the main solver (chebyshevIteration.hpp:48-140
@@ -1883,8 +1975,14 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         s->sigma = s->theta / s->delta;
 
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
         CK(cudaEventCreate(&s->ev0));
         CK(cudaEventCreate(&s->ev1));
+        CK(cudaEventCreate(&s->ev_h0));
+        CK(cudaEventCreate(&s->ev_b));
+        for (cudaEvent_t* e : {&s->ev_x, &s->ev_upd, &s->ev_out}) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        CK(cudaMalloc((void**)&s->d_xnz, sizeof(int)));
+        CK(cudaMallocHost((void**)&s->h_xnz, sizeof(int)));
         const size_t fb = sizeof(double) * (size_t)g.ntot;
         CK(cudaMalloc((void**)&s->d_x, fb));
         CK(cudaMalloc((void**)&s->d_b, fb));
@@ -1917,6 +2015,16 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         CK(cudaMemset(s->d_st, 0, sizeof(DevState)));
         CK(cudaMallocHost((void**)&s->h_st, sizeof(DevState)));
         CK(cudaMallocHost((void**)&s->h_dot, 4 * sizeof(double)));
+        {   // the host polls read the Krylov scalars through the mapping of h_st (read_state)
+            bool mapped = true;
+            for (DevState* h : {s->h_st, s->h_st_in}) {
+                if (!h) continue;
+                void* dp = nullptr;
+                mapped = mapped && cudaHostGetDevicePointer(&dp, h, 0) == cudaSuccess && dp == (void*)h;
+            }
+            cudaGetLastError();
+            s->state_mapped = mapped;
+        }
         s->hist_cap = cfg->maxit + 2;
         CK(cudaMalloc((void**)&s->d_hist, sizeof(double) * (size_t)s->hist_cap));
         const unsigned nb = std::max(max_candidate_blocks(g), 128u);   // 128: the canonical sums' blocks
@@ -1958,6 +2066,7 @@ pps_status pps_destroy(pps_solver* s)
     if (!s) return PPS_ERR_INVALID_ARG;
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
+    cudaStreamSynchronize(s->copy_stream);
     free_all(s);
     delete s;
     return PPS_OK;
@@ -2044,6 +2153,17 @@ pps_status pps_set_neumann(pps_solver* s, int face, const double* values)
     });
 }
 
+// A host array the copy engines and kernels reach directly (page-locked, registered)
+bool is_pinned(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats)
 {
     if (!s || !x || !b) return PPS_ERR_INVALID_ARG;
@@ -2051,20 +2171,67 @@ pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats)
     pps_status rc = guarded([&]() -> pps_status {
         CK(cudaSetDevice(s->device));
         const size_t fb = sizeof(double) * (size_t)s->geo.ntot;
+        // copy_stream's work on the caller's arrays ends before the call returns, an
+        // error included
+        struct Drain {
+            pps_solver* s;
+            ~Drain()
+            {
+                cudaStreamSynchronize(s->copy_stream);
+                s->spec_x = false;
+                s->out_host = nullptr;
+                s->out_issued = s->out_current = false;
+            }
+        } drain{s};
+        s->spec_restarted = false;
+        // MIXED form on pinned arrays (Dirichlet faces, no learned initial guess): b
+        // first, then the solve on it as if x were zero while x uploads behind it, and
+        // x's copy out overlapping the final residual check.  The link carries one
+        // array at a time at the same rate whichever engine drives it, so the gain is
+        // the copies hidden behind device work.
+        const bool overlap = s->cfg.form == PPS_FORM_MIXED && s->cfg.krylov != PPS_KRYLOV_CHEBYSHEV &&
+                             !s->has_neumann && !(s->net && (s->net_flags & PPS_LEARNED_INITIAL_GUESS)) &&
+                             is_pinned(x) && is_pinned(b);
         const auto a = std::chrono::steady_clock::now();
-        CK(cudaMemcpyAsync(s->d_x, x, fb, cudaMemcpyHostToDevice, s->stream));
-        CK(cudaMemcpyAsync(s->d_b, b, fb, cudaMemcpyHostToDevice, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
-        s->stats.seconds_h2d = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        if (overlap) {
+            CK(cudaEventRecord(s->ev_h0, s->stream));
+            CK(cudaMemcpyAsync(s->d_b, b, fb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaEventRecord(s->ev_b, s->stream));
+            CK(cudaStreamWaitEvent(s->copy_stream, s->ev_b, 0));   // x follows b on the link
+            CK(cudaMemcpyAsync(s->d_x, x, fb, cudaMemcpyHostToDevice, s->copy_stream));
+            CK(cudaMemsetAsync(s->d_xnz, 0, sizeof(int), s->copy_stream));
+            flag_nonzero(s->geo.ntot, s->d_x, s->d_xnz, s->copy_stream);
+            CK(cudaMemcpyAsync(s->h_xnz, s->d_xnz, sizeof(int), cudaMemcpyDeviceToHost, s->copy_stream));
+            CK(cudaEventRecord(s->ev_x, s->copy_stream));
+            s->spec_x = true;
+            s->out_host = x;
+            s->stats.seconds_h2d = 0;
+        } else {
+            CK(cudaMemcpyAsync(s->d_x, x, fb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(s->d_b, b, fb, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            s->stats.seconds_h2d = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        }
         s->stats.seconds_d2h = 0;
         pps_status r = solve_core(s, s->d_x, s->d_b);
+        if (overlap) s->stats.kernel_launches += 1;   // the test of x, launched before the count restarted
         if (r < 0) return r;
         const auto c = std::chrono::steady_clock::now();
-        CK(cudaMemcpyAsync(x, s->d_x, fb, cudaMemcpyDeviceToHost, s->stream));
+        if (!(overlap && s->out_current)) {
+            if (s->out_issued) CK(cudaStreamWaitEvent(s->stream, s->ev_out, 0));
+            CK(cudaMemcpyAsync(x, s->d_x, fb, cudaMemcpyDeviceToHost, s->stream));
+        }
         if (s->cfg.form == PPS_FORM_PARITY_FP64)
             CK(cudaMemcpyAsync(b, s->d_b, fb, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
+        CK(cudaStreamSynchronize(s->copy_stream));
         s->stats.seconds_d2h = std::chrono::duration<double>(std::chrono::steady_clock::now() - c).count();
+        if (overlap) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, s->ev_h0, s->ev_b));
+            s->stats.seconds_h2d = ms * 1e-3;
+            s->stats.copy_overlap = 1 | (s->spec_restarted ? 2 : 0) | (s->out_current ? 4 : 0);
+        }
         return r;
     });
     s->stats.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
