@@ -949,8 +949,45 @@ __device__ __forceinline__ void prolong_v4_column(const Geo& g, const Dims& dc, 
             load3(cz + 1, vn);
             xn = xi(vn);
         }
-        add(c, make_float4(0.5f * (xm.x + x0.x), 0.5f * (xm.y + x0.y), 0.5f * (xm.z + x0.z), 0.5f * (xm.w + x0.w)));
-        add(c + sk, x0);
+        const float4 xa = make_float4(0.5f * (xm.x + x0.x), 0.5f * (xm.y + x0.y), 0.5f * (xm.z + x0.z), 0.5f * (xm.w + x0.w));
+        if (all4) {
+            // both fine planes' loads before either store: f is written in place, so
+            // the compiler cannot move the second plane's loads above the first
+            // plane's store, and the pair would cost two round trips to memory
+            float4 q0 = *reinterpret_cast<const float4*>(f + c), q1 = *reinterpret_cast<const float4*>(f + c + sk);
+            float4 r0, r1, a0, a1;
+            if (DOTS) {
+                r0 = *reinterpret_cast<const float4*>(r + c);
+                r1 = *reinterpret_cast<const float4*>(r + c + sk);
+                a0 = *reinterpret_cast<const float4*>(Ap + c);
+                a1 = *reinterpret_cast<const float4*>(Ap + c + sk);
+            }
+            q0 = make_float4(q0.x + xa.x, q0.y + xa.y, q0.z + xa.z, q0.w + xa.w);
+            q1 = make_float4(q1.x + x0.x, q1.y + x0.y, q1.z + x0.z, q1.w + x0.w);
+            *reinterpret_cast<float4*>(f + c) = q0;
+            *reinterpret_cast<float4*>(f + c + sk) = q1;
+            if (DOTS) {   // plane order, element order: the sums of add()
+                zr.add(q0.x, r0.x);
+                zap.add(q0.x, a0.x);
+                zr.add(q0.y, r0.y);
+                zap.add(q0.y, a0.y);
+                zr.add(q0.z, r0.z);
+                zap.add(q0.z, a0.z);
+                zr.add(q0.w, r0.w);
+                zap.add(q0.w, a0.w);
+                zr.add(q1.x, r1.x);
+                zap.add(q1.x, a1.x);
+                zr.add(q1.y, r1.y);
+                zap.add(q1.y, a1.y);
+                zr.add(q1.z, r1.z);
+                zap.add(q1.z, a1.z);
+                zr.add(q1.w, r1.w);
+                zap.add(q1.w, a1.w);
+            }
+        } else {
+            add(c, xa);
+            add(c + sk, x0);
+        }
         xm = x0;
         x0 = xn;
         cz++;
