@@ -904,6 +904,8 @@ def profile_case(argv):
                     help="Krylov loop without --learned (fcg: flexible CG with the Chebyshev preconditioner)")
     ap.add_argument("--batch-problems", type=int, default=0,
                     help="instead: one persistent V-cycle batch of this many problems of the batched workload")
+    ap.add_argument("--fcg-staged", action="store_true",
+                    help="flexible CG's direction kernel with its inputs staged by TMA (tuning fcg_staged)")
     a = ap.parse_args(argv)
     if a.batch_problems > 0:
         edges = workloads.edges_config3(a.batch_problems, seed=3)
@@ -957,6 +959,8 @@ def profile_case(argv):
         cls = pps.FlexibleCG if a.krylov == "fcg" else pps.BiCGSTAB
         s = cls(grid, pps.ChebyshevIteration(a.degree), tolerance=1e-10, max_iteration=a.maxit,
                 form=a.form, inner_maxit=a.maxit, max_refinements=1, use_graph=a.graph)
+        if a.fcg_staged:
+            s.set_tuning({**s.tuning(), "fcg_staged": 1})
     for _ in range(a.repeat):
         x = grid.new_field()
         st = s(x, b.copy(), raise_on_error=True)

@@ -242,6 +242,10 @@ typedef struct {
     int cheb_fused;             /* 1: Chebyshev applications of degree 4 or 5 on Dirichlet grids
                                    run all their steps in one temporally blocked pass
                                    (bit-identical); 0 (default): one launch per step */
+    int fcg_staged;             /* 1: flexible CG's direction kernel on the cx 4 tiles
+                                   stages its inputs in shared memory by TMA (bit-identical;
+                                   slower on GB300 at 512^3); 0 (default): it loads them
+                                   itself */
 } pps_tuning;
 
 /* Autotuner (no reference counterpart; the reference fixes its launch shapes,

@@ -85,16 +85,18 @@ class PpsStats(C.Structure):
 class PpsTuning(C.Structure):
     _fields_ = [("cheb_ty", C.c_int), ("cheb_cx", C.c_int), ("cheb_waves", C.c_int), ("other_ty", C.c_int),
                 ("other_waves", C.c_int), ("cheb_us", C.c_double), ("other_us", C.c_double),
-                ("cheb_fused", C.c_int)]
+                ("cheb_fused", C.c_int), ("fcg_staged", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+    OPTIONAL = {"cheb_fused": 0, "fcg_staged": 0}   # keys older stored tunings lack
 
     @classmethod
     def from_dict(cls, d):
         t = cls()
         for k, _ in cls._fields_:
-            setattr(t, k, d.get(k, 0) if k == "cheb_fused" else d[k])
+            setattr(t, k, d.get(k, cls.OPTIONAL[k]) if k in cls.OPTIONAL else d[k])
         return t
 
 

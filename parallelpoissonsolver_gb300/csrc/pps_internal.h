@@ -316,7 +316,7 @@ template <typename T>
 void fast_fcg_dot(const Geo& g, const Shape& sh, const T* r, const T* z, const T* Ap, RedCtx rc, cudaStream_t s);
 template <typename T>
 void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
-                        RedCtx rc, cudaStream_t s);
+                        RedCtx rc, cudaStream_t s, bool staged);
 // The same updates and sums over the whole padded array in 16-byte vectors (fields
 // zero on the guard cells, 16-byte aligned).
 template <typename T>

@@ -18,6 +18,7 @@
 #include <initializer_list>
 #include <type_traits>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -1385,6 +1386,195 @@ __global__ void __launch_bounds__(256) k_fcg_p_stencil_v4(Geo g, Shape sh, const
     reduce_finalize<1>(v, rc);
 }
 
+// ---- bulk-copy staging (cp.async.bulk into shared memory, mbarrier completion) ----
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// one arrival that also announces the bytes the phase's bulk copies will deliver
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// one box of a tiled tensor map (coordinates x, y, z in elements; x * 4 bytes a multiple
+// of 16) into this CTA's shared memory (128-byte aligned), completing on the mbarrier;
+// the parts of the box outside the tensor arrive as zeros
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int zc,
+                                            unsigned long long* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(zc), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr int STAGE_ROW = 136;   // floats per staged row: x0 - 4 .. x0 + 131 (128 columns and their x halo)
+constexpr int STAGES = 4;        // planes in the ring
+constexpr unsigned long long STAGE_WAIT_NS = 2000000000ull;   // 2 s: a wait this long means a lost copy
+
+// floats of one staged box (ty + 2 rows), rounded up to 128 bytes (TMA destinations)
+__host__ __device__ constexpr int stage_box_floats(int ty) { return ((ty + 2) * STAGE_ROW + 31) / 32 * 32; }
+static size_t stage_smem_bytes(int ty)
+{
+    return sizeof(float) * (size_t)STAGES * 2 * stage_box_floats(ty) + sizeof(unsigned long long) * STAGES;
+}
+
+// k_fcg_p_stencil_v4 with its inputs staged by TMA.  One thread copies, for each
+// plane of the block's z range and the plane on either side, the tile's rows of z (and
+// of p_in unless beta = 0) with the x and y halo into a ring of STAGES shared-memory slots,
+// each completing on its own mbarrier; the block computes from shared memory while the
+// next planes are in flight, so the loads' latency no longer sits in the registers of
+// the computing threads.  Tiles, per-point arithmetic and per-thread sums are
+// k_fcg_p_stencil_v4's, so every output and the block sums are bit-identical to it.
+// A wait is bounded (STAGE_WAIT_NS by %globaltimer); one that runs out ends the solve
+// with PPS_TIMEOUT (state done) and the block runs to its end on whatever arrived.
+// The boxes come from tiled tensor maps over the padded fields (one copy per field and
+// plane, 136 x (ty + 2) floats); box parts outside the field arrive as zeros, which is
+// what the guard cells the register-marching kernel reads there hold.
+__global__ void __launch_bounds__(256) k_fcg_p_stencil_staged(Geo g, Shape sh, const __grid_constant__ CUtensorMap tz,
+                                                              const __grid_constant__ CUtensorMap tp,
+                                                              float* __restrict__ pout, float* __restrict__ Ap, Coef cf,
+                                                              RedCtx rc)
+{
+    pdl_enter();
+    EARLY_EXIT(&rc.st->done);
+    extern __shared__ __align__(128) unsigned char stage_raw[];
+    const int ty = blockDim.y, box = stage_box_floats(ty);
+    float* stage = reinterpret_cast<float*>(stage_raw);
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(stage_raw + sizeof(float) * (size_t)STAGES * 2 * box);
+    const int lane = threadIdx.x, wrow = threadIdx.y;
+    const Col4 q = column4(g, sh);
+    const int bx = blockIdx.x % sh.ntx, by = blockIdx.x / sh.ntx;
+    const int x0 = bx * 128, ylo = g.lo[1] + by * ty;
+    const int k0 = q.k0, k1 = q.k1, kbase = k0 - 1;
+    const int xs = x0 - 4;                              // staged rows: x0 - 4 .. x0 + 131 of rows ylo - 1 .. ylo + ty
+    const bool restart = rc.st->beta == 0.0;
+    const int nf = restart ? 1 : 2;
+    const unsigned plane_bytes = (unsigned)(nf * (ty + 2) * STAGE_ROW) * 4u;   // whole boxes, zeros included
+    if (wrow == 0 && lane == 0) {
+        for (int b = 0; b < STAGES; b++) mbar_init(&bars[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto slot_of = [&](int kk) { return (kk - kbase) % STAGES; };
+    auto at = [&](int kk, int f, int rr) { return stage + (size_t)(slot_of(kk) * 2 + f) * box + rr * STAGE_ROW; };
+    // thread 0: plane kk's box of z (and of p_in) into its slot (kk <= k1, the last plane any thread reads)
+    auto issue = [&](int kk) {
+        if (wrow != 0 || lane != 0 || kk > k1) return;
+        unsigned long long* bar = &bars[slot_of(kk)];
+        mbar_arrive_expect_tx(bar, plane_bytes);
+        tma_load_3d(at(kk, 0, 0), &tz, xs, ylo - 1, kk, bar);
+        if (!restart) tma_load_3d(at(kk, 1, 0), &tp, xs, ylo - 1, kk, bar);
+    };
+    bool lost = false;
+    auto wait_plane = [&](int kk) {
+        unsigned long long* bar = &bars[slot_of(kk)];
+        const unsigned parity = (unsigned)((kk - kbase) / STAGES) & 1u;
+        if (mbar_try_wait(bar, parity)) return;
+        const unsigned long long t0 = globaltimer_ns();
+        while (!mbar_try_wait(bar, parity)) {
+            if (globaltimer_ns() - t0 > STAGE_WAIT_NS) {
+                lost = true;
+                return;
+            }
+        }
+    };
+    for (int kk = kbase; kk < kbase + STAGES; kk++) issue(kk);
+
+    Acc<float> a1;
+    const bool live = q.j < g.hi[1];   // a warp shares its row
+    const bool act = live && q.act;
+    const bool m0 = q.i0 >= g.lo[0] && q.i0 < g.hi[0], m1 = q.i0 + 1 >= g.lo[0] && q.i0 + 1 < g.hi[0];
+    const bool m2 = q.i0 + 2 >= g.lo[0] && q.i0 + 2 < g.hi[0], m3 = q.i0 + 3 >= g.lo[0] && q.i0 + 3 < g.hi[0];
+    const bool all4 = m0 && m1 && m2 && m3;
+    const float cc = (float)cf.cc, cx = (float)cf.cx, cy = (float)cf.cy, cz = (float)cf.cz;
+    const float be = (float)rc.st->beta;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int xo = q.i0 - xs;   // the thread's float4 in a staged row (4 * lane + 4)
+    const int rr0 = wrow + 1;   // the thread's row in the staged rows
+    auto pv4 = [&](int kk, int rr) -> float4 {
+        if (!act) return zero;
+        const float4 zv = *reinterpret_cast<const float4*>(at(kk, 0, rr) + xo);
+        if (restart) return zv;
+        const float4 pv = *reinterpret_cast<const float4*>(at(kk, 1, rr) + xo);
+        return make_float4(fmx(be, pv.x, zv.x), fmx(be, pv.y, zv.y), fmx(be, pv.z, zv.z), fmx(be, pv.w, zv.w));
+    };
+    auto pv1 = [&](int kk, int o) -> float {   // o: offset in the staged row
+        const float zv = at(kk, 0, rr0)[o];
+        return restart ? zv : fmx(be, at(kk, 1, rr0)[o], zv);
+    };
+    wait_plane(kbase);
+    float4 um = pv4(kbase, rr0);
+    wait_plane(k0);
+    float4 uc = pv4(k0, rr0);
+    __syncthreads();       // plane kbase's slot is free
+    issue(kbase + STAGES);
+    long long c = q.c;
+#pragma unroll 1
+    for (int k = k0; k < k1; k++) {
+        wait_plane(k + 1);
+        const float4 up = pv4(k + 1, rr0);
+        const float4 uy = add4(pv4(k, rr0 - 1), pv4(k, rr0 + 1));
+        float left = __shfl_up_sync(0xffffffffu, uc.w, 1), right = __shfl_down_sync(0xffffffffu, uc.x, 1);
+        if (lane == 0) left = act ? pv1(k, xo - 1) : 0.f;
+        if (lane == 31) right = act && q.i0 + 4 < g.sj ? pv1(k, xo + 4) : 0.f;
+        float4 a;
+        a.x = fmx(cz, um.x + up.x, fmx(cy, uy.x, fmx(cx, left + uc.y, cc * uc.x)));
+        a.y = fmx(cz, um.y + up.y, fmx(cy, uy.y, fmx(cx, uc.x + uc.z, cc * uc.y)));
+        a.z = fmx(cz, um.z + up.z, fmx(cy, uy.z, fmx(cx, uc.y + uc.w, cc * uc.z)));
+        a.w = fmx(cz, um.w + up.w, fmx(cy, uy.w, fmx(cx, uc.z + right, cc * uc.w)));
+        if (act) {
+            if (all4) {
+                *reinterpret_cast<float4*>(pout + c) = uc;
+                *reinterpret_cast<float4*>(Ap + c) = a;
+            } else {
+                if (m0) { pout[c] = uc.x; Ap[c] = a.x; }
+                if (m1) { pout[c + 1] = uc.y; Ap[c + 1] = a.y; }
+                if (m2) { pout[c + 2] = uc.z; Ap[c + 2] = a.z; }
+                if (m3) { pout[c + 3] = uc.w; Ap[c + 3] = a.w; }
+            }
+            if (m0) a1.add(uc.x, a.x);
+            if (m1) a1.add(uc.y, a.y);
+            if (m2) a1.add(uc.z, a.z);
+            if (m3) a1.add(uc.w, a.w);
+        }
+        um = uc;
+        uc = up;
+        c += g.sk;
+        __syncthreads();   // plane k's slot is free
+        issue(k + STAGES);
+    }
+    if (lost) {
+        rc.st->status = PPS_TIMEOUT;
+        rc.st->done = 1;
+    }
+    double v[1] = {a1.value()};
+    reduce_finalize<1>(v, rc);
+}
+
 // FCG: x += alpha*p; r -= alpha*Ap; sum r.r (the convergence test, before the
 // preconditioner, which a converged iteration then skips)
 template <typename T>
@@ -2471,19 +2661,69 @@ void fast_fcg_dot_flat(const Geo& g, const Shape& sh, const T* r, const T* z, co
     launch_pdl(k_fcg_dot_flat<T>, sh.nblocks(), 32 * sh.ty, 0, s, g.ntot, r, z, Ap, rc);
     PPS_COUNT_LAUNCH();
 }
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// the driver's tensor-map encoder, fetched through the runtime (no link to the driver library)
+static EncodeTiledFn encode_tiled()
+{
+    static const EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+// A tiled map over a padded FP32 field (x, y, z = row, plane, field extents) whose
+// boxes are STAGE_ROW x rows x 1; parts of a box outside the field read as zeros.
+// False where the encoder is missing or refuses (the caller then takes another kernel).
+static bool field_map(CUtensorMap* m, const float* base, const Geo& g, int rows)
+{
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || ((uintptr_t)base & 15u) != 0 || g.sj % 4 != 0 || rows > 256) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.sj, (cuuint64_t)(g.sk / g.sj), (cuuint64_t)(g.ntot / g.sk)};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.sj * 4u, (cuuint64_t)g.sk * 4u};
+    const cuuint32_t boxd[3] = {(cuuint32_t)STAGE_ROW, (cuuint32_t)rows, 1u};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, boxd, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <typename T>
 void fast_fcg_p_stencil(const Geo& g, const Shape& sh, const T* z, const T* pin, T* pout, T* Ap, const Coef& a,
-                        RedCtx rc, cudaStream_t s)
+                        RedCtx rc, cudaStream_t s, bool staged)
 {
     if (sh.cx != 1) {   // the Chebyshev tiles: x-vectorised FP32, else the one-column tiles
         if constexpr (std::is_same<T, float>::value) {
             if (sh.cx == 4 && v4_ok<T>(g, z, pin, pout, Ap)) {
-                launch_pdl(k_fcg_p_stencil_v4, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
+                CUtensorMap mz, mp;
+                if (staged && field_map(&mz, z, g, sh.ty + 2) && field_map(&mp, pin, g, sh.ty + 2)) {
+                    const size_t smem = stage_smem_bytes(sh.ty);
+                    static int attr_set = 0;   // bytes the attribute allows
+                    if (smem > 48 * 1024 && attr_set < (int)smem) {
+                        cudaFuncSetAttribute(k_fcg_p_stencil_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+                        attr_set = (int)smem;
+                    }
+                    launch_pdl(k_fcg_p_stencil_staged, grid_of(sh), block_of(sh), smem, s, g, sh, mz, mp, pout, Ap,
+                               a, rc);
+                } else {
+                    launch_pdl(k_fcg_p_stencil_v4, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
+                }
                 PPS_COUNT_LAUNCH();
                 return;
             }
         }
-        fast_fcg_p_stencil<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), z, pin, pout, Ap, a, rc, s);
+        fast_fcg_p_stencil<T>(g, make_shape(g, sh.ty, (int)sh.nblocks(), 1), z, pin, pout, Ap, a, rc, s, staged);
         return;
     }
     launch_pdl(k_fcg_p_stencil<T>, grid_of(sh), block_of(sh), 0, s, g, sh, z, pin, pout, Ap, a, rc);
@@ -2614,7 +2854,7 @@ void state_init(DevState* st, double* hist, int maxit, double tol_abs, double to
                                         cudaStream_t);                                                           \
     template void fast_fcg_dot<T>(const Geo&, const Shape&, const T*, const T*, const T*, RedCtx, cudaStream_t); \
     template void fast_fcg_p_stencil<T>(const Geo&, const Shape&, const T*, const T*, T*, T*, const Coef&,       \
-                                        RedCtx, cudaStream_t);                                                   \
+                                        RedCtx, cudaStream_t, bool);                                             \
     template void fast_cheb_fused<T>(const Geo&, int, const T*, T*, const Coef*, const int*, cudaStream_t);      \
     template void fast_fcg_update_xr_flat<T>(const Geo&, const Shape&, T*, const T*, T*, const T*, RedCtx,       \
                                              cudaStream_t);                                                      \

@@ -1149,7 +1149,8 @@ void fast_fcg_iteration(pps_solver* s, Fields<T>& F, T* xacc, Launcher& L)
     // the direction/stencil kernel runs on the Chebyshev tiles (x-vectorised for FP32)
     const bool prof = L.profile && s->krylov_ev_used + 2 <= (int)s->krylov_ev.size();
     if (prof) CK(cudaEventRecord(s->krylov_ev[s->krylov_ev_used], st));
-    fast_fcg_p_stencil<T>(g, s->shape_cheb, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st);
+    fast_fcg_p_stencil<T>(g, s->shape_cheb, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_FCG_ALPHA), st,
+                          s->tuning.fcg_staged != 0);
     std::swap(F.p, F.Az);
     const bool flat = aligned16(xacc) && aligned16(F.p) && aligned16(F.r) && aligned16(F.AMp) && aligned16(F.z);
     if (flat) fast_fcg_update_xr_flat<T>(g, sh, xacc, F.p, F.r, F.AMp, red(s, FIN_FCG_RES), st);
@@ -1696,7 +1697,9 @@ void autotune_fields(pps_solver* s, Fields<T>& F, pps_tuning* best)
                     fast_cheb_sweep<T>(g, sh, F.Y, F.r, F.Z, F.W, c, &s->d_st->done, s->stream);
                 });
                 const double ks = time_launches<T>(s, reps, [&]() {
-                    if (fcg) fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_STORE), s->stream);
+                    if (fcg)
+                        fast_fcg_p_stencil<T>(g, sh, F.z, F.p, F.Az, F.AMp, a, red(s, FIN_STORE), s->stream,
+                                              best->fcg_staged != 0);
                     else fast_stencil_dot2<T>(g, sh, F.z, F.r, F.Az, a, red_c(s, FIN_STORE), s->stream);
                 });
                 if (weight * us + ks < best_us) {
@@ -1743,7 +1746,8 @@ bool tuning_valid(const pps_tuning* t)
         return false;
     };
     return in(t->cheb_ty, kTys, 3) && in(t->cheb_cx, kCxs, 3) && in(t->cheb_waves, kWaves, 4) &&
-           in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4) && (t->cheb_fused == 0 || t->cheb_fused == 1);
+           in(t->other_ty, kTys, 3) && in(t->other_waves, kWaves, 4) && (t->cheb_fused == 0 || t->cheb_fused == 1) &&
+           (t->fcg_staged == 0 || t->fcg_staged == 1);
 }
 
 pps_status validate(const pps_grid* g, const pps_config* c)
@@ -1957,6 +1961,7 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
         s->tuning.cheb_us = 0.0;
         s->tuning.other_us = 0.0;
         s->tuning.cheb_fused = 0;
+        s->tuning.fcg_staged = 0;
         // computeEigenvalues, global bounds (blockGrid.hpp:322-339)
         double eigMin = 0, eigMax = 0;
         for (int i = 0; i < 3; i++) {
