@@ -36,23 +36,25 @@ constexpr int TILE_V = 64;   // voxels (along x) per conv block: 4 warps x 16
 // Convolution, forward: Y[v][co] = act(bias[co] + sum_tap sum_ci X[v+off(tap)][ci] W[tap][ci][co])
 // Cin, Cout multiples of 16.  One block: one 16 x 16 output fragment (16 consecutive
 // voxels in (z, y, x) order, 16 output channels).  The K = 27 * Cin/16 steps of
-// 16 x 16 x 16 are dealt round-robin to the 4 warps, so each warp's dependent chain
-// is a quarter of K (the grids are small: at 16^3 latency, not the tensor pipe, is
-// the limit); each warp stages its A tile in its own shared slot (warp-level sync
-// only), reads the weight fragment straight from global memory, prefetches the
-// next A tile into registers, and the four partial fragments are summed at the end.
+// 16 x 16 x 16 are dealt round-robin to the NW warps, so each warp's dependent chain
+// is 1/NW of K (the grids are small: at 16^3 and below latency, not the tensor pipe,
+// is the limit; the deep layers run 54-162 steps on 16-64 blocks).  Each warp stages
+// its A tile in its own shared slot (warp-level sync only) and prefetches the next
+// step's A tile and weight fragment into registers while the current step's
+// multiply-add runs; the NW partial fragments are summed at the end.
 // ---------------------------------------------------------------------------
 constexpr int CONV_V = 16;   // voxels per block
 
-template <bool RELU, bool OUT_F32>
-__global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
-                                              const bf16* __restrict__ Wt, const float* __restrict__ bias,
-                                              void* __restrict__ Yv, int ldy, int cy0, int Cout, const int* __restrict__ stop)
+template <bool RELU, bool OUT_F32, int NW>
+__global__ void __launch_bounds__(32 * NW) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
+                                                  const bf16* __restrict__ Wt, const float* __restrict__ bias,
+                                                  void* __restrict__ Yv, int ldy, int cy0, int Cout,
+                                                  const int* __restrict__ stop)
 {
     pdl_enter();
     if (stop && *(volatile const int*)stop) return;
-    __shared__ __align__(32) bf16 sA[4][CONV_V * 16];
-    __shared__ __align__(32) float sC[4][16 * 16];
+    __shared__ __align__(32) bf16 sA[NW][CONV_V * 16];
+    __shared__ __align__(32) float sC[NW][16 * 16];
     const long long nvox = (long long)d.D * d.H * d.W;
     const long long v0 = (long long)blockIdx.x * CONV_V;
     const int co0 = blockIdx.y * 16;
@@ -71,28 +73,38 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
             val = *reinterpret_cast<const uint4*>(X + (((long long)zz * d.H + yy) * d.W + xx) * ldx + cx0 + c0 + 8 * ha);
         return val;
     };
+    auto w_at = [&](int t) {
+        const int tap = t / csteps, c0 = (t - tap * csteps) * 16;
+        return Wt + ((long long)tap * Cin + c0) * Cout + co0;
+    };
     wmma::fragment<wmma::accumulator, 16, 16, 16, float> acc;
     wmma::fill_fragment(acc, 0.0f);
+    wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> bcur, bnext;
     int t = warp;
     uint4 next = t < ksteps ? load_a(t) : make_uint4(0, 0, 0, 0);
-    for (; t < ksteps; t += 4) {
+    if (t < ksteps) wmma::load_matrix_sync(bnext, w_at(t), Cout);
+    for (; t < ksteps; t += NW) {
         *reinterpret_cast<uint4*>(&sA[warp][va * 16 + 8 * ha]) = next;
+        bcur = bnext;
         __syncwarp();
-        if (t + 4 < ksteps) next = load_a(t + 4);
-        const int tap = t / csteps, c0 = (t - tap * csteps) * 16;
+        if (t + NW < ksteps) {
+            next = load_a(t + NW);
+            wmma::load_matrix_sync(bnext, w_at(t + NW), Cout);
+        }
         wmma::fragment<wmma::matrix_a, 16, 16, 16, bf16, wmma::row_major> a;
-        wmma::fragment<wmma::matrix_b, 16, 16, 16, bf16, wmma::row_major> bfr;
         wmma::load_matrix_sync(a, sA[warp], 16);
-        wmma::load_matrix_sync(bfr, Wt + ((long long)tap * Cin + c0) * Cout + co0, Cout);
-        wmma::mma_sync(acc, a, bfr, acc);
+        wmma::mma_sync(acc, a, bcur, acc);
         __syncwarp();
     }
     wmma::store_matrix_sync(sC[warp], acc, 16, wmma::mem_row_major);
     __syncthreads();
-    for (int q = threadIdx.x; q < CONV_V * 16; q += 128) {
+    for (int q = threadIdx.x; q < CONV_V * 16; q += 32 * NW) {
         const int v = q >> 4, co = q & 15;
         if (v0 + v >= nvox) continue;
-        float val = sC[0][q] + sC[1][q] + sC[2][q] + sC[3][q] + (bias ? bias[co0 + co] : 0.0f);
+        float val = 0.0f;
+#pragma unroll
+        for (int w = 0; w < NW; w++) val += sC[w][q];
+        val += bias ? bias[co0 + co] : 0.0f;
         if (RELU) val = fmaxf(val, 0.0f);
         const long long o = (v0 + v) * ldy + cy0 + co0 + co;
         if (OUT_F32) reinterpret_cast<float*>(Yv)[o] = val;
@@ -100,17 +112,28 @@ __global__ void __launch_bounds__(128) k_conv(Dims d, const bf16* __restrict__ X
     }
 }
 
+template <int NW>
+static void conv_nw(const dim3& grid, const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W,
+                    const float* bias, void* Y, int ldy, int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
+{
+    const dim3 block(32 * NW);
+    if (out_f32) {
+        if (relu) launch_pdl(k_conv<true, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else launch_pdl(k_conv<false, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+    } else {
+        if (relu) launch_pdl(k_conv<true, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        else launch_pdl(k_conv<false, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+    }
+}
+
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
           int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
 {
     const dim3 grid((unsigned)(((long long)d.D * d.H * d.W + CONV_V - 1) / CONV_V), (unsigned)(Cout / 16));
-    if (out_f32) {
-        if (relu) launch_pdl(k_conv<true, true>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else launch_pdl(k_conv<false, true>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-    } else {
-        if (relu) launch_pdl(k_conv<true, false>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else launch_pdl(k_conv<false, false>, grid, 128, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-    }
+    // warps per block: enough that each warp's chain of K steps stays short
+    const int ksteps = 27 * (Cin / 16);
+    if (ksteps >= 64) conv_nw<16>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s);
+    else conv_nw<8>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s);
     launches_counter_add(1);
 }
 
