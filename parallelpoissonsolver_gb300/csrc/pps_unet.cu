@@ -153,15 +153,37 @@ void ensure_acts(pps_unet* u, int nx, int ny, int nz, bool grads)
 const bf16* Wb(const pps_unet* u, int l) { return u->PB + u->L[(size_t)l].w; }
 const float* Bf(const pps_unet* u, int l) { return u->P + u->L[(size_t)l].b; }
 
-void forward(pps_unet* u, const float* in, const float* rms_dev)
+// The forward pass.  With `dense_out` (inference) the glue kernels fold into the
+// convolutions next to them: the first reads the dense input scaled by 1/(*rms_dev),
+// the two after an upsampling read the coarse tensor for the upsampled channels, and
+// the last writes channel 0 times (*rms_dev) * gain into dense_out (the same values;
+// A.x0, the upsampled slots of A.cat1/A.cat2 and A.out are then not written).
+// Without it (training) every activation is stored for the backward pass.
+void forward(pps_unet* u, const float* in, const float* rms_dev, float* dense_out = nullptr, float gain = 1.0f)
 {
     Acts& A = u->A;
     cudaStream_t s = u->stream;
     const int c1 = u->c1, c2 = u->c2, c3 = u->c3;
     const long long v1 = (long long)A.s1.D * A.s1.H * A.s1.W;
-    dense_to_act(v1, in, rms_dev, A.x0, 16, s);
     const bool R = !u->linear;
-    conv(A.s1, A.x0, 16, 0, 16, Wb(u, 0), Bf(u, 0), A.e1a, c1, 0, c1, R, false, s);
+    const bool infer = dense_out != nullptr;
+    ConvIO first, up2io, up1io, last;
+    if (infer) {
+        first.dense_in = in;
+        first.rms = rms_dev;
+        up2io.up = A.e3;
+        up2io.ld_up = c3;
+        up2io.c_up = c3;
+        up1io.up = A.d2;
+        up1io.ld_up = c2;
+        up1io.c_up = c2;
+        last.dense_out = dense_out;
+        last.rms = rms_dev;
+        last.gain = gain;
+    } else {
+        dense_to_act(v1, in, rms_dev, A.x0, 16, s);
+    }
+    conv(A.s1, A.x0, 16, 0, 16, Wb(u, 0), Bf(u, 0), A.e1a, c1, 0, c1, R, false, s, first);
     conv(A.s1, A.e1a, c1, 0, c1, Wb(u, 1), Bf(u, 1), A.cat1, c2 + c1, c2, c1, R, false, s);
     pool2(A.s2, A.cat1, c2 + c1, c2, A.p1, c1, s);
     conv(A.s2, A.p1, c1, 0, c1, Wb(u, 2), Bf(u, 2), A.e2a, c2, 0, c2, R, false, s);
@@ -169,13 +191,13 @@ void forward(pps_unet* u, const float* in, const float* rms_dev)
     pool2(A.s3, A.cat2, c3 + c2, c3, A.p2, c2, s);
     conv(A.s3, A.p2, c2, 0, c2, Wb(u, 4), Bf(u, 4), A.e3a, c3, 0, c3, R, false, s);
     conv(A.s3, A.e3a, c3, 0, c3, Wb(u, 5), Bf(u, 5), A.e3, c3, 0, c3, R, false, s);
-    up2(A.s2, A.e3, c3, A.cat2, c3 + c2, 0, s);
-    conv(A.s2, A.cat2, c3 + c2, 0, c3 + c2, Wb(u, 6), Bf(u, 6), A.d2a, c2, 0, c2, R, false, s);
+    if (!infer) up2(A.s2, A.e3, c3, A.cat2, c3 + c2, 0, s);
+    conv(A.s2, A.cat2, c3 + c2, 0, c3 + c2, Wb(u, 6), Bf(u, 6), A.d2a, c2, 0, c2, R, false, s, up2io);
     conv(A.s2, A.d2a, c2, 0, c2, Wb(u, 7), Bf(u, 7), A.d2, c2, 0, c2, R, false, s);
-    up2(A.s1, A.d2, c2, A.cat1, c2 + c1, 0, s);
-    conv(A.s1, A.cat1, c2 + c1, 0, c2 + c1, Wb(u, 8), Bf(u, 8), A.d1a, c1, 0, c1, R, false, s);
+    if (!infer) up2(A.s1, A.d2, c2, A.cat1, c2 + c1, 0, s);
+    conv(A.s1, A.cat1, c2 + c1, 0, c2 + c1, Wb(u, 8), Bf(u, 8), A.d1a, c1, 0, c1, R, false, s, up1io);
     conv(A.s1, A.d1a, c1, 0, c1, Wb(u, 9), Bf(u, 9), A.d1, c1, 0, c1, R, false, s);
-    conv(A.s1, A.d1, c1, 0, c1, Wb(u, 10), Bf(u, 10), A.out, 16, 0, 16, false, true, s);
+    conv(A.s1, A.d1, c1, 0, c1, Wb(u, 10), Bf(u, 10), A.out, 16, 0, 16, false, true, s, last);
 }
 
 // gradient of layer l: weights/bias from (X, G), then the data gradient Gin = conv(G, flip(W_l))
@@ -269,8 +291,7 @@ pps_status pps_internal_unet_apply(pps_unet* u, int nx, int ny, int nz, const fl
         ensure_acts(u, nx, ny, nz, false);
         const long long nv = (long long)nx * ny * nz;
         rms(nv, in, u->dtmp, s);
-        forward(u, in, u->dtmp);
-        out_to_dense(nv, u->A.out, 16, u->dtmp, gain, out, s);
+        forward(u, in, u->dtmp, out, gain);
         u->stream = saved;
         return PPS_OK;
     });
@@ -432,8 +453,7 @@ pps_status pps_unet_forward(pps_unet* u, int nx, int ny, int nz, const float* in
             rms(nv, in_dev, u->dtmp, u->stream);
             r = u->dtmp;
         }
-        forward(u, in_dev, r);
-        out_to_dense(nv, u->A.out, 16, r, 1.0f, out_dev, u->stream);
+        forward(u, in_dev, r, out_dev, 1.0f);
         UK(cudaStreamSynchronize(u->stream));
         return PPS_OK;
     });

@@ -22,9 +22,26 @@ void set_stop_flag(const int* done);
 
 typedef __nv_bfloat16 bf16;
 
+// Optional sources and sink of a convolution that replace the glue kernels of the
+// inference pass (each gives the values the glue kernel would have stored):
+//   dense_in: the input is a dense FP32 field scaled by 1/(*rms) (rms null: 1) in
+//             channel 0 of 16, zeros elsewhere (dense_to_act);
+//   up:       input channels [0, c_up) are the nearest 2x upsampling of `up`
+//             (coarse grid, leading dimension ld_up; up2);
+//   dense_out: channel 0 of the FP32 output, times (*rms) (rms null: 1) * gain, into
+//             a dense field instead of Y (out_to_dense).
+struct ConvIO {
+    const float* dense_in = nullptr;
+    const bf16* up = nullptr;
+    int ld_up = 0, c_up = 0;
+    float* dense_out = nullptr;
+    const float* rms = nullptr;
+    float gain = 1.0f;
+};
+
 // 3x3x3 zero-padded convolution on tensor cores (Cin, Cout multiples of 16).
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
-          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s);
+          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s, const ConvIO& io = ConvIO());
 void conv_wgrad(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* G, int ldg, int cg0, int Cout,
                 float* dW, cudaStream_t s);
 void bias_grad(long long nv, const bf16* G, int ldg, int cg0, int Cout, float* db, cudaStream_t s);

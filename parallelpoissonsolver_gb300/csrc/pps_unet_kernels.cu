@@ -49,7 +49,7 @@ template <bool RELU, bool OUT_F32, int NW>
 __global__ void __launch_bounds__(32 * NW) k_conv(Dims d, const bf16* __restrict__ X, int ldx, int cx0, int Cin,
                                                   const bf16* __restrict__ Wt, const float* __restrict__ bias,
                                                   void* __restrict__ Yv, int ldy, int cy0, int Cout,
-                                                  const int* __restrict__ stop)
+                                                  const int* __restrict__ stop, ConvIO io)
 {
     pdl_enter();
     if (stop && *(volatile const int*)stop) return;
@@ -65,12 +65,23 @@ __global__ void __launch_bounds__(32 * NW) k_conv(Dims d, const bf16* __restrict
     const bool va_in = lva < nvox;
     const int xa = (int)(lva % d.W), ya = (int)((lva / d.W) % d.H), za = (int)(lva / ((long long)d.W * d.H));
     const int csteps = Cin / 16, ksteps = 27 * csteps;
+    const float in_sc = io.dense_in && io.rms ? (*io.rms > 0.0f ? 1.0f / *io.rms : 0.0f) : 1.0f;
+    const int Hc = d.H / 2, Wc = d.W / 2;
     auto load_a = [&](int t) -> uint4 {
         const int tap = t / csteps, c0 = (t - tap * csteps) * 16;
         const int zz = za + tap / 9 - 1, yy = ya + (tap / 3) % 3 - 1, xx = xa + tap % 3 - 1;
         uint4 val = make_uint4(0, 0, 0, 0);
-        if (va_in && zz >= 0 && zz < d.D && yy >= 0 && yy < d.H && xx >= 0 && xx < d.W)
-            val = *reinterpret_cast<const uint4*>(X + (((long long)zz * d.H + yy) * d.W + xx) * ldx + cx0 + c0 + 8 * ha);
+        if (va_in && zz >= 0 && zz < d.D && yy >= 0 && yy < d.H && xx >= 0 && xx < d.W) {
+            const long long vox = ((long long)zz * d.H + yy) * d.W + xx;
+            if (io.dense_in) {   // channel 0 of the first 16 (Cin = 16): the scaled dense input
+                if (ha == 0) val.x = (unsigned)__bfloat16_as_ushort(__float2bfloat16(io.dense_in[vox] * in_sc));
+            } else if (c0 < io.c_up) {   // the upsampled channels, read at the coarse voxel
+                const long long cv = ((long long)(zz >> 1) * Hc + (yy >> 1)) * Wc + (xx >> 1);
+                val = *reinterpret_cast<const uint4*>(io.up + cv * io.ld_up + c0 + 8 * ha);
+            } else {
+                val = *reinterpret_cast<const uint4*>(X + vox * ldx + cx0 + c0 + 8 * ha);
+            }
+        }
         return val;
     };
     auto w_at = [&](int t) {
@@ -106,6 +117,10 @@ __global__ void __launch_bounds__(32 * NW) k_conv(Dims d, const bf16* __restrict
         for (int w = 0; w < NW; w++) val += sC[w][q];
         val += bias ? bias[co0 + co] : 0.0f;
         if (RELU) val = fmaxf(val, 0.0f);
+        if (io.dense_out) {   // channel 0 only, scaled back
+            if (co0 + co == 0) io.dense_out[v0 + v] = val * ((io.rms ? *io.rms : 1.0f) * io.gain);
+            continue;
+        }
         const long long o = (v0 + v) * ldy + cy0 + co0 + co;
         if (OUT_F32) reinterpret_cast<float*>(Yv)[o] = val;
         else reinterpret_cast<bf16*>(Yv)[o] = __float2bfloat16(val);
@@ -114,26 +129,27 @@ __global__ void __launch_bounds__(32 * NW) k_conv(Dims d, const bf16* __restrict
 
 template <int NW>
 static void conv_nw(const dim3& grid, const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W,
-                    const float* bias, void* Y, int ldy, int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
+                    const float* bias, void* Y, int ldy, int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s,
+                    const ConvIO& io)
 {
     const dim3 block(32 * NW);
     if (out_f32) {
-        if (relu) launch_pdl(k_conv<true, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else launch_pdl(k_conv<false, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        if (relu) launch_pdl(k_conv<true, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop, io);
+        else launch_pdl(k_conv<false, true, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop, io);
     } else {
-        if (relu) launch_pdl(k_conv<true, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
-        else launch_pdl(k_conv<false, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop);
+        if (relu) launch_pdl(k_conv<true, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop, io);
+        else launch_pdl(k_conv<false, false, NW>, grid, block, 0, s, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, g_stop, io);
     }
 }
 
 void conv(const Dims& d, const bf16* X, int ldx, int cx0, int Cin, const bf16* W, const float* bias, void* Y, int ldy,
-          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s)
+          int cy0, int Cout, bool relu, bool out_f32, cudaStream_t s, const ConvIO& io)
 {
     const dim3 grid((unsigned)(((long long)d.D * d.H * d.W + CONV_V - 1) / CONV_V), (unsigned)(Cout / 16));
     // warps per block: enough that each warp's chain of K steps stays short
     const int ksteps = 27 * (Cin / 16);
-    if (ksteps >= 64) conv_nw<16>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s);
-    else conv_nw<8>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s);
+    if (ksteps >= 64) conv_nw<16>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s, io);
+    else conv_nw<8>(grid, d, X, ldx, cx0, Cin, W, bias, Y, ldy, cy0, Cout, relu, out_f32, s, io);
     launches_counter_add(1);
 }
 
