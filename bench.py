@@ -511,7 +511,7 @@ def run_learned_128(args, dev: int):
 
 
 def run_large(args, dev: int):
-    """Config 5 (default on; --no-large skips it): one 1024^3 Dirichlet solve of 64
+    """The 1024^3 charges solve (default on; --no-large skips it): one Dirichlet solve of 64
     Gaussian charges on a k^-3 background, the mixed + learned V-cycle (network on the
     16^3 level, six coarsenings; two timed solves after a warm-up) against the plain
     FP64 BiCGSTAB + Chebyshev path (one solve), both to 1e-10."""
@@ -717,7 +717,7 @@ def run_batched(args, dist: Dist):
     import parallelpoissonsolver_gb300 as pps
     from parallelpoissonsolver_gb300 import workloads
 
-    edges = workloads.edges_config3(args.batch_problems, seed=3)
+    edges = workloads.batch_edges(args.batch_problems, seed=3)
     grids = [pps.BlockGrid.cube(m) for m in edges]
     rhs = [workloads.blobs(m, 3 + i) for i, m in enumerate(edges)]
 
@@ -908,7 +908,7 @@ def profile_case(argv):
                     help="flexible CG's direction kernel with its inputs staged by TMA (tuning fcg_staged)")
     a = ap.parse_args(argv)
     if a.batch_problems > 0:
-        edges = workloads.edges_config3(a.batch_problems, seed=3)
+        edges = workloads.batch_edges(a.batch_problems, seed=3)
         bt = pps.Batch([pps.BlockGrid.cube(m) for m in edges], tolerance=1e-10, inner_tol=1e-5, method="vcycle")
         for i, m in enumerate(edges):
             b = workloads.blobs(m, 3 + i)
@@ -986,7 +986,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-compositions", action="store_true")
     ap.add_argument("--comp-size", type=int, default=256)
-    ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 charges solve (config 5, ~3 min)")
+    ap.add_argument("--no-large", action="store_true", help="skip the 1024^3 charges solve (~3 min)")
     ap.add_argument("--no-learned-128", action="store_true")
     ap.add_argument("--held-out", type=int, default=64, help="held-out right-hand sides of the 128^3 solves")
     ap.add_argument("--held-out-pairs", type=int, default=1000, help="held-out pairs the network is scored on")

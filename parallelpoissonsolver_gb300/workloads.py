@@ -9,12 +9,12 @@ Laplacian (matrixFreeOperatorA.hpp:33-38).
 
 * random_field(m, seed, slope): white noise N(0,1) filtered in Fourier space to a
   power spectrum P(k) ~ k^slope (amplitude |k|^(slope/2) on integer wavevectors,
-  k = 0 removed), normalised to unit RMS.  Config 2 uses slope -2, config 5's
-  background slope -3 at RMS 0.1.
+  k = 0 removed), normalised to unit RMS.  The 512^3 benchmark field uses slope -2,
+  the 1024^3 charges workload's background slope -3 at RMS 0.1.
 * blobs(m, seed): a sum of 1-8 Gaussian blobs, centres U[0.2,0.8]^3, widths
-  U[0.02,0.1], amplitudes N(0,1) (config 3).
+  U[0.02,0.1], amplitudes N(0,1) (the batched workload).
 * charges(m, seed, count): point-like Gaussian charges of width 2h, amplitudes +-1,
-  centres uniform (config 5).
+  centres uniform (the 1024^3 workload).
 """
 from __future__ import annotations
 
@@ -65,7 +65,7 @@ def random_field_values(m: int, seed: int, slope: float = -2.0, device=None) -> 
 
 
 def random_field(m: int, seed: int = 2, slope: float = -2.0, rms: float = 1.0, device=None) -> np.ndarray:
-    """Guard-padded b = -f for f a random field (config 2: seed 2, slope -2)."""
+    """Guard-padded b = -f for f a random field (the 512^3 benchmark: seed 2, slope -2)."""
     return _interior(m, -rms * random_field_values(m, seed, slope, device))
 
 
@@ -76,7 +76,7 @@ def _coords(m: int):
 
 
 def blobs(m: int, seed: int) -> np.ndarray:
-    """Guard-padded b = -f for a seeded sum of 1-8 Gaussian blobs (config 3)."""
+    """Guard-padded b = -f for a seeded sum of 1-8 Gaussian blobs (the batched workload)."""
     rng = np.random.default_rng(seed)
     nb = int(rng.integers(1, 9))
     c = _coords(m)
@@ -94,7 +94,7 @@ def blobs(m: int, seed: int) -> np.ndarray:
 
 def charges(m: int, seed: int = 5, count: int = 64, background_rms: float = 0.1) -> np.ndarray:
     """Guard-padded b = -f: `count` Gaussian charges of width 2h, amplitude +-1, plus a
-    k^-3 random-field background at the given RMS (config 5)."""
+    k^-3 random-field background at the given RMS (the 1024^3 workload)."""
     rng = np.random.default_rng(seed)
     h = 1.0 / (m + 1)
     c = _coords(m)
@@ -131,7 +131,7 @@ def charges_device(m: int, seed: int = 5, count: int = 64, background_rms: float
     return b
 
 
-def edges_config3(count: int = 256, seed: int = 3):
+def batch_edges(count: int = 256, seed: int = 3):
     """Grid edges of the batched configuration: uniform on {32,48,64,96,128}."""
     rng = np.random.default_rng(seed)
     return [int(v) for v in rng.choice([32, 48, 64, 96, 128], count)]
