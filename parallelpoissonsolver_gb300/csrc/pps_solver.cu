@@ -108,6 +108,7 @@ struct pps_solver {
     DevState* d_st = nullptr;
     DevState* h_st = nullptr;  // pinned
     bool state_mapped = false; // h_st and h_st_in are device-addressable at their host addresses
+    bool xnz_mapped = false;   // h_xnz likewise
     double* d_hist = nullptr;
     int hist_cap = 0;
     double* d_partials = nullptr;
@@ -1217,7 +1218,7 @@ bool x_was_nonzero(pps_solver* s, bool wait)
     }
     CK(cudaStreamWaitEvent(s->stream, s->ev_x, 0));
     s->spec_x = false;
-    return *s->h_xnz != 0;
+    return *(volatile int*)s->h_xnz != 0;
 }
 
 // After an update of x on the solver's stream: copy x to the caller's pinned array on
@@ -1369,6 +1370,12 @@ void pull_history(pps_solver* s, int n_iter, bool append)
 bool field_is_zero(pps_solver* s, const double* x)
 {
     if (((uintptr_t)x & 15u) != 0) return false;
+    if (s->xnz_mapped) {   // one pass of integer ORs; the flag is stored through its mapping
+        *(volatile int*)s->h_xnz = 0;
+        flag_nonzero(s->geo.ntot, x, s->h_xnz, s->stream);
+        CK(cudaStreamSynchronize(s->stream));
+        return *(volatile int*)s->h_xnz == 0;
+    }
     state_init(s->d_st, s->d_hist, 0, 0.0, 0.0, 0, 0, 1.0, 0, s->stream);
     fast_count_nonzero(s->geo, s->shape, x, red(s, FIN_STORE), s->stream);
     read_state(s);
@@ -2027,6 +2034,8 @@ pps_status pps_create(const pps_grid* grid, const pps_config* cfg, pps_solver** 
                 void* dp = nullptr;
                 mapped = mapped && cudaHostGetDevicePointer(&dp, h, 0) == cudaSuccess && dp == (void*)h;
             }
+            void* dp = nullptr;
+            s->xnz_mapped = cudaHostGetDevicePointer(&dp, s->h_xnz, 0) == cudaSuccess && dp == (void*)s->h_xnz;
             cudaGetLastError();
             s->state_mapped = mapped;
         }
@@ -2204,9 +2213,14 @@ pps_status pps_solve(pps_solver* s, double* x, double* b, pps_stats* stats)
             CK(cudaEventRecord(s->ev_b, s->stream));
             CK(cudaStreamWaitEvent(s->copy_stream, s->ev_b, 0));   // x follows b on the link
             CK(cudaMemcpyAsync(s->d_x, x, fb, cudaMemcpyHostToDevice, s->copy_stream));
-            CK(cudaMemsetAsync(s->d_xnz, 0, sizeof(int), s->copy_stream));
-            flag_nonzero(s->geo.ntot, s->d_x, s->d_xnz, s->copy_stream);
-            CK(cudaMemcpyAsync(s->h_xnz, s->d_xnz, sizeof(int), cudaMemcpyDeviceToHost, s->copy_stream));
+            if (s->xnz_mapped) {   // the test's flag stored through its mapping
+                *(volatile int*)s->h_xnz = 0;
+                flag_nonzero(s->geo.ntot, s->d_x, s->h_xnz, s->copy_stream);
+            } else {
+                CK(cudaMemsetAsync(s->d_xnz, 0, sizeof(int), s->copy_stream));
+                flag_nonzero(s->geo.ntot, s->d_x, s->d_xnz, s->copy_stream);
+                CK(cudaMemcpyAsync(s->h_xnz, s->d_xnz, sizeof(int), cudaMemcpyDeviceToHost, s->copy_stream));
+            }
             CK(cudaEventRecord(s->ev_x, s->copy_stream));
             s->spec_x = true;
             s->out_host = x;
