@@ -387,20 +387,34 @@ __device__ void ph_a_fcg(const Dev& D, const Item& it, Acc<float>& acc)
     const float* pin = S.par ? D.pb : D.pa;
     float* pout = S.par ? D.pa : D.pb;
     const float be = (float)S.beta, ih2 = (float)P.ih2;
-    for (int k = it.k0; k < it.k1; k++) {
-        const long long c = idx0(P, it.i, it.j, k);
-        float pc, ps;
+    // z and p_in of the planes below and above are carried along the march; the sums
+    // keep nsum's operand order
+    long long c = idx0(P, it.i, it.j, it.k0);
+    float zm = D.z[c - sk], zc = D.z[c], qm = 0.f, qc = 0.f;
+    if (be != 0.f) {
+        qm = pin[c - sk];
+        qc = pin[c];
+    }
+    for (int k = it.k0; k < it.k1; k++, c += sk) {
+        const float zp = D.z[c + sk];
+        const float zs = ((D.z[c - 1] + D.z[c + 1]) + (D.z[c - sj] + D.z[c + sj])) + (zm + zp);
+        float pc, ps, qp = 0.f;
         if (be == 0.f) {
-            pc = D.z[c];
-            ps = nsum(D.z, c, sj, sk);
+            pc = zc;
+            ps = zs;
         } else {
-            pc = fmaf(be, pin[c], D.z[c]);
-            ps = fmaf(be, nsum(pin, c, sj, sk), nsum(D.z, c, sj, sk));
+            qp = pin[c + sk];
+            pc = fmaf(be, qc, zc);
+            ps = fmaf(be, ((pin[c - 1] + pin[c + 1]) + (pin[c - sj] + pin[c + sj])) + (qm + qp), zs);
         }
         const float a = (ps - 6.f * pc) * ih2;
         pout[c] = pc;
         D.ap[c] = a;
         acc.add(pc, a);
+        zm = zc;
+        zc = zp;
+        qm = qc;
+        qc = qp;
     }
 }
 
@@ -439,12 +453,16 @@ __device__ void ph_b_refine(const Dev& D, const Item& it, double& acc)
     if (!it.on) return;
     const long long sj = P.m + 4, sk = sj * sj;
     const double* x = D.x;
-    for (int k = it.k0; k < it.k1; k++) {
-        const long long c = idx0(P, it.i, it.j, k);
-        const double s6 = ((x[c - 1] + x[c + 1]) + (x[c - sj] + x[c + sj])) + (x[c - sk] + x[c + sk]);
-        const double rv = D.b[c] - (s6 - 6.0 * x[c]) * P.ih2;
+    long long c = idx0(P, it.i, it.j, it.k0);
+    double xm = x[c - sk], xc = x[c];   // the planes below and above carried along the march
+    for (int k = it.k0; k < it.k1; k++, c += sk) {
+        const double xp = x[c + sk];
+        const double s6 = ((x[c - 1] + x[c + 1]) + (x[c - sj] + x[c + sj])) + (xm + xp);
+        const double rv = D.b[c] - (s6 - 6.0 * xc) * P.ih2;
         D.r[c] = (float)rv;
         acc = fma(rv, rv, acc);
+        xm = xc;
+        xc = xp;
     }
 }
 
@@ -458,12 +476,16 @@ __device__ void ph_cheb0(const Dev& D, const Item& it, int t)
     const float* Y = t == 0 ? D.r : (t == 1 ? D.y1 : D.y2);
     float* W = t == 0 ? D.y1 : (t == 1 ? D.y2 : D.z);
     const float cc = P.fcc[t], cn = P.fcn[t], cb = P.fcb[t], cz = P.fcz[t];
-    for (int k = it.k0; k < it.k1; k++) {
-        const long long c = idx0(P, it.i, it.j, k);
-        float w = fmaf(cn, nsum(Y, c, sj, sk), cc * Y[c]);
+    long long c = idx0(P, it.i, it.j, it.k0);
+    float ym = Y[c - sk], yc = Y[c];   // the planes below and above carried along the march
+    for (int k = it.k0; k < it.k1; k++, c += sk) {
+        const float yp = Y[c + sk];
+        float w = fmaf(cn, ((Y[c - 1] + Y[c + 1]) + (Y[c - sj] + Y[c + sj])) + (ym + yp), cc * yc);
         if (t > 0) w = fmaf(cb, D.r[c], w);
         if (t == 2) w = fmaf(cz, D.y1[c], w);
         W[c] = w;
+        ym = yc;
+        yc = yp;
     }
 }
 
@@ -474,9 +496,13 @@ __device__ void ph_r0(const Dev& D, const Item& it)
     if (!it.on) return;
     const long long sj = P.m + 4, sk = sj * sj;
     const float ih2 = (float)P.ih2;
-    for (int k = it.k0; k < it.k1; k++) {
-        const long long c = idx0(P, it.i, it.j, k);
-        D.t0[c] = D.r[c] - (nsum(D.z, c, sj, sk) - 6.f * D.z[c]) * ih2;
+    long long c = idx0(P, it.i, it.j, it.k0);
+    float zm = D.z[c - sk], zc = D.z[c];   // the planes below and above carried along the march
+    for (int k = it.k0; k < it.k1; k++, c += sk) {
+        const float zp = D.z[c + sk];
+        D.t0[c] = D.r[c] - ((((D.z[c - 1] + D.z[c + 1]) + (D.z[c - sj] + D.z[c + sj])) + (zm + zp)) - 6.f * zc) * ih2;
+        zm = zc;
+        zc = zp;
     }
 }
 
